@@ -1,0 +1,344 @@
+"""Benchmark of the faust_gb300 hot paths on one GB300 (or N ranks, weak
+scaling: every rank runs its own copy of the workload, no collective on the
+data path).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                  [--workload palm|csr_butterfly|csr_random|bsr]
+
+One JSON line is printed by rank 0.  Workloads (all inputs seeded, synthetic):
+  palm           palm4msa2 FP64, target = Sylvester Hadamard 1024 / 32,
+                 10 factors 1024^2 with prox_sp k=2048, identity init,
+                 200 iterations, power-iteration tolerance 1e-8 (default)
+  csr_butterfly  12 CSR factors 4096^2 on butterfly supports (2 nnz/row),
+                 FP32, times X 4096 x 8192
+  csr_random     5 CSR factors 1024^2 with 10 random nnz/row, FP64, times
+                 X 1024 x 512
+  bsr            4 BSR factors 16384^2, 64x64 BF16 blocks, 8 blocks per block
+                 row, times X 16384 x 4096 BF16 (FP32 accumulation)
+--impl reference times the CPU restatement of the reference algorithm
+(oracle/, all host threads) on a bounded sample of the same workload; the
+reference itself cannot be compiled here (it needs Eigen 3.4).
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "PALM4MSA time-to-rel-err (learned vs plain init, GB300); Faust·X GB/s vs HBM"
+
+
+def _peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), float(p["bf16_tflops"]), "measured"
+    except Exception:
+        return 6800.0, 1900.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            p = [x.strip() for x in ln.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                mx.append(float(p[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, p[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ---------------------------------------------------------------- workloads
+class FaustX:
+    """Faust x dense: one step = F @ X over the whole X."""
+
+    def __init__(self, name, rng):
+        import torch
+        from faust_gb300 import synth
+        self.name = name
+        self.torch = torch
+        if name == "csr_butterfly":
+            self.facs = synth.butterfly_faust_factors(12, rng, np.float32)
+            self.n, self.ncols, self.np_dtype, self.tdtype = 4096, 8192, np.float32, torch.float32
+            self.desc = "12 CSR butterfly factors 4096^2 (2 nnz/row) FP32 x X 4096x8192"
+            self.dtype = "f32"
+        elif name == "csr_random":
+            self.facs = [synth.random_csr(1024, 1024, 10, rng) for _ in range(5)]
+            self.n, self.ncols, self.np_dtype, self.tdtype = 1024, 512, np.float64, torch.float64
+            self.desc = "5 CSR 1024^2 (10 random nnz/row) FP64 x X 1024x512"
+            self.dtype = "f64"
+        elif name == "bsr":
+            import faust_gb300 as fg
+            self.n, self.ncols, self.np_dtype, self.tdtype = 16384, 4096, None, torch.bfloat16
+            self.bsr = []
+            sigma = 1.0 / np.sqrt(8 * 64)
+            for _ in range(4):
+                bp, bc, blocks = synth.random_bsr(16384, 64, 8, rng, sigma)
+                self.bsr.append(fg.BSRFactor(16384, 16384, bp, bc, synth.bf16_bits(blocks)))
+            self.desc = "4 BSR 16384^2, 64x64 BF16 blocks, 8 blocks/block-row, x X 16384x4096 BF16"
+            self.dtype = "bf16"
+        else:
+            raise ValueError(name)
+
+    def factor_bytes(self):
+        if self.name == "bsr":
+            return [f.nnz_blocks * 64 * 64 * 2 + f.nnz_blocks * 4 + f.browptr.size * 4 for f in self.bsr]
+        es = np.dtype(self.np_dtype).itemsize
+        return [f.nnz * (es + 4) + (f.shape[0] + 1) * 4 for f in self.facs]
+
+    def setup(self, ctx):
+        import faust_gb300 as fg
+        torch = self.torch
+        self.F = fg.Faust(self.bsr if self.name == "bsr" else self.facs, ctx=ctx)
+        g = torch.Generator(device="cuda").manual_seed(1234)
+        self.X = torch.randn((self.ncols, self.n), generator=g, device="cuda", dtype=torch.float32).to(self.tdtype).t()
+        self.Y = torch.empty((self.ncols, self.n), device="cuda", dtype=self.tdtype).t()
+        self.es = self.X.element_size()
+        self.xy_bytes = 2 * self.n * self.ncols * self.es
+        # algorithmic bytes per step: every factor reads X-sized input and
+        # writes a Y-sized output plus its own arrays (one launch per factor)
+        self.step_bytes = sum(b + self.xy_bytes for b in self.factor_bytes())
+        # the fused chain kernel (one launch) reads X once, writes Y once and
+        # reads each factor
+        self.fused_bytes = self.xy_bytes + sum(self.factor_bytes())
+        self.flops = (sum(2 * f.nnz * self.ncols for f in self.facs) if self.name != "bsr" else
+                      sum(2 * f.nnz_blocks * 64 * 64 * self.ncols for f in self.bsr))
+
+    def step(self, mode=0):
+        self.F.matmul_device(self.X, self.Y, mode=mode)
+
+    def kernel_bytes(self, fused):
+        return self.fused_bytes if fused else self.step_bytes / len(self.factor_bytes())
+
+    def host_step(self, Xh, Yh):
+        from faust_gb300 import _ffi
+        _ffi.check(_ffi.lib().fgb_faust_mul_host(self.F.handle, Xh.data_ptr(), self.ncols, Yh.data_ptr()),
+                   self.F.ctx.handle)
+
+
+def run_faust_x(args, rank, world):
+    import torch
+    import faust_gb300 as fg
+    from faust_gb300 import _ffi
+    torch.cuda.set_device(rank % max(1, torch.cuda.device_count()))
+    rng = np.random.default_rng(2024)
+    W = FaustX(args.workload, rng)
+    stream = torch.cuda.current_stream()
+    ctx = fg.Context(torch.cuda.current_device(), stream=stream.cuda_stream)
+    W.setup(ctx)
+    fused = False
+    if W.name != "bsr":
+        # decide which path automatic mode takes: fused when it fits
+        from ctypes import c_int
+        fused = len(W.facs) > 1
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    for _ in range(args.warmup):
+        W.step()
+    torch.cuda.synchronize()
+    _barrier(world)
+    times = []
+    launches0 = ctx.kernel_launches()
+    with ClockSampler(torch.cuda.current_device()) as clk:
+        for _ in range(args.steps):
+            flush.zero_()  # L2 flush between timed iterations
+            s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            s.record(stream)
+            W.step()
+            e.record(stream)
+            times.append((s, e))
+        torch.cuda.synchronize()
+    launches = ctx.kernel_launches() - launches0
+    ms = [a.elapsed_time(b) for a, b in times]
+    step_ms = float(np.mean(ms))
+    step_ms = _max_over_ranks(step_ms, world)
+    # end to end through the host-memory C-ABI entry point (pinned buffers)
+    Xh = W.X.t().contiguous().cpu().pin_memory()  # (ncols, n) row-major == column-major n x ncols
+    Yh = torch.empty((W.ncols, W.n), dtype=W.tdtype).pin_memory()
+    W.host_step(Xh, Yh)
+    e2e = []
+    for _ in range(max(3, min(args.steps, 10))):
+        t0 = time.perf_counter()
+        W.host_step(Xh, Yh)
+        e2e.append(time.perf_counter() - t0)
+    e2e_ms = float(np.median(e2e)) * 1e3
+    hbm, tflops, peak_kind = _peaks()
+    kb = W.kernel_bytes(fused)
+    achieved = kb / (step_ms / 1e3 / (1 if fused else len(W.factor_bytes()))) / 1e9
+    value = W.step_bytes * world / (step_ms / 1e3) / 1e9
+    out = {
+        "metric": METRIC, "submetric": "Faust.X effective GB/s (per-factor algorithmic bytes / step time)",
+        "value": round(value, 2), "unit": "GB/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(step_ms, 4), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": W.dtype, "data": "synthetic (seeded)",
+        "config": {"workload": W.name, "desc": W.desc, "l2": "flushed (256 MB write) before every timed step",
+                   "path": "fused chain kernel" if fused else "one launch per factor"},
+        "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
+                     "frac": round(achieved / hbm, 4), "traffic": None, "peak_kind": peak_kind,
+                     "kernel": "k_csr_chain_fused" if fused else "k_csr_spmm / k_bsr",
+                     "algorithmic_bytes_per_launch": int(kb)},
+        "e2e": {"value": round(W.step_bytes / (e2e_ms / 1e3) / 1e9, 2), "unit": "GB/s",
+                "ms_per_step": round(e2e_ms, 3),
+                "h2d_bytes_per_step": int(W.n * W.ncols * W.es), "d2h_bytes_per_step": int(W.n * W.ncols * W.es)},
+        "gpu_launches": int(launches),
+        "clocks": clk.summary(),
+    }
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        out["cpu_baseline"] = cpu_baseline_faust_x(W)
+    return out
+
+
+def cpu_baseline_faust_x(W, sample_cols=None):
+    from oracle import oracle as O
+    threads = os.cpu_count() or 1
+    O.set_threads(threads)
+    if W.name == "bsr":
+        return {"value": None, "unit": "GB/s", "cores": threads, "kind": "port",
+                "sample": "not run for BSR (FP64 oracle too slow for a bounded sample)"}
+    cols = sample_cols or (512 if W.name == "csr_butterfly" else W.ncols)
+    rng = np.random.default_rng(7)
+    X = np.asfortranarray(rng.standard_normal((W.n, cols)).astype(W.np_dtype))
+    O.chain_mul(W.facs, X[:, :8])
+    t0 = time.perf_counter()
+    reps = 0
+    while True:
+        O.chain_mul(W.facs, X)
+        reps += 1
+        if time.perf_counter() - t0 > 3.0:
+            break
+    dt = (time.perf_counter() - t0) / reps
+    es = np.dtype(W.np_dtype).itemsize
+    bytes_ = sum(b + 2 * W.n * cols * es for b in W.factor_bytes())
+    return {"value": round(bytes_ / dt / 1e9, 3), "unit": "GB/s", "cores": threads, "kind": "port",
+            "sample": "%d of %d columns of X, %d repetitions" % (cols, W.ncols, reps)}
+
+
+# ---------------------------------------------------------------- helpers
+def _barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def _max_over_ranks(x, world):
+    if world <= 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="csr_butterfly", choices=["csr_butterfly", "csr_random", "bsr"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        dist.init_process_group("nccl")
+    if args.impl == "reference":
+        if rank == 0:
+            out = reference_arm(args, world)
+            print(json.dumps(out), flush=True)
+        return
+    out = run_faust_x(args, rank, world)
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+def reference_arm(args, world):
+    import faust_gb300.synth  # noqa: F401  (generators only)
+    rng = np.random.default_rng(2024)
+
+    class _W:
+        pass
+
+    from faust_gb300 import synth
+    W = _W()
+    W.name = args.workload
+    if W.name == "csr_butterfly":
+        W.facs = synth.butterfly_faust_factors(12, rng, np.float32)
+        W.n, W.ncols, W.np_dtype = 4096, 8192, np.float32
+    else:
+        W.facs = [synth.random_csr(1024, 1024, 10, rng) for _ in range(5)]
+        W.n, W.ncols, W.np_dtype = 1024, 512, np.float64
+    es = np.dtype(W.np_dtype).itemsize
+    W.factor_bytes = lambda: [f.nnz * (es + 4) + (f.shape[0] + 1) * 4 for f in W.facs]
+    vals = []
+    for _ in range(max(1, args.steps)):
+        vals.append(cpu_baseline_faust_x(W))
+    v = float(np.median([x["value"] for x in vals]))
+    cb = dict(vals[0])
+    cb["value"] = v
+    return {"impl": "reference", "metric": METRIC, "value": v, "unit": "GB/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
+            "config": {"workload": W.name}, "cpu_baseline": cb,
+            "e2e": {"value": v, "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,387 @@
+// csr.cu — CSR factor kernels: single-factor SpMM (shared-memory staged
+// column tiles of X or direct gathers), the fused chain kernel that keeps the
+// whole right-to-left product of a column tile on chip, X S^T, device-side
+// transposition and dense images.
+#include <algorithm>
+
+#include "csr.cuh"
+
+namespace fgb {
+
+constexpr int SPMM_THREADS = 256;
+
+// ------------------------------------------------------------------ helpers
+template <typename T, int TC>
+struct Vec;
+template <>
+struct Vec<float, 4> {
+  using type = float4;
+};
+template <>
+struct Vec<float, 2> {
+  using type = float2;
+};
+template <>
+struct Vec<double, 2> {
+  using type = double2;
+};
+
+// Reads TC consecutive values of a shared-memory row (row-major tile) with
+// 16-byte loads where the width allows.
+template <typename T, int TC>
+__device__ __forceinline__ void load_row(const T* __restrict__ p, T (&x)[TC]) {
+  if constexpr (sizeof(T) * TC % 16 == 0) {
+    constexpr int W = 16 / sizeof(T);
+    using V = typename Vec<T, W>::type;
+#pragma unroll
+    for (int u = 0; u < TC / W; ++u) {
+      V v = reinterpret_cast<const V*>(p)[u];
+      if constexpr (W == 4) {
+        x[4 * u + 0] = v.x;
+        x[4 * u + 1] = v.y;
+        x[4 * u + 2] = v.z;
+        x[4 * u + 3] = v.w;
+      } else {
+        x[2 * u + 0] = v.x;
+        x[2 * u + 1] = v.y;
+      }
+    }
+  } else {
+#pragma unroll
+    for (int t = 0; t < TC; ++t) x[t] = p[t];
+  }
+}
+
+// Copies the column tile X[0:inner, j0:j0+TC) into shared memory as a
+// row-major inner x TC tile (zero beyond ncols).  Global reads walk each
+// column contiguously.
+template <typename T, int TC>
+__device__ __forceinline__ void stage_tile(T* __restrict__ tile, const T* __restrict__ X, long ldx, int inner,
+                                           int j0, int ncols) {
+  for (int t = 0; t < TC; ++t) {
+    const bool ok = j0 + t < ncols;
+    const T* col = X + (long)(j0 + t) * ldx;
+    for (int r = threadIdx.x; r < inner; r += blockDim.x) tile[(long)r * TC + t] = ok ? col[r] : T(0);
+  }
+}
+
+// ------------------------------------------------------------------ Y = S X
+// Grid: x = column tiles of width TC, y = row blocks.  STAGED copies the X
+// tile to shared memory first (random column indices then gather from SMEM);
+// otherwise entries are gathered from global memory / L2.
+template <typename T, int TC, bool STAGED>
+__global__ void __launch_bounds__(SPMM_THREADS)
+    k_csr_spmm(const int* __restrict__ rowptr, const int* __restrict__ colind, const T* __restrict__ val, int rows,
+               int inner, const T* __restrict__ X, int ldx, int ncols, T* __restrict__ Y, int ldy, Epi<T> epi) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T* tile = reinterpret_cast<T*>(smem_raw);
+  const int j0 = blockIdx.x * TC;
+  if (STAGED) {
+    stage_tile<T, TC>(tile, X, ldx, inner, j0, ncols);
+    __syncthreads();
+  }
+  const T s = epi.scal ? *epi.scal : T(0);
+  for (int i = blockIdx.y * blockDim.x + threadIdx.x; i < rows; i += gridDim.y * blockDim.x) {
+    T acc[TC];
+#pragma unroll
+    for (int t = 0; t < TC; ++t) acc[t] = T(0);
+    const int p1 = rowptr[i + 1];
+    for (int p = rowptr[i]; p < p1; ++p) {
+      const T v = val[p];
+      const int c = colind[p];
+      T x[TC];
+      if (STAGED) {
+        load_row<T, TC>(tile + (long)c * TC, x);
+      } else {
+#pragma unroll
+        for (int t = 0; t < TC; ++t) x[t] = (j0 + t < ncols) ? X[c + (long)(j0 + t) * ldx] : T(0);
+      }
+#pragma unroll
+      for (int t = 0; t < TC; ++t) acc[t] = fmad(v, x[t], acc[t]);
+    }
+#pragma unroll
+    for (int t = 0; t < TC; ++t)
+      if (j0 + t < ncols) Y[i + (long)(j0 + t) * ldy] = epi_apply(epi, acc[t], i, j0 + t, s);
+  }
+}
+
+template <typename T, int TC, bool STAGED>
+static fgb_status launch_spmm_tc(fgb_ctx* ctx, const int* rowptr, const int* colind, const T* val, int rows,
+                                 int inner, const T* X, int ldx, int ncols, T* Y, int ldy, const Epi<T>& epi) {
+  const int tiles = (ncols + TC - 1) / TC;
+  size_t smem = STAGED ? (size_t)inner * TC * sizeof(T) : 0;
+  int rblocks = 1;
+  if (!STAGED) {
+    // Enough blocks to cover the SMs several times.
+    long want = 4L * ctx->sm_count;
+    rblocks = (int)std::max(1L, std::min((long)((rows + SPMM_THREADS - 1) / SPMM_THREADS), want / std::max(1, tiles)));
+  }
+  auto kern = k_csr_spmm<T, TC, STAGED>;
+  if (smem > 48 * 1024) FGB_CUDA(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  dim3 grid(tiles, rblocks);
+  kern<<<grid, SPMM_THREADS, smem, ctx->stream>>>(rowptr, colind, val, rows, inner, X, ldx, ncols, Y, ldy, epi);
+  FGB_LAUNCHED(ctx);
+  return FGB_OK;
+}
+
+template <typename T>
+fgb_status launch_csr_spmm(fgb_ctx* ctx, const int* rowptr, const int* colind, const T* val, int rows, int inner,
+                           const T* X, int ldx, int ncols, T* Y, int ldy, const Epi<T>& epi) {
+  if (rows == 0 || ncols == 0) return FGB_OK;
+  constexpr int TC = 16 / sizeof(T) * 2;  // 8 floats or 4 doubles per thread
+  const size_t staged = (size_t)inner * TC * sizeof(T);
+  const long tiles = (ncols + TC - 1) / TC;
+  // Stage when the tile fits comfortably and there are enough tiles to fill
+  // the GPU; small problems (PALM blocks) gather straight from L2.
+  if (staged <= 96 * 1024 && tiles >= ctx->sm_count)
+    return launch_spmm_tc<T, TC, true>(ctx, rowptr, colind, val, rows, inner, X, ldx, ncols, Y, ldy, epi);
+  return launch_spmm_tc<T, TC / 2, false>(ctx, rowptr, colind, val, rows, inner, X, ldx, ncols, Y, ldy, epi);
+}
+
+// ------------------------------------------------------------------ Y = X S^T
+// Grid: x = output columns (rows of S), y = row blocks of X.  Each output
+// column c combines the columns of X named by row c of S.
+template <typename T>
+__global__ void __launch_bounds__(SPMM_THREADS)
+    k_dense_csrT(const T* __restrict__ X, int ldx, int xrows, const int* __restrict__ rowptr,
+                 const int* __restrict__ colind, const T* __restrict__ val, int srows, T* __restrict__ Y, int ldy,
+                 Epi<T> epi) {
+  const int c = blockIdx.x;
+  const int p0 = rowptr[c], p1 = rowptr[c + 1];
+  const T s = epi.scal ? *epi.scal : T(0);
+  for (int r = blockIdx.y * blockDim.x + threadIdx.x; r < xrows; r += gridDim.y * blockDim.x) {
+    T acc = T(0);
+    for (int p = p0; p < p1; ++p) acc = fmad(val[p], X[r + (long)colind[p] * ldx], acc);
+    Y[r + (long)c * ldy] = epi_apply(epi, acc, r, c, s);
+  }
+}
+
+template <typename T>
+fgb_status launch_dense_csrT(fgb_ctx* ctx, const T* X, int ldx, int xrows, const int* rowptr, const int* colind,
+                             const T* val, int srows, int scols, T* Y, int ldy, const Epi<T>& epi) {
+  (void)scols;
+  if (srows == 0 || xrows == 0) return FGB_OK;
+  int rblocks = std::max(1, std::min((xrows + SPMM_THREADS - 1) / SPMM_THREADS, 8));
+  dim3 grid(srows, rblocks);
+  k_dense_csrT<T><<<grid, SPMM_THREADS, 0, ctx->stream>>>(X, ldx, xrows, rowptr, colind, val, srows, Y, ldy, epi);
+  FGB_LAUNCHED(ctx);
+  return FGB_OK;
+}
+
+// ------------------------------------------------------------------ fused chain
+// One block owns the column tile X[:, j0:j0+TC) and applies every factor in
+// turn, right to left, with the intermediate tile kept in shared memory
+// (two buffers of maxdim x TC).  Only X is read from HBM and only Y written;
+// the factors are read from L2 by every block.
+template <typename T, int TC>
+__global__ void __launch_bounds__(SPMM_THREADS)
+    k_csr_chain_fused(const ChainDesc* __restrict__ desc, int nfac, const T* __restrict__ X, int ldx, int ncols,
+                      T* __restrict__ Y, int ldy, int maxdim) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T* bufA = reinterpret_cast<T*>(smem_raw);
+  T* bufB = bufA + (long)maxdim * TC;
+  const int j0 = blockIdx.x * TC;
+  stage_tile<T, TC>(bufA, X, ldx, desc[nfac - 1].cols, j0, ncols);
+  __syncthreads();
+  T* in = bufA;
+  T* out = bufB;
+  for (int f = nfac - 1; f >= 0; --f) {
+    const ChainDesc d = desc[f];
+    const T* __restrict__ val = reinterpret_cast<const T*>(d.val);
+    const bool last = (f == 0);
+    for (int i = threadIdx.x; i < d.rows; i += blockDim.x) {
+      T acc[TC];
+#pragma unroll
+      for (int t = 0; t < TC; ++t) acc[t] = T(0);
+      const int p1 = d.rowptr[i + 1];
+      for (int p = d.rowptr[i]; p < p1; ++p) {
+        const T v = val[p];
+        T x[TC];
+        load_row<T, TC>(in + (long)d.colind[p] * TC, x);
+#pragma unroll
+        for (int t = 0; t < TC; ++t) acc[t] = fmad(v, x[t], acc[t]);
+      }
+      if (last) {
+#pragma unroll
+        for (int t = 0; t < TC; ++t)
+          if (j0 + t < ncols) Y[i + (long)(j0 + t) * ldy] = acc[t];
+      } else {
+#pragma unroll
+        for (int t = 0; t < TC; ++t) out[(long)i * TC + t] = acc[t];
+      }
+    }
+    __syncthreads();
+    T* tmp = in;
+    in = out;
+    out = tmp;
+  }
+}
+
+template <typename T, int TC>
+static fgb_status launch_chain_tc(fgb_ctx* ctx, const ChainDesc* d_desc, int nfac, const T* X, int ldx, int ncols,
+                                  T* Y, int ldy, int maxdim) {
+  const size_t smem = 2 * (size_t)maxdim * TC * sizeof(T);
+  auto kern = k_csr_chain_fused<T, TC>;
+  if (smem > 48 * 1024) FGB_CUDA(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  const int tiles = (ncols + TC - 1) / TC;
+  kern<<<tiles, SPMM_THREADS, smem, ctx->stream>>>(d_desc, nfac, X, ldx, ncols, Y, ldy, maxdim);
+  FGB_LAUNCHED(ctx);
+  return FGB_OK;
+}
+
+// Picks the tile width: the widest that fits shared memory while still giving
+// at least one block per SM; returns 0 when no width fits.
+template <typename T>
+static int chain_tile_width(fgb_ctx* ctx, int maxdim, int ncols) {
+  const size_t cap = std::min<size_t>(ctx->smem_optin ? ctx->smem_optin : 227 * 1024, 200 * 1024);
+  const int widths[] = {8, 4, 2};
+  int best = 0;
+  for (int w : widths) {
+    if (sizeof(T) * w < 8) continue;  // keep 8-byte rows at least
+    if (2 * (size_t)maxdim * w * sizeof(T) > cap) continue;
+    if (!best) best = w;
+    if ((ncols + w - 1) / w >= ctx->sm_count) return w;
+    best = w;
+  }
+  return best;
+}
+
+fgb_status chain_fused(fgb_ctx* ctx, fgb_dtype dt, const ChainDesc* d_desc, int nfac, const void* X, int ldx,
+                       int ncols, void* Y, int ldy, int maxdim, bool probe_only, bool* fits) {
+  int w = (dt == FGB_F64) ? chain_tile_width<double>(ctx, maxdim, ncols)
+                          : (dt == FGB_F32 ? chain_tile_width<float>(ctx, maxdim, ncols) : 0);
+  if (fits) *fits = (w != 0);
+  if (probe_only || w == 0) return w ? FGB_OK : FGB_ERR_NOT_SUPPORTED;
+  if (dt == FGB_F64) {
+    const double* x = (const double*)X;
+    double* y = (double*)Y;
+    if (w == 8) return launch_chain_tc<double, 8>(ctx, d_desc, nfac, x, ldx, ncols, y, ldy, maxdim);
+    if (w == 4) return launch_chain_tc<double, 4>(ctx, d_desc, nfac, x, ldx, ncols, y, ldy, maxdim);
+    return launch_chain_tc<double, 2>(ctx, d_desc, nfac, x, ldx, ncols, y, ldy, maxdim);
+  }
+  const float* x = (const float*)X;
+  float* y = (float*)Y;
+  if (w == 8) return launch_chain_tc<float, 8>(ctx, d_desc, nfac, x, ldx, ncols, y, ldy, maxdim);
+  if (w == 4) return launch_chain_tc<float, 4>(ctx, d_desc, nfac, x, ldx, ncols, y, ldy, maxdim);
+  return launch_chain_tc<float, 2>(ctx, d_desc, nfac, x, ldx, ncols, y, ldy, maxdim);
+}
+
+// ------------------------------------------------------------------ transpose
+// Single-block CSR transpose whose transposed rows list entries in increasing
+// original row: a column histogram, a block scan, then an ordered scatter by
+// one warp (ranks inside each 32-entry batch come from __match_any_sync).
+template <typename T>
+__global__ void __launch_bounds__(1024)
+    k_csr_transpose(const int* __restrict__ rowptr, const int* __restrict__ colind, const T* __restrict__ val,
+                    int rows, int cols, int* __restrict__ t_rowptr, int* __restrict__ t_colind,
+                    T* __restrict__ t_val, int* __restrict__ cursor) {
+  const int nnz = rowptr[rows];
+  for (int c = threadIdx.x; c <= cols; c += blockDim.x) cursor[c] = 0;
+  __syncthreads();
+  for (int p = threadIdx.x; p < nnz; p += blockDim.x) atomicAdd(&cursor[colind[p] + 1], 1);
+  __syncthreads();
+  // Inclusive scan of cursor[1..cols] by thread 0 in chunks (cols is small
+  // for PALM factors); t_rowptr = exclusive offsets.
+  if (threadIdx.x == 0) {
+    int run = 0;
+    t_rowptr[0] = 0;
+    for (int c = 0; c < cols; ++c) {
+      run += cursor[c + 1];
+      t_rowptr[c + 1] = run;
+    }
+  }
+  __syncthreads();
+  for (int c = threadIdx.x; c < cols; c += blockDim.x) cursor[c] = t_rowptr[c];
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    const unsigned lane = threadIdx.x;
+    for (int base = 0; base < nnz; base += 32) {
+      const int p = base + (int)lane;
+      const bool ok = p < nnz;
+      int r = 0;
+      if (ok) {
+        // row of entry p: last row whose rowptr is <= p
+        int lo = 0, hi = rows - 1;
+        while (lo < hi) {
+          const int mid = (lo + hi + 1) >> 1;
+          if (rowptr[mid] <= p) lo = mid; else hi = mid - 1;
+        }
+        r = lo;
+      }
+      const int c = ok ? colind[p] : -1 - (int)lane;
+      const unsigned same = __match_any_sync(0xffffffffu, c);
+      const int rank = __popc(same & ((1u << lane) - 1u));
+      int slot = 0;
+      if (ok) slot = cursor[c] + rank;
+      __syncwarp();
+      if (ok) {
+        t_colind[slot] = r;
+        t_val[slot] = val[p];
+        // the highest lane of each column group advances the cursor
+        if ((same >> lane) == 1u) cursor[c] = slot + 1;
+      }
+      __syncwarp();
+    }
+  }
+}
+
+fgb_status csr_build_transpose(fgb_ctx* ctx, fgb_dtype dt, DevFactor& f) {
+  if (f.format != FGB_CSR) return fail(ctx, FGB_ERR_INVALID_ARG, "transpose: CSR factors only");
+  const size_t es = dtype_size(dt);
+  if (!f.t_rowptr) FGB_TRY(dmalloc(ctx, (void**)&f.t_rowptr, sizeof(int) * (f.cols + 1)));
+  if (!f.t_colind) FGB_TRY(dmalloc(ctx, (void**)&f.t_colind, sizeof(int) * std::max(1, f.cap)));
+  if (!f.t_val) FGB_TRY(dmalloc(ctx, &f.t_val, es * std::max(1, f.cap)));
+  int* cursor = nullptr;
+  FGB_TRY(dmalloc(ctx, (void**)&cursor, sizeof(int) * (f.cols + 2)));
+  if (dt == FGB_F64)
+    k_csr_transpose<double><<<1, 1024, 0, ctx->stream>>>(f.rowptr, f.colind, (const double*)f.val, f.rows, f.cols,
+                                                         f.t_rowptr, f.t_colind, (double*)f.t_val, cursor);
+  else
+    k_csr_transpose<float><<<1, 1024, 0, ctx->stream>>>(f.rowptr, f.colind, (const float*)f.val, f.rows, f.cols,
+                                                        f.t_rowptr, f.t_colind, (float*)f.t_val, cursor);
+  ctx->launches.fetch_add(1);
+  cudaError_t e = cudaGetLastError();
+  cudaStreamSynchronize(ctx->stream);
+  dfree(cursor);
+  if (e != cudaSuccess) return cuda_check(ctx, e, "csr transpose");
+  f.has_t = true;
+  return FGB_OK;
+}
+
+// ------------------------------------------------------------------ dense image
+template <typename T>
+__global__ void k_csr_to_dense(const int* __restrict__ rowptr, const int* __restrict__ colind,
+                               const T* __restrict__ val, int rows, int cols, T* __restrict__ out) {
+  const long n = (long)rows * cols;
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) out[i] = T(0);
+}
+template <typename T>
+__global__ void k_csr_scatter(const int* __restrict__ rowptr, const int* __restrict__ colind,
+                              const T* __restrict__ val, int rows, T* __restrict__ out) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < rows; i += gridDim.x * blockDim.x)
+    for (int p = rowptr[i]; p < rowptr[i + 1]; ++p) out[i + (long)colind[p] * rows] = val[p];
+}
+
+template <typename T>
+fgb_status launch_csr_to_dense(fgb_ctx* ctx, const DevFactor& f, T* out) {
+  const int g = 2 * ctx->sm_count;
+  k_csr_to_dense<T><<<g, 256, 0, ctx->stream>>>(f.rowptr, f.colind, (const T*)f.val, f.rows, f.cols, out);
+  FGB_LAUNCHED(ctx);
+  k_csr_scatter<T><<<std::max(1, std::min(g, (f.rows + 255) / 256)), 256, 0, ctx->stream>>>(
+      f.rowptr, f.colind, (const T*)f.val, f.rows, out);
+  FGB_LAUNCHED(ctx);
+  return FGB_OK;
+}
+
+template fgb_status launch_csr_spmm<float>(fgb_ctx*, const int*, const int*, const float*, int, int, const float*, int,
+                                           int, float*, int, const Epi<float>&);
+template fgb_status launch_csr_spmm<double>(fgb_ctx*, const int*, const int*, const double*, int, int, const double*,
+                                            int, int, double*, int, const Epi<double>&);
+template fgb_status launch_dense_csrT<float>(fgb_ctx*, const float*, int, int, const int*, const int*, const float*,
+                                             int, int, float*, int, const Epi<float>&);
+template fgb_status launch_dense_csrT<double>(fgb_ctx*, const double*, int, int, const int*, const int*,
+                                              const double*, int, int, double*, int, const Epi<double>&);
+template fgb_status launch_csr_to_dense<float>(fgb_ctx*, const DevFactor&, float*);
+template fgb_status launch_csr_to_dense<double>(fgb_ctx*, const DevFactor&, double*);
+
+}  // namespace fgb

@@ -1,0 +1,335 @@
+// faust.cu — the Faust handle: device-resident factor chains and the
+// Faust x dense product entry points (fgb_faust_*).
+#include <algorithm>
+#include <cstring>
+
+#include "csr.cuh"
+#include "power.cuh"
+
+namespace fgb {
+fgb_status chain_fused(fgb_ctx* ctx, fgb_dtype dt, const ChainDesc* d_desc, int nfac, const void* X, int ldx,
+                       int ncols, void* Y, int ldy, int maxdim, bool probe_only, bool* fits);
+fgb_status launch_bsr_spmm(fgb_ctx* ctx, const DevFactor& f, const __nv_bfloat16* X, int ldx, int ncols,
+                           __nv_bfloat16* Y, int ldy);
+
+void free_factor(DevFactor& f) {
+  dfree(f.rowptr);
+  dfree(f.colind);
+  dfree(f.val);
+  dfree(f.t_rowptr);
+  dfree(f.t_colind);
+  dfree(f.t_val);
+  f = DevFactor();
+}
+
+// Copies one host factor description into device memory.
+static fgb_status upload_factor(fgb_ctx* ctx, fgb_dtype dt, const fgb_factor_desc& d, DevFactor& f) {
+  const size_t es = dtype_size(dt);
+  f.format = d.format;
+  f.rows = d.rows;
+  f.cols = d.cols;
+  f.nnz = d.nnz;
+  f.cap = std::max(1, d.nnz);
+  f.bm = d.bm;
+  f.bn = d.bn;
+  int nrp = 0;
+  size_t nval = 0;
+  if (d.format == FGB_CSR) {
+    nrp = d.rows + 1;
+    nval = (size_t)d.nnz;
+  } else {
+    nrp = d.rows / d.bm + 1;
+    nval = (size_t)d.nnz * d.bm * d.bn;
+  }
+  FGB_TRY(dmalloc(ctx, (void**)&f.rowptr, sizeof(int) * nrp));
+  FGB_TRY(dmalloc(ctx, (void**)&f.colind, sizeof(int) * std::max(1, d.nnz)));
+  FGB_TRY(dmalloc(ctx, &f.val, es * std::max<size_t>(1, nval)));
+  FGB_CUDA(ctx, cudaMemcpyAsync(f.rowptr, d.rowptr, sizeof(int) * nrp, cudaMemcpyHostToDevice, ctx->stream));
+  if (d.nnz > 0) {
+    FGB_CUDA(ctx, cudaMemcpyAsync(f.colind, d.colind, sizeof(int) * d.nnz, cudaMemcpyHostToDevice, ctx->stream));
+    FGB_CUDA(ctx, cudaMemcpyAsync(f.val, d.values, es * nval, cudaMemcpyHostToDevice, ctx->stream));
+  }
+  return FGB_OK;
+}
+
+static fgb_status validate_desc(fgb_ctx* ctx, fgb_dtype dt, const fgb_factor_desc& d) {
+  if (d.rows <= 0 || d.cols <= 0 || d.nnz < 0) return fail(ctx, FGB_ERR_INVALID_ARG, "factor: bad shape or nnz");
+  if (!d.rowptr || (d.nnz > 0 && (!d.colind || !d.values)))
+    return fail(ctx, FGB_ERR_INVALID_ARG, "factor: null array");
+  if (d.format == FGB_CSR) {
+    if (dt == FGB_BF16) return fail(ctx, FGB_ERR_NOT_SUPPORTED, "CSR factors are F32 or F64");
+    if (d.rowptr[0] != 0 || d.rowptr[d.rows] != d.nnz)
+      return fail(ctx, FGB_ERR_INVALID_ARG, "CSR rowptr must start at 0 and end at nnz");
+    for (int i = 0; i < d.rows; ++i) {
+      if (d.rowptr[i + 1] < d.rowptr[i]) return fail(ctx, FGB_ERR_INVALID_ARG, "CSR rowptr not monotone");
+      for (int p = d.rowptr[i]; p < d.rowptr[i + 1]; ++p) {
+        if (d.colind[p] < 0 || d.colind[p] >= d.cols) return fail(ctx, FGB_ERR_INVALID_ARG, "CSR column out of range");
+        if (p > d.rowptr[i] && d.colind[p] <= d.colind[p - 1])
+          return fail(ctx, FGB_ERR_INVALID_ARG, "CSR columns must be sorted and unique within a row");
+      }
+    }
+  } else if (d.format == FGB_BSR) {
+    if (dt != FGB_BF16) return fail(ctx, FGB_ERR_NOT_SUPPORTED, "BSR factors are BF16 (FP32 accumulation)");
+    if (d.bm != 64 || d.bn != 64) return fail(ctx, FGB_ERR_NOT_SUPPORTED, "BSR blocks must be 64 x 64");
+    if (d.rows % d.bm || d.cols % d.bn) return fail(ctx, FGB_ERR_INVALID_ARG, "BSR shape not a multiple of the block");
+    const int nbr = d.rows / d.bm, nbc = d.cols / d.bn;
+    if (d.rowptr[0] != 0 || d.rowptr[nbr] != d.nnz)
+      return fail(ctx, FGB_ERR_INVALID_ARG, "BSR browptr must start at 0 and end at the block count");
+    for (int i = 0; i < nbr; ++i) {
+      if (d.rowptr[i + 1] < d.rowptr[i]) return fail(ctx, FGB_ERR_INVALID_ARG, "BSR browptr not monotone");
+      for (int p = d.rowptr[i]; p < d.rowptr[i + 1]; ++p)
+        if (d.colind[p] < 0 || d.colind[p] >= nbc) return fail(ctx, FGB_ERR_INVALID_ARG, "BSR block column out of range");
+    }
+  } else {
+    return fail(ctx, FGB_ERR_INVALID_ARG, "unknown factor format");
+  }
+  return FGB_OK;
+}
+
+static fgb_status ensure(fgb_ctx* ctx, void** p, size_t* have, size_t need) {
+  if (*have >= need && *p) return FGB_OK;
+  dfree(*p);
+  *p = nullptr;
+  *have = 0;
+  FGB_TRY(dmalloc(ctx, p, need));
+  *have = need;
+  return FGB_OK;
+}
+
+// One launch per factor, right to left, ping-ponging between two buffers.
+static fgb_status mul_per_factor(fgb_faust* F, const void* X, int ldx, int ncols, void* Y, int ldy) {
+  fgb_ctx* ctx = F->ctx;
+  const int J = (int)F->f.size();
+  const size_t es = dtype_size(F->dtype);
+  int maxrows = 0;
+  for (auto& f : F->f) maxrows = std::max(maxrows, f.rows);
+  if (J > 1) {
+    size_t need = (size_t)maxrows * ncols * es;
+    if (F->buf_bytes < need) {
+      dfree(F->buf[0]);
+      dfree(F->buf[1]);
+      F->buf[0] = F->buf[1] = nullptr;
+      F->buf_bytes = 0;
+      FGB_TRY(dmalloc(ctx, &F->buf[0], need));
+      FGB_TRY(dmalloc(ctx, &F->buf[1], need));
+      F->buf_bytes = need;
+    }
+  }
+  const void* in = X;
+  int ldin = ldx;
+  for (int k = J - 1; k >= 0; --k) {
+    const DevFactor& f = F->f[k];
+    void* out = (k == 0) ? Y : F->buf[(J - 1 - k) & 1];
+    int ldout = (k == 0) ? ldy : f.rows;
+    if (f.format == FGB_BSR) {
+      FGB_TRY(launch_bsr_spmm(ctx, f, (const __nv_bfloat16*)in, ldin, ncols, (__nv_bfloat16*)out, ldout));
+    } else if (F->dtype == FGB_F64) {
+      FGB_TRY(launch_csr_spmm<double>(ctx, f.rowptr, f.colind, (const double*)f.val, f.rows, f.cols,
+                                      (const double*)in, ldin, ncols, (double*)out, ldout, Epi<double>()));
+    } else {
+      FGB_TRY(launch_csr_spmm<float>(ctx, f.rowptr, f.colind, (const float*)f.val, f.rows, f.cols,
+                                     (const float*)in, ldin, ncols, (float*)out, ldout, Epi<float>()));
+    }
+    in = out;
+    ldin = ldout;
+  }
+  return FGB_OK;
+}
+
+static fgb_status fused_desc(fgb_faust* F) {
+  if (F->chain_desc) return FGB_OK;
+  std::vector<ChainDesc> h(F->f.size());
+  for (size_t i = 0; i < F->f.size(); ++i) h[i] = ChainDesc{F->f[i].rowptr, F->f[i].colind, F->f[i].val,
+                                                            F->f[i].rows, F->f[i].cols};
+  FGB_TRY(dmalloc(F->ctx, &F->chain_desc, sizeof(ChainDesc) * h.size()));
+  FGB_CUDA(F->ctx, cudaMemcpyAsync(F->chain_desc, h.data(), sizeof(ChainDesc) * h.size(), cudaMemcpyHostToDevice,
+                                   F->ctx->stream));
+  return FGB_OK;
+}
+
+static bool all_csr(const fgb_faust* F) {
+  for (auto& f : F->f)
+    if (f.format != FGB_CSR) return false;
+  return true;
+}
+
+static int max_dim(const fgb_faust* F) {
+  int m = 0;
+  for (auto& f : F->f) m = std::max(m, std::max(f.rows, f.cols));
+  return m;
+}
+
+}  // namespace fgb
+
+fgb_faust::~fgb_faust() {
+  for (auto& x : f) fgb::free_factor(x);
+  fgb::dfree(buf[0]);
+  fgb::dfree(buf[1]);
+  fgb::dfree(dx);
+  fgb::dfree(dy);
+  fgb::dfree(chain_desc);
+  if (hx) cudaFreeHost(hx);
+  if (hy) cudaFreeHost(hy);
+}
+
+using namespace fgb;
+
+extern "C" {
+
+fgb_status fgb_faust_create(fgb_ctx* ctx, fgb_dtype dtype, int nfactors, const fgb_factor_desc* factors,
+                            fgb_faust** out) {
+  if (!ctx || !out) return FGB_ERR_INVALID_ARG;
+  *out = nullptr;
+  if (nfactors <= 0 || !factors) return fail(ctx, FGB_ERR_INVALID_ARG, "a Faust needs at least one factor");
+  if (dtype_size(dtype) == 0) return fail(ctx, FGB_ERR_INVALID_ARG, "unknown dtype");
+  for (int i = 0; i < nfactors; ++i) {
+    FGB_TRY(validate_desc(ctx, dtype, factors[i]));
+    if (i > 0 && factors[i - 1].cols != factors[i].rows)
+      return fail(ctx, FGB_ERR_INVALID_ARG, "factor %d has %d rows, factor %d has %d columns", i, factors[i].rows,
+                  i - 1, factors[i - 1].cols);
+  }
+  FGB_CUDA(ctx, cudaSetDevice(ctx->device));
+  fgb_faust* F = new fgb_faust();
+  F->ctx = ctx;
+  F->dtype = dtype;
+  F->f.resize(nfactors);
+  for (int i = 0; i < nfactors; ++i) {
+    fgb_status s = upload_factor(ctx, dtype, factors[i], F->f[i]);
+    if (s != FGB_OK) {
+      delete F;
+      return s;
+    }
+  }
+  cudaError_t e = cudaStreamSynchronize(ctx->stream);
+  if (e != cudaSuccess) {
+    delete F;
+    return cuda_check(ctx, e, "fgb_faust_create");
+  }
+  *out = F;
+  return FGB_OK;
+}
+
+fgb_status fgb_faust_destroy(fgb_faust* F) {
+  if (!F) return FGB_ERR_INVALID_ARG;
+  cudaSetDevice(F->ctx->device);
+  cudaStreamSynchronize(F->ctx->stream);
+  delete F;
+  return FGB_OK;
+}
+
+fgb_status fgb_faust_shape(const fgb_faust* F, int* rows, int* cols, int* nfactors) {
+  if (!F) return FGB_ERR_INVALID_ARG;
+  if (rows) *rows = F->f.front().rows;
+  if (cols) *cols = F->f.back().cols;
+  if (nfactors) *nfactors = (int)F->f.size();
+  return FGB_OK;
+}
+
+fgb_status fgb_faust_mul(fgb_faust* F, const void* X, int ldx, int ncols, void* Y, int ldy, int mode) {
+  if (!F) return FGB_ERR_INVALID_ARG;
+  fgb_ctx* ctx = F->ctx;
+  if (!X || !Y || ncols < 0) return fail(ctx, FGB_ERR_INVALID_ARG, "fgb_faust_mul: null operand");
+  if (ldx < F->f.back().cols || ldy < F->f.front().rows)
+    return fail(ctx, FGB_ERR_INVALID_ARG, "fgb_faust_mul: leading dimension smaller than the row count");
+  if (ncols == 0) return FGB_OK;
+  FGB_CUDA(ctx, cudaSetDevice(ctx->device));
+  const bool csr = all_csr(F);
+  bool fits = false;
+  if (csr && mode != 1) {
+    FGB_TRY(fused_desc(F));
+    chain_fused(ctx, F->dtype, (const ChainDesc*)F->chain_desc, (int)F->f.size(), X, ldx, ncols, Y, ldy, max_dim(F),
+                true, &fits);
+  }
+  if (mode == 2 && !fits)
+    return fail(ctx, FGB_ERR_NOT_SUPPORTED, "fused chain: factors do not fit on chip (or not CSR)");
+  if (fits && (mode == 2 || (mode == 0 && F->f.size() > 1)))
+    return chain_fused(ctx, F->dtype, (const ChainDesc*)F->chain_desc, (int)F->f.size(), X, ldx, ncols, Y, ldy,
+                       max_dim(F), false, nullptr);
+  return mul_per_factor(F, X, ldx, ncols, Y, ldy);
+}
+
+fgb_status fgb_faust_mul_host(fgb_faust* F, const void* X, int ncols, void* Y) {
+  if (!F) return FGB_ERR_INVALID_ARG;
+  fgb_ctx* ctx = F->ctx;
+  if (!X || !Y || ncols < 0) return fail(ctx, FGB_ERR_INVALID_ARG, "fgb_faust_mul_host: null operand");
+  if (ncols == 0) return FGB_OK;
+  FGB_CUDA(ctx, cudaSetDevice(ctx->device));
+  const size_t es = dtype_size(F->dtype);
+  const int rows = F->f.front().rows, inner = F->f.back().cols;
+  const size_t xb = (size_t)inner * ncols * es, yb = (size_t)rows * ncols * es;
+  size_t need = std::max(xb, yb);
+  if (F->dxy_bytes < need) {
+    dfree(F->dx);
+    dfree(F->dy);
+    F->dx = F->dy = nullptr;
+    F->dxy_bytes = 0;
+    FGB_TRY(dmalloc(ctx, &F->dx, need));
+    FGB_TRY(dmalloc(ctx, &F->dy, need));
+    F->dxy_bytes = need;
+  }
+  FGB_CUDA(ctx, cudaMemcpyAsync(F->dx, X, xb, cudaMemcpyHostToDevice, ctx->stream));
+  FGB_TRY(fgb_faust_mul(F, F->dx, inner, ncols, F->dy, rows, 0));
+  FGB_CUDA(ctx, cudaMemcpyAsync(Y, F->dy, yb, cudaMemcpyDeviceToHost, ctx->stream));
+  FGB_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  return FGB_OK;
+}
+
+fgb_status fgb_faust_spectral_norm(fgb_faust* F, int max_iter, double threshold, double* norm, int* flag) {
+  if (!F || !norm) return FGB_ERR_INVALID_ARG;
+  fgb_ctx* ctx = F->ctx;
+  if (!all_csr(F)) return fail(ctx, FGB_ERR_NOT_SUPPORTED, "spectral norm: CSR Fausts only");
+  if (F->dtype != FGB_F64 && F->dtype != FGB_F32) return fail(ctx, FGB_ERR_NOT_SUPPORTED, "spectral norm: F32/F64");
+  if (max_iter <= 0) return fail(ctx, FGB_ERR_INVALID_ARG, "power_iteration :  nbr_iter_max <= 0");
+  FGB_CUDA(ctx, cudaSetDevice(ctx->device));
+  for (auto& f : F->f)
+    if (!f.has_t) FGB_TRY(csr_build_transpose(ctx, F->dtype, f));
+  double out = 0;
+  int fl = 0;
+  FGB_TRY(chain_spectral_norm_sync(ctx, F->dtype, F->f.data(), 0, (int)F->f.size(), max_iter, threshold, &out, &fl));
+  *norm = out;
+  if (flag) *flag = fl;
+  return FGB_OK;
+}
+
+fgb_status fgb_faust_factor_info(const fgb_faust* F, int i, int* format, int* rows, int* cols, int* nnz) {
+  if (!F || i < 0 || i >= (int)F->f.size()) return FGB_ERR_INVALID_ARG;
+  const DevFactor& f = F->f[i];
+  if (format) *format = f.format;
+  if (rows) *rows = f.rows;
+  if (cols) *cols = f.cols;
+  if (nnz) *nnz = f.nnz;
+  return FGB_OK;
+}
+
+fgb_status fgb_faust_factor_to_csr(fgb_faust* F, int i, int* host_rowptr, int* host_colind, void* host_values) {
+  if (!F || i < 0 || i >= (int)F->f.size()) return FGB_ERR_INVALID_ARG;
+  fgb_ctx* ctx = F->ctx;
+  const DevFactor& f = F->f[i];
+  if (f.format != FGB_CSR) return fail(ctx, FGB_ERR_NOT_SUPPORTED, "factor is not CSR");
+  FGB_CUDA(ctx, cudaSetDevice(ctx->device));
+  FGB_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  FGB_CUDA(ctx, cudaMemcpy(host_rowptr, f.rowptr, sizeof(int) * (f.rows + 1), cudaMemcpyDeviceToHost));
+  if (f.nnz) {
+    FGB_CUDA(ctx, cudaMemcpy(host_colind, f.colind, sizeof(int) * f.nnz, cudaMemcpyDeviceToHost));
+    FGB_CUDA(ctx, cudaMemcpy(host_values, f.val, dtype_size(F->dtype) * f.nnz, cudaMemcpyDeviceToHost));
+  }
+  return FGB_OK;
+}
+
+fgb_status fgb_faust_factor_to_dense(fgb_faust* F, int i, void* host_dense) {
+  if (!F || i < 0 || i >= (int)F->f.size() || !host_dense) return FGB_ERR_INVALID_ARG;
+  fgb_ctx* ctx = F->ctx;
+  const DevFactor& f = F->f[i];
+  if (f.format != FGB_CSR) return fail(ctx, FGB_ERR_NOT_SUPPORTED, "factor is not CSR");
+  std::vector<int> rp(f.rows + 1), ci(std::max(1, f.nnz));
+  const size_t es = dtype_size(F->dtype);
+  std::vector<unsigned char> v(es * std::max(1, f.nnz));
+  FGB_TRY(fgb_faust_factor_to_csr(F, i, rp.data(), ci.data(), v.data()));
+  std::memset(host_dense, 0, es * (size_t)f.rows * f.cols);
+  for (int r = 0; r < f.rows; ++r)
+    for (int p = rp[r]; p < rp[r + 1]; ++p)
+      std::memcpy((unsigned char*)host_dense + es * ((size_t)ci[p] * f.rows + r), v.data() + es * p, es);
+  return FGB_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,169 @@
+// fgb_internal.cuh — shared internals of libfaust_gb300 (context, device
+// factors, error plumbing, canonical reduction order).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cuda_bf16.h>
+
+#include <atomic>
+#include <cstdint>
+#include <cstdio>
+#include <string>
+#include <vector>
+
+#include "../../include/fgb.h"
+
+// Number of SMs on GB300; grids of the streaming kernels are sized in
+// multiples of it (the runtime value is read once per context).
+#define FGB_SM_COUNT_HINT 152
+
+// ---------------------------------------------------------------- context
+struct fgb_ctx {
+  int device = 0;
+  int sm_count = FGB_SM_COUNT_HINT;
+  size_t smem_optin = 0;  // cudaDevAttrMaxSharedMemoryPerBlockOptin
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  std::string err;
+  std::atomic<long long> launches{0};
+  // Host-mapped cancel flag polled by the PALM driver between iterations.
+  volatile int* cancel_host = nullptr;
+  int* cancel_dev = nullptr;
+  // glibc rand() sequence after srand(418) (power-iteration start vector),
+  // cached on the device.
+  int* rand_dev = nullptr;
+  int rand_n = 0;
+};
+
+namespace fgb {
+
+// Records a message on the context and returns the status.
+fgb_status fail(fgb_ctx* ctx, fgb_status st, const char* fmt, ...);
+// Converts a CUDA error into FGB_ERR_CUDA with a message (or OK).
+fgb_status cuda_check(fgb_ctx* ctx, cudaError_t e, const char* what);
+
+#define FGB_CUDA(ctx, call)                                      \
+  do {                                                           \
+    cudaError_t e__ = (call);                                    \
+    if (e__ != cudaSuccess) return fgb::cuda_check(ctx, e__, #call); \
+  } while (0)
+
+#define FGB_TRY(call)                  \
+  do {                                 \
+    fgb_status s__ = (call);           \
+    if (s__ != FGB_OK) return s__;     \
+  } while (0)
+
+// Counts a kernel launch and checks the launch error.
+#define FGB_LAUNCHED(ctx)                                               \
+  do {                                                                  \
+    (ctx)->launches.fetch_add(1, std::memory_order_relaxed);            \
+    cudaError_t e__ = cudaGetLastError();                               \
+    if (e__ != cudaSuccess) return fgb::cuda_check(ctx, e__, "kernel launch"); \
+  } while (0)
+
+size_t dtype_size(fgb_dtype t);
+
+// Device allocation helpers (report OOM as FGB_ERR_OOM).
+fgb_status dmalloc(fgb_ctx* ctx, void** p, size_t bytes);
+void dfree(void* p);
+
+// ---------------------------------------------------------------- device factors
+// A sparse factor resident on the device.  CSR keeps, beside its own arrays,
+// the CSR of its transpose (built on the device) for S^H X and X S products.
+struct DevFactor {
+  int format = FGB_CSR;
+  int rows = 0, cols = 0;
+  int nnz = 0;    // CSR nonzeros / BSR blocks
+  int cap = 0;    // capacity of colind/val (entries)
+  int bm = 0, bn = 0;
+  int* rowptr = nullptr;
+  int* colind = nullptr;
+  void* val = nullptr;
+  // Transpose (CSR only): rows = cols of the factor.
+  int* t_rowptr = nullptr;
+  int* t_colind = nullptr;
+  void* t_val = nullptr;
+  bool has_t = false;
+};
+
+}  // namespace fgb
+
+struct fgb_faust {
+  fgb_ctx* ctx = nullptr;
+  fgb_dtype dtype = FGB_F64;
+  std::vector<fgb::DevFactor> f;
+  // Ping-pong buffers for one-launch-per-factor products, grown on demand.
+  void* buf[2] = {nullptr, nullptr};
+  size_t buf_bytes = 0;
+  // Pinned staging buffers for the host-memory entry point.
+  void* hx = nullptr;
+  void* hy = nullptr;
+  size_t hx_bytes = 0, hy_bytes = 0;
+  void* dx = nullptr;
+  void* dy = nullptr;
+  size_t dxy_bytes = 0;
+  // Device descriptor array for the fused chain kernel.
+  void* chain_desc = nullptr;
+  ~fgb_faust();
+};
+
+namespace fgb {
+
+// ---------------------------------------------------------------- canonical order
+// Reductions over N values in column-major linear order: 256 lanes per chunk
+// of 65536 values, lane t accumulating chunk offsets = t (mod 256) in order,
+// a pairwise tree over the lanes, chunk partials added in order.  The oracle
+// (oracle/faust_oracle.cpp) restates the same order, so results agree bit for
+// bit.
+constexpr int CR_LANES = 256;
+constexpr long CR_CHUNK = 65536;
+
+__device__ __forceinline__ float fmad(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+__device__ __forceinline__ double fmad(double a, double b, double c) { return __fma_rn(a, b, c); }
+__device__ __forceinline__ float addr(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ double addr(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ float subr(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ double subr(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ float mulr(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ double mulr(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ float divr(float a, float b) { return __fdiv_rn(a, b); }
+__device__ __forceinline__ double divr(double a, double b) { return __ddiv_rn(a, b); }
+__device__ __forceinline__ float sqrtr(float a) { return __fsqrt_rn(a); }
+__device__ __forceinline__ double sqrtr(double a) { return __dsqrt_rn(a); }
+
+// Tree over 256 lane partials held in shared memory `lane` (256 threads call).
+template <typename T>
+__device__ __forceinline__ T lane_tree_256(T* lane) {
+  const int t = threadIdx.x;
+#pragma unroll
+  for (int s = CR_LANES / 2; s >= 1; s >>= 1) {
+    __syncthreads();
+    if (t < s) lane[t] = addr(lane[t], lane[t + s]);
+  }
+  __syncthreads();
+  T r = lane[0];
+  __syncthreads();
+  return r;
+}
+
+// Canonical dot product of a[0..n) and b[0..n) by one block of exactly 256
+// threads; every thread receives the result.
+template <typename T>
+__device__ T block_cdot(const T* a, const T* b, long n, T* lane) {
+  T total = T(0);
+  for (long c0 = 0; c0 < n; c0 += CR_CHUNK) {
+    long c1 = c0 + CR_CHUNK < n ? c0 + CR_CHUNK : n;
+    T acc = T(0);
+    for (long i = c0 + threadIdx.x; i < c1; i += CR_LANES) acc = fmad(a[i], b[i], acc);
+    lane[threadIdx.x] = acc;
+    T part = lane_tree_256(lane);
+    total = addr(total, part);
+  }
+  return total;
+}
+
+// Kernel helpers defined in the .cu files.
+fgb_status csr_build_transpose(fgb_ctx* ctx, fgb_dtype dt, DevFactor& f);
+
+}  // namespace fgb

@@ -1,0 +1,243 @@
+// power.cu — power iteration for spectral norms of CSR chains, one block per
+// chain, vectors in shared memory, the whole loop on the device (no host
+// round trip per iteration), with palm4msa2's step-size epilogue.
+#include <cmath>
+#include <cstdlib>
+#include <cstring>
+#include <vector>
+
+#include "power.cuh"
+
+namespace fgb {
+
+void pi_chain_build(const DevFactor* F, int lo, int hi, PIChain& ch) {
+  std::memset(&ch, 0, sizeof(ch));
+  if (hi <= lo) {
+    ch.empty = 1;
+    return;
+  }
+  for (int i = lo; i < hi; ++i)
+    if (F[i].nnz == 0) ch.zero = 1;
+  const int rows = F[lo].rows, cols = F[hi - 1].cols;
+  auto fwd = [&](int i) { return PIOp{F[i].rowptr, F[i].colind, F[i].val, F[i].rows, 0}; };
+  auto adj = [&](int i) { return PIOp{F[i].t_rowptr, F[i].t_colind, F[i].t_val, F[i].cols, 0}; };
+  if (cols < rows) {
+    // F^H F: x -> F^H (F x); F x applies F[hi-1] first.
+    ch.n = cols;
+    for (int i = hi - 1; i >= lo; --i) ch.ops[ch.nops++] = fwd(i);
+    for (int i = lo; i < hi; ++i) ch.ops[ch.nops++] = adj(i);
+  } else {
+    // F F^H: x -> F (F^H x); F^H x applies F[lo]^H first.
+    ch.n = rows;
+    for (int i = lo; i < hi; ++i) ch.ops[ch.nops++] = adj(i);
+    for (int i = hi - 1; i >= lo; --i) ch.ops[ch.nops++] = fwd(i);
+  }
+}
+
+template <typename T>
+__device__ __forceinline__ T absd(T x) {
+  return x < T(0) ? -x : x;
+}
+
+// Faust::power_iteration on the chain operator: start vector from
+// srand(418)/rand() mapped to [-1,1] (Eigen Random), loop while
+// |l_old - l| > thr or |l| <= thr (at most max_iter), normalise by 1/||x||,
+// x = A x, stop with 0 on a zero vector, l = <x_norm, x>.  Result:
+// |sqrt(l)| (Transform::spectralNorm).
+template <typename TF, typename TC>
+__global__ void __launch_bounds__(PI_THREADS)
+    k_power_iteration(const __grid_constant__ PIChain ca, const __grid_constant__ PIChain cb, int max_iter, TC thr,
+                      const int* __restrict__ rnd, PIOut* out, const __grid_constant__ PIPalm palm, int maxn) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  TC* buf0 = reinterpret_cast<TC*>(smem_raw);
+  TC* buf1 = buf0 + maxn;
+  TC* buf2 = buf1 + maxn;
+  TC* lane = buf2 + maxn;
+  const PIChain& ch = (blockIdx.x == 0) ? ca : cb;
+  double result = 1.0;
+  int flag = 0;
+  int st = 0;
+  if (ch.empty) {
+    result = 1.0;
+  } else if (ch.zero) {
+    result = 0.0;
+  } else {
+    const int n = ch.n;
+    TC* bufs[3] = {buf0, buf1, buf2};
+    int xi = 0;
+    for (int i = threadIdx.x; i < n; i += blockDim.x)
+      bufs[0][i] = addr(TC(-1), divr(mulr(TC(2), (TC)rnd[i]), (TC)RAND_MAX));
+    __syncthreads();
+    TC lam_old = TC(1), lam = TC(0);
+    int it = 0;
+    bool zero_vec = false;
+    const TC athr = absd(thr);
+    while ((absd(subr(lam_old, lam)) > athr || absd(lam) <= athr) && it < max_iter) {
+      ++it;
+      lam_old = lam;
+      TC* x = bufs[xi];
+      const TC nrm = sqrtr(block_cdot<TC>(x, x, n, lane));
+      if (nrm == TC(0)) {
+        st = FGB_ERR_ZERO_NORM;
+        break;
+      }
+      const TC inv = divr(TC(1), nrm);
+      for (int i = threadIdx.x; i < n; i += blockDim.x) x[i] = mulr(x[i], inv);
+      __syncthreads();
+      // products ping-pong between the two buffers other than x, which keeps
+      // the normalised vector for the dot product
+      int si = xi, di = (xi + 1) % 3;
+      for (int o = 0; o < ch.nops; ++o) {
+        const PIOp op = ch.ops[o];
+        const TF* __restrict__ val = reinterpret_cast<const TF*>(op.val);
+        const TC* src = bufs[si];
+        TC* dst = bufs[di];
+        for (int r = threadIdx.x; r < op.rows; r += blockDim.x) {
+          TC acc = TC(0);
+          const int p1 = op.rowptr[r + 1];
+          for (int p = op.rowptr[r]; p < p1; ++p) acc = fmad((TC)val[p], src[op.colind[p]], acc);
+          dst[r] = acc;
+        }
+        __syncthreads();
+        si = di;
+        di = 3 - xi - si;
+      }
+      const TC* res = bufs[si];
+      int nz = 0;
+      for (int i = threadIdx.x; i < n; i += blockDim.x) nz |= (res[i] != TC(0));
+      if (!__syncthreads_or(nz)) {
+        zero_vec = true;
+        break;
+      }
+      lam = block_cdot<TC>(x, res, n, lane);
+      xi = si;
+    }
+    if (st == 0) {
+      if (zero_vec) {
+        result = 0.0;
+        flag = 0;
+      } else {
+        flag = (it < max_iter) ? it : -1;
+        result = (double)absd(sqrtr(lam));
+      }
+    }
+  }
+  if (threadIdx.x == 0) {
+    out->norm[blockIdx.x] = result;
+    out->flag[blockIdx.x] = flag;
+    if (st) atomicCAS(&out->status, 0, st);
+    __threadfence();
+    const unsigned prev = atomicAdd(&out->done, 1u);
+    if (prev == gridDim.x - 1) {
+      __threadfence();
+      out->done = 0;
+      if (palm.enabled) {
+        TF* c = reinterpret_cast<TF*>(palm.c);
+        TF* alpha = reinterpret_cast<TF*>(palm.alpha);
+        const TF lamv = *reinterpret_cast<const TF*>(palm.lambda);
+        TF cv;
+        if (palm.constant_step) {
+          cv = divr(TF(1), (TF)palm.step_size);
+        } else {
+          const double nR = out->norm[0], nL = out->norm[1];
+          if (isnan(nR) || isnan(nL)) atomicCAS(&out->status, 0, (int)FGB_ERR_NAN);
+          if ((nR == 0.0 && (palm.it > 0 || !palm.r2l)) || (nL == 0.0 && (palm.it > 0 || palm.r2l)))
+            atomicCAS(&out->status, 0, (int)FGB_ERR_ZERO_NORM);
+          const double tnR = (double)(TF)nR, tnL = (double)(TF)nL, l = (double)lamv;
+          double cc = __dmul_rn(1.001, l);
+          cc = __dmul_rn(cc, l);
+          cc = __dmul_rn(cc, tnR);
+          cc = __dmul_rn(cc, tnR);
+          cc = __dmul_rn(cc, tnL);
+          cc = __dmul_rn(cc, tnL);
+          cv = (TF)cc;
+        }
+        *c = cv;
+        *alpha = divr(lamv, cv);
+      }
+    }
+  }
+}
+
+fgb_status pi_rand_device(fgb_ctx* ctx, int n, const int** d_rand) {
+  if (ctx->rand_n < n) {
+    // glibc rand() after srand(418) = random()'s TYPE_3 generator with a
+    // 128-byte state, reproduced with initstate_r/random_r so the caller's
+    // global generator is left alone.
+    std::vector<int> h(n);
+    static thread_local char state[128];
+    struct random_data rd;
+    std::memset(&rd, 0, sizeof(rd));
+    std::memset(state, 0, sizeof(state));
+    initstate_r(418u, state, sizeof(state), &rd);
+    for (int i = 0; i < n; ++i) {
+      int32_t r;
+      random_r(&rd, &r);
+      h[i] = r;
+    }
+    if (ctx->rand_dev) cudaFree(ctx->rand_dev);
+    ctx->rand_dev = nullptr;
+    ctx->rand_n = 0;
+    FGB_TRY(dmalloc(ctx, (void**)&ctx->rand_dev, sizeof(int) * n));
+    FGB_CUDA(ctx, cudaMemcpy(ctx->rand_dev, h.data(), sizeof(int) * n, cudaMemcpyHostToDevice));
+    ctx->rand_n = n;
+  }
+  *d_rand = ctx->rand_dev;
+  return FGB_OK;
+}
+
+template <typename TF, typename TC>
+static fgb_status launch_pi_t(fgb_ctx* ctx, const PIChain& a, const PIChain& b, int max_iter, double thr,
+                              const int* d_rand, PIOut* d_out, const PIPalm& palm) {
+  const int maxn = std::max(a.n, b.n) > 0 ? std::max(a.n, b.n) : 1;
+  const size_t smem = (3 * (size_t)maxn + PI_THREADS) * sizeof(TC);
+  if (smem > ctx->smem_optin)
+    return fail(ctx, FGB_ERR_NOT_SUPPORTED, "power iteration: vector of %d entries does not fit on chip", maxn);
+  auto kern = k_power_iteration<TF, TC>;
+  if (smem > 48 * 1024) FGB_CUDA(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  kern<<<2, PI_THREADS, smem, ctx->stream>>>(a, b, max_iter, (TC)thr, d_rand, d_out, palm, maxn);
+  FGB_LAUNCHED(ctx);
+  return FGB_OK;
+}
+
+fgb_status launch_power_iteration(fgb_ctx* ctx, fgb_dtype tf, bool fp64, const PIChain& a, const PIChain& b,
+                                  int max_iter, double thr, const int* d_rand, PIOut* d_out, const PIPalm& palm) {
+  if (a.nops > PI_MAX_OPS || b.nops > PI_MAX_OPS) return fail(ctx, FGB_ERR_NOT_SUPPORTED, "power iteration: chain too long");
+  if (tf == FGB_F64) return launch_pi_t<double, double>(ctx, a, b, max_iter, thr, d_rand, d_out, palm);
+  if (tf == FGB_F32) {
+    if (fp64) return launch_pi_t<float, double>(ctx, a, b, max_iter, thr, d_rand, d_out, palm);
+    return launch_pi_t<float, float>(ctx, a, b, max_iter, thr, d_rand, d_out, palm);
+  }
+  return fail(ctx, FGB_ERR_NOT_SUPPORTED, "power iteration: F32 or F64 factors");
+}
+
+fgb_status chain_spectral_norm_sync(fgb_ctx* ctx, fgb_dtype dt, const DevFactor* F, int lo, int hi, int max_iter,
+                                    double thr, double* norm, int* flag) {
+  PIChain a, b;
+  pi_chain_build(F, lo, hi, a);
+  std::memset(&b, 0, sizeof(b));
+  b.empty = 1;
+  const int* rnd = nullptr;
+  FGB_TRY(pi_rand_device(ctx, std::max(1, a.n), &rnd));
+  PIOut* d_out = nullptr;
+  FGB_TRY(dmalloc(ctx, (void**)&d_out, sizeof(PIOut)));
+  FGB_CUDA(ctx, cudaMemsetAsync(d_out, 0, sizeof(PIOut), ctx->stream));
+  PIPalm palm;
+  std::memset(&palm, 0, sizeof(palm));
+  fgb_status s = launch_power_iteration(ctx, dt, true, a, b, max_iter, thr, rnd, d_out, palm);
+  PIOut h;
+  std::memset(&h, 0, sizeof(h));
+  if (s == FGB_OK) {
+    cudaError_t e = cudaMemcpyAsync(&h, d_out, sizeof(PIOut), cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) s = cuda_check(ctx, e, "spectral norm");
+  }
+  dfree(d_out);
+  if (s != FGB_OK) return s;
+  if (h.status) return fail(ctx, (fgb_status)h.status, "Can't normalize a zero-norm vector.");
+  *norm = h.norm[0];
+  *flag = h.flag[0];
+  return FGB_OK;
+}
+
+}  // namespace fgb

@@ -1,0 +1,199 @@
+/* fgb.h — C ABI of faust_gb300: FAuST's Faust x dense product and palm4msa2
+ * factor update on one GB300 (sm_103a).
+ *
+ * This ABI plays the role that libgm.so (the gpu_mod backend) plays for the
+ * reference: FAuST's GPU2 layer dlopen()s a C library and calls plain
+ * functions on opaque handles (src/faust_linear_operator/GPU2/
+ * faust_gpu_mod_utils.h:24-97, faust_gpu_mod_utils.cpp:26-92).  Each entry
+ * point below names the reference interface it replaces.
+ *
+ * Conventions
+ *  - Dense matrices are column-major with a leading dimension (Eigen default,
+ *    src/faust_linear_operator/CPU/faust_MatDense.h:142).
+ *  - CSR factors: int32 rowptr (rows+1), int32 colind sorted inside each row,
+ *    values (src/faust_linear_operator/CPU/faust_MatSparse.h:456-462).
+ *  - BSR factors: int32 browptr (rows/bm+1), int32 bcolind, blocks of bm x bn
+ *    stored column-major one after another (faust_MatBSR.h:122-145).
+ *  - Every call returns an fgb_status; no C++ exception crosses the ABI.  The
+ *    message of the last failure of a context is fgb_last_error(ctx).  The
+ *    reference raises std::logic_error / std::runtime_error /
+ *    std::domain_error for the same conditions (faust_exception.h:64-67).
+ *  - Calls on one context are not thread-safe; use one context per host thread
+ *    (as GPUModHandler, faust_gpu_mod_utils.cpp:26-92).
+ *  - Work is queued on the context's stream; *_host entry points and the
+ *    PALM drivers synchronise before returning.
+ */
+#ifndef FGB_H
+#define FGB_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Exported even when the library is compiled with -fvisibility=hidden. */
+#if defined(__GNUC__)
+#pragma GCC visibility push(default)
+#endif
+
+typedef enum fgb_status {
+  FGB_OK = 0,
+  FGB_ERR_INVALID_ARG = 1,
+  FGB_ERR_OOM = 2,
+  FGB_ERR_CUDA = 3,
+  FGB_ERR_NAN = 4,       /* NaN in a norm or in lambda (faust_palm4msa2020.hpp:593-597,482-490) */
+  FGB_ERR_ZERO_NORM = 5, /* zero norm (faust_palm4msa2020.hpp:598-610, faust_MatDense.hpp:1246-1249) */
+  FGB_ERR_CANCELLED = 6, /* fgb_cancel() was called (the reference's SIGINT flag, faust_palm4msa2020.cpp:9-28) */
+  FGB_ERR_TIMEOUT = 7,   /* a bounded device-side wait ran out */
+  FGB_ERR_NOT_SUPPORTED = 8
+} fgb_status;
+
+typedef enum fgb_dtype { FGB_F32 = 0, FGB_F64 = 1, FGB_BF16 = 2 } fgb_dtype;
+
+typedef enum fgb_format { FGB_CSR = 0, FGB_BSR = 1 } fgb_format;
+
+typedef struct fgb_ctx fgb_ctx;
+typedef struct fgb_faust fgb_faust;
+
+/* ------------------------------------------------------------------ context
+ * Replaces gp_funcs->set_dev / set_stream (faust_gpu_mod_utils.h:100-102). */
+fgb_status fgb_ctx_create(int device, void* cuda_stream, fgb_ctx** out);
+fgb_status fgb_ctx_destroy(fgb_ctx* ctx);
+const char* fgb_last_error(const fgb_ctx* ctx);
+fgb_status fgb_ctx_synchronize(fgb_ctx* ctx);
+/* Asks a running palm4msa2 call of this context to stop at the next outer
+ * iteration (the reference's palm4msa2 SIGINT flag,
+ * faust_palm4msa2020.hpp:239-242).  Safe to call from another thread. */
+fgb_status fgb_cancel(fgb_ctx* ctx);
+/* Number of kernels this context launched since creation (diagnostics). */
+long long fgb_ctx_kernel_launches(const fgb_ctx* ctx);
+
+/* ------------------------------------------------------------------ Faust */
+typedef struct fgb_factor_desc {
+  int format;         /* fgb_format */
+  int rows, cols;
+  int nnz;            /* CSR: nonzeros; BSR: nonzero blocks */
+  int bm, bn;         /* BSR block size (ignored for CSR) */
+  const int* rowptr;  /* CSR rowptr[rows+1] / BSR browptr[rows/bm+1] */
+  const int* colind;  /* CSR colind[nnz] / BSR bcolind[nnz] */
+  const void* values; /* CSR values[nnz] / BSR blocks[nnz*bm*bn] */
+} fgb_factor_desc;
+
+/* Builds a device-resident Faust from factors held in HOST memory (copied).
+ * Replaces TransformHelper<FPP,GPU2>(const TransformHelper<FPP,Cpu>&) /
+ * MatSparse<FPP,GPU2>(const MatSparse<FPP,Cpu>&) -> spm_funcs->togpu
+ * (src/faust_linear_operator/GPU2/faust_MatSparse_gpu.cpp.in). */
+fgb_status fgb_faust_create(fgb_ctx* ctx, fgb_dtype dtype, int nfactors, const fgb_factor_desc* factors,
+                            fgb_faust** out);
+fgb_status fgb_faust_destroy(fgb_faust* F);
+fgb_status fgb_faust_shape(const fgb_faust* F, int* rows, int* cols, int* nfactors);
+
+/* Y = F X with X, Y in DEVICE memory (column-major), queued on the context
+ * stream.  Factors are applied right to left as Transform<FPP,GPU2>::multiply
+ * (faust_Transform_gpu.hpp:505-522) / Transform<FPP,Cpu>::multiply
+ * (CPU/faust_Transform.hpp:1814-1855); replaces spm_funcs->mul_gpu_dsm_ext
+ * (faust_MatSparse_gpu.cpp.in:462-471) and bsr_funcs->mul_gpu_dsm_ext
+ * (faust_MatBSR_gpu.cpp.in:108-140).  X and Y must not overlap.  BF16 Fausts
+ * take BF16 X and produce BF16 Y with FP32 accumulation.
+ * mode: 0 = automatic, 1 = one launch per factor, 2 = fused chain (fails
+ * with FGB_ERR_NOT_SUPPORTED when the chain does not fit on chip). */
+fgb_status fgb_faust_mul(fgb_faust* F, const void* X, int ldx, int ncols, void* Y, int ldy, int mode);
+
+/* Y = F X with X, Y in HOST memory: copy in, product, copy out, synchronous.
+ * Replaces TransformHelper<FPP,Cpu>::multiply(const FPP* A, int A_ncols,
+ * FPP* C) (CPU/faust_TransformHelper.hpp:406-433) and
+ * TransformHelper<FPP,GPU2>::multiply(const MatDense<FPP,Cpu>&)
+ * (GPU2/faust_TransformHelper_gpu.hpp:439-444). */
+fgb_status fgb_faust_mul_host(fgb_faust* F, const void* X, int ncols, void* Y);
+
+/* 2-norm by power iteration in FP64, TransformHelper::spectralNorm
+ * (CPU/faust_TransformHelper.hpp:1200-1218, CPU/faust_Transform.hpp:683-708,
+ * faust_linear_algebra.hpp:806-899).  flag = iterations, or -1 when max_iter
+ * was reached.  CSR Fausts only. */
+fgb_status fgb_faust_spectral_norm(fgb_faust* F, int max_iter, double threshold, double* norm, int* flag);
+
+/* Factor i copied to host: dense column-major (rows*cols values) or CSR
+ * arrays (rowptr[rows+1], colind[nnz], values[nnz]; query nnz first). */
+fgb_status fgb_faust_factor_info(const fgb_faust* F, int i, int* format, int* rows, int* cols, int* nnz);
+fgb_status fgb_faust_factor_to_dense(fgb_faust* F, int i, void* host_dense);
+fgb_status fgb_faust_factor_to_csr(fgb_faust* F, int i, int* host_rowptr, int* host_colind, void* host_values);
+
+/* ------------------------------------------------------------------ projections
+ * Constraint kinds: ConstraintName (faust_ConstraintGeneric.h:49-70). */
+typedef enum fgb_cons_kind {
+  FGB_SP = 0,       /* prox_sp        faust_prox.hpp:71-96   */
+  FGB_SPCOL = 1,    /* prox_spcol     faust_prox.hpp:112-143 */
+  FGB_SPLIN = 2,    /* prox_splin     faust_prox.hpp:145-177 */
+  FGB_SPLINCOL = 3, /* prox_splincol  faust_prox.hpp:179-202 */
+  FGB_NORMCOL = 4,  /* prox_normcol   faust_prox.hpp:204-246 */
+  FGB_NORMLIN = 5,  /* prox_normlin   faust_prox.hpp:248-254 */
+  FGB_SUPP = 6,     /* prox_supp      faust_prox.hpp:375-385 */
+  FGB_SP_POS = 7    /* prox_sp with pos=true */
+} fgb_cons_kind;
+
+typedef struct fgb_constraint {
+  int kind;           /* fgb_cons_kind */
+  int rows, cols;     /* shape of the constrained factor */
+  long long k;        /* sparsity level (SP, SPCOL, SPLIN, SPLINCOL, SP_POS) */
+  double s;           /* norm value (NORMCOL, NORMLIN) */
+  int normalized;     /* ConstraintGeneric normalizing flag */
+  int pos;            /* ConstraintGeneric pos flag */
+  const void* supp;   /* SUPP: rows*cols column-major support (HOST memory), same dtype */
+} fgb_constraint;
+
+/* In-place projection of the dense DEVICE matrix M (rows x cols,
+ * column-major, ld = rows), ConstraintGeneric::project
+ * (faust_ConstraintGeneric.hpp:229-246).  Replaces dsm_funcs->prox_sp /
+ * prox_spcol / prox_splin (faust_MatDense_gpu.cpp.in:746-763) and the CPU
+ * round trips of GPU2/faust_prox_gpu.hpp:102-149.  Supports are chosen as
+ * std::partial_sort with comparator |a| > |b| chooses them
+ * (faust_prox.hpp:52-69), ties included.  F32 and F64. */
+fgb_status fgb_prox(fgb_ctx* ctx, fgb_dtype dtype, const fgb_constraint* cons, void* M);
+
+/* ------------------------------------------------------------------ PALM4MSA */
+typedef struct fgb_palm_params {
+  int nb_it;                 /* StoppingCriterion num_its (faust_StoppingCriterion.hpp:112-154) */
+  int is_update_way_R2L;     /* default 0 */
+  int packing_RL;            /* default 1 */
+  int no_normalization;      /* default 0 */
+  int no_lambda;             /* default 0 */
+  double norm2_threshold;    /* default 1e-6 */
+  int norm2_max_iter;        /* default 100 */
+  int constant_step_size;    /* default 0 */
+  double step_size;          /* default 1e-16 (pyfaust ParamsPalm4MSA) */
+  int no_lambda_error;       /* the reference's NO_LAMBDA_ERROR environment switch */
+  int norm2_fp64;            /* F32 runs: spectral norms in FP64 */
+} fgb_palm_params;
+
+fgb_status fgb_palm_params_default(fgb_palm_params* p);
+
+/* palm4msa2 (src/algorithm/factorization/faust_palm4msa2020.h:45-72,
+ * .hpp:46-301) with factors_format = AllDynamic and no MHTP, on the GPU.
+ * A: rows x cols column-major in HOST memory.  init_facts: NULL (zero/eye
+ * initialisation of :115-149) or an array of nfacts host pointers to dense
+ * column-major factors.  lambda: in = initial lambda, out = final lambda.
+ * out: the resulting Faust (device resident), to be released with
+ * fgb_faust_destroy.  F32 and F64. */
+fgb_status fgb_palm4msa2(fgb_ctx* ctx, fgb_dtype dtype, const void* A, int rows, int cols, int nfacts,
+                         const fgb_constraint* cons, const fgb_palm_params* params, const void* const* init_facts,
+                         double* lambda, fgb_faust** out);
+
+/* Same with A already in DEVICE memory (column-major, ld = rows). */
+fgb_status fgb_palm4msa2_device(fgb_ctx* ctx, fgb_dtype dtype, const void* A_dev, int rows, int cols, int nfacts,
+                                const fgb_constraint* cons, const fgb_palm_params* params,
+                                const void* const* init_facts, double* lambda, fgb_faust** out);
+
+/* calc_rel_err (faust_palm4msa2020.hpp:35-44): ||lambda F - A||_F / ||A||_F
+ * with A in DEVICE memory. */
+fgb_status fgb_rel_err(fgb_faust* F, const void* A_dev, double lambda, double* out);
+
+#if defined(__GNUC__)
+#pragma GCC visibility pop
+#endif
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* FGB_H */

@@ -1,0 +1,1057 @@
+// faust_oracle.cpp — TEST INFRASTRUCTURE ONLY.
+//
+// CPU restatement of the two FAuST (macnetic/faust) hot paths that faust_gb300
+// rebuilds on GB300, used solely as the checker by tests/, by
+// __graft_entry__.smoke() and by bench.py's cpu_baseline / reference legs.
+// Nothing in the product library links, loads or calls this file.
+//
+//  * Faust x dense (right-to-left chain of CSR / BSR factors):
+//      src/faust_linear_operator/CPU/faust_Transform.hpp:1713-1855
+//      src/faust_linear_operator/CPU/faust_MatSparse.hpp:219-264
+//      src/faust_linear_operator/CPU/faust_MatBSR.hpp:827-836
+//  * palm4msa2 (L2R and R2L sweeps, AllDynamic factors):
+//      src/algorithm/factorization/faust_palm4msa2020.hpp:1-676
+//      src/faust_linear_operator/CPU/faust_linear_algebra.hpp:806-899 (power iteration)
+//      src/faust_linear_operator/CPU/faust_Transform.hpp:683-708 (spectralNorm)
+//      src/faust_linear_operator/CPU/faust_prox.hpp:52-385 (projections)
+//      src/algorithm/constraint/faust_prox_gen.hpp:117-208 (sparse/dense output rule)
+//
+// Parity status.  The reference cannot be compiled here (Eigen 3.4 is absent),
+// so no reference-produced numbers exist: floating-point parity is UNPINNED
+// against the reference's own outputs.  What is pinned:
+//   - the top-k support rule: this file calls libstdc++ std::partial_sort with
+//     the reference comparator |a| > |b| (faust_prox.hpp:52-69), so its tie
+//     behaviour is the reference's by construction;
+//   - the algorithm's step order, scalars and error rules, cited per function.
+//
+// Floating-point operation order.  Eigen's summation order cannot be restated
+// without Eigen, so this restatement fixes one explicit order and the CUDA
+// kernels follow the same order, giving bit-identical FP64/FP32 results:
+//   * every product entry  y = sum_p a_p * x_p  is a sequential fused
+//     multiply-add over the sparse operand's entries in stored order
+//     (rows sorted by column; transposed products walk the transpose's CSR,
+//     i.e. in increasing original row), starting from +0;
+//   * every reduction (sum of squares, dot product) over N values in
+//     column-major linear order uses 256 lanes inside chunks of 65536 values:
+//     lane t accumulates (by fma) the values whose chunk offset is = t mod 256,
+//     in increasing order; lanes are combined by the pairwise tree
+//     t += t+128, t += t+64, ..., t += t+1; chunk partials are added in order;
+//   * element-wise updates are single rounded operations: e = (lambda*p) - a,
+//     d = d - (alpha*g);  normalisation multiplies by (1/norm).
+// Products are associated as a sparse chain (each factor applied to a dense
+// block in turn) instead of the reference's dense packed GEMMs; the maths is
+// the same and differs from an Eigen run by rounding only.
+//
+// Compile: see oracle/build_oracle.sh (g++ -O2 -ffp-contract=off -fopenmp).
+
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstdlib>
+#include <cstring>
+#include <cstdio>
+#include <functional>
+#include <stdexcept>
+#include <string>
+#include <utility>
+#include <vector>
+
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+namespace orc {
+
+// ---------------------------------------------------------------- status codes
+// Mirror of the product's fgb_status values.
+enum { OK = 0, ERR_INVALID = 1, ERR_NAN = 4, ERR_ZERO_NORM = 5 };
+
+static thread_local std::string g_err;
+
+struct Error : std::runtime_error {
+  int code;
+  Error(int c, const std::string& m) : std::runtime_error(m), code(c) {}
+};
+
+// ---------------------------------------------------------------- CSR factor
+template <typename T>
+struct Csr {
+  int rows = 0, cols = 0;
+  std::vector<int> rowptr;  // rows+1
+  std::vector<int> colind;  // nnz, sorted inside each row
+  std::vector<T> val;
+  int nnz() const { return rowptr.empty() ? 0 : rowptr[rows]; }
+};
+
+// Dense column-major matrix.
+template <typename T>
+struct Dense {
+  int rows = 0, cols = 0;
+  std::vector<T> a;
+  Dense() {}
+  Dense(int r, int c) : rows(r), cols(c), a((size_t)r * c, T(0)) {}
+  T& at(int i, int j) { return a[(size_t)j * rows + i]; }
+  const T& at(int i, int j) const { return a[(size_t)j * rows + i]; }
+};
+
+// MatSparse(MatDense) keeps the non-zero entries, row-major, sorted columns
+// (faust_MatSparse.hpp constructor from MatDense).
+template <typename T>
+static Csr<T> dense_to_csr(const Dense<T>& M) {
+  Csr<T> S;
+  S.rows = M.rows;
+  S.cols = M.cols;
+  S.rowptr.assign(M.rows + 1, 0);
+  for (int i = 0; i < M.rows; ++i) {
+    for (int j = 0; j < M.cols; ++j) {
+      T v = M.at(i, j);
+      if (v != T(0)) {
+        S.colind.push_back(j);
+        S.val.push_back(v);
+      }
+    }
+    S.rowptr[i + 1] = (int)S.colind.size();
+  }
+  return S;
+}
+
+template <typename T>
+static Dense<T> csr_to_dense(const Csr<T>& S) {
+  Dense<T> M(S.rows, S.cols);
+  for (int i = 0; i < S.rows; ++i)
+    for (int p = S.rowptr[i]; p < S.rowptr[i + 1]; ++p) M.at(i, S.colind[p]) = S.val[p];
+  return M;
+}
+
+// CSR of the transpose; entries of each transposed row come in increasing
+// original row index.
+template <typename T>
+static Csr<T> csr_transpose(const Csr<T>& S) {
+  Csr<T> R;
+  R.rows = S.cols;
+  R.cols = S.rows;
+  R.rowptr.assign(S.cols + 1, 0);
+  const int nnz = S.nnz();
+  for (int p = 0; p < nnz; ++p) R.rowptr[S.colind[p] + 1]++;
+  for (int j = 0; j < S.cols; ++j) R.rowptr[j + 1] += R.rowptr[j];
+  R.colind.resize(nnz);
+  R.val.resize(nnz);
+  std::vector<int> fill(R.rowptr.begin(), R.rowptr.end() - 1);
+  for (int i = 0; i < S.rows; ++i)
+    for (int p = S.rowptr[i]; p < S.rowptr[i + 1]; ++p) {
+      int q = fill[S.colind[p]]++;
+      R.colind[q] = i;
+      R.val[q] = S.val[p];
+    }
+  return R;
+}
+
+template <typename T>
+static Csr<T> csr_identity(int rows, int cols) {
+  // MatSparse::setEyes (faust_MatSparse.hpp:533-560): ones on the diagonal.
+  Csr<T> S;
+  S.rows = rows;
+  S.cols = cols;
+  S.rowptr.assign(rows + 1, 0);
+  int m = std::min(rows, cols);
+  for (int i = 0; i < rows; ++i) {
+    if (i < m) {
+      S.colind.push_back(i);
+      S.val.push_back(T(1));
+    }
+    S.rowptr[i + 1] = (int)S.colind.size();
+  }
+  return S;
+}
+
+template <typename T>
+static Csr<T> csr_zero(int rows, int cols) {
+  Csr<T> S;
+  S.rows = rows;
+  S.cols = cols;
+  S.rowptr.assign(rows + 1, 0);
+  return S;
+}
+
+static inline float fma_(float a, float b, float c) { return std::fmaf(a, b, c); }
+static inline double fma_(double a, double b, double c) { return std::fma(a, b, c); }
+
+// ---------------------------------------------------------------- products
+// Y = S * X.  y[i,j] = sequential fma over row i of S (faust_MatSparse.hpp:253-254).
+template <typename T>
+static Dense<T> spmm(const Csr<T>& S, const Dense<T>& X) {
+  if (S.cols != X.rows) throw Error(ERR_INVALID, "spmm: dimension mismatch");
+  Dense<T> Y(S.rows, X.cols);
+#pragma omp parallel for schedule(static)
+  for (int j = 0; j < X.cols; ++j) {
+    const T* x = &X.a[(size_t)j * X.rows];
+    T* y = &Y.a[(size_t)j * Y.rows];
+    for (int i = 0; i < S.rows; ++i) {
+      T acc = T(0);
+      for (int p = S.rowptr[i]; p < S.rowptr[i + 1]; ++p) acc = fma_(S.val[p], x[S.colind[p]], acc);
+      y[i] = acc;
+    }
+  }
+  return Y;
+}
+
+// Y = X * S^T given the CSR of S: y[r, c] = sum over row c of S of v * x[r, col].
+template <typename T>
+static Dense<T> dense_times_csrT(const Dense<T>& X, const Csr<T>& S) {
+  if (X.cols != S.cols) throw Error(ERR_INVALID, "dense_times_csrT: dimension mismatch");
+  Dense<T> Y(X.rows, S.rows);
+#pragma omp parallel for schedule(static)
+  for (int c = 0; c < S.rows; ++c) {
+    T* y = &Y.a[(size_t)c * Y.rows];
+    for (int r = 0; r < X.rows; ++r) {
+      T acc = T(0);
+      for (int p = S.rowptr[c]; p < S.rowptr[c + 1]; ++p)
+        acc = fma_(S.val[p], X.a[(size_t)S.colind[p] * X.rows + r], acc);
+      y[r] = acc;
+    }
+  }
+  return Y;
+}
+
+// A factor together with the CSR of its transpose (built once per factor).
+template <typename T>
+struct Factor {
+  Csr<T> S, St;
+  Factor() {}
+  explicit Factor(Csr<T> s) : S(std::move(s)) { St = csr_transpose(S); }
+};
+
+// Y = S^H X  (real: S^T X) via the transposed CSR.
+template <typename T>
+static Dense<T> spmm_H(const Factor<T>& F, const Dense<T>& X) { return spmm(F.St, X); }
+// Y = X S    via the transposed CSR:  y[r,c] = sum_{i in col c of S} S[i,c] x[r,i].
+template <typename T>
+static Dense<T> dense_times_csr(const Dense<T>& X, const Factor<T>& F) { return dense_times_csrT(X, F.St); }
+// Y = X S^H  via the CSR of S.
+template <typename T>
+static Dense<T> dense_times_csrH(const Dense<T>& X, const Factor<T>& F) { return dense_times_csrT(X, F.S); }
+
+// ---------------------------------------------------------------- reductions
+static const int CR_LANES = 256;
+static const size_t CR_CHUNK = 65536;
+
+// Canonical fma reduction of sum_i a[i]*b[i] over column-major linear order.
+template <typename T>
+static T cdot(const T* a, const T* b, size_t n) {
+  T total = T(0);
+  for (size_t c0 = 0; c0 < n; c0 += CR_CHUNK) {
+    size_t c1 = std::min(n, c0 + CR_CHUNK);
+    T lane[CR_LANES];
+    for (int t = 0; t < CR_LANES; ++t) lane[t] = T(0);
+    for (size_t i = c0; i < c1; ++i) {
+      int t = (int)((i - c0) % CR_LANES);
+      lane[t] = fma_(a[i], b[i], lane[t]);
+    }
+    for (int s = CR_LANES / 2; s >= 1; s /= 2)
+      for (int t = 0; t < s; ++t) lane[t] = lane[t] + lane[t + s];
+    total = total + lane[0];
+  }
+  return total;
+}
+template <typename T>
+static T csumsq(const T* a, size_t n) { return cdot(a, a, n); }
+template <typename T>
+static T cnorm(const T* a, size_t n) { return std::sqrt(csumsq(a, n)); }
+
+// MatDense::normalize (faust_MatDense.hpp:1225-1250): multiply by FPP(1.0/n),
+// domain_error on a zero norm.
+template <typename T>
+static void normalize(Dense<T>& M) {
+  T n = cnorm(M.a.data(), M.a.size());
+  if (n == T(0)) throw Error(ERR_ZERO_NORM, "the norm is zero, can't normalize.");
+  T s = T(1.0 / n);
+  for (auto& v : M.a) v = v * s;
+}
+
+// ---------------------------------------------------------------- projections
+// sort_idx + partial_sort_comp (faust_prox.hpp:52-69): indices of the s
+// largest |v| as selected by std::partial_sort with comparator |a| > |b|.
+template <typename T>
+static void sort_idx(const std::vector<T>& v, std::vector<int>& idx, int s) {
+  std::vector<std::pair<int, T>> vp(v.size());
+  for (size_t i = 0; i < v.size(); ++i) vp[i] = std::make_pair((int)i, v[i]);
+  std::partial_sort(vp.begin(), vp.begin() + s, vp.end(),
+                    [](const std::pair<int, T>& p1, const std::pair<int, T>& p2) {
+                      return std::fabs(p1.second) > std::fabs(p2.second);
+                    });
+  idx.resize(s);
+  for (int i = 0; i < s; ++i) idx[i] = vp[i].first;
+}
+
+// pre_prox_pos (faust_prox.hpp:307-320)
+template <typename T>
+static void pre_prox_pos(Dense<T>& M) {
+  for (auto& v : M.a)
+    if (v < T(0)) v = T(0);
+}
+
+// prox_sp (faust_prox.hpp:71-96)
+template <typename T>
+static void prox_sp(Dense<T>& M, long k, bool normalized, bool pos) {
+  const size_t N = M.a.size();
+  if (pos) pre_prox_pos(M);
+  if (k <= 0) {
+    std::fill(M.a.begin(), M.a.end(), T(0));
+  } else if ((size_t)k < N) {
+    const std::vector<T> vec(M.a);
+    std::vector<int> index;
+    sort_idx(vec, index, (int)k);
+    std::fill(M.a.begin(), M.a.end(), T(0));
+    for (int i : index) M.a[i] = vec[i];
+  }
+  if (normalized) normalize(M);
+}
+
+// prox_spcol (faust_prox.hpp:112-143)
+template <typename T>
+static void prox_spcol(Dense<T>& M, long k, bool normalized, bool pos) {
+  if (pos) pre_prox_pos(M);
+  if (k <= 0) {
+    std::fill(M.a.begin(), M.a.end(), T(0));
+  } else if (k < M.rows) {
+    Dense<T> out(M.rows, M.cols);
+    for (int j = 0; j < M.cols; ++j) {
+      std::vector<T> col(M.a.begin() + (size_t)j * M.rows, M.a.begin() + (size_t)(j + 1) * M.rows);
+      std::vector<int> idx;
+      sort_idx(col, idx, (int)k);
+      for (int i : idx) out.at(i, j) = col[i];
+    }
+    M = out;
+  }
+  if (normalized) normalize(M);
+}
+
+// prox_splin (faust_prox.hpp:145-177)
+template <typename T>
+static void prox_splin(Dense<T>& M, long k, bool normalized, bool pos) {
+  if (pos) pre_prox_pos(M);
+  if (k <= 0) {
+    std::fill(M.a.begin(), M.a.end(), T(0));
+  } else if (k < M.cols) {
+    Dense<T> out(M.rows, M.cols);
+    for (int i = 0; i < M.rows; ++i) {
+      std::vector<T> row(M.cols);
+      for (int j = 0; j < M.cols; ++j) row[j] = M.at(i, j);
+      std::vector<int> idx;
+      sort_idx(row, idx, (int)k);
+      for (int j : idx) out.at(i, j) = row[j];
+    }
+    M = out;
+  }
+  if (normalized) normalize(M);
+}
+
+// prox_splincol (faust_prox.hpp:179-202).  As in the reference, `pos` is
+// applied to M after the two copies were taken, so it has no effect on the
+// result; spcol entries win and splin fills the remaining positions.
+template <typename T>
+static void prox_splincol(Dense<T>& M, long k, bool normalized, bool pos) {
+  Dense<T> Mspcol = M, Msplin = M;
+  if (pos) pre_prox_pos(M);
+  prox_spcol(Mspcol, k, false, false);
+  prox_splin(Msplin, k, false, false);
+  for (size_t i = 0; i < M.a.size(); ++i)
+    if (Mspcol.a[i] != T(0)) Msplin.a[i] = T(0);
+  for (size_t i = 0; i < M.a.size(); ++i) Mspcol.a[i] = Mspcol.a[i] + Msplin.a[i];
+  M = Mspcol;
+  if (normalized) normalize(M);
+}
+
+// prox_normcol (faust_prox.hpp:204-246): column j scaled by s/||col_j||
+// (a zero column stays zero); s < 0 is an error; s == 0 zeroes M.
+template <typename T>
+static void prox_normcol(Dense<T>& M, double s, bool normalized, bool pos) {
+  if (pos) pre_prox_pos(M);
+  if (s < 0) throw Error(ERR_INVALID, "Faust::prox_normcol : s < 0 ");
+  if (s == 0) {
+    std::fill(M.a.begin(), M.a.end(), T(0));
+  } else {
+    for (int j = 0; j < M.cols; ++j) {
+      T* col = &M.a[(size_t)j * M.rows];
+      T nrm = cnorm(col, (size_t)M.rows);
+      T scal = nrm;
+      if (scal != T(0)) scal = T(s) / scal;
+      for (int i = 0; i < M.rows; ++i) col[i] = col[i] * scal;
+    }
+  }
+  if (normalized) normalize(M);
+}
+
+// prox_normlin (faust_prox.hpp:248-254): normcol of the transpose.
+template <typename T>
+static void prox_normlin(Dense<T>& M, double s, bool normalized, bool pos) {
+  Dense<T> Tm(M.cols, M.rows);
+  for (int i = 0; i < M.rows; ++i)
+    for (int j = 0; j < M.cols; ++j) Tm.at(j, i) = M.at(i, j);
+  prox_normcol(Tm, s, normalized, pos);
+  for (int i = 0; i < M.rows; ++i)
+    for (int j = 0; j < M.cols; ++j) M.at(i, j) = Tm.at(j, i);
+}
+
+// prox_supp (faust_prox.hpp:375-385): element-wise product with the support.
+template <typename T>
+static void prox_supp(Dense<T>& M, const T* supp, bool normalized, bool pos) {
+  if (pos) pre_prox_pos(M);
+  for (size_t i = 0; i < M.a.size(); ++i) M.a[i] = M.a[i] * supp[i];
+  if (normalized) normalize(M);
+}
+
+// Constraint kinds; values mirror include/fgb.h.
+enum ConsKind { C_SP = 0, C_SPCOL = 1, C_SPLIN = 2, C_SPLINCOL = 3, C_NORMCOL = 4, C_NORMLIN = 5, C_SUPP = 6, C_SP_POS = 7 };
+
+template <typename T>
+struct Cons {
+  int kind;
+  long k;
+  double s;
+  bool normalized, pos;
+  int rows, cols;
+  const T* supp;  // rows*cols column-major, C_SUPP only
+};
+
+// ConstraintGeneric::project_gen dispatch (faust_ConstraintGeneric.hpp:248-257,
+// faust_ConstraintInt.hpp:203-230, faust_ConstraintFPP.hpp:152-167).
+// The result becomes the new factor; a dense prox image is kept as a full CSR
+// (every entry), which yields the same products as a dense factor under the
+// sequential fma order, so the dense/sparse output rule of prox_*_gen
+// (faust_prox_gen.hpp) does not change any value.
+template <typename T>
+static void project(const Cons<T>& c, Dense<T>& D) {
+  switch (c.kind) {
+    case C_SP: prox_sp(D, c.k, c.normalized, c.pos); break;
+    case C_SP_POS: prox_sp(D, c.k, c.normalized, true); break;
+    case C_SPCOL: prox_spcol(D, c.k, c.normalized, c.pos); break;
+    case C_SPLIN: prox_splin(D, c.k, c.normalized, c.pos); break;
+    case C_SPLINCOL: prox_splincol(D, c.k, c.normalized, c.pos); break;
+    case C_NORMCOL: prox_normcol(D, c.s, c.normalized, c.pos); break;
+    case C_NORMLIN: prox_normlin(D, c.s, c.normalized, c.pos); break;
+    case C_SUPP: prox_supp(D, c.supp, c.normalized, c.pos); break;
+    default: throw Error(ERR_INVALID, "project : cannot project with this constraint name");
+  }
+}
+
+// ---------------------------------------------------------------- power iteration
+// glibc rand() after srand(418) without touching the global generator:
+// srand/rand are random()'s TYPE_3 additive feedback generator with a
+// 128-byte state, reproduced with initstate_r/random_r.
+static std::vector<int> glibc_rand_seq(unsigned seed, int n) {
+  std::vector<int> out(n);
+  static thread_local char state[128];
+  struct random_data rd;
+  std::memset(&rd, 0, sizeof(rd));
+  std::memset(state, 0, sizeof(state));
+  initstate_r(seed, state, sizeof(state), &rd);
+  for (int i = 0; i < n; ++i) {
+    int32_t r;
+    random_r(&rd, &r);
+    out[i] = r;
+  }
+  return out;
+}
+
+// Vect::setRand (faust_Vect.hpp:364-367) after srand(0xF4+'u'+57) = srand(418)
+// (faust_linear_algebra.hpp:843-847).  Eigen 3.4's Random() maps rand() to
+// x + (y-x)*Scalar(rand())/Scalar(RAND_MAX) with [x,y] = [-1,1]; that mapping
+// is restated from Eigen's documented behaviour (Eigen is not available here).
+template <typename T>
+static std::vector<T> power_iteration_start(int n) {
+  std::vector<int> r = glibc_rand_seq(418u, n);
+  std::vector<T> x(n);
+  for (int i = 0; i < n; ++i) x[i] = T(-1) + (T(2) * T(r[i])) / T(RAND_MAX);
+  return x;
+}
+
+// The operator whose largest eigenvalue is sought: a list of (factor, adjoint?)
+// applied right to left.
+template <typename T>
+struct ChainOp {
+  std::vector<std::pair<const Factor<T>*, bool>> ops;  // applied in vector order
+  int n = 0;
+};
+
+template <typename T>
+static std::vector<T> apply_chain_vec(const ChainOp<T>& A, const std::vector<T>& x) {
+  Dense<T> v(A.n, 1);
+  v.a = x;
+  for (auto& op : A.ops) {
+    v = op.second ? spmm_H(*op.first, v) : spmm(op.first->S, v);
+  }
+  return v.a;
+}
+
+// Faust::power_iteration (faust_linear_algebra.hpp:806-899).
+template <typename T>
+static T power_iteration(const ChainOp<T>& A, int max_iter, T threshold, int& flag) {
+  if (max_iter <= 0) throw Error(ERR_INVALID, "power_iteration :  nbr_iter_max <= 0");
+  const int n = A.n;
+  std::vector<T> xk = power_iteration_start<T>(n);
+  std::vector<T> xk_norm(n);
+  T lambda_old = T(1), lambda = T(0);
+  int i = 0;
+  flag = 0;
+  const T thr = std::fabs(threshold);
+  while ((std::fabs(lambda_old - lambda) > thr || std::fabs(lambda) <= thr) && i < max_iter) {
+    i++;
+    lambda_old = lambda;
+    // Vect::normalize (faust_Vect.hpp:389-395): scale by 1/norm.
+    T nrm = cnorm(xk.data(), (size_t)n);
+    if (nrm == T(0)) throw Error(ERR_ZERO_NORM, "Can't normalize a zero-norm vector.");
+    T inv = T(1) / nrm;
+    for (int t = 0; t < n; ++t) xk_norm[t] = xk[t] * inv;
+    xk = apply_chain_vec(A, xk_norm);
+    bool zero = true;
+    for (int t = 0; t < n; ++t)
+      if (xk[t] != T(0)) { zero = false; break; }
+    if (zero) return T(0);  // flag keeps its initial 0 (:884-888)
+    lambda = cdot(xk_norm.data(), xk.data(), (size_t)n);
+  }
+  flag = (i < max_iter) ? i : -1;
+  return lambda;
+}
+
+// Transform::spectralNorm (faust_Transform.hpp:683-708) of the product
+// F[lo] ... F[hi-1]: empty -> 1; a factor without entries -> 0; otherwise
+// sqrt of the power iteration on (F^H F) when cols < rows, else (F F^H).
+template <typename T>
+static double spectral_norm(const std::vector<Factor<T>>& F, int lo, int hi, int max_iter, T thr, int& flag) {
+  flag = 0;
+  if (hi <= lo) return 1.0;
+  for (int i = lo; i < hi; ++i)
+    if (F[i].S.nnz() == 0) return 0.0;
+  ChainOp<T> A;
+  const int rows = F[lo].S.rows, cols = F[hi - 1].S.cols;
+  if (cols < rows) {
+    // AtA = F^H F: x -> F^H (F x).  F x applies F[hi-1] first.
+    A.n = cols;
+    for (int i = hi - 1; i >= lo; --i) A.ops.push_back({&F[i], false});
+    for (int i = lo; i < hi; ++i) A.ops.push_back({&F[i], true});
+  } else {
+    // AtA = F F^H: x -> F (F^H x).  F^H x applies F[lo]^H first.
+    A.n = rows;
+    for (int i = lo; i < hi; ++i) A.ops.push_back({&F[i], true});
+    for (int i = hi - 1; i >= lo; --i) A.ops.push_back({&F[i], false});
+  }
+  T lam = power_iteration(A, max_iter, thr, flag);
+  return std::fabs((double)std::sqrt(lam));
+}
+
+// ---------------------------------------------------------------- palm4msa2
+struct PalmParams {
+  int nb_it;
+  int is_update_way_R2L;
+  int packing_RL;
+  int no_normalization;
+  int no_lambda;
+  double norm2_threshold;
+  int norm2_max_iter;
+  int constant_step_size;
+  double step_size;
+  int no_lambda_error;
+  int norm2_fp64;
+};
+
+// Spectral norm of a chain, optionally computed on FP64 copies of the factors.
+template <typename T>
+static double chain_norm(const std::vector<Factor<T>>& F, int lo, int hi, const PalmParams& p, int& flag) {
+  if (p.norm2_fp64 && !std::is_same<T, double>::value) {
+    std::vector<Factor<double>> Fd;
+    Fd.reserve(hi - lo);
+    for (int i = lo; i < hi; ++i) {
+      Csr<double> s;
+      s.rows = F[i].S.rows;
+      s.cols = F[i].S.cols;
+      s.rowptr = F[i].S.rowptr;
+      s.colind = F[i].S.colind;
+      s.val.assign(F[i].S.val.begin(), F[i].S.val.end());
+      Fd.emplace_back(std::move(s));
+    }
+    return spectral_norm<double>(Fd, 0, hi - lo, p.norm2_max_iter, p.norm2_threshold, flag);
+  }
+  return spectral_norm<T>(F, lo, hi, p.norm2_max_iter, (T)p.norm2_threshold, flag);
+}
+
+// Dense product F[lo] ... F[hi-1] applied to the dense block X (right to left).
+template <typename T>
+static Dense<T> chain_apply(const std::vector<Factor<T>>& F, int lo, int hi, Dense<T> X) {
+  for (int i = hi - 1; i >= lo; --i) X = spmm(F[i].S, X);
+  return X;
+}
+
+template <typename T>
+struct PalmTrace {
+  std::vector<double> lambdas;  // lambda after each outer iteration
+  std::vector<double> c_values; // step constant c per factor update
+  std::vector<int> norm_iters;  // power-iteration counts (R then L) per update
+  std::vector<int> topk_case;   // per global top-k: 0 unique, 1 prefix rule, 2 heap order decides
+};
+
+// Classifies a global top-k selection: with t the k-th largest magnitude,
+// G = #{|v| > t}, E = #{|v| == t}: case 0 when G + E == k (unique set);
+// case 1 when no |v| > t occurs after the position where the running count of
+// |v| >= t reaches k (the set is then the first k such positions); case 2
+// otherwise (the heap's internal order decides which ties stay).
+template <typename T>
+static int topk_case(const std::vector<T>& v, long k) {
+  const size_t N = v.size();
+  if (k <= 0 || (size_t)k >= N) return 0;
+  std::vector<T> mags(N);
+  for (size_t i = 0; i < N; ++i) mags[i] = std::fabs(v[i]);
+  std::vector<T> tmp(mags);
+  std::nth_element(tmp.begin(), tmp.begin() + (k - 1), tmp.end(), std::greater<T>());
+  const T t = tmp[k - 1];
+  size_t G = 0, E = 0;
+  for (auto m : mags) { if (m > t) ++G; else if (m == t) ++E; }
+  if (G + E == (size_t)k) return 0;
+  size_t cnt = 0, tau = N;
+  for (size_t i = 0; i < N; ++i)
+    if (mags[i] >= t && ++cnt == (size_t)k) { tau = i; break; }
+  for (size_t i = tau + 1; i < N; ++i)
+    if (mags[i] > t) {
+      if (getenv("ORC_TOPK_STATS")) {
+        // number of heap replacements made by the selection
+        std::vector<T> h(mags.begin(), mags.begin() + k);
+        std::make_heap(h.begin(), h.end(), std::greater<T>());
+        size_t ins = 0, cand = 0;
+        for (size_t j = k; j < N; ++j) {
+          if (mags[j] > h.front()) {
+            std::pop_heap(h.begin(), h.end(), std::greater<T>());
+            h.back() = mags[j];
+            std::push_heap(h.begin(), h.end(), std::greater<T>());
+            ++ins;
+          }
+        }
+        T m0 = *std::min_element(mags.begin(), mags.begin() + k);
+        for (size_t j = k; j < N; ++j) cand += mags[j] > m0;
+        fprintf(stderr, "case2 N=%zu k=%ld G=%zu E=%zu tau=%zu ins=%zu cand=%zu\n", N, k, G, E, tau, ins, cand);
+      }
+      return 2;
+    }
+  return 1;
+}
+
+// Faust::palm4msa2 (faust_palm4msa2020.hpp:46-301) with update_fact
+// (:527-676), compute_n_apply_grad2's products (:362-439) and update_lambda
+// (:441-493), factors_format = AllDynamic, no MHTP.
+template <typename T>
+static void palm4msa2(const Dense<T>& A, const std::vector<Cons<T>>& cons, std::vector<Factor<T>>& S, T& lambda,
+                      const PalmParams& p, PalmTrace<T>* trace) {
+  const int J = (int)cons.size();
+  if (J == 0) throw Error(ERR_INVALID, "No constraint passed to palm4msa.");
+  const double lipschitz = 1.001;  // LIPSCHITZ_MULTIPLICATOR (faust_palm4msa2020.h:36)
+  std::vector<Cons<T>> C = cons;
+  if (p.no_normalization)
+    for (auto& c : C) c.normalized = false;
+  const bool R2L = p.is_update_way_R2L != 0;
+  // Initial factors (:115-149): the first factor to update is zero, the others identity.
+  if ((int)S.size() != J) {
+    S.clear();
+    for (int i = 0; i < J; ++i) {
+      bool zero = R2L ? (i == J - 1) : (i == 0);
+      S.emplace_back(zero ? csr_zero<T>(C[i].rows, C[i].cols) : csr_identity<T>(C[i].rows, C[i].cols));
+    }
+  }
+  T c = T(1.0 / p.step_size);
+  // pR[i] (L2R) / pL[i] (R2L): dense packed products computed by init_ite.
+  std::vector<Dense<T>> packed(J);
+  for (int it = 0; it < p.nb_it; ++it) {
+    // init_ite (:175-236)
+    if (!R2L) {
+      // pR[J-1] empty; pR[i] = S[i+1] * pR[i+1], packed dense.
+      if (J >= 2) {
+        packed[J - 2] = csr_to_dense(S[J - 1].S);
+        for (int i = J - 3; i >= 0; --i) packed[i] = spmm(S[i + 1].S, packed[i + 1]);
+      }
+    } else {
+      // pL[0] empty; pL[i] = pL[i-1] * S[i-1], packed dense.
+      if (J >= 2) {
+        packed[1] = csr_to_dense(S[0].S);
+        for (int i = 2; i < J; ++i) packed[i] = dense_times_csr(packed[i - 1], S[i - 1]);
+      }
+    }
+    for (int step = 0; step < J; ++step) {
+      const int f = R2L ? (J - 1 - step) : step;
+      // Step size (:563-617).
+      double nR = 1.0, nL = 1.0;
+      int flR = 0, flL = 0;
+      if (p.constant_step_size) {
+        c = T(1.0 / p.step_size);
+      } else {
+        if (f + 1 < J) nR = chain_norm(S, f + 1, J, p, flR);
+        if (f > 0) nL = chain_norm(S, 0, f, p, flL);
+        if (std::isnan(nL) || std::isnan(nR))
+          throw Error(ERR_NAN, "2-norm computation error: R or L 2-norm is NaN.");
+        if ((nR == 0 && (it > 0 || !R2L)) || (nL == 0 && (it > 0 || R2L)))
+          throw Error(ERR_ZERO_NORM,
+                      "2-norm computation error in computation of descent step inverse: R or L 2-norm is zero.");
+        // LIPSCHITZ_MULTIPLICATOR is the double literal 1.001, so the product
+        // is evaluated in double and rounded once to FPP (:616).
+        const double tnR = (double)T(nR), tnL = (double)T(nL), lam = (double)lambda;
+        c = T(lipschitz * lam * lam * tnR * tnR * tnL * tnL);
+        if (trace) {
+          trace->norm_iters.push_back(flR);
+          trace->norm_iters.push_back(flL);
+        }
+      }
+      if (trace) trace->c_values.push_back((double)c);
+      const bool hasL = f > 0, hasR = f + 1 < J;
+      const int n = C[f].rows, m = C[f].cols;
+      (void)n;
+      (void)m;
+      // P = L * D * R.
+      Dense<T> P;
+      if (!R2L) {
+        P = hasR ? spmm(S[f].S, packed[f]) : csr_to_dense(S[f].S);
+        for (int l = f - 1; l >= 0; --l) P = spmm(S[l].S, P);
+      } else {
+        P = hasL ? dense_times_csr(packed[f], S[f]) : csr_to_dense(S[f].S);
+        for (int l = f + 1; l < J; ++l) P = dense_times_csr(P, S[l]);
+      }
+      // E = lambda * P - A.
+      if (P.rows != A.rows || P.cols != A.cols) throw Error(ERR_INVALID, "palm4msa2: factor dimensions do not match A");
+      for (size_t i = 0; i < P.a.size(); ++i) P.a[i] = (lambda * P.a[i]) - A.a[i];
+      // G = L^H * E * R^H.
+      Dense<T> G = std::move(P);
+      if (!R2L) {
+        for (int l = 0; l < f; ++l) G = spmm_H(S[l], G);
+        for (int l = J - 1; l > f; --l) G = dense_times_csrH(G, S[l]);
+      } else {
+        for (int l = J - 1; l > f; --l) G = dense_times_csrH(G, S[l]);
+        for (int l = 0; l < f; ++l) G = spmm_H(S[l], G);
+      }
+      // D = S_f - (lambda/c) G.
+      Dense<T> D = csr_to_dense(S[f].S);
+      const T alpha = lambda / c;
+      for (size_t i = 0; i < D.a.size(); ++i) D.a[i] = D.a[i] - (alpha * G.a[i]);
+      // Projection and replacement (:644-673).
+      if (trace && (C[f].kind == C_SP || C[f].kind == C_SP_POS)) {
+        std::vector<T> v(D.a);
+        if (C[f].kind == C_SP_POS || C[f].pos)
+          for (auto& x : v) if (x < T(0)) x = T(0);
+        trace->topk_case.push_back(topk_case(v, C[f].k));
+      }
+      project(C[f], D);
+      S[f] = Factor<T>(dense_to_csr(D));
+    }
+    // update_lambda (:441-493)
+    if (!p.no_lambda) {
+      Dense<T> S_mat;
+      const int n = J;
+      // The reuse rule of :449-468 applies when pR[0] and pL[n-1] are single
+      // packed factors (always with packing_RL; with two factors otherwise).
+      bool reuse = p.packing_RL || J <= 2;
+      if (J == 1) {
+        S_mat = csr_to_dense(S[0].S);
+      } else if (reuse) {
+        long lhs = (long)S[0].S.cols * (long)C[1].rows;            // S[0].cols * pR[0].rows
+        long rhs = (long)C[n - 2].cols * (long)S[n - 1].S.rows;    // pL[n-1].cols * S[n-1].rows
+        if (lhs < rhs) {
+          // S = S[0] * pR[0]; pR[0] is fresh in R2L, from init_ite in L2R.
+          if (!R2L)
+            S_mat = spmm(S[0].S, packed[0]);
+          else
+            S_mat = chain_apply(S, 0, J - 1, csr_to_dense(S[J - 1].S));
+        } else {
+          // S = pL[n-1] * S[n-1]; pL[n-1] is fresh in L2R, from init_ite in R2L.
+          if (!R2L)
+            S_mat = chain_apply(S, 0, J - 1, csr_to_dense(S[J - 1].S));
+          else
+            S_mat = dense_times_csr(packed[n - 1], S[n - 1]);
+        }
+      } else {
+        S_mat = chain_apply(S, 0, J - 1, csr_to_dense(S[J - 1].S));
+      }
+      // tr(A^H S) = <A, S> and ||S||_F.
+      T tr = cdot(A.a.data(), S_mat.a.data(), A.a.size());
+      T nS = cnorm(S_mat.a.data(), S_mat.a.size());
+      bool skip = false;
+      if (nS == T(0)) {
+        if (p.no_lambda_error) skip = true;
+        else throw Error(ERR_ZERO_NORM, "Error in update_lambda: S Frobenius norm is zero, can't compute lambda.");
+      }
+      if (!skip && (std::isnan(tr) || std::isnan(nS))) {
+        if (p.no_lambda_error) skip = true;
+        else throw Error(ERR_NAN, "Error in update_lambda: S (the Faust) contains nan elements in at least one of its matrices, can't compute lambda.");
+      }
+      if (!skip) lambda = tr / (nS * nS);
+    }
+    if (trace) trace->lambdas.push_back((double)lambda);
+  }
+}
+
+// calc_rel_err (faust_palm4msa2020.hpp:35-44): ||lambda*S - A||_F / ||A||_F.
+template <typename T>
+static double rel_err(const std::vector<Factor<T>>& S, const Dense<T>& A, T lambda) {
+  const int J = (int)S.size();
+  Dense<T> P = chain_apply(S, 0, J - 1, csr_to_dense(S[J - 1].S));
+  for (size_t i = 0; i < P.a.size(); ++i) P.a[i] = (lambda * P.a[i]) - A.a[i];
+  return (double)(cnorm(P.a.data(), P.a.size()) / cnorm(A.a.data(), A.a.size()));
+}
+
+// ---------------------------------------------------------------- BSR
+// BSRMat::mul (faust_MatBSR.hpp:827-836): for each stored block (row-block
+// order, then stored order) prod.block(r,0,bm,nc) += B * X.block(c,0,bn,nc).
+// Accumulated in FP64 here: this is the FP64 oracle of the BF16 kernel.
+static void bsr_mul_f64(int m, int n, int bm, int bn, const int* browptr, const int* bcolind, const double* blocks,
+                        const double* X, int ldx, int nc, double* Y, int ldy) {
+  const int nbr = m / bm;
+#pragma omp parallel for schedule(dynamic)
+  for (int j = 0; j < nc; ++j) {
+    for (int br = 0; br < nbr; ++br) {
+      double* y = Y + (size_t)j * ldy + (size_t)br * bm;
+      for (int r = 0; r < bm; ++r) y[r] = 0.0;
+      for (int p = browptr[br]; p < browptr[br + 1]; ++p) {
+        const double* B = blocks + (size_t)p * bm * bn;
+        const double* x = X + (size_t)j * ldx + (size_t)bcolind[p] * bn;
+        for (int cc = 0; cc < bn; ++cc) {
+          const double xv = x[cc];
+          const double* bc = B + (size_t)cc * bm;
+          for (int r = 0; r < bm; ++r) y[r] += bc[r] * xv;
+        }
+      }
+    }
+  }
+  (void)n;
+}
+
+}  // namespace orc
+
+// ====================================================================== C API
+using namespace orc;
+
+template <typename T>
+static std::vector<Factor<T>> unpack_chain(int nfac, const int* dims, const int* rowptr, const int* colind,
+                                           const T* val) {
+  // dims: [rows0, cols0, nnz0, rows1, ...]; rowptr/colind/val concatenated.
+  std::vector<Factor<T>> F;
+  size_t rp = 0, nz = 0;
+  for (int f = 0; f < nfac; ++f) {
+    Csr<T> s;
+    s.rows = dims[3 * f];
+    s.cols = dims[3 * f + 1];
+    int nnz = dims[3 * f + 2];
+    s.rowptr.assign(rowptr + rp, rowptr + rp + s.rows + 1);
+    s.colind.assign(colind + nz, colind + nz + nnz);
+    s.val.assign(val + nz, val + nz + nnz);
+    rp += s.rows + 1;
+    nz += nnz;
+    F.emplace_back(std::move(s));
+  }
+  return F;
+}
+
+#define ORC_TRY(...)                  \
+  try {                               \
+    __VA_ARGS__;                      \
+    return OK;                        \
+  } catch (const Error& e) {          \
+    g_err = e.what();                 \
+    return e.code;                    \
+  } catch (const std::exception& e) { \
+    g_err = e.what();                 \
+    return ERR_INVALID;               \
+  }
+
+template <typename T>
+static int chain_mul_impl(int nfac, const int* dims, const int* rowptr, const int* colind, const T* val,
+                          const T* X, int xrows, int ncols, T* Y) {
+  ORC_TRY({
+    auto F = unpack_chain<T>(nfac, dims, rowptr, colind, val);
+    Dense<T> M(xrows, ncols);
+    std::memcpy(M.a.data(), X, sizeof(T) * (size_t)xrows * ncols);
+    M = chain_apply(F, 0, nfac, std::move(M));
+    std::memcpy(Y, M.a.data(), sizeof(T) * M.a.size());
+  })
+}
+
+template <typename T>
+static std::vector<Cons<T>> unpack_cons(int J, const int* ikind, const long* ik, const double* s, const int* flags,
+                                        const int* cdims, const T* supp_concat) {
+  std::vector<Cons<T>> C(J);
+  size_t off = 0;
+  for (int i = 0; i < J; ++i) {
+    C[i].kind = ikind[i];
+    C[i].k = ik[i];
+    C[i].s = s[i];
+    C[i].normalized = (flags[2 * i] != 0);
+    C[i].pos = (flags[2 * i + 1] != 0);
+    C[i].rows = cdims[2 * i];
+    C[i].cols = cdims[2 * i + 1];
+    C[i].supp = nullptr;
+    if (C[i].kind == C_SUPP) {
+      C[i].supp = supp_concat + off;
+      off += (size_t)C[i].rows * C[i].cols;
+    }
+  }
+  return C;
+}
+
+template <typename T>
+static int palm_impl(const T* A, int rows, int cols, int J, const int* ikind, const long* ik, const double* s,
+                     const int* flags, const int* cdims, const T* supp, const PalmParams* p, const T* init_dense,
+                     double init_lambda, T* out_factors, double* out_lambda, double* out_lambdas, double* out_c,
+                     int* out_norm_iters, int* out_topk_case) {
+  ORC_TRY({
+    Dense<T> Am(rows, cols);
+    std::memcpy(Am.a.data(), A, sizeof(T) * (size_t)rows * cols);
+    auto C = unpack_cons<T>(J, ikind, ik, s, flags, cdims, supp);
+    std::vector<Factor<T>> S;
+    if (init_dense) {
+      size_t off = 0;
+      for (int i = 0; i < J; ++i) {
+        Dense<T> M(C[i].rows, C[i].cols);
+        std::memcpy(M.a.data(), init_dense + off, sizeof(T) * M.a.size());
+        off += M.a.size();
+        S.emplace_back(dense_to_csr(M));
+      }
+    }
+    T lambda = T(init_lambda);
+    PalmTrace<T> tr;
+    palm4msa2(Am, C, S, lambda, *p, &tr);
+    size_t off = 0;
+    for (int i = 0; i < J; ++i) {
+      Dense<T> M = csr_to_dense(S[i].S);
+      std::memcpy(out_factors + off, M.a.data(), sizeof(T) * M.a.size());
+      off += M.a.size();
+    }
+    *out_lambda = (double)lambda;
+    if (out_lambdas)
+      for (size_t i = 0; i < tr.lambdas.size(); ++i) out_lambdas[i] = tr.lambdas[i];
+    if (out_c)
+      for (size_t i = 0; i < tr.c_values.size(); ++i) out_c[i] = tr.c_values[i];
+    if (out_norm_iters)
+      for (size_t i = 0; i < tr.norm_iters.size(); ++i) out_norm_iters[i] = tr.norm_iters[i];
+    if (out_topk_case)
+      for (size_t i = 0; i < tr.topk_case.size(); ++i) out_topk_case[i] = tr.topk_case[i];
+  })
+}
+
+extern "C" {
+
+const char* orc_last_error() { return g_err.c_str(); }
+
+int orc_set_threads(int n) {
+#ifdef _OPENMP
+  if (n > 0) omp_set_num_threads(n);
+  return omp_get_max_threads();
+#else
+  (void)n;
+  return 1;
+#endif
+}
+
+int orc_chain_mul_f64(int nfac, const int* dims, const int* rowptr, const int* colind, const double* val,
+                      const double* X, int xrows, int ncols, double* Y) {
+  return chain_mul_impl<double>(nfac, dims, rowptr, colind, val, X, xrows, ncols, Y);
+}
+int orc_chain_mul_f32(int nfac, const int* dims, const int* rowptr, const int* colind, const float* val,
+                      const float* X, int xrows, int ncols, float* Y) {
+  return chain_mul_impl<float>(nfac, dims, rowptr, colind, val, X, xrows, ncols, Y);
+}
+
+int orc_bsr_mul_f64(int m, int n, int bm, int bn, const int* browptr, const int* bcolind, const double* blocks,
+                    const double* X, int ldx, int nc, double* Y, int ldy) {
+  ORC_TRY(bsr_mul_f64(m, n, bm, bn, browptr, bcolind, blocks, X, ldx, nc, Y, ldy));
+}
+
+// Indices selected by sort_idx (std::partial_sort, comparator |a|>|b|).
+int orc_topk_f64(long n, const double* v, int k, int* idx_out) {
+  ORC_TRY({
+    std::vector<double> vv(v, v + n);
+    std::vector<int> idx;
+    sort_idx(vv, idx, k);
+    std::memcpy(idx_out, idx.data(), sizeof(int) * k);
+  })
+}
+int orc_topk_f32(long n, const float* v, int k, int* idx_out) {
+  ORC_TRY({
+    std::vector<float> vv(v, v + n);
+    std::vector<int> idx;
+    sort_idx(vv, idx, k);
+    std::memcpy(idx_out, idx.data(), sizeof(int) * k);
+  })
+}
+
+// In-place projection of a dense column-major rows x cols matrix.
+int orc_prox_f64(int kind, long k, double s, int normalized, int pos, double* M, int rows, int cols,
+                 const double* supp) {
+  ORC_TRY({
+    Dense<double> D(rows, cols);
+    std::memcpy(D.a.data(), M, sizeof(double) * D.a.size());
+    Cons<double> c{kind, k, s, normalized != 0, pos != 0, rows, cols, supp};
+    project(c, D);
+    std::memcpy(M, D.a.data(), sizeof(double) * D.a.size());
+  })
+}
+int orc_prox_f32(int kind, long k, double s, int normalized, int pos, float* M, int rows, int cols,
+                 const float* supp) {
+  ORC_TRY({
+    Dense<float> D(rows, cols);
+    std::memcpy(D.a.data(), M, sizeof(float) * D.a.size());
+    Cons<float> c{kind, k, s, normalized != 0, pos != 0, rows, cols, supp};
+    project(c, D);
+    std::memcpy(M, D.a.data(), sizeof(float) * D.a.size());
+  })
+}
+
+// Spectral norm of a CSR chain (FP64), as TransformHelper::spectralNorm.
+int orc_spectral_norm_f64(int nfac, const int* dims, const int* rowptr, const int* colind, const double* val,
+                          int max_iter, double thr, double* out, int* flag) {
+  ORC_TRY({
+    auto F = unpack_chain<double>(nfac, dims, rowptr, colind, val);
+    *out = spectral_norm<double>(F, 0, nfac, max_iter, thr, *flag);
+  })
+}
+
+int orc_rand_start_f64(int n, double* out) {
+  ORC_TRY({
+    auto x = power_iteration_start<double>(n);
+    std::memcpy(out, x.data(), sizeof(double) * n);
+  })
+}
+
+int orc_canonical_dot_f64(long n, const double* a, const double* b, double* out) {
+  ORC_TRY(*out = cdot(a, b, (size_t)n));
+}
+int orc_canonical_dot_f32(long n, const float* a, const float* b, float* out) {
+  ORC_TRY(*out = cdot(a, b, (size_t)n));
+}
+
+int orc_palm4msa2_f64(const double* A, int rows, int cols, int J, const int* kind, const long* k, const double* s,
+                      const int* flags, const int* cdims, const double* supp, const PalmParams* p,
+                      const double* init_dense, double init_lambda, double* out_factors, double* out_lambda,
+                      double* out_lambdas, double* out_c, int* out_norm_iters, int* out_topk_case) {
+  return palm_impl<double>(A, rows, cols, J, kind, k, s, flags, cdims, supp, p, init_dense, init_lambda, out_factors,
+                           out_lambda, out_lambdas, out_c, out_norm_iters, out_topk_case);
+}
+int orc_palm4msa2_f32(const float* A, int rows, int cols, int J, const int* kind, const long* k, const double* s,
+                      const int* flags, const int* cdims, const float* supp, const PalmParams* p,
+                      const float* init_dense, double init_lambda, float* out_factors, double* out_lambda,
+                      double* out_lambdas, double* out_c, int* out_norm_iters, int* out_topk_case) {
+  return palm_impl<float>(A, rows, cols, J, kind, k, s, flags, cdims, supp, p, init_dense, init_lambda, out_factors,
+                          out_lambda, out_lambdas, out_c, out_norm_iters, out_topk_case);
+}
+
+// calc_rel_err for dense factors given column-major, concatenated.
+int orc_rel_err_f64(const double* A, int rows, int cols, int J, const int* cdims, const double* factors,
+                    double lambda, double* out) {
+  ORC_TRY({
+    Dense<double> Am(rows, cols);
+    std::memcpy(Am.a.data(), A, sizeof(double) * Am.a.size());
+    std::vector<Factor<double>> S;
+    size_t off = 0;
+    for (int i = 0; i < J; ++i) {
+      Dense<double> M(cdims[2 * i], cdims[2 * i + 1]);
+      std::memcpy(M.a.data(), factors + off, sizeof(double) * M.a.size());
+      off += M.a.size();
+      S.emplace_back(dense_to_csr(M));
+    }
+    *out = rel_err(S, Am, lambda);
+  })
+}
+
+}  // extern "C"

@@ -1,0 +1,205 @@
+"""ctypes front end of the CPU oracle (TEST INFRASTRUCTURE ONLY).
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU legs import this
+module; the product package never does.  The oracle restates FAuST's
+Faust x dense chain (src/faust_linear_operator/CPU/faust_Transform.hpp:1713-1855)
+and palm4msa2 (src/algorithm/factorization/faust_palm4msa2020.hpp:46-676) on the
+CPU; see faust_oracle.cpp for the operation order it fixes.  Parity against
+the reference's own numerical outputs is unpinned (the reference needs Eigen,
+which is absent); the top-k tie rule is pinned by calling std::partial_sort.
+"""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB_PATH = os.path.join(_HERE, "_build", "liborc.so")
+_lib = None
+
+# Constraint kinds (same values as include/fgb.h).
+SP, SPCOL, SPLIN, SPLINCOL, NORMCOL, NORMLIN, SUPP, SP_POS = range(8)
+
+
+class PalmParams(ctypes.Structure):
+    _fields_ = [
+        ("nb_it", ctypes.c_int),
+        ("is_update_way_R2L", ctypes.c_int),
+        ("packing_RL", ctypes.c_int),
+        ("no_normalization", ctypes.c_int),
+        ("no_lambda", ctypes.c_int),
+        ("norm2_threshold", ctypes.c_double),
+        ("norm2_max_iter", ctypes.c_int),
+        ("constant_step_size", ctypes.c_int),
+        ("step_size", ctypes.c_double),
+        ("no_lambda_error", ctypes.c_int),
+        ("norm2_fp64", ctypes.c_int),
+    ]
+
+
+def build():
+    subprocess.check_call(["sh", os.path.join(_HERE, "build_oracle.sh")])
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(_LIB_PATH):
+            build()
+        _lib = ctypes.CDLL(_LIB_PATH)
+        _lib.orc_last_error.restype = ctypes.c_char_p
+    return _lib
+
+
+def _p(a):
+    return a.ctypes.data_as(ctypes.c_void_p) if a is not None else None
+
+
+def _check(rc):
+    if rc != 0:
+        raise RuntimeError("oracle error %d: %s" % (rc, lib().orc_last_error().decode()))
+
+
+def set_threads(n):
+    return lib().orc_set_threads(int(n))
+
+
+def _pack_chain(factors, dtype):
+    """factors: list of scipy.sparse CSR matrices (sorted indices)."""
+    dims, rp, ci, vv = [], [], [], []
+    for f in factors:
+        f = f.tocsr()
+        f.sort_indices()
+        dims += [f.shape[0], f.shape[1], f.nnz]
+        rp.append(f.indptr.astype(np.int32))
+        ci.append(f.indices.astype(np.int32))
+        vv.append(f.data.astype(dtype))
+    cat = lambda xs, dt: np.ascontiguousarray(np.concatenate(xs) if xs else np.zeros(0, dt), dtype=dt)
+    return (np.asarray(dims, np.int32), cat(rp, np.int32), cat(ci, np.int32), cat(vv, dtype))
+
+
+def chain_mul(factors, X):
+    """Y = S_0 ... S_{J-1} X, right to left (Transform::multiply)."""
+    dtype = X.dtype
+    assert dtype in (np.float32, np.float64)
+    dims, rp, ci, vv = _pack_chain(factors, dtype)
+    Xf = np.asfortranarray(X)
+    Y = np.zeros((factors[0].shape[0], X.shape[1]), dtype=dtype, order="F")
+    fn = lib().orc_chain_mul_f64 if dtype == np.float64 else lib().orc_chain_mul_f32
+    _check(fn(len(factors), _p(dims), _p(rp), _p(ci), _p(vv), _p(Xf), X.shape[0], X.shape[1], _p(Y)))
+    return Y
+
+
+def bsr_mul_f64(m, n, bm, bn, browptr, bcolind, blocks, X):
+    """Y = B X in FP64 (BSRMat::mul); blocks is (bnnz, bm*bn) column-major per block."""
+    Xf = np.asfortranarray(X, dtype=np.float64)
+    Y = np.zeros((m, X.shape[1]), np.float64, order="F")
+    bp = np.ascontiguousarray(browptr, np.int32)
+    bc = np.ascontiguousarray(bcolind, np.int32)
+    bl = np.ascontiguousarray(blocks, np.float64)
+    _check(lib().orc_bsr_mul_f64(m, n, bm, bn, _p(bp), _p(bc), _p(bl), _p(Xf), Xf.shape[0], X.shape[1], _p(Y), m))
+    return Y
+
+
+def topk(v, k):
+    """Indices kept by sort_idx: std::partial_sort with comparator |a| > |b|."""
+    v = np.ascontiguousarray(v)
+    out = np.zeros(k, np.int32)
+    fn = lib().orc_topk_f64 if v.dtype == np.float64 else lib().orc_topk_f32
+    _check(fn(ctypes.c_long(v.size), _p(v), k, _p(out)))
+    return out
+
+
+def prox(kind, M, k=0, s=1.0, normalized=True, pos=False, supp=None):
+    M = np.array(M, order="F", copy=True)
+    sup = None if supp is None else np.asfortranarray(supp, dtype=M.dtype)
+    fn = lib().orc_prox_f64 if M.dtype == np.float64 else lib().orc_prox_f32
+    _check(fn(kind, ctypes.c_long(k), ctypes.c_double(s), int(normalized), int(pos), _p(M), M.shape[0], M.shape[1],
+              _p(sup)))
+    return M
+
+
+def spectral_norm(factors, max_iter=100, thr=1e-6):
+    dims, rp, ci, vv = _pack_chain(factors, np.float64)
+    out = ctypes.c_double()
+    flag = ctypes.c_int()
+    _check(lib().orc_spectral_norm_f64(len(factors), _p(dims), _p(rp), _p(ci), _p(vv), max_iter,
+                                       ctypes.c_double(thr), ctypes.byref(out), ctypes.byref(flag)))
+    return out.value, flag.value
+
+
+def rand_start(n):
+    out = np.zeros(n, np.float64)
+    _check(lib().orc_rand_start_f64(n, _p(out)))
+    return out
+
+
+def canonical_dot(a, b):
+    a = np.ascontiguousarray(a)
+    b = np.ascontiguousarray(b, dtype=a.dtype)
+    if a.dtype == np.float64:
+        out = ctypes.c_double()
+        _check(lib().orc_canonical_dot_f64(ctypes.c_long(a.size), _p(a), _p(b), ctypes.byref(out)))
+    else:
+        out = ctypes.c_float()
+        _check(lib().orc_canonical_dot_f32(ctypes.c_long(a.size), _p(a), _p(b), ctypes.byref(out)))
+    return out.value
+
+
+def _pack_cons(cons, dtype):
+    J = len(cons)
+    kind = np.array([c["kind"] for c in cons], np.int32)
+    k = np.array([c.get("k", 0) for c in cons], np.int64)
+    s = np.array([c.get("s", 1.0) for c in cons], np.float64)
+    flags = np.array(sum([[int(c.get("normalized", True)), int(c.get("pos", False))] for c in cons], []), np.int32)
+    cdims = np.array(sum([[c["rows"], c["cols"]] for c in cons], []), np.int32)
+    supps = [np.asfortranarray(c["supp"], dtype=dtype).ravel(order="F") for c in cons if c["kind"] == SUPP]
+    supp = np.ascontiguousarray(np.concatenate(supps) if supps else np.zeros(1, dtype), dtype=dtype)
+    return J, kind, k, s, flags, cdims, supp
+
+
+def palm4msa2(A, cons, nb_it, is_update_way_R2L=False, packing_RL=True, no_normalization=False, no_lambda=False,
+              norm2_threshold=1e-6, norm2_max_iter=100, constant_step_size=False, step_size=1e-16,
+              no_lambda_error=False, norm2_fp64=False, init_facts=None, init_lambda=1.0):
+    """palm4msa2 restatement.  cons: list of dicts(kind,k,s,normalized,pos,rows,cols,supp).
+
+    Returns (factors as dense column-major arrays, lambda, trace dict)."""
+    dtype = A.dtype
+    Af = np.asfortranarray(A)
+    J, kind, k, s, flags, cdims, supp = _pack_cons(cons, dtype)
+    p = PalmParams(nb_it, int(is_update_way_R2L), int(packing_RL), int(no_normalization), int(no_lambda),
+                   norm2_threshold, norm2_max_iter, int(constant_step_size), step_size, int(no_lambda_error),
+                   int(norm2_fp64))
+    sizes = [c["rows"] * c["cols"] for c in cons]
+    out = np.zeros(sum(sizes), dtype)
+    init = None
+    if init_facts is not None:
+        init = np.ascontiguousarray(np.concatenate([np.asfortranarray(f, dtype=dtype).ravel(order="F")
+                                                    for f in init_facts]))
+    lam = ctypes.c_double()
+    lambdas = np.zeros(max(nb_it, 1), np.float64)
+    cvals = np.zeros(max(nb_it * J, 1), np.float64)
+    niters = np.zeros(max(2 * nb_it * J, 1), np.int32)
+    tcase = np.full(max(nb_it * J, 1), -1, np.int32)
+    fn = lib().orc_palm4msa2_f64 if dtype == np.float64 else lib().orc_palm4msa2_f32
+    _check(fn(_p(Af), A.shape[0], A.shape[1], J, _p(kind), _p(k), _p(s), _p(flags), _p(cdims), _p(supp),
+              ctypes.byref(p), _p(init), ctypes.c_double(init_lambda), _p(out), ctypes.byref(lam), _p(lambdas),
+              _p(cvals), _p(niters), _p(tcase)))
+    facts, off = [], 0
+    for c, sz in zip(cons, sizes):
+        facts.append(out[off:off + sz].reshape((c["rows"], c["cols"]), order="F"))
+        off += sz
+    return facts, lam.value, {"lambdas": lambdas[:nb_it], "c": cvals[:nb_it * J], "norm_iters": niters,
+                               "topk_case": tcase[tcase >= 0]}
+
+
+def rel_err(A, facts, lam):
+    Af = np.asfortranarray(A, dtype=np.float64)
+    cd = np.array(sum([[f.shape[0], f.shape[1]] for f in facts], []), np.int32)
+    fl = np.ascontiguousarray(np.concatenate([np.asfortranarray(f, dtype=np.float64).ravel(order="F")
+                                              for f in facts]))
+    out = ctypes.c_double()
+    _check(lib().orc_rel_err_f64(_p(Af), A.shape[0], A.shape[1], len(facts), _p(cd), _p(fl), ctypes.c_double(lam),
+                                 ctypes.byref(out)))
+    return out.value

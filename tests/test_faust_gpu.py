@@ -1,0 +1,153 @@
+"""GPU parity of the Faust x dense path through the C ABI against the oracle.
+
+CSR chains are compared BIT FOR BIT (both sides use the same sequential fma
+order per output entry).  BSR (BF16 operands, FP32 accumulation) is compared
+against the FP64 oracle with a stated tolerance.
+"""
+import numpy as np
+import pytest
+
+from faust_gb300 import synth
+
+pytestmark = pytest.mark.gpu
+
+
+def _torch():
+    import torch
+    return torch
+
+
+def _colmajor_cuda(X):
+    torch = _torch()
+    return torch.from_numpy(np.ascontiguousarray(X.T)).cuda().t()
+
+
+def _to_np(Yt):
+    return Yt.t().contiguous().cpu().numpy().T
+
+
+@pytest.mark.parametrize("mode", [0, 1, 2])
+def test_csr_chain_config1_bitexact(fgb, oracle, mode):
+    """5 CSR 1024x1024 (10 nnz/row) FP64 factors x X 1024x512."""
+    rng = np.random.default_rng(11)
+    facs = [synth.random_csr(1024, 1024, 10, rng) for _ in range(5)]
+    X = synth.dense_colmajor(1024, 512, rng)
+    ref = oracle.chain_mul(facs, X)
+    F = fgb.Faust(facs)
+    Y = _to_np(F.matmul_device(_colmajor_cuda(X), mode=mode))
+    assert np.array_equal(Y, ref)
+    rel = np.linalg.norm(Y - ref) / np.linalg.norm(ref)
+    assert rel <= 1e-12
+
+
+def test_csr_chain_host_entry_point(fgb, oracle):
+    rng = np.random.default_rng(12)
+    facs = [synth.random_csr(300, 200, 7, rng), synth.random_csr(200, 450, 3, rng), synth.random_csr(450, 450, 9, rng)]
+    X = synth.dense_colmajor(450, 33, rng)
+    F = fgb.Faust(facs)
+    Y = F @ X
+    assert np.array_equal(Y, oracle.chain_mul(facs, X))
+
+
+@pytest.mark.parametrize("dtype", [np.float32, np.float64])
+@pytest.mark.parametrize("ncols", [1, 3, 8, 129])
+def test_csr_chain_ragged(fgb, oracle, dtype, ncols):
+    rng = np.random.default_rng(ncols)
+    dims = [64, 100, 37, 250, 64]
+    facs = []
+    for a, b in zip(dims[:-1], dims[1:]):
+        m = synth.random_csr(a, b, min(4, b), rng, dtype).tolil()
+        m[a // 2, :] = 0  # an empty row
+        facs.append(m.tocsr())
+    X = synth.dense_colmajor(dims[-1], ncols, rng, dtype)
+    F = fgb.Faust(facs, dtype=dtype)
+    ref = oracle.chain_mul(facs, X)
+    for mode in (0, 1):
+        Y = _to_np(F.matmul_device(_colmajor_cuda(X), mode=mode))
+        assert np.array_equal(Y, ref)
+
+
+def test_csr_butterfly_fp32_bitexact(fgb, oracle):
+    rng = np.random.default_rng(13)
+    facs = synth.butterfly_faust_factors(10, rng, np.float32)
+    X = synth.dense_colmajor(1024, 256, rng, np.float32)
+    F = fgb.Faust(facs)
+    ref = oracle.chain_mul(facs, X)
+    for mode in (0, 1):
+        assert np.array_equal(_to_np(F.matmul_device(_colmajor_cuda(X), mode=mode)), ref)
+
+
+def test_csr_butterfly_config3b_column_subset(fgb, oracle):
+    """Full size (12 factors of 4096^2, X 4096 x 8192 FP32): columns of Y
+    depend only on the same columns of X, so a column subset is checked
+    bit for bit against the oracle."""
+    torch = _torch()
+    rng = np.random.default_rng(14)
+    facs = synth.butterfly_faust_factors(12, rng, np.float32)
+    F = fgb.Faust(facs)
+    g = torch.Generator(device="cuda").manual_seed(0)
+    Xt = torch.randn((8192, 4096), generator=g, device="cuda", dtype=torch.float32).t()
+    Yt = F.matmul_device(Xt)
+    cols = [0, 1, 7, 4095, 4096, 8191]
+    Xs = Xt[:, cols].t().contiguous().cpu().numpy().T
+    ref = oracle.chain_mul(facs, np.asfortranarray(Xs))
+    got = Yt[:, cols].t().contiguous().cpu().numpy().T
+    assert np.array_equal(got, ref)
+
+
+def _bsr_factors(fgb, n, nfac, rng):
+    sigma = 1.0 / np.sqrt(8 * 64)
+    out, f32 = [], []
+    for _ in range(nfac):
+        bp, bc, blocks = synth.random_bsr(n, 64, 8 if n >= 512 else 2, rng, sigma)
+        bits = synth.bf16_bits(blocks)
+        out.append(fgb.BSRFactor(n, n, bp, bc, bits))
+        f32.append((bp, bc, synth.bf16_to_f32(bits).reshape(blocks.shape)))
+    return out, f32
+
+
+def _oracle_bsr_chain(oracle, n, f32, X, round_bf16):
+    Y = X.astype(np.float64)
+    for bp, bc, blocks in reversed(f32):
+        flat = np.ascontiguousarray(blocks.transpose(0, 2, 1).reshape(len(bc), -1), np.float64)
+        Y = oracle.bsr_mul_f64(n, n, 64, 64, bp, bc, flat, Y)
+        if round_bf16:
+            Y = synth.bf16_to_f32(synth.bf16_bits(Y.astype(np.float32))).reshape(Y.shape).astype(np.float64)
+    return Y
+
+
+@pytest.mark.parametrize("n,ncols", [(512, 256), (1024, 384)])
+def test_bsr_chain_bf16(fgb, oracle, n, ncols):
+    """BF16 blocks, FP32 accumulation; tolerance: 1e-2 relative Frobenius
+    against the FP64 oracle with BF16 rounding of each intermediate product
+    (the kernel stores intermediates in BF16), which bounds FP32-vs-FP64
+    accumulation plus one BF16 rounding per factor."""
+    torch = _torch()
+    rng = np.random.default_rng(n)
+    facs, f32 = _bsr_factors(fgb, n, 3, rng)
+    F = fgb.Faust(facs)
+    X = rng.standard_normal((n, ncols)).astype(np.float32)
+    Xb = synth.bf16_to_f32(synth.bf16_bits(X)).reshape(X.shape)
+    Xt = torch.from_numpy(np.ascontiguousarray(Xb.T)).to(torch.bfloat16).cuda().t()
+    Yt = F.matmul_device(Xt)
+    Y = Yt.t().float().cpu().numpy().T.astype(np.float64)
+    ref = _oracle_bsr_chain(oracle, n, f32, Xb, round_bf16=True)
+    rel = np.linalg.norm(Y - ref) / np.linalg.norm(ref)
+    assert rel < 1e-2, rel
+
+
+def test_spectral_norm_matches_oracle(fgb, oracle):
+    rng = np.random.default_rng(21)
+    facs = [synth.random_csr(128, 128, 5, rng) for _ in range(4)]
+    F = fgb.Faust(facs)
+    got = F.norm(2, max_iter=200, threshold=1e-10)
+    ref, _ = oracle.spectral_norm(facs, max_iter=200, thr=1e-10)
+    assert got == ref
+
+
+def test_invalid_factor_is_rejected(fgb):
+    import scipy.sparse as sp
+    m = sp.csr_matrix(np.eye(4))
+    m.indices[1] = 7  # column out of range
+    with pytest.raises(Exception):
+        fgb.Faust([m])
