@@ -264,6 +264,133 @@ def cpu_baseline_faust_x(W, sample_cols=None):
             "sample": "%d of %d columns of X, %d repetitions" % (cols, W.ncols, reps)}
 
 
+# ---------------------------------------------------------------- PALM4MSA
+PALM_N, PALM_J, PALM_K, PALM_ITS, PALM_THR = 1024, 10, 2048, 200, 1e-8
+
+
+def _palm_problem():
+    from faust_gb300 import fact, synth
+    H = synth.hadamard(PALM_N) / 32.0
+    cons = [fact.ConstraintInt("sp", PALM_N, PALM_N, PALM_K) for _ in range(PALM_J)]
+    params = fact.ParamsPalm4MSA(cons, PALM_ITS, norm2_threshold=PALM_THR, norm2_max_iter=100)
+    return H, cons, params
+
+
+def run_palm(args, rank, world):
+    import ctypes
+    import torch
+    import faust_gb300 as fg
+    from faust_gb300 import _ffi, fact
+    torch.cuda.set_device(rank % max(1, torch.cuda.device_count()))
+    H, cons, params = _palm_problem()
+    ctx = fg.Context(torch.cuda.current_device())
+    Hd = torch.from_numpy(np.ascontiguousarray(H.T)).cuda().t()  # column-major, device resident
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    res = None
+    for _ in range(args.warmup):
+        res = fact.palm4msa(Hd, cons, params, ctx=ctx)
+        res.faust.close()
+    torch.cuda.synchronize()
+    _barrier(world)
+    times = []
+    launches0 = ctx.kernel_launches()
+    with ClockSampler(torch.cuda.current_device()) as clk:
+        for _ in range(args.steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            res = fact.palm4msa(Hd, cons, params, ctx=ctx)
+            times.append(time.perf_counter() - t0)
+            if _ != args.steps - 1:
+                res.faust.close()
+    launches = (ctx.kernel_launches() - launches0) // max(1, args.steps)
+    step_s = float(np.mean(times))
+    step_s = _max_over_ranks(step_s, world)
+    # relative error of the result (outside the timed region)
+    err = ctypes.c_double()
+    _ffi.check(_ffi.lib().fgb_rel_err(res.faust.handle, Hd.data_ptr(), res.lambda_, ctypes.byref(err)), ctx.handle)
+    res.faust.close()
+    # end to end through the host-memory C-ABI entry point: A from host
+    # memory in, every factor back to host memory
+    Hh = np.asfortranarray(H)
+    e2e = []
+    d2h = 0
+    for _ in range(max(2, min(args.steps, 3))):
+        t0 = time.perf_counter()
+        r = fact.palm4msa(Hh, cons, params, ctx=ctx)
+        facs = [r.faust.factors(i) for i in range(PALM_J)]
+        e2e.append(time.perf_counter() - t0)
+        d2h = sum(f.nnz * 12 + (f.shape[0] + 1) * 4 for f in facs)
+        r.faust.close()
+    e2e_s = float(np.median(e2e))
+    hbm, tflops, peak_kind = _peaks()
+    roof = palm_roofline(ctx, hbm, peak_kind)
+    out = {
+        "metric": METRIC, "submetric": "palm4msa2 FP64 time to the plain 200-iteration relative error (s per run)",
+        "value": round(step_s, 5), "unit": "s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(step_s * 1e3, 3), "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64", "data": "synthetic (Sylvester Hadamard 1024 / 32)",
+        "config": {"workload": "palm4msa2 Hadamard 1024/32, 10 factors sp k=2048, identity init, 200 its, "
+                               "power-iteration tol 1e-8 (max 100), FP64",
+                   "l2": "flushed (256 MB write) before every timed run", "rel_err": err.value,
+                   "lambda": res.lambda_},
+        "roofline": roof,
+        "e2e": {"value": round(e2e_s, 5), "unit": "s", "h2d_bytes_per_step": int(H.nbytes),
+                "d2h_bytes_per_step": int(d2h)},
+        "gpu_launches": int(launches),
+        "clocks": clk.summary(),
+    }
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        out["cpu_baseline"] = cpu_baseline_palm()
+    return out
+
+
+def palm_roofline(ctx, hbm, peak_kind):
+    """The sparse x dense product of the PALM gradient chain (k_csr_spmm on a
+    1024 x 1024 FP64 factor with 2048 entries times a dense 1024 x 1024
+    block), timed alone with CUDA events over repeated launches."""
+    import torch
+    import faust_gb300 as fg
+    from faust_gb300 import synth
+    rng = np.random.default_rng(3)
+    import scipy.sparse as sp
+    S = sp.random(PALM_N, PALM_N, density=PALM_K / PALM_N ** 2, random_state=3, format="csr")
+    S.sort_indices()
+    F = fg.Faust([S], ctx=ctx)
+    X = torch.randn((PALM_N, PALM_N), device="cuda", dtype=torch.float64).t()
+    Y = torch.empty((PALM_N, PALM_N), device="cuda", dtype=torch.float64).t()
+    for _ in range(5):
+        F.matmul_device(X, Y, mode=1)
+    s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    reps = 200
+    s.record()
+    for _ in range(reps):
+        F.matmul_device(X, Y, mode=1)
+    e.record()
+    torch.cuda.synchronize()
+    us = s.elapsed_time(e) * 1e3 / reps
+    nbytes = 2 * PALM_N * PALM_N * 8 + S.nnz * 12 + (PALM_N + 1) * 4
+    achieved = nbytes / (us * 1e-6) / 1e9
+    F.close()
+    return {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
+            "frac": round(achieved / hbm, 4), "traffic": None, "peak_kind": peak_kind,
+            "kernel": "k_csr_spmm (PALM gradient product, 1024^2 FP64, 2048 nnz)",
+            "algorithmic_bytes_per_launch": int(nbytes), "us_per_launch": round(us, 3),
+            "note": "operands are L2-resident (16 MB), so achieved can exceed HBM bandwidth"}
+
+
+def cpu_baseline_palm(its=5):
+    from oracle import oracle as O
+    H, cons, params = _palm_problem()
+    threads = os.cpu_count() or 1
+    O.set_threads(threads)
+    t0 = time.perf_counter()
+    O.palm4msa2(H, [c.oracle_dict() for c in cons], its, norm2_threshold=PALM_THR, norm2_max_iter=100)
+    dt = time.perf_counter() - t0
+    return {"value": round(dt * PALM_ITS / its, 3), "unit": "s", "cores": threads, "kind": "port",
+            "sample": "%d of %d iterations timed (%.2f s), scaled to the full run" % (its, PALM_ITS, dt)}
+
+
 # ---------------------------------------------------------------- helpers
 def _barrier(world):
     if world > 1:
@@ -287,7 +414,7 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="csr_butterfly", choices=["csr_butterfly", "csr_random", "bsr"])
+    ap.add_argument("--workload", default="palm", choices=["palm", "csr_butterfly", "csr_random", "bsr"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
@@ -302,7 +429,7 @@ def main():
             out = reference_arm(args, world)
             print(json.dumps(out), flush=True)
         return
-    out = run_faust_x(args, rank, world)
+    out = run_palm(args, rank, world) if args.workload == "palm" else run_faust_x(args, rank, world)
     if rank == 0:
         print(json.dumps(out), flush=True)
     if world > 1:
@@ -313,6 +440,17 @@ def main():
 def reference_arm(args, world):
     import faust_gb300.synth  # noqa: F401  (generators only)
     rng = np.random.default_rng(2024)
+    if args.workload == "palm":
+        vals = [cpu_baseline_palm(its=3) for _ in range(max(1, args.steps))]
+        v = float(np.median([x["value"] for x in vals]))
+        cb = dict(vals[0])
+        cb["value"] = v
+        return {"impl": "reference", "metric": METRIC, "value": v, "unit": "s", "n_gpus": world,
+                "steps": args.steps, "warmup": args.warmup, "higher_is_better": False,
+                "config": {"workload": "palm4msa2 Hadamard 1024/32, 10 factors sp k=2048, identity init, 200 its, "
+                                       "power-iteration tol 1e-8 (max 100), FP64"},
+                "cpu_baseline": cb,
+                "e2e": {"value": v, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
     class _W:
         pass

@@ -1,12 +1,431 @@
-// bsr_tc.cu — BSR x dense on the tcgen05 tensor cores (placeholder until the
-// TMEM kernel lands: declines every shape).
+// bsr_tc.cu — BSR x dense on the 5th-generation tensor cores (tcgen05, TMEM
+// accumulators, TMA-fed shared memory), BF16 operands, FP32 accumulation.
+//
+// BSRMat::mul (faust_MatBSR.hpp:827-836): Y(block row r) = sum over the
+// stored blocks (r, c) of B_rc X(block row c).  The kernel computes Y^T tiles:
+// for a tile of 128 columns j of X and one block row r,
+//    D[j, y] = sum_blocks sum_c X[64*bc + c, j] * B[y, c]      (M=128, N=64)
+// so the MMA's A operand is a 128 x 64 slab of X (its columns are contiguous
+// in the column-major X: K-major, loaded by TMA with 128-byte swizzle) and the
+// B operand is one 64 x 64 block stored row by row on the device (K-major,
+// also TMA-loaded).  Each block contributes four K=16 MMAs; the 128 x 64 FP32
+// accumulator lives in TMEM (four buffers rotate so the epilogue of one item
+// overlaps the MMAs of the next).
+//
+// Warp roles (192 threads): warp 0 issues TMA loads, warp 1 issues MMAs (one
+// lane), warps 2-5 drain TMEM (tcgen05.ld), convert to BF16 and store Y.
+// Persistent grid (one CTA per SM); work items (column tile, block row) are
+// ordered column tile major so the CTAs in flight share the same X columns
+// in L2.  Every mbarrier wait is bounded: on expiry the CTA records an error,
+// stops issuing, waits (bounded) for its own copies, frees TMEM and returns.
+#include <cuda.h>
+
+#include <algorithm>
+#include <cstring>
+
 #include "fgb_internal.cuh"
 
 namespace fgb {
-fgb_status launch_bsr_tc(fgb_ctx* ctx, const DevFactor& f, const __nv_bfloat16* X, int ldx, int ncols,
-                         __nv_bfloat16* Y, int ldy, bool* taken) {
-  (void)ctx; (void)f; (void)X; (void)ldx; (void)ncols; (void)Y; (void)ldy;
-  *taken = false;
+
+namespace tc {
+
+constexpr int BLK = 64;         // BSR block size
+constexpr int TM = 128;         // columns of X per tile (MMA M)
+constexpr int STAGES = 6;
+constexpr int A_BYTES = TM * BLK * 2;   // 16 KB
+constexpr int B_BYTES = BLK * BLK * 2;  // 8 KB
+constexpr int STAGE_BYTES = A_BYTES + B_BYTES;
+constexpr int ACC_BUFS = 4;
+constexpr int TMEM_COLS = ACC_BUFS * BLK;  // 256
+constexpr int THREADS = 192;
+constexpr unsigned WAIT_LIMIT = 1u << 22;
+
+__device__ __forceinline__ uint32_t su32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(su32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(su32(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(su32(bar)) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n"
+      " .reg .pred p;\n"
+      " mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      " selp.u32 %0, 1, 0, p;\n"
+      "}\n"
+      : "=r"(ok)
+      : "r"(su32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// Bounded wait: false when the limit ran out or another role aborted.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, volatile int* abort_flag) {
+  for (unsigned i = 0; i < WAIT_LIMIT; ++i) {
+    if (mbar_try_wait(bar, parity)) return true;
+    if (*abort_flag) return false;
+  }
+  return false;
+}
+
+__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, int c0, int c1, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
+          su32(dst)),
+      "l"(map), "r"(c0), "r"(c1), "r"(su32(bar))
+      : "memory");
+}
+
+__device__ __forceinline__ void fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+// Shared-memory matrix descriptor: K-major tile with 128-byte swizzle, rows
+// of 128 bytes, 8-row groups 1024 bytes apart (tile base 1024-byte aligned).
+__device__ __forceinline__ uint64_t sdesc_k128(uint32_t saddr) {
+  uint64_t d = 0;
+  d |= (uint64_t)((saddr & 0x3FFFFu) >> 4);  // start address
+  d |= (uint64_t)1 << 16;                     // leading byte offset (unused with this swizzle)
+  d |= (uint64_t)(1024 >> 4) << 32;           // stride byte offset: 8 rows x 128 B
+  d |= (uint64_t)1 << 46;                     // descriptor version
+  d |= (uint64_t)2 << 61;                     // 128-byte swizzle
+  return d;
+}
+
+// Instruction descriptor of kind::f16: D F32, A and B BF16, both K-major,
+// N = 64, M = 128.
+constexpr uint32_t IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BLK >> 3) << 17) |
+                           ((uint32_t)(TM >> 4) << 24);
+
+__device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t accumulate) {
+  asm volatile(
+      "{\n"
+      " .reg .pred p;\n"
+      " setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n"
+      "}\n" ::"r"(d_tmem),
+      "l"(adesc), "l"(bdesc), "r"(IDESC), "r"(accumulate)
+      : "memory");
+}
+__device__ __forceinline__ void mma_commit(uint64_t* bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(su32(bar))
+               : "memory");
+}
+
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+      "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+      "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+        "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+        "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(taddr));
+}
+__device__ __forceinline__ void tmem_ld_wait() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+
+__device__ __forceinline__ uint32_t pack_bf16(uint32_t lo, uint32_t hi) {
+  const __nv_bfloat162 v = __floats2bfloat162_rn(__uint_as_float(lo), __uint_as_float(hi));
+  return *reinterpret_cast<const uint32_t*>(&v);
+}
+
+struct Shared {
+  uint64_t full[STAGES];
+  uint64_t empty[STAGES];
+  uint64_t acc_full[ACC_BUFS];
+  uint64_t acc_empty[ACC_BUFS];
+  uint32_t tmem_base;
+  int abort_flag;
+};
+
+__global__ void __launch_bounds__(THREADS, 1)
+    k_bsr_tc(const __grid_constant__ CUtensorMap tmX, const __grid_constant__ CUtensorMap tmB,
+             const int* __restrict__ browptr, const int* __restrict__ bcolind, int nbr, int mtiles,
+             __nv_bfloat16* __restrict__ Y, long ldy, int* __restrict__ err) {
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  // stage buffers start at a 1024-byte boundary (128-byte swizzle atoms)
+  unsigned char* base = reinterpret_cast<unsigned char*>(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  Shared* sh = reinterpret_cast<Shared*>(base + STAGES * STAGE_BYTES);
+  const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+  const long items = (long)mtiles * nbr;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < STAGES; ++s) {
+      mbar_init(&sh->full[s], 1);
+      mbar_init(&sh->empty[s], 1);
+    }
+    for (int a = 0; a < ACC_BUFS; ++a) {
+      mbar_init(&sh->acc_full[a], 1);
+      mbar_init(&sh->acc_empty[a], 4);
+    }
+    sh->abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(su32(&sh->tmem_base)),
+                 "r"((uint32_t)TMEM_COLS));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  fence_before();
+  __syncthreads();
+  fence_after();
+  const uint32_t tmem = sh->tmem_base;
+  volatile int* abort_flag = &sh->abort_flag;
+
+  if (warp == 0) {
+    // ---------------------------------------------------------------- producer
+    if (lane == 0) {
+      int s = 0;
+      uint32_t ph = 0;
+      long issued = 0, waited_ok = 1;
+      int pend[STAGES];  // parity of the last load issued into each stage, or -1
+      for (int u = 0; u < STAGES; ++u) pend[u] = -1;
+      for (long it = blockIdx.x; it < items && waited_ok; it += gridDim.x) {
+        const int mt = (int)(it / nbr), br = (int)(it % nbr);
+        const int p0 = browptr[br], p1 = browptr[br + 1];
+        for (int p = p0; p < p1; ++p) {
+          if (!mbar_wait(&sh->empty[s], ph ^ 1u, abort_flag)) {
+            waited_ok = 0;
+            break;
+          }
+          unsigned char* st = base + s * STAGE_BYTES;
+          mbar_expect_tx(&sh->full[s], STAGE_BYTES);
+          tma_load_2d(st, &tmX, bcolind[p] * BLK, mt * TM, &sh->full[s]);
+          tma_load_2d(st + A_BYTES, &tmB, 0, p * BLK, &sh->full[s]);
+          pend[s] = (int)ph;
+          ++issued;
+          if (++s == STAGES) {
+            s = 0;
+            ph ^= 1u;
+          }
+        }
+      }
+      if (!waited_ok) {
+        atomicExch(err, 1);
+        *abort_flag = 1;
+      }
+      // on an abort, the copies this thread issued must land before the
+      // shared memory is released (bounded waits)
+      if (*abort_flag)
+        for (int u = 0; u < STAGES; ++u)
+          if (pend[u] >= 0)
+            for (unsigned i = 0; i < WAIT_LIMIT && !mbar_try_wait(&sh->full[u], (uint32_t)pend[u]); ++i) {
+            }
+      (void)issued;
+    }
+  } else if (warp == 1) {
+    // ---------------------------------------------------------------- MMA issuer
+    if (lane == 0) {
+      int s = 0, a = 0;
+      uint32_t ph = 0, aph = 0;
+      bool ok = true;
+      for (long it = blockIdx.x; it < items && ok; it += gridDim.x) {
+        const int br = (int)(it % nbr);
+        const int p0 = browptr[br], p1 = browptr[br + 1];
+        if (p1 == p0) continue;  // empty block row: the epilogue writes zeros
+        if (!mbar_wait(&sh->acc_empty[a], aph ^ 1u, abort_flag)) {
+          ok = false;
+          break;
+        }
+        fence_after();
+        const uint32_t d = tmem + (uint32_t)(a * BLK);
+        for (int p = p0; p < p1; ++p) {
+          if (!mbar_wait(&sh->full[s], ph, abort_flag)) {
+            ok = false;
+            break;
+          }
+          fence_after();
+          const uint32_t sa = su32(base + s * STAGE_BYTES), sb = sa + A_BYTES;
+          const uint64_t ad = sdesc_k128(sa), bd = sdesc_k128(sb);
+#pragma unroll
+          for (int k = 0; k < BLK / 16; ++k)
+            mma_bf16(d, ad + (uint64_t)((k * 32) >> 4), bd + (uint64_t)((k * 32) >> 4), (p > p0 || k > 0) ? 1u : 0u);
+          mma_commit(&sh->empty[s]);
+          if (++s == STAGES) {
+            s = 0;
+            ph ^= 1u;
+          }
+        }
+        if (!ok) break;
+        mma_commit(&sh->acc_full[a]);
+        if (++a == ACC_BUFS) {
+          a = 0;
+          aph ^= 1u;
+        }
+      }
+      if (!ok) {
+        atomicExch(err, 1);
+        *abort_flag = 1;
+      }
+    }
+  } else {
+    // ---------------------------------------------------------------- epilogue
+    const int q = warp & 3;  // TMEM lane quadrant this warp may access
+    int a = 0;
+    uint32_t aph = 0;
+    bool ok = true;
+    for (long it = blockIdx.x; it < items && ok; it += gridDim.x) {
+      const int mt = (int)(it / nbr), br = (int)(it % nbr);
+      const int p0 = browptr[br], p1 = browptr[br + 1];
+      const long j = (long)mt * TM + q * 32 + lane;
+      uint4* dst = reinterpret_cast<uint4*>(Y + j * ldy + (long)br * BLK);
+      if (p1 == p0) {
+        const uint4 z = make_uint4(0, 0, 0, 0);
+#pragma unroll
+        for (int u = 0; u < 8; ++u) dst[u] = z;
+        continue;
+      }
+      bool got = true;
+      if (lane == 0) got = mbar_wait(&sh->acc_full[a], aph, abort_flag);
+      got = __shfl_sync(0xffffffffu, got ? 1 : 0, 0) != 0;
+      if (!got) {
+        ok = false;
+        break;
+      }
+      fence_after();
+      uint32_t r[32];
+      uint32_t packed[32];
+      const uint32_t taddr = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(a * BLK);
+      tmem_ld32(taddr, r);
+      tmem_ld_wait();
+#pragma unroll
+      for (int u = 0; u < 16; ++u) packed[u] = pack_bf16(r[2 * u], r[2 * u + 1]);
+      tmem_ld32(taddr + 32, r);
+      tmem_ld_wait();
+#pragma unroll
+      for (int u = 0; u < 16; ++u) packed[16 + u] = pack_bf16(r[2 * u], r[2 * u + 1]);
+      fence_before();
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&sh->acc_empty[a]);
+#pragma unroll
+      for (int u = 0; u < 8; ++u)
+        dst[u] = make_uint4(packed[4 * u], packed[4 * u + 1], packed[4 * u + 2], packed[4 * u + 3]);
+      if (++a == ACC_BUFS) {
+        a = 0;
+        aph ^= 1u;
+      }
+    }
+    if (!ok && lane == 0) {
+      atomicExch(err, 1);
+      *abort_flag = 1;
+    }
+  }
+  fence_before();
+  __syncthreads();
+  fence_after();
+  __syncwarp();
+  if (warp == 1) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"((uint32_t)TMEM_COLS));
+}
+
+// Re-lays a column-major block (the ABI's storage) out row by row, the
+// K-major operand layout of the kernel.
+__global__ void k_blocks_rowmajor(const __nv_bfloat16* __restrict__ in, __nv_bfloat16* __restrict__ out, long nblk) {
+  for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < nblk * BLK * BLK; e += (long)gridDim.x * blockDim.x) {
+    const long p = e / (BLK * BLK);
+    const int w = (int)(e % (BLK * BLK));
+    const int r = w / BLK, c = w % BLK;
+    out[e] = in[p * BLK * BLK + (long)c * BLK + r];
+  }
+}
+
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+static EncodeTiledFn encode_fn() {
+  static EncodeTiledFn fn = nullptr;
+  static bool tried = false;
+  if (!tried) {
+    tried = true;
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPoint("cuTensorMapEncodeTiled", &p, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = (EncodeTiledFn)p;
+    cudaGetLastError();
+  }
+  return fn;
+}
+
+static bool make_map(CUtensorMap* m, const void* base, uint64_t inner, uint64_t outer, uint64_t row_bytes,
+                     uint32_t box_inner, uint32_t box_outer) {
+  EncodeTiledFn fn = encode_fn();
+  if (!fn) return false;
+  cuuint64_t dims[2] = {inner, outer};
+  cuuint64_t strides[1] = {row_bytes};
+  cuuint32_t box[2] = {box_inner, box_outer};
+  cuuint32_t es[2] = {1, 1};
+  return fn(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(base), dims, strides, box, es,
+            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+}  // namespace tc
+
+// Row-major copy of a factor's blocks (the kernel's K-major operand), built
+// when the factor is uploaded.
+fgb_status bsr_tc_prepare(fgb_ctx* ctx, DevFactor& f) {
+  if (f.format != FGB_BSR || f.bm != tc::BLK || f.bn != tc::BLK || f.nnz == 0) return FGB_OK;
+  FGB_TRY(dmalloc(ctx, &f.aux, (size_t)f.nnz * tc::BLK * tc::BLK * 2));
+  tc::k_blocks_rowmajor<<<2 * ctx->sm_count, 256, 0, ctx->stream>>>((const __nv_bfloat16*)f.val,
+                                                                   (__nv_bfloat16*)f.aux, (long)f.nnz);
+  FGB_LAUNCHED(ctx);
   return FGB_OK;
 }
+
+static int* g_err = nullptr;
+
+fgb_status launch_bsr_tc(fgb_ctx* ctx, const DevFactor& f, const __nv_bfloat16* X, int ldx, int ncols,
+                         __nv_bfloat16* Y, int ldy, bool* taken) {
+  *taken = false;
+  if (getenv("FGB_BSR_SIMT")) return FGB_OK;
+  // shapes the kernel takes: 64 x 64 blocks, whole 128-column tiles,
+  // 16-byte aligned rows and bases
+  if (f.bm != 64 || f.bn != 64 || f.nnz == 0) return FGB_OK;
+  if (ncols % tc::TM || ldx % 8 || ldy % 8) return FGB_OK;
+  if (((uintptr_t)X & 15) || ((uintptr_t)Y & 15)) return FGB_OK;
+  const size_t smem = tc::STAGES * tc::STAGE_BYTES + sizeof(tc::Shared) + 1024;
+  if (smem > ctx->smem_optin) return FGB_OK;
+  const __nv_bfloat16* blocks = (const __nv_bfloat16*)f.aux;
+  if (!blocks) return FGB_OK;
+  CUtensorMap mx, mb;
+  if (!tc::make_map(&mx, X, (uint64_t)f.cols, (uint64_t)ncols, (uint64_t)ldx * 2, tc::BLK, tc::TM)) return FGB_OK;
+  if (!tc::make_map(&mb, blocks, (uint64_t)tc::BLK, (uint64_t)f.nnz * tc::BLK, tc::BLK * 2, tc::BLK, tc::BLK))
+    return FGB_OK;
+  if (!g_err) {
+    FGB_TRY(dmalloc(ctx, (void**)&g_err, sizeof(int)));
+    FGB_CUDA(ctx, cudaMemset(g_err, 0, sizeof(int)));
+  }
+  static bool attr = false;
+  if (!attr) {
+    FGB_CUDA(ctx, cudaFuncSetAttribute(tc::k_bsr_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    attr = true;
+  }
+  const int nbr = f.rows / tc::BLK, mtiles = ncols / tc::TM;
+  const long items = (long)nbr * mtiles;
+  const int grid = (int)std::min<long>(items, ctx->sm_count);
+  tc::k_bsr_tc<<<grid, tc::THREADS, smem, ctx->stream>>>(mx, mb, f.rowptr, f.colind, nbr, mtiles, Y, (long)ldy, g_err);
+  FGB_LAUNCHED(ctx);
+  *taken = true;
+  return FGB_OK;
+}
+
+// Error flag of the tensor-core kernel (a bounded wait ran out); cleared on read.
+fgb_status bsr_tc_status(fgb_ctx* ctx) {
+  if (!g_err) return FGB_OK;
+  int h = 0;
+  FGB_CUDA(ctx, cudaMemcpyAsync(&h, g_err, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  FGB_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  if (h) {
+    FGB_CUDA(ctx, cudaMemset(g_err, 0, sizeof(int)));
+    return fail(ctx, FGB_ERR_TIMEOUT, "BSR tensor-core kernel: a bounded wait ran out");
+  }
+  return FGB_OK;
+}
+
 }  // namespace fgb

@@ -173,8 +173,25 @@ fgb_status launch_dense_csrT(fgb_ctx* ctx, const T* X, int ldx, int xrows, const
 // turn, right to left, with the intermediate tile kept in shared memory
 // (two buffers of maxdim x TC).  Only X is read from HBM and only Y written;
 // the factors are read from L2 by every block.
+constexpr int CHAIN_THREADS = 1024;
+
 template <typename T, int TC>
-__global__ void __launch_bounds__(SPMM_THREADS)
+__device__ __forceinline__ void chain_row(const ChainDesc& d, const T* __restrict__ val, const T* __restrict__ in,
+                                          int i, T (&acc)[TC]) {
+#pragma unroll
+  for (int t = 0; t < TC; ++t) acc[t] = T(0);
+  const int p1 = __ldg(d.rowptr + i + 1);
+  for (int p = __ldg(d.rowptr + i); p < p1; ++p) {
+    const T v = __ldg(val + p);
+    T x[TC];
+    load_row<T, TC>(in + (long)__ldg(d.colind + p) * TC, x);
+#pragma unroll
+    for (int t = 0; t < TC; ++t) acc[t] = fmad(v, x[t], acc[t]);
+  }
+}
+
+template <typename T, int TC>
+__global__ void __launch_bounds__(CHAIN_THREADS)
     k_csr_chain_fused(const ChainDesc* __restrict__ desc, int nfac, const T* __restrict__ X, int ldx, int ncols,
                       T* __restrict__ Y, int ldy, int maxdim) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -189,25 +206,25 @@ __global__ void __launch_bounds__(SPMM_THREADS)
     const ChainDesc d = desc[f];
     const T* __restrict__ val = reinterpret_cast<const T*>(d.val);
     const bool last = (f == 0);
-    for (int i = threadIdx.x; i < d.rows; i += blockDim.x) {
-      T acc[TC];
-#pragma unroll
-      for (int t = 0; t < TC; ++t) acc[t] = T(0);
-      const int p1 = d.rowptr[i + 1];
-      for (int p = d.rowptr[i]; p < p1; ++p) {
-        const T v = val[p];
-        T x[TC];
-        load_row<T, TC>(in + (long)d.colind[p] * TC, x);
-#pragma unroll
-        for (int t = 0; t < TC; ++t) acc[t] = fmad(v, x[t], acc[t]);
-      }
+    // two rows per pass: independent load chains
+    for (int i = threadIdx.x; i < d.rows; i += 2 * blockDim.x) {
+      const int i2 = i + blockDim.x;
+      T a1[TC], a2[TC];
+      chain_row<T, TC>(d, val, in, i, a1);
+      if (i2 < d.rows) chain_row<T, TC>(d, val, in, i2, a2);
       if (last) {
 #pragma unroll
         for (int t = 0; t < TC; ++t)
-          if (j0 + t < ncols) Y[i + (long)(j0 + t) * ldy] = acc[t];
+          if (j0 + t < ncols) {
+            Y[i + (long)(j0 + t) * ldy] = a1[t];
+            if (i2 < d.rows) Y[i2 + (long)(j0 + t) * ldy] = a2[t];
+          }
       } else {
 #pragma unroll
-        for (int t = 0; t < TC; ++t) out[(long)i * TC + t] = acc[t];
+        for (int t = 0; t < TC; ++t) {
+          out[(long)i * TC + t] = a1[t];
+          if (i2 < d.rows) out[(long)i2 * TC + t] = a2[t];
+        }
       }
     }
     __syncthreads();
@@ -224,7 +241,7 @@ static fgb_status launch_chain_tc(fgb_ctx* ctx, const ChainDesc* d_desc, int nfa
   auto kern = k_csr_chain_fused<T, TC>;
   if (smem > 48 * 1024) FGB_CUDA(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   const int tiles = (ncols + TC - 1) / TC;
-  kern<<<tiles, SPMM_THREADS, smem, ctx->stream>>>(d_desc, nfac, X, ldx, ncols, Y, ldy, maxdim);
+  kern<<<tiles, CHAIN_THREADS, smem, ctx->stream>>>(d_desc, nfac, X, ldx, ncols, Y, ldy, maxdim);
   FGB_LAUNCHED(ctx);
   return FGB_OK;
 }

@@ -74,15 +74,9 @@ fgb_status fgb_ctx_create(int device, void* cuda_stream, fgb_ctx** out) {
   int optin = 0;
   cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device);
   ctx->smem_optin = (size_t)optin;
-  if (cuda_stream) {
-    ctx->stream = (cudaStream_t)cuda_stream;
-  } else {
-    if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) {
-      delete ctx;
-      return FGB_ERR_CUDA;
-    }
-    ctx->own_stream = true;
-  }
+  // The caller's stream is used as given; NULL is the legacy default stream.
+  ctx->stream = (cudaStream_t)cuda_stream;
+  ctx->own_stream = false;
   void* hp = nullptr;
   if (cudaHostAlloc(&hp, sizeof(int), cudaHostAllocMapped) == cudaSuccess) {
     ctx->cancel_host = (volatile int*)hp;

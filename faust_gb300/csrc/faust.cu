@@ -12,7 +12,10 @@ fgb_status chain_fused(fgb_ctx* ctx, fgb_dtype dt, const ChainDesc* d_desc, int 
 fgb_status launch_bsr_spmm(fgb_ctx* ctx, const DevFactor& f, const __nv_bfloat16* X, int ldx, int ncols,
                            __nv_bfloat16* Y, int ldy);
 
+fgb_status bsr_tc_prepare(fgb_ctx* ctx, DevFactor& f);
+
 void free_factor(DevFactor& f) {
+  dfree(f.aux);
   dfree(f.rowptr);
   dfree(f.colind);
   dfree(f.val);
@@ -49,6 +52,7 @@ static fgb_status upload_factor(fgb_ctx* ctx, fgb_dtype dt, const fgb_factor_des
     FGB_CUDA(ctx, cudaMemcpyAsync(f.colind, d.colind, sizeof(int) * d.nnz, cudaMemcpyHostToDevice, ctx->stream));
     FGB_CUDA(ctx, cudaMemcpyAsync(f.val, d.values, es * nval, cudaMemcpyHostToDevice, ctx->stream));
   }
+  if (d.format == FGB_BSR) FGB_TRY(bsr_tc_prepare(ctx, f));
   return FGB_OK;
 }
 

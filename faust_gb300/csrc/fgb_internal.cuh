@@ -55,11 +55,13 @@ fgb_status cuda_check(fgb_ctx* ctx, cudaError_t e, const char* what);
   } while (0)
 
 // Counts a kernel launch and checks the launch error.
-#define FGB_LAUNCHED(ctx)                                               \
-  do {                                                                  \
-    (ctx)->launches.fetch_add(1, std::memory_order_relaxed);            \
-    cudaError_t e__ = cudaGetLastError();                               \
-    if (e__ != cudaSuccess) return fgb::cuda_check(ctx, e__, "kernel launch"); \
+#define FGB_STR2(x) #x
+#define FGB_STR(x) FGB_STR2(x)
+#define FGB_LAUNCHED(ctx)                                                                  \
+  do {                                                                                     \
+    (ctx)->launches.fetch_add(1, std::memory_order_relaxed);                               \
+    cudaError_t e__ = cudaGetLastError();                                                  \
+    if (e__ != cudaSuccess) return fgb::cuda_check(ctx, e__, "kernel launch at " __FILE__ ":" FGB_STR(__LINE__)); \
   } while (0)
 
 size_t dtype_size(fgb_dtype t);
@@ -85,6 +87,8 @@ struct DevFactor {
   int* t_colind = nullptr;
   void* t_val = nullptr;
   bool has_t = false;
+  // BSR: row-major copy of the blocks for the tensor-core kernel.
+  void* aux = nullptr;
 };
 
 }  // namespace fgb

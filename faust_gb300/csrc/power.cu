@@ -1,6 +1,7 @@
 // power.cu — power iteration for spectral norms of CSR chains, one block per
 // chain, vectors in shared memory, the whole loop on the device (no host
 // round trip per iteration), with palm4msa2's step-size epilogue.
+#include <algorithm>
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
@@ -16,8 +17,9 @@ void pi_chain_build(const DevFactor* F, int lo, int hi, PIChain& ch) {
     ch.empty = 1;
     return;
   }
-  for (int i = lo; i < hi; ++i)
-    if (F[i].nnz == 0) ch.zero = 1;
+  for (int i = lo; i < hi; ++i) {
+    ch.maxdim = std::max(ch.maxdim, std::max(F[i].rows, F[i].cols));
+  }
   const int rows = F[lo].rows, cols = F[hi - 1].cols;
   auto fwd = [&](int i) { return PIOp{F[i].rowptr, F[i].colind, F[i].val, F[i].rows, 0}; };
   auto adj = [&](int i) { return PIOp{F[i].t_rowptr, F[i].t_colind, F[i].t_val, F[i].cols, 0}; };
@@ -57,9 +59,14 @@ __global__ void __launch_bounds__(PI_THREADS)
   double result = 1.0;
   int flag = 0;
   int st = 0;
+  // a factor without entries makes the product zero (nnz read on the device:
+  // factors produced by the PALM loop only know it there)
+  bool zero = false;
+  if (!ch.empty)
+    for (int o = 0; o < ch.nops; ++o) zero |= ch.ops[o].rowptr[ch.ops[o].rows] == 0;
   if (ch.empty) {
     result = 1.0;
-  } else if (ch.zero) {
+  } else if (zero) {
     result = 0.0;
   } else {
     const int n = ch.n;
@@ -189,7 +196,7 @@ fgb_status pi_rand_device(fgb_ctx* ctx, int n, const int** d_rand) {
 template <typename TF, typename TC>
 static fgb_status launch_pi_t(fgb_ctx* ctx, const PIChain& a, const PIChain& b, int max_iter, double thr,
                               const int* d_rand, PIOut* d_out, const PIPalm& palm) {
-  const int maxn = std::max(a.n, b.n) > 0 ? std::max(a.n, b.n) : 1;
+  const int maxn = std::max(1, std::max(a.maxdim, b.maxdim));
   const size_t smem = (3 * (size_t)maxn + PI_THREADS) * sizeof(TC);
   if (smem > ctx->smem_optin)
     return fail(ctx, FGB_ERR_NOT_SUPPORTED, "power iteration: vector of %d entries does not fit on chip", maxn);

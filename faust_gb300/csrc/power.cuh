@@ -20,13 +20,14 @@ struct PIOp {
 };
 
 // The operator F F^H (or F^H F) of one chain, as a list of products applied
-// in order to the vector.  empty: no factor (norm 1); zero: a factor without
-// entries (norm 0), as Transform::spectralNorm.
+// in order to the vector.  empty: no factor (norm 1); a factor without
+// entries gives norm 0 (checked on the device), as Transform::spectralNorm.
 struct PIChain {
   int nops;
   int n;
+  int maxdim;  // longest intermediate vector
   int empty;
-  int zero;
+  int pad;
   PIOp ops[PI_MAX_OPS];
 };
 

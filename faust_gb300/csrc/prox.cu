@@ -1,0 +1,824 @@
+// prox.cu — projections (faust_prox.hpp) of a dense device matrix, all
+// decisions taken on the device so that a palm4msa2 iteration can be replayed
+// as a CUDA graph.
+//
+// Global top-k (prox_sp) reproduces the support std::partial_sort selects
+// with the comparator |a| > |b| (faust_prox.hpp:52-69), ties included:
+//  1. radix select on magnitude keys gives t (the k-th largest |v|),
+//     G = #{|v| > t} and E = #{|v| == t};
+//  2. if G + E == k the set is unique; if t == 0 the tied entries are zeros
+//     and drop out of the sparse factor whichever are chosen;
+//  3. otherwise, with tau the position where the running count of |v| >= t
+//     reaches k: when no |v| > t lies after tau, heap selection keeps exactly
+//     the entries |v| >= t at positions <= tau (every such entry entered the
+//     heap before its minimum reached t, and none was evicted afterwards);
+//  4. otherwise the heap itself decides which ties stay: one block replays the
+//     selection (make_heap on the first k entries, then each later entry
+//     larger than the heap top replaces it through the hole-to-leaf
+//     adjustment and sift-up of the standard heap), after a parallel filter
+//     that drops entries not larger than the top at the start of each chunk.
+// Per-row / per-column top-k (prox_splin / prox_spcol) replay the same heap
+// selection per line, one thread per line.
+#include <algorithm>
+#include <cstring>
+
+#include "prox.cuh"
+
+namespace fgb {
+
+constexpr int PX_THREADS = 256;
+constexpr int HEAP_CHUNK = 2048;
+constexpr int LINE_KMAX = 64;
+
+__device__ __forceinline__ unsigned long long mag_key(double v) {
+  return (unsigned long long)__double_as_longlong(v) & 0x7fffffffffffffffULL;
+}
+__device__ __forceinline__ unsigned long long mag_key(float v) {
+  return (unsigned long long)(__float_as_uint(v) & 0x7fffffffu);
+}
+template <typename T>
+__device__ __forceinline__ T pos_adj(T v, int pos) {
+  return (pos && v < T(0)) ? T(0) : v;
+}
+
+// ------------------------------------------------------------------ workspace
+fgb_status prox_work_reserve(fgb_ctx* ctx, ProxWork& w, long elems, int rows) {
+  if (w.cap_elems >= elems && w.cap_rows >= rows && w.state) return FGB_OK;
+  prox_work_free(w);
+  FGB_TRY(dmalloc(ctx, (void**)&w.state, sizeof(TopkState)));
+  FGB_TRY(dmalloc(ctx, (void**)&w.hist, sizeof(unsigned) * 2048));
+  FGB_TRY(dmalloc(ctx, (void**)&w.flags, (size_t)std::max(1L, elems)));
+  const long nchunks = (elems + 8191) / 8192 + 2;
+  FGB_TRY(dmalloc(ctx, (void**)&w.chunk_cnt, sizeof(long long) * 2 * nchunks));
+  FGB_TRY(dmalloc(ctx, (void**)&w.partials, sizeof(double) * (elems / CR_CHUNK + 2)));
+  FGB_TRY(dmalloc(ctx, (void**)&w.scal, sizeof(double) * 4));
+  FGB_TRY(dmalloc(ctx, (void**)&w.row_cnt, sizeof(int) * (rows + 2)));
+  FGB_CUDA(ctx, cudaMemsetAsync(w.flags, 0, (size_t)std::max(1L, elems), ctx->stream));
+  FGB_CUDA(ctx, cudaMemsetAsync(w.hist, 0, sizeof(unsigned) * 2048, ctx->stream));
+  w.cap_elems = elems;
+  w.cap_rows = rows;
+  return FGB_OK;
+}
+
+void prox_work_free(ProxWork& w) {
+  dfree(w.state);
+  dfree(w.hist);
+  dfree(w.flags);
+  dfree(w.chunk_cnt);
+  dfree(w.partials);
+  dfree(w.scal);
+  dfree(w.row_cnt);
+  dfree(w.supp);
+  w = ProxWork();
+}
+
+// ------------------------------------------------------------------ radix select
+// One pass over an 11-bit (or shorter) digit of the magnitude keys whose
+// higher bits equal the prefix found so far; the last block to finish picks
+// the bucket holding the k_rem-th largest key.
+template <typename T>
+__global__ void __launch_bounds__(PX_THREADS)
+    k_radix_pass(const T* __restrict__ M, long N, int pos, int shift, int bits, TopkState* st,
+                 unsigned* __restrict__ hist) {
+  __shared__ unsigned sh[2048];
+  __shared__ int is_last;
+  const int nb = 1 << bits;
+  for (int i = threadIdx.x; i < nb; i += blockDim.x) sh[i] = 0;
+  __syncthreads();
+  const unsigned long long prefix = st->prefix, mask = st->mask;
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < N; i += (long)gridDim.x * blockDim.x) {
+    const unsigned long long key = mag_key(pos_adj(M[i], pos));
+    if ((key & mask) == prefix) atomicAdd(&sh[(key >> shift) & (nb - 1)], 1u);
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < nb; i += blockDim.x)
+    if (sh[i]) atomicAdd(&hist[i], sh[i]);
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) is_last = (atomicAdd(&st->blocks_done, 1u) == gridDim.x - 1);
+  __syncthreads();
+  if (!is_last) return;
+  __threadfence();
+  for (int i = threadIdx.x; i < nb; i += blockDim.x) {
+    sh[i] = __ldcg(&hist[i]);
+    hist[i] = 0;
+  }
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    const int lane = threadIdx.x;
+    const int per = nb / 32;
+    unsigned long long s = 0;
+    for (int j = 0; j < per; ++j) s += sh[nb - 1 - (lane * per + j)];
+    unsigned long long incl = s;
+    for (int o = 1; o < 32; o <<= 1) {
+      const unsigned long long y = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += y;
+    }
+    const unsigned long long excl = incl - s;
+    const long long krem = st->k_rem;
+    const unsigned ball = __ballot_sync(0xffffffffu, (long long)excl < krem && krem <= (long long)incl);
+    const int L = ball ? __ffs(ball) - 1 : -1;
+    if (lane == L) {
+      unsigned long long cum = excl;
+      for (int j = 0; j < per; ++j) {
+        const int b = nb - 1 - (lane * per + j);
+        const unsigned long long h = sh[b];
+        if ((long long)(cum + h) >= krem) {
+          st->G += (long long)cum;
+          st->k_rem = krem - (long long)cum;
+          st->prefix = prefix | ((unsigned long long)b << shift);
+          st->mask = mask | ((unsigned long long)(nb - 1) << shift);
+          st->E = (long long)h;
+          break;
+        }
+        cum += h;
+      }
+    }
+    if (L < 0 && lane == 0) st->status = FGB_ERR_INVALID_ARG;
+  }
+  if (threadIdx.x == 0) st->blocks_done = 0;
+}
+
+// ------------------------------------------------------------------ tie case
+// Decides the tie case; for ties with t > 0 finds tau and whether an entry
+// |v| > t lies after it.
+template <typename T>
+__global__ void __launch_bounds__(PX_THREADS)
+    k_tie_case(const T* __restrict__ M, long N, int pos, long chunk, TopkState* st, long long* __restrict__ cnt) {
+  __shared__ int is_last;
+  __shared__ long long s_ge[PX_THREADS], s_gt[PX_THREADS];
+  __shared__ long long c_target, c_base_gt, c_idx;
+  const unsigned long long t = st->prefix;
+  const long long k_rem = st->k_rem, E = st->E, G = st->G;
+  if (E == k_rem || t == 0) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+      st->t = t;
+      st->sel_case = (E == k_rem) ? 0 : 3;
+    }
+    return;
+  }
+  const long k = G + k_rem;
+  // per-chunk counts of keys >= t and > t
+  const long c0 = blockIdx.x * chunk, c1 = min(N, c0 + chunk);
+  long long ge = 0, gt = 0;
+  for (long i = c0 + threadIdx.x; i < c1; i += blockDim.x) {
+    const unsigned long long key = mag_key(pos_adj(M[i], pos));
+    ge += key >= t;
+    gt += key > t;
+  }
+  s_ge[threadIdx.x] = ge;
+  s_gt[threadIdx.x] = gt;
+  __syncthreads();
+  for (int s = PX_THREADS / 2; s >= 1; s >>= 1) {
+    if (threadIdx.x < s) {
+      s_ge[threadIdx.x] += s_ge[threadIdx.x + s];
+      s_gt[threadIdx.x] += s_gt[threadIdx.x + s];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    cnt[2 * blockIdx.x] = s_ge[0];
+    cnt[2 * blockIdx.x + 1] = s_gt[0];
+  }
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) is_last = (atomicAdd(&st->blocks_done, 1u) == gridDim.x - 1);
+  __syncthreads();
+  if (!is_last) return;
+  __threadfence();
+  if (threadIdx.x == 0) {
+    long long cum_ge = 0, cum_gt = 0;
+    long idx = -1;
+    for (long b = 0; b < gridDim.x; ++b) {
+      const long long g = __ldcg(&cnt[2 * b]), h = __ldcg(&cnt[2 * b + 1]);
+      if (cum_ge + g >= k) {
+        idx = b;
+        break;
+      }
+      cum_ge += g;
+      cum_gt += h;
+    }
+    c_idx = idx;
+    c_target = k - cum_ge;  // rank of tau inside the chunk (1-based)
+    c_base_gt = cum_gt;
+  }
+  __syncthreads();
+  if (c_idx < 0) {
+    if (threadIdx.x == 0) st->status = FGB_ERR_INVALID_ARG;
+    return;
+  }
+  // exact tau inside chunk c_idx: each thread takes a contiguous slice
+  const long b0 = c_idx * chunk, b1 = min(N, b0 + chunk);
+  const long len = b1 - b0, per = (len + PX_THREADS - 1) / PX_THREADS;
+  const long s0 = b0 + threadIdx.x * per, s1 = min(b1, s0 + per);
+  ge = 0;
+  gt = 0;
+  for (long i = s0; i < s1; ++i) {
+    const unsigned long long key = mag_key(pos_adj(M[i], pos));
+    ge += key >= t;
+    gt += key > t;
+  }
+  s_ge[threadIdx.x] = ge;
+  s_gt[threadIdx.x] = gt;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    long long run_ge = 0, run_gt = 0;
+    int who = -1;
+    for (int u = 0; u < PX_THREADS; ++u) {
+      if (run_ge + s_ge[u] >= c_target) {
+        who = u;
+        break;
+      }
+      run_ge += s_ge[u];
+      run_gt += s_gt[u];
+    }
+    s_ge[0] = who;
+    s_gt[0] = run_ge;
+    s_gt[1] = run_gt;
+    if (who < 0) st->status = FGB_ERR_INVALID_ARG;
+  }
+  __syncthreads();
+  if ((long long)threadIdx.x == s_ge[0]) {
+    long long run_ge = s_gt[0], run_gt = s_gt[1];
+    for (long i = s0; i < s1; ++i) {
+      const unsigned long long key = mag_key(pos_adj(M[i], pos));
+      run_ge += key >= t;
+      run_gt += key > t;
+      if (run_ge == c_target) {
+        const long long gt_before = c_base_gt + run_gt;
+        st->tau = i;
+        st->t = t;
+        st->sel_case = (gt_before == G) ? 1 : 2;
+        break;
+      }
+    }
+  }
+  if (threadIdx.x == 0) st->blocks_done = 0;
+}
+
+// ------------------------------------------------------------------ heap replay
+struct HeapView {
+  unsigned long long* key;
+  int* idx;
+};
+
+// Standard binary-heap adjustment with the comparator "larger key first":
+// move the hole to a leaf along the child preferred by the comparator (the
+// left child only when it is strictly preferred), then sift the value up.
+__device__ void heap_adjust(HeapView h, int hole, int len, unsigned long long vkey, int vidx) {
+  const int top = hole;
+  int child = hole;
+  while (child < (len - 1) / 2) {
+    child = 2 * (child + 1);
+    if (h.key[child] > h.key[child - 1]) child--;
+    h.key[hole] = h.key[child];
+    h.idx[hole] = h.idx[child];
+    hole = child;
+  }
+  if ((len & 1) == 0 && child == (len - 2) / 2) {
+    child = 2 * (child + 1);
+    h.key[hole] = h.key[child - 1];
+    h.idx[hole] = h.idx[child - 1];
+    hole = child - 1;
+  }
+  int parent = (hole - 1) / 2;
+  while (hole > top && h.key[parent] > vkey) {
+    h.key[hole] = h.key[parent];
+    h.idx[hole] = h.idx[parent];
+    hole = parent;
+    parent = (hole - 1) / 2;
+  }
+  h.key[hole] = vkey;
+  h.idx[hole] = vidx;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(PX_THREADS)
+    k_heap_replay(const T* __restrict__ M, long N, int pos, int k, TopkState* st, unsigned char* __restrict__ flags,
+                  unsigned long long* gkey, int* gidx, int use_smem) {
+  if (st->sel_case != 2) return;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ int s_cnt[PX_THREADS];
+  __shared__ int s_ncand;
+  unsigned long long* ckey = reinterpret_cast<unsigned long long*>(smem_raw);  // HEAP_CHUNK keys
+  int* cidx = reinterpret_cast<int*>(ckey + HEAP_CHUNK);                         // HEAP_CHUNK candidates
+  HeapView h;
+  if (use_smem) {
+    h.key = reinterpret_cast<unsigned long long*>(cidx + HEAP_CHUNK);
+    h.idx = reinterpret_cast<int*>(h.key + k);
+  } else {
+    h.key = gkey;
+    h.idx = gidx;
+  }
+  for (int i = threadIdx.x; i < k; i += blockDim.x) {
+    h.key[i] = mag_key(pos_adj(M[i], pos));
+    h.idx[i] = i;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0 && k >= 2) {
+    int parent = (k - 2) / 2;
+    while (true) {
+      heap_adjust(h, parent, k, h.key[parent], h.idx[parent]);
+      if (parent == 0) break;
+      parent--;
+    }
+  }
+  __syncthreads();
+  constexpr int PER = HEAP_CHUNK / PX_THREADS;
+  for (long c0 = k; c0 < N; c0 += HEAP_CHUNK) {
+    const unsigned long long topk = h.key[0];
+    const long c1 = min(N, c0 + HEAP_CHUNK);
+    // parallel filter: only keys above the current top can enter
+    int cnt = 0;
+    const long base = c0 + threadIdx.x * PER;
+    unsigned long long kk[PER];
+#pragma unroll
+    for (int u = 0; u < PER; ++u) {
+      const long i = base + u;
+      kk[u] = (i < c1) ? mag_key(pos_adj(M[i], pos)) : 0ULL;
+      cnt += (i < c1) && kk[u] > topk;
+    }
+    s_cnt[threadIdx.x] = cnt;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      int run = 0;
+      for (int u = 0; u < PX_THREADS; ++u) {
+        const int c = s_cnt[u];
+        s_cnt[u] = run;
+        run += c;
+      }
+      s_ncand = run;
+    }
+    __syncthreads();
+    int off = s_cnt[threadIdx.x];
+#pragma unroll
+    for (int u = 0; u < PER; ++u) {
+      const long i = base + u;
+      if (i < c1 && kk[u] > topk) {
+        ckey[off] = kk[u];
+        cidx[off] = (int)i;
+        ++off;
+      }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      const int nc = s_ncand;
+      for (int q = 0; q < nc; ++q)
+        if (ckey[q] > h.key[0]) heap_adjust(h, 0, k, ckey[q], cidx[q]);
+    }
+    __syncthreads();
+  }
+  const unsigned long long t = st->t;
+  for (int i = threadIdx.x; i < k; i += blockDim.x)
+    if (h.key[i] == t) flags[h.idx[i]] = 1;
+}
+
+// ------------------------------------------------------------------ sp apply
+template <typename T>
+__global__ void k_sp_apply(T* __restrict__ M, long N, int pos, const TopkState* st, unsigned char* __restrict__ flags) {
+  const unsigned long long t = st->t;
+  const int cs = st->sel_case;
+  const long long tau = st->tau;
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < N; i += (long)gridDim.x * blockDim.x) {
+    const T v = pos_adj(M[i], pos);
+    const unsigned long long key = mag_key(v);
+    bool keep = key > t;
+    if (!keep && key == t) {
+      if (cs == 0) keep = true;
+      else if (cs == 1) keep = i <= tau;
+      else if (cs == 2) keep = flags[i] != 0;
+    }
+    if (cs == 2) flags[i] = 0;
+    M[i] = keep ? v : T(0);
+  }
+}
+
+template <typename T>
+__global__ void k_pos_only(T* __restrict__ M, long N) {
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < N; i += (long)gridDim.x * blockDim.x)
+    if (M[i] < T(0)) M[i] = T(0);
+}
+
+template <typename T>
+__global__ void k_zero(T* __restrict__ M, long N) {
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < N; i += (long)gridDim.x * blockDim.x) M[i] = T(0);
+}
+
+// ------------------------------------------------------------------ line top-k
+// Heap selection of the k largest |v| of one line (a column or a row),
+// marking flags |= bit at the kept positions.  One thread per line.
+template <typename T>
+__global__ void k_line_topk(const T* __restrict__ M, int rows, int cols, int by_col, int k, int pos,
+                            unsigned char* __restrict__ flags, unsigned char bit) {
+  const int nlines = by_col ? cols : rows;
+  const int len = by_col ? rows : cols;
+  const int line = blockIdx.x * blockDim.x + threadIdx.x;
+  if (line >= nlines) return;
+  auto at = [&](int e) -> long { return by_col ? (long)line * rows + e : (long)e * rows + line; };
+  if (k >= len) {
+    for (int e = 0; e < len; ++e) flags[at(e)] |= bit;
+    return;
+  }
+  unsigned long long hk[LINE_KMAX];
+  int hi[LINE_KMAX];
+  HeapView h{hk, hi};
+  for (int e = 0; e < k; ++e) {
+    hk[e] = mag_key(pos_adj(M[at(e)], pos));
+    hi[e] = e;
+  }
+  if (k >= 2) {
+    int parent = (k - 2) / 2;
+    while (true) {
+      heap_adjust(h, parent, k, hk[parent], hi[parent]);
+      if (parent == 0) break;
+      parent--;
+    }
+  }
+  for (int e = k; e < len; ++e) {
+    const unsigned long long key = mag_key(pos_adj(M[at(e)], pos));
+    if (key > hk[0]) heap_adjust(h, 0, k, key, e);
+  }
+  for (int e = 0; e < k; ++e) flags[at(hi[e])] |= bit;
+}
+
+template <typename T>
+__global__ void k_flag_apply(T* __restrict__ M, long N, int pos, unsigned char* __restrict__ flags) {
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < N; i += (long)gridDim.x * blockDim.x) {
+    const T v = pos_adj(M[i], pos);
+    M[i] = flags[i] ? v : T(0);
+    flags[i] = 0;
+  }
+}
+
+// ------------------------------------------------------------------ norms
+// normcol: one block per column; canonical norm of the column, scale by
+// s / norm (a zero column stays zero).  normlin: the same per row.
+template <typename T>
+__global__ void __launch_bounds__(PX_THREADS)
+    k_normline(T* __restrict__ M, int rows, int cols, int by_col, double s, int pos) {
+  __shared__ T lane[PX_THREADS];
+  const int line = blockIdx.x;
+  const int len = by_col ? rows : cols;
+  auto at = [&](long e) -> long { return by_col ? (long)line * rows + e : e * rows + line; };
+  T total = T(0);
+  for (long c0 = 0; c0 < len; c0 += CR_CHUNK) {
+    const long c1 = min((long)len, c0 + CR_CHUNK);
+    T acc = T(0);
+    for (long e = c0 + threadIdx.x; e < c1; e += CR_LANES) {
+      const T v = pos_adj(M[at(e)], pos);
+      acc = fmad(v, v, acc);
+    }
+    lane[threadIdx.x] = acc;
+    total = addr(total, lane_tree_256(lane));
+  }
+  T scal = sqrtr(total);
+  if (scal != T(0)) scal = divr((T)s, scal);
+  for (long e = threadIdx.x; e < len; e += blockDim.x) M[at(e)] = mulr(pos_adj(M[at(e)], pos), scal);
+}
+
+template <typename T>
+__global__ void k_supp(T* __restrict__ M, long N, const T* __restrict__ S, int pos) {
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < N; i += (long)gridDim.x * blockDim.x)
+    M[i] = mulr(pos_adj(M[i], pos), S[i]);
+}
+
+// Canonical sum of squares: one block per chunk of 65536 entries.
+template <typename T>
+__global__ void __launch_bounds__(PX_THREADS) k_chunk_sumsq(const T* __restrict__ M, long N, double* partials) {
+  __shared__ T lane[PX_THREADS];
+  const long c0 = blockIdx.x * CR_CHUNK, c1 = min(N, c0 + CR_CHUNK);
+  T acc = T(0);
+  for (long i = c0 + threadIdx.x; i < c1; i += CR_LANES) acc = fmad(M[i], M[i], acc);
+  lane[threadIdx.x] = acc;
+  const T part = lane_tree_256(lane);
+  if (threadIdx.x == 0) reinterpret_cast<T*>(partials)[blockIdx.x] = part;
+}
+
+// MatDense::normalize (faust_MatDense.hpp:1225-1250): scale = FPP(1.0/norm),
+// domain_error (here FGB_ERR_ZERO_NORM) on a zero norm.
+template <typename T>
+__global__ void k_norm_finalize(const double* partials, int nchunks, double* scal, int* status) {
+  T total = T(0);
+  for (int c = 0; c < nchunks; ++c) total = addr(total, reinterpret_cast<const T*>(partials)[c]);
+  const T n = sqrtr(total);
+  T inv = T(0);
+  if (n == T(0)) {
+    if (status) atomicCAS(status, 0, (int)FGB_ERR_ZERO_NORM);
+  } else {
+    inv = (T)__ddiv_rn(1.0, (double)n);
+  }
+  reinterpret_cast<T*>(scal)[0] = inv;
+  scal[1] = (double)n;
+}
+
+template <typename T>
+__global__ void k_scale(T* __restrict__ M, long N, const double* scal) {
+  const T s = reinterpret_cast<const T*>(scal)[0];
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < N; i += (long)gridDim.x * blockDim.x)
+    M[i] = mulr(M[i], s);
+}
+
+__global__ void k_status_merge(const TopkState* st, int* status) {
+  if (st->status) atomicCAS(status, 0, st->status);
+}
+
+// ------------------------------------------------------------------ dense -> CSR
+template <typename T>
+__global__ void k_d2c_count(const T* __restrict__ M, int rows, int cols, int* __restrict__ cnt) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= rows) return;
+  int c = 0;
+  for (int j = 0; j < cols; ++j) c += M[i + (long)j * rows] != T(0);
+  cnt[i] = c;
+}
+
+__global__ void __launch_bounds__(1024) k_d2c_scan(const int* __restrict__ cnt, int rows, int* __restrict__ rowptr,
+                                                   int cap, int* status) {
+  __shared__ int part[1024];
+  const int per = (rows + blockDim.x - 1) / blockDim.x;
+  const int r0 = threadIdx.x * per, r1 = min(rows, r0 + per);
+  int s = 0;
+  for (int r = r0; r < r1; ++r) s += cnt[r];
+  part[threadIdx.x] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int run = 0;
+    for (int u = 0; u < (int)blockDim.x; ++u) {
+      const int v = part[u];
+      part[u] = run;
+      run += v;
+    }
+    rowptr[rows] = run;
+    if (run > cap && status) atomicCAS(status, 0, (int)FGB_ERR_INVALID_ARG);
+  }
+  __syncthreads();
+  int run = part[threadIdx.x];
+  for (int r = r0; r < r1; ++r) {
+    rowptr[r] = run;
+    run += cnt[r];
+  }
+}
+
+template <typename T>
+__global__ void k_d2c_write(const T* __restrict__ M, int rows, int cols, const int* __restrict__ rowptr,
+                            int* __restrict__ colind, T* __restrict__ val, int cap) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= rows) return;
+  int p = rowptr[i];
+  for (int j = 0; j < cols; ++j) {
+    const T v = M[i + (long)j * rows];
+    if (v != T(0)) {
+      if (p < cap) {
+        colind[p] = j;
+        val[p] = v;
+      }
+      ++p;
+    }
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(1024)
+    k_csr_transpose_dev(const int* __restrict__ rowptr, const int* __restrict__ colind, const T* __restrict__ val,
+                        int rows, int cols, int* __restrict__ t_rowptr, int* __restrict__ t_colind,
+                        T* __restrict__ t_val, int* __restrict__ cursor, int cap) {
+  const int nnz = min(rowptr[rows], cap);
+  for (int c = threadIdx.x; c <= cols; c += blockDim.x) cursor[c] = 0;
+  __syncthreads();
+  for (int p = threadIdx.x; p < nnz; p += blockDim.x) atomicAdd(&cursor[colind[p] + 1], 1);
+  __syncthreads();
+  {
+    __shared__ int part[1024];
+    const int per = (cols + blockDim.x - 1) / blockDim.x;
+    const int c0 = threadIdx.x * per, c1 = min(cols, c0 + per);
+    int s = 0;
+    for (int c = c0; c < c1; ++c) s += cursor[c + 1];
+    part[threadIdx.x] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      int run = 0;
+      for (int u = 0; u < (int)blockDim.x; ++u) {
+        const int v = part[u];
+        part[u] = run;
+        run += v;
+      }
+      t_rowptr[cols] = run;
+    }
+    __syncthreads();
+    int run = part[threadIdx.x];
+    for (int c = c0; c < c1; ++c) {
+      t_rowptr[c] = run;
+      run += cursor[c + 1];
+    }
+  }
+  __syncthreads();
+  for (int c = threadIdx.x; c < cols; c += blockDim.x) cursor[c] = t_rowptr[c];
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    const unsigned lane = threadIdx.x;
+    for (int base = 0; base < nnz; base += 32) {
+      const int p = base + (int)lane;
+      const bool ok = p < nnz;
+      int r = 0;
+      if (ok) {
+        int lo = 0, hi = rows - 1;
+        while (lo < hi) {
+          const int mid = (lo + hi + 1) >> 1;
+          if (rowptr[mid] <= p) lo = mid;
+          else hi = mid - 1;
+        }
+        r = lo;
+      }
+      const int c = ok ? colind[p] : -1 - (int)lane;
+      const unsigned same = __match_any_sync(0xffffffffu, c);
+      const int rank = __popc(same & ((1u << lane) - 1u));
+      int slot = 0;
+      if (ok) slot = cursor[c] + rank;
+      __syncwarp();
+      if (ok) {
+        t_colind[slot] = r;
+        t_val[slot] = val[p];
+        if ((same >> lane) == 1u) cursor[c] = slot + 1;
+      }
+      __syncwarp();
+    }
+  }
+}
+
+__global__ void k_topk_init(TopkState* st, long long k) {
+  TopkState z;
+  memset(&z, 0, sizeof(z));
+  z.k_rem = k;
+  *st = z;
+}
+
+// ------------------------------------------------------------------ host side
+static int grid_for(fgb_ctx* ctx, long n) {
+  long g = (n + PX_THREADS - 1) / PX_THREADS;
+  return (int)std::max(1L, std::min(g, 4L * ctx->sm_count));
+}
+
+template <typename T>
+static fgb_status queue_normalize(fgb_ctx* ctx, ProxWork& w, T* M, long N, int* d_status) {
+  const int nchunks = (int)((N + CR_CHUNK - 1) / CR_CHUNK);
+  k_chunk_sumsq<T><<<nchunks, PX_THREADS, 0, ctx->stream>>>(M, N, w.partials);
+  FGB_LAUNCHED(ctx);
+  k_norm_finalize<T><<<1, 1, 0, ctx->stream>>>(w.partials, nchunks, w.scal, d_status);
+  FGB_LAUNCHED(ctx);
+  k_scale<T><<<grid_for(ctx, N), PX_THREADS, 0, ctx->stream>>>(M, N, w.scal);
+  FGB_LAUNCHED(ctx);
+  return FGB_OK;
+}
+
+template <typename T>
+static fgb_status queue_sp(fgb_ctx* ctx, ProxWork& w, T* M, long N, long k, int pos, int* d_status) {
+  k_topk_init<<<1, 1, 0, ctx->stream>>>(w.state, k);
+  FGB_LAUNCHED(ctx);
+  const int g = grid_for(ctx, N);
+  if (sizeof(T) == 8) {
+    const int shifts[6] = {52, 41, 30, 19, 8, 0};
+    const int bits[6] = {11, 11, 11, 11, 11, 8};
+    for (int p = 0; p < 6; ++p) {
+      k_radix_pass<T><<<g, PX_THREADS, 0, ctx->stream>>>(M, N, pos, shifts[p], bits[p], w.state, w.hist);
+      FGB_LAUNCHED(ctx);
+    }
+  } else {
+    const int shifts[3] = {20, 9, 0};
+    const int bits[3] = {11, 11, 9};
+    for (int p = 0; p < 3; ++p) {
+      k_radix_pass<T><<<g, PX_THREADS, 0, ctx->stream>>>(M, N, pos, shifts[p], bits[p], w.state, w.hist);
+      FGB_LAUNCHED(ctx);
+    }
+  }
+  const long chunk = std::max(8192L, (N + 2047) / 2048);
+  const int nch = (int)((N + chunk - 1) / chunk);
+  k_tie_case<T><<<nch, PX_THREADS, 0, ctx->stream>>>(M, N, pos, chunk, w.state, w.chunk_cnt);
+  FGB_LAUNCHED(ctx);
+  const size_t heap_smem = (size_t)HEAP_CHUNK * (8 + 4) + (size_t)k * 12;
+  const bool use_smem = heap_smem <= std::min<size_t>(ctx->smem_optin, 200 * 1024);
+  unsigned long long* gkey = nullptr;
+  int* gidx = nullptr;
+  size_t smem = (size_t)HEAP_CHUNK * (8 + 4);
+  if (use_smem) {
+    smem = heap_smem;
+  } else {
+    return fail(ctx, FGB_ERR_NOT_SUPPORTED, "prox_sp: k = %ld too large for the on-chip tie replay", k);
+  }
+  auto kern = k_heap_replay<T>;
+  if (smem > 48 * 1024) FGB_CUDA(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  kern<<<1, PX_THREADS, smem, ctx->stream>>>(M, N, pos, (int)k, w.state, w.flags, gkey, gidx, use_smem ? 1 : 0);
+  FGB_LAUNCHED(ctx);
+  k_sp_apply<T><<<g, PX_THREADS, 0, ctx->stream>>>(M, N, pos, w.state, w.flags);
+  FGB_LAUNCHED(ctx);
+  if (d_status) {
+    k_status_merge<<<1, 1, 0, ctx->stream>>>(w.state, d_status);
+    FGB_LAUNCHED(ctx);
+  }
+  return FGB_OK;
+}
+
+template <typename T>
+fgb_status launch_prox(fgb_ctx* ctx, ProxWork& w, const fgb_constraint& c, T* M, int rows, int cols,
+                       const T* supp_dev, int* d_status) {
+  const long N = (long)rows * cols;
+  FGB_TRY(prox_work_reserve(ctx, w, N, std::max(rows, cols)));
+  const int g = grid_for(ctx, N);
+  int pos = c.pos != 0;
+  switch (c.kind) {
+    case FGB_SP_POS:
+      pos = 1;
+      /* fall through */
+    case FGB_SP: {
+      // prox_sp (faust_prox.hpp:71-96)
+      if (c.k <= 0) {
+        k_zero<T><<<g, PX_THREADS, 0, ctx->stream>>>(M, N);
+        FGB_LAUNCHED(ctx);
+      } else if (c.k < N) {
+        FGB_TRY(queue_sp<T>(ctx, w, M, N, (long)c.k, pos, d_status));
+      } else if (pos) {
+        k_pos_only<T><<<g, PX_THREADS, 0, ctx->stream>>>(M, N);
+        FGB_LAUNCHED(ctx);
+      }
+      break;
+    }
+    case FGB_SPCOL:
+    case FGB_SPLIN:
+    case FGB_SPLINCOL: {
+      // prox_spcol / prox_splin / prox_splincol (faust_prox.hpp:112-202);
+      // splincol ignores pos, as the reference applies it after copying.
+      if (c.kind == FGB_SPLINCOL) pos = 0;
+      if (c.k <= 0) {
+        k_zero<T><<<g, PX_THREADS, 0, ctx->stream>>>(M, N);
+        FGB_LAUNCHED(ctx);
+        break;
+      }
+      if (c.k > LINE_KMAX && !((c.kind == FGB_SPCOL && c.k >= rows) || (c.kind == FGB_SPLIN && c.k >= cols) ||
+                               (c.kind == FGB_SPLINCOL && c.k >= rows && c.k >= cols)))
+        return fail(ctx, FGB_ERR_NOT_SUPPORTED, "per-line top-k supports k <= %d", LINE_KMAX);
+      const int k = (int)std::min<long long>(c.k, LINE_KMAX + (long long)std::max(rows, cols));
+      if (c.kind != FGB_SPLIN) {
+        k_line_topk<T><<<(cols + 127) / 128, 128, 0, ctx->stream>>>(M, rows, cols, 1, std::min(k, rows), pos,
+                                                                   w.flags, 1);
+        FGB_LAUNCHED(ctx);
+      }
+      if (c.kind != FGB_SPCOL) {
+        k_line_topk<T><<<(rows + 127) / 128, 128, 0, ctx->stream>>>(M, rows, cols, 0, std::min(k, cols), pos,
+                                                                   w.flags, 2);
+        FGB_LAUNCHED(ctx);
+      }
+      k_flag_apply<T><<<g, PX_THREADS, 0, ctx->stream>>>(M, N, pos, w.flags);
+      FGB_LAUNCHED(ctx);
+      break;
+    }
+    case FGB_NORMCOL:
+    case FGB_NORMLIN: {
+      if (c.s < 0) return fail(ctx, FGB_ERR_INVALID_ARG, "Faust::prox_normcol : s < 0 ");
+      if (c.s == 0) {
+        k_zero<T><<<g, PX_THREADS, 0, ctx->stream>>>(M, N);
+        FGB_LAUNCHED(ctx);
+      } else {
+        const bool by_col = c.kind == FGB_NORMCOL;
+        k_normline<T><<<by_col ? cols : rows, PX_THREADS, 0, ctx->stream>>>(M, rows, cols, by_col ? 1 : 0, c.s, pos);
+        FGB_LAUNCHED(ctx);
+      }
+      break;
+    }
+    case FGB_SUPP: {
+      if (!supp_dev) return fail(ctx, FGB_ERR_INVALID_ARG, "prox_supp: missing support");
+      k_supp<T><<<g, PX_THREADS, 0, ctx->stream>>>(M, N, supp_dev, pos);
+      FGB_LAUNCHED(ctx);
+      break;
+    }
+    default:
+      return fail(ctx, FGB_ERR_INVALID_ARG, "project : cannot project with this constraint name");
+  }
+  if (c.normalized) FGB_TRY(queue_normalize<T>(ctx, w, M, N, d_status));
+  return FGB_OK;
+}
+
+template <typename T>
+fgb_status launch_dense_to_csr(fgb_ctx* ctx, ProxWork& w, const T* M, DevFactor& f) {
+  FGB_TRY(prox_work_reserve(ctx, w, (long)f.rows * f.cols, std::max(f.rows, f.cols)));
+  const int rb = (f.rows + 127) / 128;
+  k_d2c_count<T><<<rb, 128, 0, ctx->stream>>>(M, f.rows, f.cols, w.row_cnt);
+  FGB_LAUNCHED(ctx);
+  k_d2c_scan<<<1, 1024, 0, ctx->stream>>>(w.row_cnt, f.rows, f.rowptr, f.cap, nullptr);
+  FGB_LAUNCHED(ctx);
+  k_d2c_write<T><<<rb, 128, 0, ctx->stream>>>(M, f.rows, f.cols, f.rowptr, f.colind, (T*)f.val, f.cap);
+  FGB_LAUNCHED(ctx);
+  if (f.t_rowptr) {
+    k_csr_transpose_dev<T><<<1, 1024, 0, ctx->stream>>>(f.rowptr, f.colind, (const T*)f.val, f.rows, f.cols,
+                                                        f.t_rowptr, f.t_colind, (T*)f.t_val, w.row_cnt, f.cap);
+    FGB_LAUNCHED(ctx);
+  }
+  return FGB_OK;
+}
+
+template fgb_status launch_prox<float>(fgb_ctx*, ProxWork&, const fgb_constraint&, float*, int, int, const float*,
+                                       int*);
+template fgb_status launch_prox<double>(fgb_ctx*, ProxWork&, const fgb_constraint&, double*, int, int,
+                                        const double*, int*);
+template fgb_status launch_dense_to_csr<float>(fgb_ctx*, ProxWork&, const float*, DevFactor&);
+template fgb_status launch_dense_to_csr<double>(fgb_ctx*, ProxWork&, const double*, DevFactor&);
+
+}  // namespace fgb

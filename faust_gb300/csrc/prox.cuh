@@ -1,0 +1,56 @@
+// prox.cuh — projections of a dense device matrix (ConstraintGeneric::project)
+// and the dense -> CSR factor conversion used by palm4msa2.
+#pragma once
+
+#include "fgb_internal.cuh"
+
+namespace fgb {
+
+// Device state of one global top-k selection (prox_sp).
+struct TopkState {
+  unsigned long long prefix;  // bits of the threshold found so far
+  unsigned long long mask;
+  unsigned long long t;       // key of the k-th largest magnitude
+  long long k_rem;            // rank still to find inside the current prefix
+  long long G;                // #{key > t}
+  long long E;                // #{key == t}
+  long long tau;              // position of the k-th key >= t (linear order)
+  int sel_case;               // 0 unique / keep all, 1 prefix rule, 2 heap order, 3 t == 0
+  int status;
+  unsigned blocks_done;
+  unsigned pad;
+};
+
+// Scratch owned by a context-level prox workspace (sized for rows*cols).
+struct ProxWork {
+  long cap_elems = 0;
+  int cap_rows = 0;
+  TopkState* state = nullptr;
+  unsigned* hist = nullptr;          // 2048 bins
+  unsigned char* flags = nullptr;    // one byte per entry
+  long long* chunk_cnt = nullptr;    // per-chunk counts (tau search / reductions)
+  double* partials = nullptr;        // per-chunk reduction partials
+  double* scal = nullptr;            // scalars: [0] = inverse norm (as FPP), [1] = norm
+  int* row_cnt = nullptr;            // rows+1
+  void* supp = nullptr;              // device copy of a support (SUPP)
+  size_t supp_bytes = 0;
+};
+
+fgb_status prox_work_reserve(fgb_ctx* ctx, ProxWork& w, long elems, int rows);
+void prox_work_free(ProxWork& w);
+
+// Queues the projection of the dense rows x cols matrix M (column-major,
+// ld = rows) in place.  supp_dev: device support for FGB_SUPP.  The first
+// failure status is written to *d_status (device int) when not null.
+template <typename T>
+fgb_status launch_prox(fgb_ctx* ctx, ProxWork& w, const fgb_constraint& c, T* M, int rows, int cols,
+                       const T* supp_dev, int* d_status);
+
+// Queues dense -> CSR conversion of the non-zero entries of M into the
+// factor f (whose arrays must have capacity for every entry it may receive:
+// f.cap >= nonzeros); f.nnz is updated on the host only by the caller reading
+// rowptr[rows] back.  Also rebuilds the transpose CSR when f.t_* is set.
+template <typename T>
+fgb_status launch_dense_to_csr(fgb_ctx* ctx, ProxWork& w, const T* M, DevFactor& f);
+
+}  // namespace fgb

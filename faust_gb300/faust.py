@@ -28,8 +28,18 @@ class Context:
     """A device + stream pair (fgb_ctx); one per host thread."""
 
     def __init__(self, device=0, stream=None):
+        """stream: a cudaStream_t handle (int); by default torch's current
+        stream on that device, so that work is ordered with torch's."""
+        if stream is None:
+            try:
+                import torch
+                if torch.cuda.is_available():
+                    stream = torch.cuda.current_stream(device).cuda_stream
+            except ImportError:
+                pass
         h = ctypes.c_void_p()
-        check(_ffi.lib().fgb_ctx_create(int(device), stream, ctypes.byref(h)))
+        check(_ffi.lib().fgb_ctx_create(int(device), ctypes.c_void_p(stream or 0), ctypes.byref(h)))
+        self.stream = stream or 0
         self.handle = h
         self.device = device
 
@@ -82,6 +92,17 @@ class BSRFactor:
     @property
     def nnz_blocks(self):
         return int(self.bcolind.size)
+
+
+def _is_colmajor(T):
+    rows, cols = T.shape
+    return (T.stride(0) == 1 or rows == 1) and (cols == 1 or T.stride(1) >= rows)
+
+
+def _ld(T):
+    """Leading dimension of a column-major tensor (any value >= rows works
+    for a single column)."""
+    return T.stride(1) if T.shape[1] > 1 else max(1, T.shape[0])
 
 
 def _csr_desc(m, keep):
@@ -169,12 +190,14 @@ class Faust:
         if X.shape[0] != rows_in:
             raise ValueError("dimensions do not match")
         # column-major storage = transpose of a contiguous (ncols, rows) tensor
-        if not (X.stride(0) == 1 and X.stride(1) >= rows_in):
+        if not _is_colmajor(X):
             Xc = X.t().contiguous().t()
         if Y is None:
             Y = torch.empty((ncols, self.shape[0]), dtype=X.dtype, device=X.device).t()
-        check(_ffi.lib().fgb_faust_mul(self.handle, Xc.data_ptr(), Xc.stride(1), ncols, Y.data_ptr(), Y.stride(1),
-                                       int(mode)), self.ctx.handle)
+        elif not _is_colmajor(Y):
+            raise ValueError("Y must be column-major")
+        check(_ffi.lib().fgb_faust_mul(self.handle, Xc.data_ptr(), _ld(Xc), ncols, Y.data_ptr(), _ld(Y), int(mode)),
+              self.ctx.handle)
         return Y
 
     def norm(self, ord=2, max_iter=100, threshold=1e-6):

@@ -57,7 +57,9 @@ typedef struct fgb_ctx fgb_ctx;
 typedef struct fgb_faust fgb_faust;
 
 /* ------------------------------------------------------------------ context
- * Replaces gp_funcs->set_dev / set_stream (faust_gpu_mod_utils.h:100-102). */
+ * Replaces gp_funcs->set_dev / set_stream (faust_gpu_mod_utils.h:100-102).
+ * All work of the context is queued on cuda_stream (a cudaStream_t; NULL is
+ * the legacy default stream). */
 fgb_status fgb_ctx_create(int device, void* cuda_stream, fgb_ctx** out);
 fgb_status fgb_ctx_destroy(fgb_ctx* ctx);
 const char* fgb_last_error(const fgb_ctx* ctx);

@@ -151,3 +151,34 @@ def test_invalid_factor_is_rejected(fgb):
     m.indices[1] = 7  # column out of range
     with pytest.raises(Exception):
         fgb.Faust([m])
+
+
+def test_bsr_tensor_core_matches_cuda_core_path(fgb, monkeypatch):
+    """The tcgen05 kernel (whole 128-column tiles) against the CUDA-core
+    kernel on the same BF16 inputs: both accumulate in FP32, in different
+    orders, so agreement is within BF16 output rounding (2^-8 relative)."""
+    torch = _torch()
+    rng = np.random.default_rng(31)
+    n = 1024
+    facs, _ = _bsr_factors(fgb, n, 1, rng)
+    F = fgb.Faust(facs)
+    X = torch.randn((512, n), device="cuda", dtype=torch.float32).to(torch.bfloat16).t()
+    Yt = F.matmul_device(X).float()
+    monkeypatch.setenv("FGB_BSR_SIMT", "1")
+    Ys = F.matmul_device(X).float()
+    rel = (torch.linalg.norm(Yt - Ys) / torch.linalg.norm(Ys)).item()
+    assert rel < 8e-3, rel
+
+
+def test_bsr_ragged_columns_use_cuda_core_path(fgb, oracle):
+    torch = _torch()
+    rng = np.random.default_rng(32)
+    n = 512
+    facs, f32 = _bsr_factors(fgb, n, 2, rng)
+    F = fgb.Faust(facs)
+    X = rng.standard_normal((n, 77)).astype(np.float32)
+    Xb = synth.bf16_to_f32(synth.bf16_bits(X)).reshape(X.shape)
+    Yt = F.matmul_device(torch.from_numpy(np.ascontiguousarray(Xb.T)).to(torch.bfloat16).cuda().t())
+    Y = Yt.t().float().cpu().numpy().T.astype(np.float64)
+    ref = _oracle_bsr_chain(oracle, n, f32, Xb, round_bf16=True)
+    assert np.linalg.norm(Y - ref) / np.linalg.norm(ref) < 1e-2

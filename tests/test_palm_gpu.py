@@ -1,0 +1,182 @@
+"""GPU parity of the projections and of palm4msa2 against the oracle.
+
+Supports (integer/index work) are compared bit for bit; values too, since
+GPU and oracle follow the same floating-point operation order.  The top-k
+inputs include heavy ties, where the heap order of std::partial_sort
+decides which entries stay.
+"""
+import numpy as np
+import pytest
+
+from faust_gb300 import fact, synth
+
+pytestmark = pytest.mark.gpu
+
+
+def _cuda_colmajor(M):
+    import torch
+    return torch.from_numpy(np.ascontiguousarray(M.T)).cuda().t()
+
+
+def _host(Mt):
+    return Mt.t().contiguous().cpu().numpy().T
+
+
+def _gpu_prox(M, c):
+    Mt = _cuda_colmajor(M)
+    fact.prox(Mt, c)
+    return _host(Mt)
+
+
+def _tie_matrix(rng, rows, cols, levels, dtype=np.float64):
+    return rng.integers(-levels, levels + 1, size=(rows, cols)).astype(dtype) / 8.0
+
+
+@pytest.mark.parametrize("seed", range(8))
+@pytest.mark.parametrize("dtype", [np.float64, np.float32])
+def test_prox_sp_ties_bitexact(oracle, seed, dtype):
+    rng = np.random.default_rng(seed)
+    rows, cols = [(64, 64), (100, 37), (257, 129), (1024, 64)][seed % 4]
+    M = _tie_matrix(rng, rows, cols, 1 + seed % 4, dtype)
+    k = int(rng.integers(1, rows * cols))
+    c = fact.ConstraintInt("sp", rows, cols, k, normalized=bool(seed % 2), pos=bool(seed % 3 == 0))
+    got = _gpu_prox(M, c)
+    ref = oracle.prox(oracle.SP, M, k=k, normalized=c.normalized, pos=c.pos)
+    assert np.array_equal(got, ref)
+
+
+def test_prox_sp_heap_order_case(oracle):
+    """Ties at the threshold with larger entries after the k-th tie: the
+    heap layout decides (the replay path)."""
+    rng = np.random.default_rng(99)
+    found = 0
+    for trial in range(40):
+        n = 200
+        v = np.where(rng.random(n) < 0.5, 1.0, rng.choice([0.5, 2.0, 3.0], size=n))
+        k = int(rng.integers(5, 60))
+        M = v.reshape(20, 10)
+        got = _gpu_prox(M, fact.ConstraintInt("sp", 20, 10, k, normalized=False))
+        ref = oracle.prox(oracle.SP, M, k=k, normalized=False)
+        assert np.array_equal(got, ref), trial
+        found += 1
+    assert found == 40
+
+
+@pytest.mark.parametrize("name,kind", [("spcol", 1), ("splin", 2), ("splincol", 3)])
+@pytest.mark.parametrize("seed", range(4))
+def test_prox_lines_bitexact(oracle, name, kind, seed):
+    rng = np.random.default_rng(100 + seed)
+    rows, cols = [(40, 30), (64, 64), (17, 200), (512, 33)][seed]
+    M = _tie_matrix(rng, rows, cols, 2) if seed % 2 else rng.standard_normal((rows, cols))
+    k = [1, 4, 5, 7][seed]
+    c = fact.ConstraintInt(name, rows, cols, k, pos=(seed == 2))
+    got = _gpu_prox(M, c)
+    ref = oracle.prox(kind, M, k=k, pos=c.pos)
+    assert np.array_equal(got, ref)
+
+
+def test_prox_norms_supp_bitexact(oracle):
+    rng = np.random.default_rng(7)
+    M = rng.standard_normal((50, 20))
+    for name, kind, s in [("normcol", 4, 2.0), ("normlin", 5, 0.5)]:
+        for normalized in (False, True):
+            c = fact.ConstraintReal(name, 50, 20, s, normalized=normalized)
+            assert np.array_equal(_gpu_prox(M, c), oracle.prox(kind, M, s=s, normalized=normalized))
+    supp = (rng.random((50, 20)) < 0.3).astype(np.float64)
+    c = fact.ConstraintMat("supp", supp)
+    assert np.array_equal(_gpu_prox(M, c), oracle.prox(6, M, supp=supp))
+
+
+def test_prox_zero_norm_is_an_error():
+    with pytest.raises(Exception):
+        _gpu_prox(np.zeros((8, 8)), fact.ConstraintInt("sp", 8, 8, 3))
+
+
+def _factors_dense(res):
+    F = res.faust
+    return [F.factors(i).toarray() for i in range(F.numfactors())]
+
+
+def _compare_palm(oracle, A, cons, its, **kw):
+    params = fact.ParamsPalm4MSA(cons, its, **kw)
+    res = fact.palm4msa(A, cons, params)
+    okw = dict(kw)
+    okw.pop("init_facts", None)
+    facts_o, lam_o, _ = oracle.palm4msa2(A, [c.oracle_dict() for c in cons], its,
+                                         init_facts=kw.get("init_facts"), **okw)
+    got = _factors_dense(res)
+    for g, o in zip(got, facts_o):
+        assert np.array_equal(g.astype(o.dtype), o)
+    assert res.lambda_ == lam_o
+    return res, facts_o, lam_o
+
+
+@pytest.mark.parametrize("n", [32, 64])
+def test_palm_hadamard_bitexact(oracle, n):
+    J = int(np.log2(n))
+    H = synth.hadamard(n) / np.sqrt(n)
+    cons = [fact.ConstraintInt("sp", n, n, 2 * n) for _ in range(J)]
+    _compare_palm(oracle, H, cons, 60, norm2_threshold=1e-8)
+
+
+def test_palm_hadamard_r2l_bitexact(oracle):
+    n = 32
+    H = synth.hadamard(n) / np.sqrt(n)
+    cons = [fact.ConstraintInt("sp", n, n, 2 * n) for _ in range(5)]
+    _compare_palm(oracle, H, cons, 20, norm2_threshold=1e-8, is_update_way_R2L=True)
+
+
+def test_palm_fixture_config_compared_palm2_bitexact(oracle):
+    """The reference's own palm4msa2 test settings and fixture
+    (misc/test/src/C++/palm4msa_2020.cpp.in:81-121)."""
+    import os
+    data = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden",
+                                "config_compared_palm2_data.npy"))
+    cons = [fact.ConstraintInt("splin", 500, 32, 5), fact.ConstraintReal("normcol", 32, 32, 1.0, normalized=True)]
+    _compare_palm(oracle, data, cons, 200, packing_RL=False, norm2_threshold=1e-15, norm2_max_iter=1000)
+
+
+def test_palm_splincol_fp32_fp64_norms(oracle):
+    """Batched-PALM instance shape: splincol k=4, FP32, FP64 step-size norms."""
+    rng = np.random.default_rng(5)
+    n = 96
+    P = [synth.random_csr(n, n, 4, rng, np.float64).toarray() for _ in range(3)]
+    A = (P[0] @ P[1] @ P[2] + 1e-3 * rng.standard_normal((n, n))).astype(np.float32)
+    cons = [fact.ConstraintInt("splincol", n, n, 4) for _ in range(4)]
+    _compare_palm(oracle, A, cons, 30, norm2_fp64=True)
+
+
+def test_palm_butterfly_supp_fp32(oracle):
+    """Learned-warm-start shape: 8 butterfly supp factors of a 256 x 256
+    Gaussian kernel matrix, FP32."""
+    rng = np.random.default_rng(6)
+    x = rng.random((256, 3))
+    d2 = ((x[:, None, :] - x[None, :, :]) ** 2).sum(-1)
+    K = np.exp(-d2 / (2 * 0.2 ** 2)).astype(np.float32)
+    sups = synth.butterfly_supports(8, np.float32)
+    cons = [fact.ConstraintMat("supp", s.toarray()) for s in sups]
+    init = [s.toarray() for s in sups]
+    _compare_palm(oracle, K, cons, 25, init_facts=init)
+
+
+def test_palm_config2_first_iterations_bitexact(oracle):
+    """Full-size Hadamard 1024 / 32, 10 factors, sp k=2048: the first three
+    iterations against the oracle."""
+    n = 1024
+    H = synth.hadamard(n) / 32.0
+    cons = [fact.ConstraintInt("sp", n, n, 2048) for _ in range(10)]
+    oracle.set_threads(16)
+    _compare_palm(oracle, H, cons, 3, norm2_threshold=1e-8)
+
+
+def test_palm_cancel_flag_is_honoured():
+    """fgb_cancel set before the run stops it at the first check."""
+    import faust_gb300 as fg
+    ctx = fg.Context(0)
+    n = 32
+    H = synth.hadamard(n) / np.sqrt(n)
+    cons = [fact.ConstraintInt("sp", n, n, 2 * n) for _ in range(5)]
+    ctx.cancel()
+    with pytest.raises(Exception) as e:
+        fact.palm4msa(H, cons, fact.ParamsPalm4MSA(cons, 50), ctx=ctx)
+    assert "CANCELLED" in str(e.value)
