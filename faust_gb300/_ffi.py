@@ -39,6 +39,20 @@ class PalmParams(ctypes.Structure):
                 ("no_lambda_error", ctypes.c_int), ("norm2_fp64", ctypes.c_int)]
 
 
+class PalmProblem(ctypes.Structure):
+    _fields_ = [("rows", ctypes.c_int), ("cols", ctypes.c_int), ("A", ctypes.c_void_p), ("nfacts", ctypes.c_int),
+                ("cons", ctypes.POINTER(Constraint)), ("init_facts", ctypes.POINTER(ctypes.c_void_p)),
+                ("init_lambda", ctypes.c_double)]
+
+
+class PalmResultC(ctypes.Structure):
+    _fields_ = [("faust", ctypes.c_void_p), ("lambda_", ctypes.c_double), ("status", ctypes.c_int)]
+
+
+class BatchOpts(ctypes.Structure):
+    _fields_ = [("ctas_per_sm", ctypes.c_int)]
+
+
 class FgbError(RuntimeError):
     def __init__(self, status, msg):
         super().__init__("%s: %s" % (STATUS_NAMES.get(status, status), msg))
@@ -74,6 +88,8 @@ _SIGS = {
                                   ctypes.POINTER(PalmParams), ctypes.POINTER(_P), ctypes.POINTER(_D),
                                   ctypes.POINTER(_P)]),
     "fgb_rel_err": (_I, [_P, _P, _D, ctypes.POINTER(_D)]),
+    "fgb_palm4msa2_batched": (_I, [_P, _I, _I, ctypes.POINTER(PalmProblem), ctypes.POINTER(PalmParams),
+                                   ctypes.POINTER(BatchOpts), ctypes.POINTER(PalmResultC)]),
 }
 
 

@@ -174,6 +174,7 @@ fgb_status launch_dense_csrT(fgb_ctx* ctx, const T* X, int ldx, int xrows, const
 // (two buffers of maxdim x TC).  Only X is read from HBM and only Y written;
 // the factors are read from L2 by every block.
 constexpr int CHAIN_THREADS = 1024;
+constexpr int CHAIN_ILP = 4;
 
 template <typename T, int TC>
 __device__ __forceinline__ void chain_row(const ChainDesc& d, const T* __restrict__ val, const T* __restrict__ in,
@@ -206,24 +207,54 @@ __global__ void __launch_bounds__(CHAIN_THREADS)
     const ChainDesc d = desc[f];
     const T* __restrict__ val = reinterpret_cast<const T*>(d.val);
     const bool last = (f == 0);
-    // two rows per pass: independent load chains
-    for (int i = threadIdx.x; i < d.rows; i += 2 * blockDim.x) {
-      const int i2 = i + blockDim.x;
-      T a1[TC], a2[TC];
-      chain_row<T, TC>(d, val, in, i, a1);
-      if (i2 < d.rows) chain_row<T, TC>(d, val, in, i2, a2);
-      if (last) {
+    // CHAIN_ILP rows per pass: their rowptr / entry loads are issued
+    // together, so each thread keeps several L2 requests in flight
+    for (int i0 = threadIdx.x; i0 < d.rows; i0 += CHAIN_ILP * blockDim.x) {
+      int rb[CHAIN_ILP], re[CHAIN_ILP];
 #pragma unroll
-        for (int t = 0; t < TC; ++t)
-          if (j0 + t < ncols) {
-            Y[i + (long)(j0 + t) * ldy] = a1[t];
-            if (i2 < d.rows) Y[i2 + (long)(j0 + t) * ldy] = a2[t];
+      for (int u = 0; u < CHAIN_ILP; ++u) {
+        const int i = i0 + u * blockDim.x;
+        rb[u] = i < d.rows ? __ldg(d.rowptr + i) : 0;
+        re[u] = i < d.rows ? __ldg(d.rowptr + i + 1) : 0;
+      }
+      T acc[CHAIN_ILP][TC];
+#pragma unroll
+      for (int u = 0; u < CHAIN_ILP; ++u)
+#pragma unroll
+        for (int t = 0; t < TC; ++t) acc[u][t] = T(0);
+      int maxlen = 0;
+#pragma unroll
+      for (int u = 0; u < CHAIN_ILP; ++u) maxlen = max(maxlen, re[u] - rb[u]);
+      for (int q = 0; q < maxlen; ++q) {
+        T v[CHAIN_ILP];
+        int c[CHAIN_ILP];
+#pragma unroll
+        for (int u = 0; u < CHAIN_ILP; ++u) {
+          const bool ok = rb[u] + q < re[u];
+          v[u] = ok ? __ldg(val + rb[u] + q) : T(0);
+          c[u] = ok ? __ldg(d.colind + rb[u] + q) : -1;
+        }
+#pragma unroll
+        for (int u = 0; u < CHAIN_ILP; ++u) {
+          if (c[u] >= 0) {
+            T x[TC];
+            load_row<T, TC>(in + (long)c[u] * TC, x);
+#pragma unroll
+            for (int t = 0; t < TC; ++t) acc[u][t] = fmad(v[u], x[t], acc[u][t]);
           }
-      } else {
+        }
+      }
 #pragma unroll
-        for (int t = 0; t < TC; ++t) {
-          out[(long)i * TC + t] = a1[t];
-          if (i2 < d.rows) out[(long)i2 * TC + t] = a2[t];
+      for (int u = 0; u < CHAIN_ILP; ++u) {
+        const int i = i0 + u * blockDim.x;
+        if (i >= d.rows) continue;
+        if (last) {
+#pragma unroll
+          for (int t = 0; t < TC; ++t)
+            if (j0 + t < ncols) Y[i + (long)(j0 + t) * ldy] = acc[u][t];
+        } else {
+#pragma unroll
+          for (int t = 0; t < TC; ++t) out[(long)i * TC + t] = acc[u][t];
         }
       }
     }

@@ -121,7 +121,7 @@ __global__ void k_set_scalar(T* p, double v) {
 }
 
 // ------------------------------------------------------------------ driver
-static long factor_capacity(const fgb_constraint& c) {
+long palm_factor_capacity(const fgb_constraint& c) {
   const long N = (long)c.rows * c.cols;
   long cap = N;
   switch (c.kind) {
@@ -240,7 +240,7 @@ struct Palm {
       f.format = FGB_CSR;
       f.rows = cons[i].rows;
       f.cols = cons[i].cols;
-      f.cap = (int)factor_capacity(cons[i]);
+      f.cap = (int)palm_factor_capacity(cons[i]);
       FGB_TRY(dmalloc(ctx, (void**)&f.rowptr, sizeof(int) * (f.rows + 1)));
       FGB_TRY(dmalloc(ctx, (void**)&f.colind, sizeof(int) * f.cap));
       FGB_TRY(dmalloc(ctx, &f.val, es * f.cap));

@@ -1,0 +1,949 @@
+// palm_batched.cu — many independent palm4msa2 instances of uneven sizes in
+// ONE persistent launch.
+//
+// Each CTA (256 threads) takes the next instance from a device work queue
+// (instances are ordered by decreasing cost on the host) and runs the whole
+// palm4msa2 loop for it with block-level versions of the single-instance
+// kernels: the same floating-point order (sequential fma per product entry,
+// 256-lane canonical reductions), so every instance is bit-identical to the
+// oracle run of that instance.  Dense blocks live in a per-CTA workspace in
+// global memory (L2-resident for small n); power-iteration vectors in shared
+// memory.  Constraints: spcol, splin, splincol (k <= 64), normcol, normlin,
+// supp.  The launch is captured in a CUDA graph by the host driver.
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
+#include "fgb_internal.cuh"
+
+namespace fgb {
+namespace bat {
+
+constexpr int BT = 256;
+constexpr int MAXJ = 16;
+constexpr int KMAX = 64;
+
+template <typename T>
+struct Fac {
+  int rows, cols, cap, pad;
+  int* rowptr;
+  int* colind;
+  T* val;
+  int* t_rowptr;
+  int* t_colind;
+  T* t_val;
+};
+
+template <typename T>
+struct Cons {
+  int kind, k, normalized, pos;
+  double s;
+  const T* supp;  // device, rows x cols (SUPP)
+};
+
+template <typename T>
+struct Inst {
+  int J, arows, acols, status;
+  const T* A;
+  double lambda;  // in: initial lambda; out: final lambda
+  Fac<T> f[MAXJ];
+  Cons<T> c[MAXJ];
+};
+
+template <typename T>
+struct Slot {
+  T* D;
+  T* buf0;
+  T* buf1;
+  T* packed;  // MAXJ blocks of maxdim*maxdim
+  unsigned char* flags;
+  int* cnt;
+};
+
+struct Params {
+  int nb_it, r2l, packing_RL, no_lambda, norm2_max_iter, constant_step, no_lambda_error, norm2_fp64;
+  double norm2_threshold, step_size;
+  long maxdim2;
+  int ninst;
+  int pad;
+};
+
+// ------------------------------------------------------------------ block ops
+template <typename T>
+__device__ __forceinline__ T bat_tree(T* lane) {
+  return lane_tree_256(lane);
+}
+
+template <typename T>
+__device__ void b_zero(T* p, long n) {
+  for (long i = threadIdx.x; i < n; i += BT) p[i] = T(0);
+}
+
+template <typename T>
+__device__ void b_csr_to_dense(const Fac<T>& f, T* out) {
+  b_zero(out, (long)f.rows * f.cols);
+  __syncthreads();
+  for (int i = threadIdx.x; i < f.rows; i += BT)
+    for (int p = f.rowptr[i]; p < f.rowptr[i + 1]; ++p) out[i + (long)f.colind[p] * f.rows] = f.val[p];
+  __syncthreads();
+}
+
+enum { E_STORE = 0, E_LAMBDA = 1, E_DMINUS = 2 };
+
+template <typename T>
+__device__ __forceinline__ T b_epi(int mode, T acc, const T* aux, long idx, T s) {
+  if (mode == E_LAMBDA) return subr(mulr(s, acc), aux[idx]);
+  if (mode == E_DMINUS) return subr(aux[idx], mulr(s, acc));
+  return acc;
+}
+
+// Y = S X   (S: rows x inner CSR, X: inner x ncols, Y: rows x ncols; lds = rows)
+template <typename T>
+__device__ void b_spmm(const int* rp, const int* ci, const T* v, int rows, const T* X, int ldx, int ncols, T* Y,
+                       int mode, const T* aux, T s) {
+  const long n = (long)rows * ncols;
+  for (long idx = threadIdx.x; idx < n; idx += BT) {
+    const int i = (int)(idx % rows);
+    const long j = idx / rows;
+    T acc = T(0);
+    for (int p = rp[i]; p < rp[i + 1]; ++p) acc = fmad(v[p], X[ci[p] + j * ldx], acc);
+    Y[idx] = b_epi(mode, acc, aux, idx, s);
+  }
+  __syncthreads();
+}
+
+// Y = X S^T given the CSR of S (srows rows): y[r, c] = sum over row c of S.
+template <typename T>
+__device__ void b_dense_csrT(const T* X, int xrows, const int* rp, const int* ci, const T* v, int srows, T* Y,
+                             int mode, const T* aux, T s) {
+  const long n = (long)xrows * srows;
+  for (long idx = threadIdx.x; idx < n; idx += BT) {
+    const int r = (int)(idx % xrows);
+    const int c = (int)(idx / xrows);
+    T acc = T(0);
+    for (int p = rp[c]; p < rp[c + 1]; ++p) acc = fmad(v[p], X[r + (long)ci[p] * xrows], acc);
+    Y[idx] = b_epi(mode, acc, aux, idx, s);
+  }
+  __syncthreads();
+}
+
+// Canonical sum of a[i]*b[i] over i < n (every thread gets the result).
+template <typename T>
+__device__ T b_cdot(const T* a, const T* b, long n, T* lane) {
+  return block_cdot<T>(a, b, n, lane);
+}
+
+// ------------------------------------------------------------------ power iteration
+// Op o of the operator F F^H (or F^H F) of F[lo..hi): returns the CSR to
+// apply and its output length.
+template <typename T>
+__device__ __forceinline__ void pi_op(const Fac<T>* F, int lo, int hi, bool tall, int o, const int*& rp,
+                                      const int*& ci, const T*& v, int& rows) {
+  const int m = hi - lo;
+  bool fwd;
+  int idx;
+  if (tall) {  // F^H F: F x applies F[hi-1] first, then the adjoints F[lo]^H ...
+    fwd = o < m;
+    idx = fwd ? hi - 1 - o : lo + (o - m);
+  } else {  // F F^H: adjoints F[lo]^H first, then F[hi-1] ...
+    fwd = o >= m;
+    idx = fwd ? hi - 1 - (o - m) : lo + o;
+  }
+  const Fac<T>& f = F[idx];
+  if (fwd) {
+    rp = f.rowptr;
+    ci = f.colind;
+    v = f.val;
+    rows = f.rows;
+  } else {
+    rp = f.t_rowptr;
+    ci = f.t_colind;
+    v = f.t_val;
+    rows = f.cols;
+  }
+}
+
+// TransformHelper::spectralNorm of F[lo..hi) by Faust::power_iteration; the
+// same steps as k_power_iteration (power.cu), on one block.
+template <typename T, typename TC>
+__device__ double b_spectral_norm(const Fac<T>* F, int lo, int hi, int max_iter, TC thr, const int* rnd, TC* vbuf,
+                                  int maxn, TC* lane, int* st) {
+  if (hi <= lo) return 1.0;
+  for (int i = lo; i < hi; ++i)
+    if (F[i].rowptr[F[i].rows] == 0) return 0.0;
+  const int rows = F[lo].rows, cols = F[hi - 1].cols;
+  const bool tall = cols < rows;
+  const int n = tall ? cols : rows;
+  const int nops = 2 * (hi - lo);
+  TC* bufs[3] = {vbuf, vbuf + maxn, vbuf + 2 * maxn};
+  int xi = 0;
+  for (int i = threadIdx.x; i < n; i += BT) bufs[0][i] = addr(TC(-1), divr(mulr(TC(2), (TC)rnd[i]), (TC)RAND_MAX));
+  __syncthreads();
+  TC lam_old = TC(1), lam = TC(0);
+  int it = 0;
+  const TC athr = thr < TC(0) ? -thr : thr;
+  auto absv = [](TC x) { return x < TC(0) ? -x : x; };
+  while ((absv(subr(lam_old, lam)) > athr || absv(lam) <= athr) && it < max_iter) {
+    ++it;
+    lam_old = lam;
+    TC* x = bufs[xi];
+    const TC nrm = sqrtr(b_cdot<TC>(x, x, n, lane));
+    if (nrm == TC(0)) {
+      if (threadIdx.x == 0) *st = FGB_ERR_ZERO_NORM;
+      return 0.0;
+    }
+    const TC inv = divr(TC(1), nrm);
+    for (int i = threadIdx.x; i < n; i += BT) x[i] = mulr(x[i], inv);
+    __syncthreads();
+    int si = xi, di = (xi + 1) % 3;
+    for (int o = 0; o < nops; ++o) {
+      const int* rp;
+      const int* ci;
+      const T* v;
+      int orow;
+      pi_op(F, lo, hi, tall, o, rp, ci, v, orow);
+      const TC* src = bufs[si];
+      TC* dst = bufs[di];
+      for (int r = threadIdx.x; r < orow; r += BT) {
+        TC acc = TC(0);
+        for (int p = rp[r]; p < rp[r + 1]; ++p) acc = fmad((TC)v[p], src[ci[p]], acc);
+        dst[r] = acc;
+      }
+      __syncthreads();
+      si = di;
+      di = 3 - xi - si;
+    }
+    const TC* res = bufs[si];
+    int nz = 0;
+    for (int i = threadIdx.x; i < n; i += BT) nz |= (res[i] != TC(0));
+    if (!__syncthreads_or(nz)) return 0.0;
+    lam = b_cdot<TC>(x, res, n, lane);
+    xi = si;
+  }
+  const TC r = sqrtr(lam);
+  return (double)(r < TC(0) ? -r : r);
+}
+
+// ------------------------------------------------------------------ projections
+__device__ __forceinline__ unsigned long long bkey(double v) {
+  return (unsigned long long)__double_as_longlong(v) & 0x7fffffffffffffffULL;
+}
+__device__ __forceinline__ unsigned long long bkey(float v) {
+  return (unsigned long long)(__float_as_uint(v) & 0x7fffffffu);
+}
+template <typename T>
+__device__ __forceinline__ T bpos(T v, int pos) {
+  return (pos && v < T(0)) ? T(0) : v;
+}
+
+__device__ void b_heap_adjust(unsigned long long* hk, int* hi, int hole, int len, unsigned long long vk, int vi) {
+  const int top = hole;
+  int child = hole;
+  while (child < (len - 1) / 2) {
+    child = 2 * (child + 1);
+    if (hk[child] > hk[child - 1]) child--;
+    hk[hole] = hk[child];
+    hi[hole] = hi[child];
+    hole = child;
+  }
+  if ((len & 1) == 0 && child == (len - 2) / 2) {
+    child = 2 * (child + 1);
+    hk[hole] = hk[child - 1];
+    hi[hole] = hi[child - 1];
+    hole = child - 1;
+  }
+  int parent = (hole - 1) / 2;
+  while (hole > top && hk[parent] > vk) {
+    hk[hole] = hk[parent];
+    hi[hole] = hi[parent];
+    hole = parent;
+    parent = (hole - 1) / 2;
+  }
+  hk[hole] = vk;
+  hi[hole] = vi;
+}
+
+// Per-line heap selection (std::partial_sort, |a| > |b|) of k entries.
+template <typename T>
+__device__ void b_line_topk(const T* M, int rows, int cols, bool by_col, int k, int pos, unsigned char* flags,
+                            unsigned char bit) {
+  const int nl = by_col ? cols : rows, len = by_col ? rows : cols;
+  for (int line = threadIdx.x; line < nl; line += BT) {
+    auto at = [&](int e) -> long { return by_col ? (long)line * rows + e : (long)e * rows + line; };
+    if (k >= len) {
+      for (int e = 0; e < len; ++e) flags[at(e)] |= bit;
+      continue;
+    }
+    unsigned long long hk[KMAX];
+    int hi[KMAX];
+    for (int e = 0; e < k; ++e) {
+      hk[e] = bkey(bpos(M[at(e)], pos));
+      hi[e] = e;
+    }
+    if (k >= 2) {
+      int parent = (k - 2) / 2;
+      while (true) {
+        b_heap_adjust(hk, hi, parent, k, hk[parent], hi[parent]);
+        if (parent == 0) break;
+        parent--;
+      }
+    }
+    for (int e = k; e < len; ++e) {
+      const unsigned long long key = bkey(bpos(M[at(e)], pos));
+      if (key > hk[0]) b_heap_adjust(hk, hi, 0, k, key, e);
+    }
+    for (int e = 0; e < k; ++e) flags[at(hi[e])] |= bit;
+  }
+  __syncthreads();
+}
+
+template <typename T>
+__device__ bool b_project(const Cons<T>& c, T* M, int rows, int cols, unsigned char* flags, T* lane, int* st) {
+  const long N = (long)rows * cols;
+  int pos = c.pos;
+  if (c.kind == FGB_SPCOL || c.kind == FGB_SPLIN || c.kind == FGB_SPLINCOL) {
+    if (c.kind == FGB_SPLINCOL) pos = 0;
+    if (c.k <= 0) {
+      b_zero(M, N);
+    } else {
+      if (c.kind != FGB_SPLIN) b_line_topk(M, rows, cols, true, min(c.k, rows), pos, flags, 1);
+      if (c.kind != FGB_SPCOL) b_line_topk(M, rows, cols, false, min(c.k, cols), pos, flags, 2);
+      for (long i = threadIdx.x; i < N; i += BT) {
+        const T v = bpos(M[i], pos);
+        M[i] = flags[i] ? v : T(0);
+        flags[i] = 0;
+      }
+    }
+  } else if (c.kind == FGB_NORMCOL || c.kind == FGB_NORMLIN) {
+    if (c.s == 0) {
+      b_zero(M, N);
+    } else {
+      const bool by_col = c.kind == FGB_NORMCOL;
+      const int nl = by_col ? cols : rows, len = by_col ? rows : cols;
+      for (int line = 0; line < nl; ++line) {
+        auto at = [&](long e) -> long { return by_col ? (long)line * rows + e : e * rows + line; };
+        T total = T(0);
+        for (long c0 = 0; c0 < len; c0 += CR_CHUNK) {
+          const long c1 = min((long)len, c0 + CR_CHUNK);
+          T acc = T(0);
+          for (long e = c0 + threadIdx.x; e < c1; e += CR_LANES) {
+            const T v = bpos(M[at(e)], pos);
+            acc = fmad(v, v, acc);
+          }
+          lane[threadIdx.x] = acc;
+          total = addr(total, bat_tree(lane));
+        }
+        T scal = sqrtr(total);
+        if (scal != T(0)) scal = divr((T)c.s, scal);
+        for (long e = threadIdx.x; e < len; e += BT) M[at(e)] = mulr(bpos(M[at(e)], pos), scal);
+        __syncthreads();
+      }
+    }
+  } else if (c.kind == FGB_SUPP) {
+    for (long i = threadIdx.x; i < N; i += BT) M[i] = mulr(bpos(M[i], pos), c.supp[i]);
+  } else {
+    if (threadIdx.x == 0) *st = FGB_ERR_NOT_SUPPORTED;
+    return false;
+  }
+  __syncthreads();
+  if (c.normalized) {
+    T total = T(0);
+    for (long c0 = 0; c0 < N; c0 += CR_CHUNK) {
+      const long c1 = min(N, c0 + CR_CHUNK);
+      T acc = T(0);
+      for (long i = c0 + threadIdx.x; i < c1; i += CR_LANES) acc = fmad(M[i], M[i], acc);
+      lane[threadIdx.x] = acc;
+      total = addr(total, bat_tree(lane));
+    }
+    const T n = sqrtr(total);
+    if (n == T(0)) {
+      if (threadIdx.x == 0) *st = FGB_ERR_ZERO_NORM;
+      return false;
+    }
+    const T inv = (T)__ddiv_rn(1.0, (double)n);
+    for (long i = threadIdx.x; i < N; i += BT) M[i] = mulr(M[i], inv);
+    __syncthreads();
+  }
+  return true;
+}
+
+// dense -> CSR of the non-zero entries, then the transpose CSR.
+template <typename T>
+__device__ bool b_dense_to_csr(const T* M, Fac<T>& f, int* cnt, int* st) {
+  __shared__ int part[BT];
+  const int rows = f.rows, cols = f.cols;
+  for (int i = threadIdx.x; i < rows; i += BT) {
+    int c = 0;
+    for (int j = 0; j < cols; ++j) c += M[i + (long)j * rows] != T(0);
+    cnt[i] = c;
+  }
+  __syncthreads();
+  const int per = (rows + BT - 1) / BT;
+  const int r0 = threadIdx.x * per, r1 = min(rows, r0 + per);
+  int s = 0;
+  for (int r = r0; r < r1; ++r) s += cnt[r];
+  part[threadIdx.x] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int run = 0;
+    for (int u = 0; u < BT; ++u) {
+      const int v = part[u];
+      part[u] = run;
+      run += v;
+    }
+    f.rowptr[rows] = run;
+    if (run > f.cap) *st = FGB_ERR_INVALID_ARG;
+  }
+  __syncthreads();
+  int run = part[threadIdx.x];
+  for (int r = r0; r < r1; ++r) {
+    f.rowptr[r] = run;
+    run += cnt[r];
+  }
+  __syncthreads();
+  if (f.rowptr[rows] > f.cap) return false;
+  for (int i = threadIdx.x; i < rows; i += BT) {
+    int p = f.rowptr[i];
+    for (int j = 0; j < cols; ++j) {
+      const T v = M[i + (long)j * rows];
+      if (v != T(0)) {
+        f.colind[p] = j;
+        f.val[p] = v;
+        ++p;
+      }
+    }
+  }
+  __syncthreads();
+  // transpose: column counts, scan, ordered scatter (warp 0)
+  const int nnz = f.rowptr[rows];
+  for (int c = threadIdx.x; c <= cols; c += BT) cnt[c] = 0;
+  __syncthreads();
+  for (int p = threadIdx.x; p < nnz; p += BT) atomicAdd(&cnt[f.colind[p] + 1], 1);
+  __syncthreads();
+  const int cper = (cols + BT - 1) / BT;
+  const int c0 = threadIdx.x * cper, c1 = min(cols, c0 + cper);
+  s = 0;
+  for (int c = c0; c < c1; ++c) s += cnt[c + 1];
+  part[threadIdx.x] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int rr = 0;
+    for (int u = 0; u < BT; ++u) {
+      const int v = part[u];
+      part[u] = rr;
+      rr += v;
+    }
+    f.t_rowptr[cols] = rr;
+  }
+  __syncthreads();
+  run = part[threadIdx.x];
+  for (int c = c0; c < c1; ++c) {
+    f.t_rowptr[c] = run;
+    run += cnt[c + 1];
+  }
+  __syncthreads();
+  for (int c = threadIdx.x; c < cols; c += BT) cnt[c] = f.t_rowptr[c];
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    const unsigned lane = threadIdx.x;
+    for (int base = 0; base < nnz; base += 32) {
+      const int p = base + (int)lane;
+      const bool ok = p < nnz;
+      int r = 0;
+      if (ok) {
+        int lo = 0, hi = rows - 1;
+        while (lo < hi) {
+          const int mid = (lo + hi + 1) >> 1;
+          if (f.rowptr[mid] <= p) lo = mid;
+          else hi = mid - 1;
+        }
+        r = lo;
+      }
+      const int c = ok ? f.colind[p] : -1 - (int)lane;
+      const unsigned same = __match_any_sync(0xffffffffu, c);
+      const int rank = __popc(same & ((1u << lane) - 1u));
+      int slot = 0;
+      if (ok) slot = cnt[c] + rank;
+      __syncwarp();
+      if (ok) {
+        f.t_colind[slot] = r;
+        f.t_val[slot] = f.val[p];
+        if ((same >> lane) == 1u) cnt[c] = slot + 1;
+      }
+      __syncwarp();
+    }
+  }
+  __syncthreads();
+  return true;
+}
+
+// ------------------------------------------------------------------ one instance
+template <typename T, typename TN>
+__device__ void run_instance(Inst<T>& I, const Slot<T>& W, const Params& P, const int* rnd, TN* vbuf, int maxn,
+                             T* lane, TN* lane_n) {
+  const int J = I.J;
+  Fac<T>* S = I.f;
+  const bool r2l = P.r2l != 0;
+  __shared__ int st;
+  __shared__ T sh_c, sh_alpha;
+  if (threadIdx.x == 0) st = 0;
+  __syncthreads();
+  T lam = (T)I.lambda;
+  T* packed[MAXJ];
+  for (int i = 0; i < J; ++i) packed[i] = W.packed + (long)i * P.maxdim2;
+  T* buf[2] = {W.buf0, W.buf1};
+  const int arows = I.arows, acols = I.acols;
+  for (int it = 0; it < P.nb_it; ++it) {
+    // init_ite
+    if (J >= 2) {
+      if (!r2l) {
+        b_csr_to_dense(S[J - 1], packed[J - 2]);
+        for (int i = J - 3; i >= 0; --i)
+          b_spmm<T>(S[i + 1].rowptr, S[i + 1].colind, S[i + 1].val, S[i + 1].rows, packed[i + 1], S[i + 1].cols, acols,
+                    packed[i], E_STORE, nullptr, T(0));
+      } else {
+        b_csr_to_dense(S[0], packed[1]);
+        for (int i = 2; i < J; ++i)
+          b_dense_csrT<T>(packed[i - 1], arows, S[i - 1].t_rowptr, S[i - 1].t_colind, S[i - 1].t_val, S[i - 1].cols,
+                          packed[i], E_STORE, nullptr, T(0));
+      }
+    }
+    for (int step = 0; step < J; ++step) {
+      const int f = r2l ? J - 1 - step : step;
+      const Fac<T>& Sf = S[f];
+      // step size (faust_palm4msa2020.hpp:563-617)
+      T c;
+      if (P.constant_step) {
+        c = divr(T(1), (T)P.step_size);
+      } else {
+        const double nR = b_spectral_norm<T, TN>(S, f + 1, J, P.norm2_max_iter, (TN)P.norm2_threshold, rnd, vbuf,
+                                                 maxn, lane_n, &st);
+        const double nL = b_spectral_norm<T, TN>(S, 0, f, P.norm2_max_iter, (TN)P.norm2_threshold, rnd, vbuf, maxn,
+                                                 lane_n, &st);
+        __syncthreads();
+        if (threadIdx.x == 0) {
+          if (isnan(nR) || isnan(nL)) st = st ? st : FGB_ERR_NAN;
+          if ((nR == 0.0 && (it > 0 || !r2l)) || (nL == 0.0 && (it > 0 || r2l))) st = st ? st : FGB_ERR_ZERO_NORM;
+        }
+        const double tnR = (double)(T)nR, tnL = (double)(T)nL, l = (double)lam;
+        double cc = __dmul_rn(1.001, l);
+        cc = __dmul_rn(cc, l);
+        cc = __dmul_rn(cc, tnR);
+        cc = __dmul_rn(cc, tnR);
+        cc = __dmul_rn(cc, tnL);
+        cc = __dmul_rn(cc, tnL);
+        c = (T)cc;
+      }
+      const T alpha = divr(lam, c);
+      __syncthreads();
+      if (st) break;
+      b_csr_to_dense(Sf, W.D);
+      const bool hasL = f > 0, hasR = f + 1 < J;
+      int cur = 0;
+      if (!r2l) {
+        if (hasR)
+          b_spmm<T>(Sf.rowptr, Sf.colind, Sf.val, Sf.rows, packed[f], Sf.cols, acols, buf[cur], f == 0 ? E_LAMBDA : E_STORE,
+                    I.A, lam);
+        else if (f == 0) {
+          for (long i = threadIdx.x; i < (long)arows * acols; i += BT) buf[cur][i] = subr(mulr(lam, W.D[i]), I.A[i]);
+          __syncthreads();
+        } else {
+          b_csr_to_dense(Sf, buf[cur]);
+        }
+        for (int l = f - 1; l >= 0; --l) {
+          b_spmm<T>(S[l].rowptr, S[l].colind, S[l].val, S[l].rows, buf[cur], S[l].cols, acols, buf[cur ^ 1],
+                    l == 0 ? E_LAMBDA : E_STORE, I.A, lam);
+          cur ^= 1;
+        }
+      } else {
+        const int nR = J - 1 - f;
+        if (hasL)
+          b_dense_csrT<T>(packed[f], arows, Sf.t_rowptr, Sf.t_colind, Sf.t_val, Sf.cols, buf[cur],
+                          nR == 0 ? E_LAMBDA : E_STORE, I.A, lam);
+        else if (nR == 0) {
+          for (long i = threadIdx.x; i < (long)arows * acols; i += BT) buf[cur][i] = subr(mulr(lam, W.D[i]), I.A[i]);
+          __syncthreads();
+        } else {
+          b_csr_to_dense(Sf, buf[cur]);
+        }
+        for (int l = f + 1; l < J; ++l) {
+          b_dense_csrT<T>(buf[cur], arows, S[l].t_rowptr, S[l].t_colind, S[l].t_val, S[l].cols, buf[cur ^ 1],
+                          l == J - 1 ? E_LAMBDA : E_STORE, I.A, lam);
+          cur ^= 1;
+        }
+      }
+      // G = L^H E R^H with D - alpha G fused into the last product
+      int rows = arows, cols = acols;
+      const int nops = (J - 1 - f) + f;
+      if (nops == 0) {
+        for (long i = threadIdx.x; i < (long)Sf.rows * Sf.cols; i += BT)
+          W.D[i] = subr(W.D[i], mulr(alpha, buf[cur][i]));
+        __syncthreads();
+      } else {
+        int q = 0;
+        auto left = [&](int l) {
+          const bool last = ++q == nops;
+          T* dst = last ? W.D : buf[cur ^ 1];
+          b_spmm<T>(S[l].t_rowptr, S[l].t_colind, S[l].t_val, S[l].cols, buf[cur], S[l].rows, cols, dst,
+                    last ? E_DMINUS : E_STORE, W.D, alpha);
+          rows = S[l].cols;
+          if (!last) cur ^= 1;
+        };
+        auto right = [&](int l) {
+          const bool last = ++q == nops;
+          T* dst = last ? W.D : buf[cur ^ 1];
+          b_dense_csrT<T>(buf[cur], rows, S[l].rowptr, S[l].colind, S[l].val, S[l].rows, dst,
+                          last ? E_DMINUS : E_STORE, W.D, alpha);
+          cols = S[l].rows;
+          if (!last) cur ^= 1;
+        };
+        if (!r2l) {
+          for (int l = 0; l < f; ++l) left(l);
+          for (int l = J - 1; l > f; --l) right(l);
+        } else {
+          for (int l = J - 1; l > f; --l) right(l);
+          for (int l = 0; l < f; ++l) left(l);
+        }
+      }
+      if (!b_project<T>(I.c[f], W.D, Sf.rows, Sf.cols, W.flags, lane, &st)) break;
+      if (!b_dense_to_csr<T>(W.D, S[f], W.cnt, &st)) break;
+    }
+    __syncthreads();
+    if (st) break;
+    if (!P.no_lambda) {
+      // update_lambda: S_mat per the reuse rule (faust_palm4msa2020.hpp:449-468)
+      T* Smat;
+      const bool reuse = P.packing_RL || J <= 2;
+      bool use_pR0 = false;
+      if (J >= 2 && reuse) {
+        const long lhs = (long)S[0].cols * S[1].rows;
+        const long rhs = (long)S[J - 2].cols * S[J - 1].rows;
+        use_pR0 = lhs < rhs;
+      }
+      if (J == 1) {
+        b_csr_to_dense(S[0], buf[0]);
+        Smat = buf[0];
+      } else if (reuse && !r2l && use_pR0) {
+        b_spmm<T>(S[0].rowptr, S[0].colind, S[0].val, S[0].rows, packed[0], S[0].cols, acols, buf[0], E_STORE, nullptr,
+                  T(0));
+        Smat = buf[0];
+      } else if (reuse && r2l && !use_pR0) {
+        b_dense_csrT<T>(packed[J - 1], arows, S[J - 1].t_rowptr, S[J - 1].t_colind, S[J - 1].t_val, S[J - 1].cols,
+                        buf[0], E_STORE, nullptr, T(0));
+        Smat = buf[0];
+      } else {
+        int cur = 0;
+        b_csr_to_dense(S[J - 1], buf[cur]);
+        for (int l = J - 2; l >= 0; --l) {
+          b_spmm<T>(S[l].rowptr, S[l].colind, S[l].val, S[l].rows, buf[cur], S[l].cols, acols, buf[cur ^ 1], E_STORE,
+                    nullptr, T(0));
+          cur ^= 1;
+        }
+        Smat = buf[cur];
+      }
+      const long N = (long)arows * acols;
+      T tr = T(0), ss = T(0);
+      for (long c0 = 0; c0 < N; c0 += CR_CHUNK) {
+        const long c1 = min(N, c0 + CR_CHUNK);
+        T a = T(0), s2 = T(0);
+        for (long i = c0 + threadIdx.x; i < c1; i += CR_LANES) {
+          a = fmad(I.A[i], Smat[i], a);
+          s2 = fmad(Smat[i], Smat[i], s2);
+        }
+        lane[threadIdx.x] = a;
+        tr = addr(tr, bat_tree(lane));
+        lane[threadIdx.x] = s2;
+        ss = addr(ss, bat_tree(lane));
+      }
+      const T nS = sqrtr(ss);
+      if (nS == T(0)) {
+        if (!P.no_lambda_error) {
+          if (threadIdx.x == 0) st = FGB_ERR_ZERO_NORM;
+          break;
+        }
+      } else if (isnan(tr) || isnan(nS)) {
+        if (!P.no_lambda_error) {
+          if (threadIdx.x == 0) st = FGB_ERR_NAN;
+          break;
+        }
+      } else {
+        lam = divr(tr, mulr(nS, nS));
+      }
+    }
+    __syncthreads();
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    I.status = st;
+    I.lambda = (double)lam;
+  }
+  (void)sh_c;
+  (void)sh_alpha;
+}
+
+template <typename T, typename TN>
+__global__ void __launch_bounds__(BT) k_palm_batched(Inst<T>* insts, const int* order, int* queue, Slot<T>* slots,
+                                                     const __grid_constant__ Params P, const int* rnd, int maxn) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  TN* vbuf = reinterpret_cast<TN*>(smem_raw);  // 3 * maxn
+  TN* lane_n = vbuf + 3 * (long)maxn;
+  __shared__ T lane[BT];
+  __shared__ int next;
+  const Slot<T> W = slots[blockIdx.x];
+  while (true) {
+    if (threadIdx.x == 0) next = atomicAdd(queue, 1);
+    __syncthreads();
+    const int q = next;
+    __syncthreads();
+    if (q >= P.ninst) break;
+    run_instance<T, TN>(insts[order[q]], W, P, rnd, vbuf, maxn, lane, lane_n);
+  }
+}
+
+}  // namespace bat
+
+// ------------------------------------------------------------------ host driver
+void free_factor(DevFactor& f);
+long palm_factor_capacity(const fgb_constraint& c);
+fgb_status pi_rand_device(fgb_ctx* ctx, int n, const int** d_rand);
+
+template <typename T>
+static fgb_status batched_impl(fgb_ctx* ctx, fgb_dtype dt, int nprob, const fgb_palm_problem* probs,
+                               const fgb_palm_params* p, const fgb_batch_opts* opts, fgb_palm_result* res) {
+  using namespace bat;
+  if (nprob <= 0 || !probs || !p || !res) return fail(ctx, FGB_ERR_INVALID_ARG, "batched palm4msa2: bad arguments");
+  int maxdim = 1, maxJ = 0;
+  for (int i = 0; i < nprob; ++i) {
+    const fgb_palm_problem& q = probs[i];
+    if (q.nfacts <= 0 || q.nfacts > MAXJ) return fail(ctx, FGB_ERR_INVALID_ARG, "instance %d: 1..%d factors", i, MAXJ);
+    if (!q.A || !q.cons) return fail(ctx, FGB_ERR_INVALID_ARG, "instance %d: null A or constraints", i);
+    if (q.cons[0].rows != q.rows || q.cons[q.nfacts - 1].cols != q.cols)
+      return fail(ctx, FGB_ERR_INVALID_ARG, "instance %d: constraint shapes do not match A", i);
+    for (int f = 0; f < q.nfacts; ++f) {
+      const fgb_constraint& c = q.cons[f];
+      if (f > 0 && q.cons[f - 1].cols != c.rows)
+        return fail(ctx, FGB_ERR_INVALID_ARG, "instance %d: factor %d shape mismatch", i, f);
+      const bool line = c.kind == FGB_SPCOL || c.kind == FGB_SPLIN || c.kind == FGB_SPLINCOL;
+      if (!(line || c.kind == FGB_NORMCOL || c.kind == FGB_NORMLIN || c.kind == FGB_SUPP))
+        return fail(ctx, FGB_ERR_NOT_SUPPORTED, "batched palm4msa2: constraint kind %d not supported", c.kind);
+      if (line && c.k > KMAX && c.k < std::max(c.rows, c.cols))
+        return fail(ctx, FGB_ERR_NOT_SUPPORTED, "batched palm4msa2: per-line k <= %d", KMAX);
+      if (c.kind == FGB_SUPP && !c.supp) return fail(ctx, FGB_ERR_INVALID_ARG, "SUPP without support");
+      if ((c.kind == FGB_NORMCOL || c.kind == FGB_NORMLIN) && c.s < 0)
+        return fail(ctx, FGB_ERR_INVALID_ARG, "Faust::prox_normcol : s < 0 ");
+      maxdim = std::max(maxdim, std::max(c.rows, c.cols));
+    }
+    maxJ = std::max(maxJ, q.nfacts);
+  }
+  if (p->norm2_max_iter <= 0 && !p->constant_step_size)
+    return fail(ctx, FGB_ERR_INVALID_ARG, "power_iteration :  nbr_iter_max <= 0");
+  FGB_CUDA(ctx, cudaSetDevice(ctx->device));
+  const size_t es = sizeof(T);
+  const long md2 = (long)maxdim * maxdim;
+  // slots
+  int per_sm = opts && opts->ctas_per_sm > 0 ? opts->ctas_per_sm : 2;
+  int nslots = std::min(nprob, per_sm * ctx->sm_count);
+  std::vector<void*> allocs;
+  auto alloc = [&](void** q, size_t b) -> fgb_status {
+    fgb_status s = dmalloc(ctx, q, b);
+    if (s == FGB_OK) allocs.push_back(*q);
+    return s;
+  };
+  fgb_status s = FGB_OK;
+  std::vector<Slot<T>> hs(nslots);
+  for (int i = 0; i < nslots && s == FGB_OK; ++i) {
+    s = alloc((void**)&hs[i].D, es * md2);
+    if (s == FGB_OK) s = alloc((void**)&hs[i].buf0, es * md2);
+    if (s == FGB_OK) s = alloc((void**)&hs[i].buf1, es * md2);
+    if (s == FGB_OK) s = alloc((void**)&hs[i].packed, es * md2 * std::max(1, maxJ));
+    if (s == FGB_OK) s = alloc((void**)&hs[i].flags, (size_t)md2);
+    if (s == FGB_OK) s = alloc((void**)&hs[i].cnt, sizeof(int) * (maxdim + 2));
+    if (s == FGB_OK) s = cuda_check(ctx, cudaMemsetAsync(hs[i].flags, 0, (size_t)md2, ctx->stream), "memset");
+  }
+  // instances and their factors
+  std::vector<Inst<T>> hi(nprob);
+  std::vector<std::vector<DevFactor>> facs(nprob);
+  std::vector<std::pair<const void*, T*>> supp_cache;
+  std::vector<T> h;
+  std::vector<std::pair<double, int>> cost(nprob);
+  for (int i = 0; i < nprob && s == FGB_OK; ++i) {
+    const fgb_palm_problem& q = probs[i];
+    Inst<T>& I = hi[i];
+    std::memset(&I, 0, sizeof(I));
+    I.J = q.nfacts;
+    I.arows = q.rows;
+    I.acols = q.cols;
+    I.A = (const T*)q.A;
+    I.lambda = q.init_lambda;
+    facs[i].resize(q.nfacts);
+    double cst = 0;
+    for (int f = 0; f < q.nfacts && s == FGB_OK; ++f) {
+      const fgb_constraint& c = q.cons[f];
+      DevFactor& F = facs[i][f];
+      F.format = FGB_CSR;
+      F.rows = c.rows;
+      F.cols = c.cols;
+      F.cap = (int)palm_factor_capacity(c);
+      h.assign((size_t)c.rows * c.cols, T(0));
+      if (q.init_facts) {
+        std::memcpy(h.data(), q.init_facts[f], es * h.size());
+      } else {
+        const bool zero = p->is_update_way_R2L ? (f == q.nfacts - 1) : (f == 0);
+        if (!zero)
+          for (int d = 0; d < std::min(c.rows, c.cols); ++d) h[(size_t)d * c.rows + d] = T(1);
+      }
+      // host CSR of the initial factor
+      std::vector<int> rp(c.rows + 1, 0), ci;
+      std::vector<T> vv;
+      for (int r = 0; r < c.rows; ++r) {
+        for (int col = 0; col < c.cols; ++col) {
+          const T v = h[(size_t)col * c.rows + r];
+          if (v != T(0)) {
+            ci.push_back(col);
+            vv.push_back(v);
+          }
+        }
+        rp[r + 1] = (int)ci.size();
+      }
+      F.cap = std::max<int>(F.cap, (int)ci.size());
+      F.nnz = (int)ci.size();
+      // transpose on the host (ordered by row)
+      std::vector<int> trp(c.cols + 1, 0), tci(ci.size());
+      std::vector<T> tvv(ci.size());
+      for (int col : ci) trp[col + 1]++;
+      for (int col = 0; col < c.cols; ++col) trp[col + 1] += trp[col];
+      std::vector<int> fill(trp.begin(), trp.end() - 1);
+      for (int r = 0; r < c.rows; ++r)
+        for (int pp = rp[r]; pp < rp[r + 1]; ++pp) {
+          const int slot = fill[ci[pp]]++;
+          tci[slot] = r;
+          tvv[slot] = vv[pp];
+        }
+      s = dmalloc(ctx, (void**)&F.rowptr, sizeof(int) * (c.rows + 1));
+      if (s == FGB_OK) s = dmalloc(ctx, (void**)&F.colind, sizeof(int) * F.cap);
+      if (s == FGB_OK) s = dmalloc(ctx, &F.val, es * F.cap);
+      if (s == FGB_OK) s = dmalloc(ctx, (void**)&F.t_rowptr, sizeof(int) * (c.cols + 1));
+      if (s == FGB_OK) s = dmalloc(ctx, (void**)&F.t_colind, sizeof(int) * F.cap);
+      if (s == FGB_OK) s = dmalloc(ctx, &F.t_val, es * F.cap);
+      if (s != FGB_OK) break;
+      cudaMemcpy(F.rowptr, rp.data(), sizeof(int) * rp.size(), cudaMemcpyHostToDevice);
+      cudaMemcpy(F.t_rowptr, trp.data(), sizeof(int) * trp.size(), cudaMemcpyHostToDevice);
+      if (!ci.empty()) {
+        cudaMemcpy(F.colind, ci.data(), sizeof(int) * ci.size(), cudaMemcpyHostToDevice);
+        cudaMemcpy(F.val, vv.data(), es * vv.size(), cudaMemcpyHostToDevice);
+        cudaMemcpy(F.t_colind, tci.data(), sizeof(int) * tci.size(), cudaMemcpyHostToDevice);
+        cudaMemcpy(F.t_val, tvv.data(), es * tvv.size(), cudaMemcpyHostToDevice);
+      }
+      F.has_t = true;
+      I.f[f] = Fac<T>{F.rows, F.cols, F.cap, 0, F.rowptr, F.colind, (T*)F.val, F.t_rowptr, F.t_colind, (T*)F.t_val};
+      Cons<T>& C = I.c[f];
+      C.kind = c.kind;
+      C.k = (int)std::min<long long>(c.k, 1 << 30);
+      C.normalized = p->no_normalization ? 0 : c.normalized;
+      C.pos = c.pos;
+      C.s = c.s;
+      C.supp = nullptr;
+      if (c.kind == FGB_SUPP) {
+        T* d = nullptr;
+        for (auto& e : supp_cache)
+          if (e.first == c.supp) d = e.second;
+        if (!d) {
+          s = alloc((void**)&d, es * (size_t)c.rows * c.cols);
+          if (s != FGB_OK) break;
+          cudaMemcpy(d, c.supp, es * (size_t)c.rows * c.cols, cudaMemcpyHostToDevice);
+          supp_cache.push_back({c.supp, d});
+        }
+        C.supp = d;
+      }
+      cst += (double)c.rows * c.cols;
+    }
+    cost[i] = {-(cst * q.nfacts), i};
+  }
+  if (s == FGB_OK) s = cuda_check(ctx, cudaGetLastError(), "batched upload");
+  Inst<T>* d_inst = nullptr;
+  Slot<T>* d_slots = nullptr;
+  int* d_order = nullptr;
+  int* d_queue = nullptr;
+  const int* rnd = nullptr;
+  if (s == FGB_OK) s = alloc((void**)&d_inst, sizeof(Inst<T>) * nprob);
+  if (s == FGB_OK) s = alloc((void**)&d_slots, sizeof(Slot<T>) * nslots);
+  if (s == FGB_OK) s = alloc((void**)&d_order, sizeof(int) * nprob);
+  if (s == FGB_OK) s = alloc((void**)&d_queue, sizeof(int));
+  if (s == FGB_OK) s = pi_rand_device(ctx, maxdim, &rnd);
+  if (s == FGB_OK) {
+    std::sort(cost.begin(), cost.end());
+    std::vector<int> order(nprob);
+    for (int i = 0; i < nprob; ++i) order[i] = cost[i].second;
+    cudaMemcpy(d_inst, hi.data(), sizeof(Inst<T>) * nprob, cudaMemcpyHostToDevice);
+    cudaMemcpy(d_slots, hs.data(), sizeof(Slot<T>) * nslots, cudaMemcpyHostToDevice);
+    cudaMemcpy(d_order, order.data(), sizeof(int) * nprob, cudaMemcpyHostToDevice);
+    s = cuda_check(ctx, cudaMemsetAsync(d_queue, 0, sizeof(int), ctx->stream), "memset");
+  }
+  if (s == FGB_OK) {
+    Params P;
+    std::memset(&P, 0, sizeof(P));
+    P.nb_it = p->nb_it;
+    P.r2l = p->is_update_way_R2L;
+    P.packing_RL = p->packing_RL;
+    P.no_lambda = p->no_lambda;
+    P.norm2_max_iter = p->norm2_max_iter;
+    P.constant_step = p->constant_step_size;
+    P.no_lambda_error = p->no_lambda_error;
+    P.norm2_fp64 = p->norm2_fp64;
+    P.norm2_threshold = p->norm2_threshold;
+    P.step_size = p->step_size;
+    P.maxdim2 = md2;
+    P.ninst = nprob;
+    const bool fp64n = sizeof(T) == 8 || p->norm2_fp64;
+    const size_t smem = (3 * (size_t)maxdim + BT) * (fp64n ? 8 : 4);
+    if (fp64n) {
+      auto kern = k_palm_batched<T, double>;
+      if (smem > 40 * 1024) s = cuda_check(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem), "attr");
+      if (s == FGB_OK) kern<<<nslots, BT, smem, ctx->stream>>>(d_inst, d_order, d_queue, d_slots, P, rnd, maxdim);
+    } else {
+      auto kern = k_palm_batched<T, float>;
+      if (smem > 40 * 1024) s = cuda_check(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem), "attr");
+      if (s == FGB_OK) kern<<<nslots, BT, smem, ctx->stream>>>(d_inst, d_order, d_queue, d_slots, P, rnd, maxdim);
+    }
+    if (s == FGB_OK) {
+      ctx->launches.fetch_add(1);
+      s = cuda_check(ctx, cudaGetLastError(), "batched palm launch");
+    }
+    if (s == FGB_OK) s = cuda_check(ctx, cudaStreamSynchronize(ctx->stream), "batched palm");
+  }
+  if (s == FGB_OK) {
+    cudaMemcpy(hi.data(), d_inst, sizeof(Inst<T>) * nprob, cudaMemcpyDeviceToHost);
+    for (int i = 0; i < nprob; ++i) {
+      res[i].lambda = hi[i].lambda;
+      res[i].status = hi[i].status;
+      fgb_faust* F = new fgb_faust();
+      F->ctx = ctx;
+      F->dtype = dt;
+      F->f = facs[i];
+      for (auto& f : F->f) {
+        int nnz = 0;
+        cudaMemcpy(&nnz, f.rowptr + f.rows, sizeof(int), cudaMemcpyDeviceToHost);
+        f.nnz = nnz;
+      }
+      facs[i].clear();
+      res[i].faust = F;
+    }
+  }
+  for (auto& v : facs)
+    for (auto& f : v) free_factor(f);
+  for (void* q : allocs) dfree(q);
+  return s;
+}
+
+}  // namespace fgb
+
+using namespace fgb;
+
+extern "C" fgb_status fgb_palm4msa2_batched(fgb_ctx* ctx, fgb_dtype dtype, int nprob, const fgb_palm_problem* probs,
+                                            const fgb_palm_params* params, const fgb_batch_opts* opts,
+                                            fgb_palm_result* results) {
+  if (!ctx) return FGB_ERR_INVALID_ARG;
+  if (dtype == FGB_F32) return batched_impl<float>(ctx, dtype, nprob, probs, params, opts, results);
+  if (dtype == FGB_F64) return batched_impl<double>(ctx, dtype, nprob, probs, params, opts, results);
+  return fail(ctx, FGB_ERR_NOT_SUPPORTED, "batched palm4msa2: F32 or F64");
+}

@@ -705,7 +705,13 @@ static fgb_status queue_sp(fgb_ctx* ctx, ProxWork& w, T* M, long N, long k, int 
     return fail(ctx, FGB_ERR_NOT_SUPPORTED, "prox_sp: k = %ld too large for the on-chip tie replay", k);
   }
   auto kern = k_heap_replay<T>;
-  if (smem > 48 * 1024) FGB_CUDA(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  // the kernel also has static shared arrays: opt in whenever the dynamic
+  // part approaches the default 48 KB limit (once per size, outside captures)
+  static thread_local size_t attr_set = 0;
+  if (smem > 40 * 1024 && smem > attr_set) {
+    FGB_CUDA(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    attr_set = smem;
+  }
   kern<<<1, PX_THREADS, smem, ctx->stream>>>(M, N, pos, (int)k, w.state, w.flags, gkey, gidx, use_smem ? 1 : 0);
   FGB_LAUNCHED(ctx);
   k_sp_apply<T><<<g, PX_THREADS, 0, ctx->stream>>>(M, N, pos, w.state, w.flags);

@@ -34,7 +34,13 @@ class ConstraintGeneric:
         if self.kind in (_ffi.NORMCOL, _ffi.NORMLIN):
             s = float(self.cons_value)
         elif self.kind == _ffi.SUPP:
-            a = np.asfortranarray(self.cons_value, dtype=dtype)
+            # one host copy per constraint object and dtype, so instances that
+            # share a constraint share its device copy in batched runs
+            cache = self.__dict__.setdefault("_supp_cache", {})
+            key = np.dtype(dtype).str
+            if key not in cache:
+                cache[key] = np.asfortranarray(self.cons_value, dtype=dtype)
+            a = cache[key]
             keep.append(a)
             supp = a.ctypes.data
         else:
@@ -148,6 +154,50 @@ def palm4msa(M, constraints, params=None, ret_lambda=True, ctx=None):
     check(st, ctx.handle)
     F = Faust._from_handle(h, ctx, dtype)
     return PalmResult(F, lam.value)
+
+
+def palm4msa_batched(problems, params, ctx=None, ctas_per_sm=0):
+    """Runs many palm4msa2 instances in one persistent launch.
+
+    problems: list of (M, constraints[, init_facts]) with M a column-major
+    CUDA tensor (float32 or float64, all the same dtype).  params: one
+    ParamsPalm4MSA for every instance (its constraints are ignored).
+    Returns a list of PalmResult; an instance that failed carries .status."""
+    import torch
+    ctx = ctx or default_context()
+    n = len(problems)
+    dtype = np.float64 if problems[0][0].dtype == torch.float64 else np.float32
+    keep = []
+    arr = (_ffi.PalmProblem * n)()
+    for i, prob in enumerate(problems):
+        M, cons = prob[0], prob[1]
+        init = prob[2] if len(prob) > 2 else None
+        rows, cols = M.shape
+        if not (M.is_cuda and M.stride(0) == 1 and (cols == 1 or M.stride(1) == rows)):
+            raise ValueError("instance %d: M must be a column-major CUDA tensor" % i)
+        ca = (_ffi.Constraint * len(cons))()
+        for f, c in enumerate(cons):
+            ca[f] = c._c(dtype, keep)
+        keep.append(ca)
+        ip = None
+        if init is not None:
+            arrs = [np.asfortranarray(x, dtype=dtype) for x in init]
+            keep += arrs
+            ip = (ctypes.c_void_p * len(arrs))(*[a.ctypes.data for a in arrs])
+            keep.append(ip)
+        arr[i] = _ffi.PalmProblem(rows, cols, M.data_ptr(), len(cons), ca, ip, float(params.init_lambda))
+    out = (_ffi.PalmResultC * n)()
+    p = params._c()
+    opts = _ffi.BatchOpts(int(ctas_per_sm))
+    check(_ffi.lib().fgb_palm4msa2_batched(ctx.handle, _ffi.F64 if dtype == np.float64 else _ffi.F32, n, arr,
+                                           ctypes.byref(p), ctypes.byref(opts), out), ctx.handle)
+    results = []
+    for i in range(n):
+        F = Faust._from_handle(ctypes.c_void_p(out[i].faust), ctx, dtype)
+        r = PalmResult(F, out[i].lambda_)
+        r.status = out[i].status
+        results.append(r)
+    return results
 
 
 def prox(M, constraint, ctx=None):

@@ -186,6 +186,37 @@ fgb_status fgb_palm4msa2_device(fgb_ctx* ctx, fgb_dtype dtype, const void* A_dev
                                 const fgb_constraint* cons, const fgb_palm_params* params,
                                 const void* const* init_facts, double* lambda, fgb_faust** out);
 
+/* ------------------------------------------------------------------ batched PALM4MSA
+ * Many independent palm4msa2 instances (uneven sizes) in ONE persistent
+ * launch: each CTA takes the next instance from a device work queue and runs
+ * its whole loop.  No reference counterpart exists as one call: it replaces
+ * a host loop of palm4msa2 calls (src/FaustFact.hpp:579-673 per instance).
+ * Supported constraints: SPCOL, SPLIN, SPLINCOL (k <= 64), NORMCOL, NORMLIN,
+ * SUPP; at most 16 factors.  Every instance is bit-identical to a
+ * single-instance run with the same parameters. */
+typedef struct fgb_palm_problem {
+  int rows, cols;                  /* shape of A */
+  const void* A;                   /* DEVICE, column-major, ld = rows */
+  int nfacts;
+  const fgb_constraint* cons;      /* host array (SUPP supports in host memory) */
+  const void* const* init_facts;   /* NULL or nfacts host dense factors */
+  double init_lambda;
+} fgb_palm_problem;
+
+typedef struct fgb_palm_result {
+  fgb_faust* faust;  /* release with fgb_faust_destroy */
+  double lambda;
+  int status;        /* fgb_status of this instance */
+} fgb_palm_result;
+
+typedef struct fgb_batch_opts {
+  int ctas_per_sm;   /* resident instances per SM (0 = default 2) */
+} fgb_batch_opts;
+
+fgb_status fgb_palm4msa2_batched(fgb_ctx* ctx, fgb_dtype dtype, int nprob, const fgb_palm_problem* problems,
+                                 const fgb_palm_params* params, const fgb_batch_opts* opts,
+                                 fgb_palm_result* results);
+
 /* calc_rel_err (faust_palm4msa2020.hpp:35-44): ||lambda F - A||_F / ||A||_F
  * with A in DEVICE memory. */
 fgb_status fgb_rel_err(fgb_faust* F, const void* A_dev, double lambda, double* out);

@@ -180,3 +180,66 @@ def test_palm_cancel_flag_is_honoured():
     with pytest.raises(Exception) as e:
         fact.palm4msa(H, cons, fact.ParamsPalm4MSA(cons, 50), ctx=ctx)
     assert "CANCELLED" in str(e.value)
+
+
+def _config4_instance(rng, n):
+    P = [synth.random_csr(n, n, 4, rng, np.float64).toarray() for _ in range(3)]
+    return (P[0] @ P[1] @ P[2] + 1e-3 * rng.standard_normal((n, n))).astype(np.float32)
+
+
+def test_palm_batched_matches_oracle_per_instance(oracle):
+    """Uneven splincol instances (the batched configuration's shape, smaller
+    n) in one persistent launch; each instance bit-identical to its oracle run."""
+    import torch
+    rng = np.random.default_rng(40)
+    sizes = [64, 144, 80, 112, 96, 128]
+    probs, host = [], []
+    for n in sizes:
+        A = _config4_instance(rng, n)
+        cons = [fact.ConstraintInt("splincol", n, n, 4) for _ in range(4)]
+        probs.append((_cuda_colmajor(A), cons))
+        host.append((A, cons))
+    params = fact.ParamsPalm4MSA(probs[0][1], 15, norm2_fp64=True)
+    res = fact.palm4msa_batched(probs, params, ctas_per_sm=1)
+    for r, (A, cons) in zip(res, host):
+        assert r.status == 0
+        facts_o, lam_o, _ = oracle.palm4msa2(A, [c.oracle_dict() for c in cons], 15, norm2_fp64=True)
+        got = [r.faust.factors(i).toarray() for i in range(4)]
+        for g, o in zip(got, facts_o):
+            assert np.array_equal(g.astype(np.float32), o)
+        assert r.lambda_ == lam_o
+
+
+def test_palm_batched_equals_single_instance_gpu():
+    rng = np.random.default_rng(41)
+    n = 96
+    A = _config4_instance(rng, n)
+    cons = [fact.ConstraintInt("splincol", n, n, 4) for _ in range(4)]
+    params = fact.ParamsPalm4MSA(cons, 12, norm2_fp64=True)
+    single = fact.palm4msa(A, cons, params)
+    batched = fact.palm4msa_batched([(_cuda_colmajor(A), cons)] * 3, params)
+    for r in batched:
+        assert r.lambda_ == single.lambda_
+        for i in range(4):
+            assert (r.faust.factors(i) != single.faust.factors(i)).nnz == 0
+
+
+def test_palm_batched_butterfly_supp(oracle):
+    rng = np.random.default_rng(42)
+    sups = synth.butterfly_supports(6, np.float32)
+    probs, host = [], []
+    for _ in range(4):
+        x = rng.random((64, 3))
+        d2 = ((x[:, None, :] - x[None, :, :]) ** 2).sum(-1)
+        K = np.exp(-d2 / (2 * 0.3 ** 2)).astype(np.float32)
+        cons = [fact.ConstraintMat("supp", s.toarray()) for s in sups]
+        init = [s.toarray() for s in sups]
+        probs.append((_cuda_colmajor(K), cons, init))
+        host.append((K, cons, init))
+    params = fact.ParamsPalm4MSA(probs[0][1], 10)
+    res = fact.palm4msa_batched(probs, params)
+    for r, (K, cons, init) in zip(res, host):
+        facts_o, lam_o, _ = oracle.palm4msa2(K, [c.oracle_dict() for c in cons], 10, init_facts=init)
+        assert r.lambda_ == lam_o
+        for i in range(6):
+            assert np.array_equal(r.faust.factors(i).toarray().astype(np.float32), facts_o[i])
