@@ -90,6 +90,17 @@ _SIGS = {
     "fgb_rel_err": (_I, [_P, _P, _D, ctypes.POINTER(_D)]),
     "fgb_palm4msa2_batched": (_I, [_P, _I, _I, ctypes.POINTER(PalmProblem), ctypes.POINTER(PalmParams),
                                    ctypes.POINTER(BatchOpts), ctypes.POINTER(PalmResultC)]),
+    # include/fgb_mlp.h
+    "fgb_gemm_bf16": (_I, [_P, _I, _I, _I, _P, ctypes.c_long, _P, ctypes.c_long, _P, ctypes.c_long, _I, _P, _I, _I,
+                           _P]),
+    "fgb_mlp_transpose_bf16": (_I, [_P, _I, _I, _P, ctypes.c_long, _P, ctypes.c_long]),
+    "fgb_mlp_relu_grad": (_I, [_P, ctypes.c_long, _P, _P, _P]),
+    "fgb_mlp_colsum": (_I, [_P, _I, _I, _P, ctypes.c_long, _P]),
+    "fgb_mlp_mse_grad": (_I, [_P, ctypes.c_long, _P, _P, ctypes.c_float, _P, _P]),
+    "fgb_mlp_adam": (_I, [_P, ctypes.c_long, _P, _P, _P, _P, _P, ctypes.c_float, ctypes.c_float, ctypes.c_float,
+                          ctypes.c_float, _I]),
+    "fgb_mlp_f32_to_bf16": (_I, [_P, ctypes.c_long, _P, _P]),
+    "fgb_mlp_bf16_to_f32": (_I, [_P, ctypes.c_long, _P, _P]),
 }
 
 

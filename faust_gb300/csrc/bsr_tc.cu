@@ -23,7 +23,7 @@
 #include <algorithm>
 #include <cstring>
 
-#include "fgb_internal.cuh"
+#include "tc_common.cuh"
 
 namespace fgb {
 
@@ -31,108 +31,13 @@ namespace tc {
 
 constexpr int BLK = 64;         // BSR block size
 constexpr int TM = 128;         // columns of X per tile (MMA M)
-constexpr int STAGES = 6;
+constexpr int STAGES = 8;
 constexpr int A_BYTES = TM * BLK * 2;   // 16 KB
 constexpr int B_BYTES = BLK * BLK * 2;  // 8 KB
 constexpr int STAGE_BYTES = A_BYTES + B_BYTES;
 constexpr int ACC_BUFS = 4;
 constexpr int TMEM_COLS = ACC_BUFS * BLK;  // 256
 constexpr int THREADS = 192;
-constexpr unsigned WAIT_LIMIT = 1u << 22;
-
-__device__ __forceinline__ uint32_t su32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
-
-__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(su32(bar)), "r"(count) : "memory");
-}
-__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(su32(bar)), "r"(bytes) : "memory");
-}
-__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
-  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(su32(bar)) : "memory");
-}
-__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
-  uint32_t ok;
-  asm volatile(
-      "{\n"
-      " .reg .pred p;\n"
-      " mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
-      " selp.u32 %0, 1, 0, p;\n"
-      "}\n"
-      : "=r"(ok)
-      : "r"(su32(bar)), "r"(parity)
-      : "memory");
-  return ok != 0;
-}
-// Bounded wait: false when the limit ran out or another role aborted.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, volatile int* abort_flag) {
-  for (unsigned i = 0; i < WAIT_LIMIT; ++i) {
-    if (mbar_try_wait(bar, parity)) return true;
-    if (*abort_flag) return false;
-  }
-  return false;
-}
-
-__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, int c0, int c1, uint64_t* bar) {
-  asm volatile(
-      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
-          su32(dst)),
-      "l"(map), "r"(c0), "r"(c1), "r"(su32(bar))
-      : "memory");
-}
-
-__device__ __forceinline__ void fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
-__device__ __forceinline__ void fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
-
-// Shared-memory matrix descriptor: K-major tile with 128-byte swizzle, rows
-// of 128 bytes, 8-row groups 1024 bytes apart (tile base 1024-byte aligned).
-__device__ __forceinline__ uint64_t sdesc_k128(uint32_t saddr) {
-  uint64_t d = 0;
-  d |= (uint64_t)((saddr & 0x3FFFFu) >> 4);  // start address
-  d |= (uint64_t)1 << 16;                     // leading byte offset (unused with this swizzle)
-  d |= (uint64_t)(1024 >> 4) << 32;           // stride byte offset: 8 rows x 128 B
-  d |= (uint64_t)1 << 46;                     // descriptor version
-  d |= (uint64_t)2 << 61;                     // 128-byte swizzle
-  return d;
-}
-
-// Instruction descriptor of kind::f16: D F32, A and B BF16, both K-major,
-// N = 64, M = 128.
-constexpr uint32_t IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BLK >> 3) << 17) |
-                           ((uint32_t)(TM >> 4) << 24);
-
-__device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t accumulate) {
-  asm volatile(
-      "{\n"
-      " .reg .pred p;\n"
-      " setp.ne.b32 p, %4, 0;\n"
-      " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n"
-      "}\n" ::"r"(d_tmem),
-      "l"(adesc), "l"(bdesc), "r"(IDESC), "r"(accumulate)
-      : "memory");
-}
-__device__ __forceinline__ void mma_commit(uint64_t* bar) {
-  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(su32(bar))
-               : "memory");
-}
-
-__device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
-  asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
-      "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
-      "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
-      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
-        "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
-        "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
-      : "r"(taddr));
-}
-__device__ __forceinline__ void tmem_ld_wait() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
-
-__device__ __forceinline__ uint32_t pack_bf16(uint32_t lo, uint32_t hi) {
-  const __nv_bfloat162 v = __floats2bfloat162_rn(__uint_as_float(lo), __uint_as_float(hi));
-  return *reinterpret_cast<const uint32_t*>(&v);
-}
 
 struct Shared {
   uint64_t full[STAGES];
@@ -179,45 +84,56 @@ __global__ void __launch_bounds__(THREADS, 1)
 
   if (warp == 0) {
     // ---------------------------------------------------------------- producer
-    if (lane == 0) {
-      int s = 0;
-      uint32_t ph = 0;
-      long issued = 0, waited_ok = 1;
-      int pend[STAGES];  // parity of the last load issued into each stage, or -1
-      for (int u = 0; u < STAGES; ++u) pend[u] = -1;
-      for (long it = blockIdx.x; it < items && waited_ok; it += gridDim.x) {
-        const int mt = (int)(it / nbr), br = (int)(it % nbr);
-        const int p0 = browptr[br], p1 = browptr[br + 1];
-        for (int p = p0; p < p1; ++p) {
-          if (!mbar_wait(&sh->empty[s], ph ^ 1u, abort_flag)) {
-            waited_ok = 0;
+    // The whole warp walks the items; the block indices of an item are read
+    // with one coalesced load (32 per round) and lane 0 issues the TMA loads.
+    int s = 0;
+    uint32_t ph = 0;
+    bool waited_ok = true;
+    int pend[STAGES];  // parity of the last load issued into each stage, or -1
+    for (int u = 0; u < STAGES; ++u) pend[u] = -1;
+    for (long it = blockIdx.x; it < items && waited_ok; it += gridDim.x) {
+      const int mt = (int)(it / nbr), br = (int)(it % nbr);
+      const int p0 = browptr[br], p1 = browptr[br + 1];
+      for (int pb = p0; pb < p1 && waited_ok; pb += 32) {
+        const int mine = (pb + lane < p1) ? bcolind[pb + lane] : 0;
+        const int nb = min(32, p1 - pb);
+        for (int q = 0; q < nb; ++q) {
+          const int bc = __shfl_sync(0xffffffffu, mine, q);
+          bool ok = true;
+          if (lane == 0) ok = mbar_wait(&sh->empty[s], ph ^ 1u, abort_flag);
+          ok = __shfl_sync(0xffffffffu, ok ? 1 : 0, 0) != 0;
+          if (!ok) {
+            waited_ok = false;
             break;
           }
-          unsigned char* st = base + s * STAGE_BYTES;
-          mbar_expect_tx(&sh->full[s], STAGE_BYTES);
-          tma_load_2d(st, &tmX, bcolind[p] * BLK, mt * TM, &sh->full[s]);
-          tma_load_2d(st + A_BYTES, &tmB, 0, p * BLK, &sh->full[s]);
+          if (lane == 0) {
+            unsigned char* st = base + s * STAGE_BYTES;
+            mbar_expect_tx(&sh->full[s], STAGE_BYTES);
+            tma_load_2d(st, &tmX, bc * BLK, mt * TM, &sh->full[s]);
+            tma_load_2d(st + A_BYTES, &tmB, 0, (pb + q) * BLK, &sh->full[s]);
+          }
           pend[s] = (int)ph;
-          ++issued;
           if (++s == STAGES) {
             s = 0;
             ph ^= 1u;
           }
         }
       }
+    }
+    if (lane == 0) {
       if (!waited_ok) {
         atomicExch(err, 1);
         *abort_flag = 1;
       }
-      // on an abort, the copies this thread issued must land before the
-      // shared memory is released (bounded waits)
+      // on an abort, the copies this warp issued must land before the shared
+      // memory is released (bounded waits)
       if (*abort_flag)
         for (int u = 0; u < STAGES; ++u)
           if (pend[u] >= 0)
             for (unsigned i = 0; i < WAIT_LIMIT && !mbar_try_wait(&sh->full[u], (uint32_t)pend[u]); ++i) {
             }
-      (void)issued;
     }
+    __syncwarp();
   } else if (warp == 1) {
     // ---------------------------------------------------------------- MMA issuer
     if (lane == 0) {
@@ -244,7 +160,8 @@ __global__ void __launch_bounds__(THREADS, 1)
           const uint64_t ad = sdesc_k128(sa), bd = sdesc_k128(sb);
 #pragma unroll
           for (int k = 0; k < BLK / 16; ++k)
-            mma_bf16(d, ad + (uint64_t)((k * 32) >> 4), bd + (uint64_t)((k * 32) >> 4), (p > p0 || k > 0) ? 1u : 0u);
+            mma_bf16(d, ad + (uint64_t)((k * 32) >> 4), bd + (uint64_t)((k * 32) >> 4), idesc_bf16(TM, BLK),
+                     (p > p0 || k > 0) ? 1u : 0u);
           mma_commit(&sh->empty[s]);
           if (++s == STAGES) {
             s = 0;
@@ -333,10 +250,6 @@ __global__ void k_blocks_rowmajor(const __nv_bfloat16* __restrict__ in, __nv_bfl
   }
 }
 
-typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
-                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
-                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
-
 static EncodeTiledFn encode_fn() {
   static EncodeTiledFn fn = nullptr;
   static bool tried = false;
@@ -352,8 +265,8 @@ static EncodeTiledFn encode_fn() {
   return fn;
 }
 
-static bool make_map(CUtensorMap* m, const void* base, uint64_t inner, uint64_t outer, uint64_t row_bytes,
-                     uint32_t box_inner, uint32_t box_outer) {
+bool make_map_bf16(CUtensorMap* m, const void* base, uint64_t inner, uint64_t outer, uint64_t row_bytes,
+                   uint32_t box_inner, uint32_t box_outer) {
   EncodeTiledFn fn = encode_fn();
   if (!fn) return false;
   cuuint64_t dims[2] = {inner, outer};
@@ -394,8 +307,8 @@ fgb_status launch_bsr_tc(fgb_ctx* ctx, const DevFactor& f, const __nv_bfloat16* 
   const __nv_bfloat16* blocks = (const __nv_bfloat16*)f.aux;
   if (!blocks) return FGB_OK;
   CUtensorMap mx, mb;
-  if (!tc::make_map(&mx, X, (uint64_t)f.cols, (uint64_t)ncols, (uint64_t)ldx * 2, tc::BLK, tc::TM)) return FGB_OK;
-  if (!tc::make_map(&mb, blocks, (uint64_t)tc::BLK, (uint64_t)f.nnz * tc::BLK, tc::BLK * 2, tc::BLK, tc::BLK))
+  if (!tc::make_map_bf16(&mx, X, (uint64_t)f.cols, (uint64_t)ncols, (uint64_t)ldx * 2, tc::BLK, tc::TM)) return FGB_OK;
+  if (!tc::make_map_bf16(&mb, blocks, (uint64_t)tc::BLK, (uint64_t)f.nnz * tc::BLK, tc::BLK * 2, tc::BLK, tc::BLK))
     return FGB_OK;
   if (!g_err) {
     FGB_TRY(dmalloc(ctx, (void**)&g_err, sizeof(int)));

@@ -8,7 +8,7 @@
 
 namespace fgb {
 
-constexpr int SPMM_THREADS = 256;
+constexpr int SPMM_THREADS = 512;
 
 // ------------------------------------------------------------------ helpers
 template <typename T, int TC>

@@ -151,16 +151,18 @@ __device__ __forceinline__ T lane_tree_256(T* lane) {
   return r;
 }
 
-// Canonical dot product of a[0..n) and b[0..n) by one block of exactly 256
-// threads; every thread receives the result.
+// Canonical dot product of a[0..n) and b[0..n) by one block of at least 256
+// threads (threads 0..255 hold the lanes); every thread receives the result.
 template <typename T>
 __device__ T block_cdot(const T* a, const T* b, long n, T* lane) {
   T total = T(0);
   for (long c0 = 0; c0 < n; c0 += CR_CHUNK) {
     long c1 = c0 + CR_CHUNK < n ? c0 + CR_CHUNK : n;
-    T acc = T(0);
-    for (long i = c0 + threadIdx.x; i < c1; i += CR_LANES) acc = fmad(a[i], b[i], acc);
-    lane[threadIdx.x] = acc;
+    if (threadIdx.x < CR_LANES) {
+      T acc = T(0);
+      for (long i = c0 + threadIdx.x; i < c1; i += CR_LANES) acc = fmad(a[i], b[i], acc);
+      lane[threadIdx.x] = acc;
+    }
     T part = lane_tree_256(lane);
     total = addr(total, part);
   }

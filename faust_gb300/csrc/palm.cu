@@ -230,7 +230,7 @@ struct Palm {
     k_set_scalar<T><<<1, 1, 0, ctx->stream>>>(lam, init_lambda);
     FGB_LAUNCHED(ctx);
     FGB_TRY(pi_rand_device(ctx, maxdim, &rnd));
-    FGB_TRY(prox_work_reserve(ctx, pw, (long)maxdim * maxdim, maxdim));
+    FGB_TRY(prox_work_reserve(ctx, pw, (long)maxdim * maxdim, 2 * maxdim + 2));
     packed.assign(J, nullptr);
     supp.assign(J, nullptr);
     S.resize(J);
@@ -281,7 +281,7 @@ struct Palm {
         FGB_TRY(dmalloc(ctx, &f.t_val, es * f.cap));
       }
       FGB_CUDA(ctx, cudaMemcpyAsync(D, h.data(), es * h.size(), cudaMemcpyHostToDevice, ctx->stream));
-      FGB_TRY(launch_dense_to_csr<T>(ctx, pw, D, f));
+      FGB_TRY(launch_dense_to_csr<T>(ctx, pw, D, f, status));
       FGB_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     }
     return FGB_OK;
@@ -416,7 +416,7 @@ struct Palm {
     }
     // ---- projection and replacement
     FGB_TRY(launch_prox<T>(ctx, pw, cons[f], D, Sf.rows, Sf.cols, supp[f], status));
-    FGB_TRY(launch_dense_to_csr<T>(ctx, pw, D, S[f]));
+    FGB_TRY(launch_dense_to_csr<T>(ctx, pw, D, S[f], status));
     return FGB_OK;
   }
 

@@ -46,15 +46,31 @@ __device__ __forceinline__ T absd(T x) {
 // |l_old - l| > thr or |l| <= thr (at most max_iter), normalise by 1/||x||,
 // x = A x, stop with 0 on a zero vector, l = <x_norm, x>.  Result:
 // |sqrt(l)| (Transform::spectralNorm).
+//
+// The CSR arrays of the chain's products are copied into shared memory once
+// (as many as fit after the vectors), so each of the ~2*len products of an
+// iteration is a shared-memory pass; the rest are read from L2.
+struct PIStaged {
+  const int* rp;
+  const int* ci;
+  const void* v;
+  int rows;
+  int pad;
+};
+
 template <typename TF, typename TC>
 __global__ void __launch_bounds__(PI_THREADS)
     k_power_iteration(const __grid_constant__ PIChain ca, const __grid_constant__ PIChain cb, int max_iter, TC thr,
-                      const int* __restrict__ rnd, PIOut* out, const __grid_constant__ PIPalm palm, int maxn) {
+                      const int* __restrict__ rnd, PIOut* out, const __grid_constant__ PIPalm palm, int maxn,
+                      int smem_bytes) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ PIStaged ops[PI_MAX_OPS];
   TC* buf0 = reinterpret_cast<TC*>(smem_raw);
   TC* buf1 = buf0 + maxn;
   TC* buf2 = buf1 + maxn;
   TC* lane = buf2 + maxn;
+  unsigned char* pool = reinterpret_cast<unsigned char*>(lane + CR_LANES);
+  const long pool_bytes = smem_bytes - (long)(pool - smem_raw);
   const PIChain& ch = (blockIdx.x == 0) ? ca : cb;
   double result = 1.0;
   int flag = 0;
@@ -70,6 +86,43 @@ __global__ void __launch_bounds__(PI_THREADS)
     result = 0.0;
   } else {
     const int n = ch.n;
+    // stage the products' CSR arrays (16-byte aligned pieces) while they fit
+    if (threadIdx.x == 0) {
+      long off = 0;
+      for (int o = 0; o < ch.nops; ++o) {
+        const PIOp op = ch.ops[o];
+        const int nnz = op.rowptr[op.rows];
+        const long need = ((long)(op.rows + 1) * 4 + 15) / 16 * 16 + ((long)nnz * 4 + 15) / 16 * 16 +
+                          ((long)nnz * sizeof(TF) + 15) / 16 * 16;
+        if (off + need <= pool_bytes) {
+          int* rp = reinterpret_cast<int*>(pool + off);
+          off += ((long)(op.rows + 1) * 4 + 15) / 16 * 16;
+          int* ci = reinterpret_cast<int*>(pool + off);
+          off += ((long)nnz * 4 + 15) / 16 * 16;
+          TF* v = reinterpret_cast<TF*>(pool + off);
+          off += ((long)nnz * sizeof(TF) + 15) / 16 * 16;
+          ops[o] = PIStaged{rp, ci, v, op.rows, 1};
+        } else {
+          ops[o] = PIStaged{op.rowptr, op.colind, op.val, op.rows, 0};
+        }
+      }
+    }
+    __syncthreads();
+    for (int o = 0; o < ch.nops; ++o) {
+      if (!ops[o].pad) continue;
+      const PIOp op = ch.ops[o];
+      const int nnz = op.rowptr[op.rows];
+      int* rp = const_cast<int*>(ops[o].rp);
+      int* ci = const_cast<int*>(ops[o].ci);
+      TF* v = reinterpret_cast<TF*>(const_cast<void*>(ops[o].v));
+      const TF* gv = reinterpret_cast<const TF*>(op.val);
+      for (int i = threadIdx.x; i <= op.rows; i += blockDim.x) rp[i] = op.rowptr[i];
+      for (int i = threadIdx.x; i < nnz; i += blockDim.x) {
+        ci[i] = op.colind[i];
+        v[i] = gv[i];
+      }
+    }
+    __syncthreads();
     TC* bufs[3] = {buf0, buf1, buf2};
     int xi = 0;
     for (int i = threadIdx.x; i < n; i += blockDim.x)
@@ -95,14 +148,14 @@ __global__ void __launch_bounds__(PI_THREADS)
       // the normalised vector for the dot product
       int si = xi, di = (xi + 1) % 3;
       for (int o = 0; o < ch.nops; ++o) {
-        const PIOp op = ch.ops[o];
-        const TF* __restrict__ val = reinterpret_cast<const TF*>(op.val);
+        const PIStaged op = ops[o];
+        const TF* __restrict__ val = reinterpret_cast<const TF*>(op.v);
         const TC* src = bufs[si];
         TC* dst = bufs[di];
         for (int r = threadIdx.x; r < op.rows; r += blockDim.x) {
           TC acc = TC(0);
-          const int p1 = op.rowptr[r + 1];
-          for (int p = op.rowptr[r]; p < p1; ++p) acc = fmad((TC)val[p], src[op.colind[p]], acc);
+          const int p1 = op.rp[r + 1];
+          for (int p = op.rp[r]; p < p1; ++p) acc = fmad((TC)val[p], src[op.ci[p]], acc);
           dst[r] = acc;
         }
         __syncthreads();
@@ -197,12 +250,19 @@ template <typename TF, typename TC>
 static fgb_status launch_pi_t(fgb_ctx* ctx, const PIChain& a, const PIChain& b, int max_iter, double thr,
                               const int* d_rand, PIOut* d_out, const PIPalm& palm) {
   const int maxn = std::max(1, std::max(a.maxdim, b.maxdim));
-  const size_t smem = (3 * (size_t)maxn + PI_THREADS) * sizeof(TC);
-  if (smem > ctx->smem_optin)
+  const size_t vec = (3 * (size_t)maxn + CR_LANES) * sizeof(TC);
+  const size_t cap = std::min<size_t>(ctx->smem_optin > 4096 ? ctx->smem_optin - 4096 : 0, 220 * 1024);
+  if (vec > cap)
     return fail(ctx, FGB_ERR_NOT_SUPPORTED, "power iteration: vector of %d entries does not fit on chip", maxn);
+  // the rest of shared memory stages the chain's CSR arrays
+  const size_t smem = cap;
   auto kern = k_power_iteration<TF, TC>;
-  if (smem > 48 * 1024) FGB_CUDA(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  kern<<<2, PI_THREADS, smem, ctx->stream>>>(a, b, max_iter, (TC)thr, d_rand, d_out, palm, maxn);
+  static thread_local size_t attr_set = 0;
+  if (smem > attr_set) {
+    FGB_CUDA(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    attr_set = smem;
+  }
+  kern<<<2, PI_THREADS, smem, ctx->stream>>>(a, b, max_iter, (TC)thr, d_rand, d_out, palm, maxn, (int)smem);
   FGB_LAUNCHED(ctx);
   return FGB_OK;
 }

@@ -27,7 +27,6 @@
 namespace fgb {
 
 constexpr int PX_THREADS = 256;
-constexpr int HEAP_CHUNK = 2048;
 constexpr int LINE_KMAX = 64;
 
 __device__ __forceinline__ unsigned long long mag_key(double v) {
@@ -69,6 +68,7 @@ void prox_work_free(ProxWork& w) {
   dfree(w.scal);
   dfree(w.row_cnt);
   dfree(w.supp);
+  dfree(w.heap);
   w = ProxWork();
 }
 
@@ -257,120 +257,133 @@ __global__ void __launch_bounds__(PX_THREADS)
 }
 
 // ------------------------------------------------------------------ heap replay
+// A heap node: magnitude key and position, read and written as one 16-byte
+// shared-memory access.
+struct __align__(16) HNode {
+  unsigned long long key;
+  long long idx;
+};
+
 struct HeapView {
-  unsigned long long* key;
-  int* idx;
+  HNode* n;
 };
 
 // Standard binary-heap adjustment with the comparator "larger key first":
 // move the hole to a leaf along the child preferred by the comparator (the
 // left child only when it is strictly preferred), then sift the value up.
-__device__ void heap_adjust(HeapView h, int hole, int len, unsigned long long vkey, int vidx) {
+__device__ void heap_adjust(HeapView h, int hole, int len, HNode v) {
   const int top = hole;
   int child = hole;
   while (child < (len - 1) / 2) {
     child = 2 * (child + 1);
-    if (h.key[child] > h.key[child - 1]) child--;
-    h.key[hole] = h.key[child];
-    h.idx[hole] = h.idx[child];
+    const HNode r = h.n[child], l = h.n[child - 1];
+    if (r.key > l.key) {
+      h.n[hole] = l;
+      child--;
+    } else {
+      h.n[hole] = r;
+    }
     hole = child;
   }
   if ((len & 1) == 0 && child == (len - 2) / 2) {
     child = 2 * (child + 1);
-    h.key[hole] = h.key[child - 1];
-    h.idx[hole] = h.idx[child - 1];
+    h.n[hole] = h.n[child - 1];
     hole = child - 1;
   }
   int parent = (hole - 1) / 2;
-  while (hole > top && h.key[parent] > vkey) {
-    h.key[hole] = h.key[parent];
-    h.idx[hole] = h.idx[parent];
+  while (hole > top) {
+    const HNode pn = h.n[parent];
+    if (!(pn.key > v.key)) break;
+    h.n[hole] = pn;
     hole = parent;
     parent = (hole - 1) / 2;
   }
-  h.key[hole] = vkey;
-  h.idx[hole] = vidx;
+  h.n[hole] = v;
 }
+
+constexpr int HR_CHUNK = 8192;
+constexpr int HR_PER = HR_CHUNK / PX_THREADS;  // 32 entries per thread
 
 template <typename T>
 __global__ void __launch_bounds__(PX_THREADS)
     k_heap_replay(const T* __restrict__ M, long N, int pos, int k, TopkState* st, unsigned char* __restrict__ flags,
-                  unsigned long long* gkey, int* gidx, int use_smem) {
+                  HNode* gheap, int use_smem) {
   if (st->sel_case != 2) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  __shared__ int s_cnt[PX_THREADS];
+  __shared__ int warp_tot[PX_THREADS / 32];
   __shared__ int s_ncand;
-  unsigned long long* ckey = reinterpret_cast<unsigned long long*>(smem_raw);  // HEAP_CHUNK keys
-  int* cidx = reinterpret_cast<int*>(ckey + HEAP_CHUNK);                         // HEAP_CHUNK candidates
+  HNode* cand = reinterpret_cast<HNode*>(smem_raw);  // HR_CHUNK candidates
   HeapView h;
-  if (use_smem) {
-    h.key = reinterpret_cast<unsigned long long*>(cidx + HEAP_CHUNK);
-    h.idx = reinterpret_cast<int*>(h.key + k);
-  } else {
-    h.key = gkey;
-    h.idx = gidx;
-  }
-  for (int i = threadIdx.x; i < k; i += blockDim.x) {
-    h.key[i] = mag_key(pos_adj(M[i], pos));
-    h.idx[i] = i;
-  }
+  h.n = use_smem ? cand + HR_CHUNK : gheap;
+  for (int i = threadIdx.x; i < k; i += blockDim.x) h.n[i] = HNode{mag_key(pos_adj(M[i], pos)), i};
   __syncthreads();
   if (threadIdx.x == 0 && k >= 2) {
     int parent = (k - 2) / 2;
     while (true) {
-      heap_adjust(h, parent, k, h.key[parent], h.idx[parent]);
+      heap_adjust(h, parent, k, h.n[parent]);
       if (parent == 0) break;
       parent--;
     }
   }
   __syncthreads();
-  constexpr int PER = HEAP_CHUNK / PX_THREADS;
-  for (long c0 = k; c0 < N; c0 += HEAP_CHUNK) {
-    const unsigned long long topk = h.key[0];
-    const long c1 = min(N, c0 + HEAP_CHUNK);
-    // parallel filter: only keys above the current top can enter
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (long c0 = k; c0 < N; c0 += HR_CHUNK) {
+    const unsigned long long topk = h.n[0].key;
+    const long c1 = min(N, c0 + HR_CHUNK);
+    // parallel filter (a key not above the current top can never enter):
+    // thread t looks at entries c0 + t + 256*u, keeping chunk order per warp
+    // slice through a two-level scan
+    unsigned long long kk[HR_PER];
     int cnt = 0;
-    const long base = c0 + threadIdx.x * PER;
-    unsigned long long kk[PER];
+    const long base = c0 + (long)threadIdx.x * HR_PER;
 #pragma unroll
-    for (int u = 0; u < PER; ++u) {
+    for (int u = 0; u < HR_PER; ++u) {
       const long i = base + u;
       kk[u] = (i < c1) ? mag_key(pos_adj(M[i], pos)) : 0ULL;
       cnt += (i < c1) && kk[u] > topk;
     }
-    s_cnt[threadIdx.x] = cnt;
+    if (__syncthreads_count(cnt) == 0) continue;
+    int incl = cnt;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += y;
+    }
+    if (lane == 31) warp_tot[warp] = incl;
     __syncthreads();
     if (threadIdx.x == 0) {
       int run = 0;
-      for (int u = 0; u < PX_THREADS; ++u) {
-        const int c = s_cnt[u];
-        s_cnt[u] = run;
-        run += c;
+      for (int w = 0; w < PX_THREADS / 32; ++w) {
+        const int t = warp_tot[w];
+        warp_tot[w] = run;
+        run += t;
       }
       s_ncand = run;
     }
     __syncthreads();
-    int off = s_cnt[threadIdx.x];
+    int off = warp_tot[warp] + incl - cnt;
 #pragma unroll
-    for (int u = 0; u < PER; ++u) {
+    for (int u = 0; u < HR_PER; ++u) {
       const long i = base + u;
-      if (i < c1 && kk[u] > topk) {
-        ckey[off] = kk[u];
-        cidx[off] = (int)i;
-        ++off;
-      }
+      if (i < c1 && kk[u] > topk) cand[off++] = HNode{kk[u], i};
     }
     __syncthreads();
     if (threadIdx.x == 0) {
       const int nc = s_ncand;
-      for (int q = 0; q < nc; ++q)
-        if (ckey[q] > h.key[0]) heap_adjust(h, 0, k, ckey[q], cidx[q]);
+      unsigned long long top = h.n[0].key;
+      for (int q = 0; q < nc; ++q) {
+        const HNode c = cand[q];
+        if (c.key > top) {
+          heap_adjust(h, 0, k, c);
+          top = h.n[0].key;
+        }
+      }
     }
     __syncthreads();
   }
   const unsigned long long t = st->t;
   for (int i = threadIdx.x; i < k; i += blockDim.x)
-    if (h.key[i] == t) flags[h.idx[i]] = 1;
+    if (h.n[i].key == t) flags[h.n[i].idx] = 1;
 }
 
 // ------------------------------------------------------------------ sp apply
@@ -419,26 +432,22 @@ __global__ void k_line_topk(const T* __restrict__ M, int rows, int cols, int by_
     for (int e = 0; e < len; ++e) flags[at(e)] |= bit;
     return;
   }
-  unsigned long long hk[LINE_KMAX];
-  int hi[LINE_KMAX];
-  HeapView h{hk, hi};
-  for (int e = 0; e < k; ++e) {
-    hk[e] = mag_key(pos_adj(M[at(e)], pos));
-    hi[e] = e;
-  }
+  HNode hn[LINE_KMAX];
+  HeapView h{hn};
+  for (int e = 0; e < k; ++e) hn[e] = HNode{mag_key(pos_adj(M[at(e)], pos)), e};
   if (k >= 2) {
     int parent = (k - 2) / 2;
     while (true) {
-      heap_adjust(h, parent, k, hk[parent], hi[parent]);
+      heap_adjust(h, parent, k, hn[parent]);
       if (parent == 0) break;
       parent--;
     }
   }
   for (int e = k; e < len; ++e) {
     const unsigned long long key = mag_key(pos_adj(M[at(e)], pos));
-    if (key > hk[0]) heap_adjust(h, 0, k, key, e);
+    if (key > hn[0].key) heap_adjust(h, 0, k, HNode{key, e});
   }
-  for (int e = 0; e < k; ++e) flags[at(hi[e])] |= bit;
+  for (int e = 0; e < k; ++e) flags[at((int)hn[e].idx)] |= bit;
 }
 
 template <typename T>
@@ -694,15 +703,23 @@ static fgb_status queue_sp(fgb_ctx* ctx, ProxWork& w, T* M, long N, long k, int 
   const int nch = (int)((N + chunk - 1) / chunk);
   k_tie_case<T><<<nch, PX_THREADS, 0, ctx->stream>>>(M, N, pos, chunk, w.state, w.chunk_cnt);
   FGB_LAUNCHED(ctx);
-  const size_t heap_smem = (size_t)HEAP_CHUNK * (8 + 4) + (size_t)k * 12;
-  const bool use_smem = heap_smem <= std::min<size_t>(ctx->smem_optin, 200 * 1024);
-  unsigned long long* gkey = nullptr;
-  int* gidx = nullptr;
-  size_t smem = (size_t)HEAP_CHUNK * (8 + 4);
-  if (use_smem) {
-    smem = heap_smem;
-  } else {
-    return fail(ctx, FGB_ERR_NOT_SUPPORTED, "prox_sp: k = %ld too large for the on-chip tie replay", k);
+  // candidates of one chunk, then the heap itself when it fits on chip;
+  // larger heaps live in the workspace
+  const size_t cand_bytes = (size_t)HR_CHUNK * sizeof(HNode);
+  const size_t heap_bytes = (size_t)k * sizeof(HNode);
+  const size_t cap = std::min<size_t>(ctx->smem_optin > 8192 ? ctx->smem_optin - 8192 : 0, 200 * 1024);
+  const bool use_smem = cand_bytes + heap_bytes <= cap;
+  size_t smem = use_smem ? cand_bytes + heap_bytes : cand_bytes;
+  HNode* gheap = nullptr;
+  if (!use_smem) {
+    if (w.heap_cap < k) {
+      dfree(w.heap);
+      w.heap = nullptr;
+      w.heap_cap = 0;
+      FGB_TRY(dmalloc(ctx, &w.heap, heap_bytes));
+      w.heap_cap = k;
+    }
+    gheap = reinterpret_cast<HNode*>(w.heap);
   }
   auto kern = k_heap_replay<T>;
   // the kernel also has static shared arrays: opt in whenever the dynamic
@@ -712,7 +729,7 @@ static fgb_status queue_sp(fgb_ctx* ctx, ProxWork& w, T* M, long N, long k, int 
     FGB_CUDA(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     attr_set = smem;
   }
-  kern<<<1, PX_THREADS, smem, ctx->stream>>>(M, N, pos, (int)k, w.state, w.flags, gkey, gidx, use_smem ? 1 : 0);
+  kern<<<1, PX_THREADS, smem, ctx->stream>>>(M, N, pos, (int)k, w.state, w.flags, gheap, use_smem ? 1 : 0);
   FGB_LAUNCHED(ctx);
   k_sp_apply<T><<<g, PX_THREADS, 0, ctx->stream>>>(M, N, pos, w.state, w.flags);
   FGB_LAUNCHED(ctx);
@@ -802,21 +819,131 @@ fgb_status launch_prox(fgb_ctx* ctx, ProxWork& w, const fgb_constraint& c, T* M,
   return FGB_OK;
 }
 
+// dense -> CSR and CSR of the transpose.  One warp per row (lanes over
+// columns) and one warp per column (lanes over rows) count the non-zero
+// entries, a block scans both count arrays, then the same warps write the
+// entries by ballot compaction, which keeps rows in column order and
+// columns in row order.
 template <typename T>
-fgb_status launch_dense_to_csr(fgb_ctx* ctx, ProxWork& w, const T* M, DevFactor& f) {
-  FGB_TRY(prox_work_reserve(ctx, w, (long)f.rows * f.cols, std::max(f.rows, f.cols)));
-  const int rb = (f.rows + 127) / 128;
-  k_d2c_count<T><<<rb, 128, 0, ctx->stream>>>(M, f.rows, f.cols, w.row_cnt);
-  FGB_LAUNCHED(ctx);
-  k_d2c_scan<<<1, 1024, 0, ctx->stream>>>(w.row_cnt, f.rows, f.rowptr, f.cap, nullptr);
-  FGB_LAUNCHED(ctx);
-  k_d2c_write<T><<<rb, 128, 0, ctx->stream>>>(M, f.rows, f.cols, f.rowptr, f.colind, (T*)f.val, f.cap);
-  FGB_LAUNCHED(ctx);
-  if (f.t_rowptr) {
-    k_csr_transpose_dev<T><<<1, 1024, 0, ctx->stream>>>(f.rowptr, f.colind, (const T*)f.val, f.rows, f.cols,
-                                                        f.t_rowptr, f.t_colind, (T*)f.t_val, w.row_cnt, f.cap);
-    FGB_LAUNCHED(ctx);
+__global__ void __launch_bounds__(256)
+    k_d2c_count_rc(const T* __restrict__ M, int rows, int cols, int* __restrict__ rcnt, int* __restrict__ ccnt,
+                   int with_cols) {
+  const long w = (blockIdx.x * (long)blockDim.x + threadIdx.x) / 32;
+  const int lane = threadIdx.x & 31;
+  if (w < rows) {
+    int c = 0;
+    for (int j = lane; j < cols; j += 32) c += M[w + (long)j * rows] != T(0);
+    for (int o = 16; o; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+    if (lane == 0) rcnt[w] = c;
+  } else if (with_cols && w < (long)rows + cols) {
+    const long col = w - rows;
+    int c = 0;
+    for (int i = lane; i < rows; i += 32) c += M[i + col * rows] != T(0);
+    for (int o = 16; o; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+    if (lane == 0) ccnt[col] = c;
   }
+}
+
+__device__ void block_excl_scan(const int* __restrict__ cnt, int n, int* __restrict__ ptr, int* part) {
+  const int per = (n + blockDim.x - 1) / blockDim.x;
+  const int r0 = threadIdx.x * per, r1 = min(n, r0 + per);
+  int s = 0;
+  for (int r = r0; r < r1; ++r) s += cnt[r];
+  part[threadIdx.x] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int run = 0;
+    for (int u = 0; u < (int)blockDim.x; ++u) {
+      const int v = part[u];
+      part[u] = run;
+      run += v;
+    }
+    ptr[n] = run;
+  }
+  __syncthreads();
+  int run = part[threadIdx.x];
+  for (int r = r0; r < r1; ++r) {
+    ptr[r] = run;
+    run += cnt[r];
+  }
+  __syncthreads();
+}
+
+// An entry count above the factor's capacity (which the constraint bounds)
+// is reported through *status and the offsets are clamped so that later
+// kernels stay inside the arrays.
+__global__ void __launch_bounds__(1024) k_d2c_scan_rc(const int* __restrict__ rcnt, int rows, const int* __restrict__ ccnt,
+                                                      int cols, int* __restrict__ rowptr, int* __restrict__ t_rowptr,
+                                                      int with_cols, int cap, int* status) {
+  __shared__ int part[1024];
+  block_excl_scan(rcnt, rows, rowptr, part);
+  if (with_cols) block_excl_scan(ccnt, cols, t_rowptr, part);
+  if (rowptr[rows] > cap) {
+    for (int r = threadIdx.x; r <= rows; r += blockDim.x) rowptr[r] = min(rowptr[r], cap);
+    if (with_cols)
+      for (int c = threadIdx.x; c <= cols; c += blockDim.x) t_rowptr[c] = min(t_rowptr[c], cap);
+    if (threadIdx.x == 0 && status) atomicCAS(status, 0, (int)FGB_ERR_INVALID_ARG);
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256)
+    k_d2c_write_rc(const T* __restrict__ M, int rows, int cols, const int* __restrict__ rowptr,
+                   int* __restrict__ colind, T* __restrict__ val, const int* __restrict__ t_rowptr,
+                   int* __restrict__ t_colind, T* __restrict__ t_val, int cap, int with_cols) {
+  const long w = (blockIdx.x * (long)blockDim.x + threadIdx.x) / 32;
+  const unsigned lane = threadIdx.x & 31;
+  const unsigned lt = (1u << lane) - 1u;
+  if (w < rows) {
+    int base = rowptr[w];
+    for (int j0 = 0; j0 < cols; j0 += 32) {
+      const int j = j0 + (int)lane;
+      const T v = j < cols ? M[w + (long)j * rows] : T(0);
+      const unsigned m = __ballot_sync(0xffffffffu, v != T(0));
+      if (v != T(0)) {
+        const int p = base + __popc(m & lt);
+        if (p < cap) {
+          colind[p] = j;
+          val[p] = v;
+        }
+      }
+      base += __popc(m);
+    }
+  } else if (with_cols && w < (long)rows + cols) {
+    const long col = w - rows;
+    int base = t_rowptr[col];
+    for (int i0 = 0; i0 < rows; i0 += 32) {
+      const int i = i0 + (int)lane;
+      const T v = i < rows ? M[i + col * rows] : T(0);
+      const unsigned m = __ballot_sync(0xffffffffu, v != T(0));
+      if (v != T(0)) {
+        const int p = base + __popc(m & lt);
+        if (p < cap) {
+          t_colind[p] = i;
+          t_val[p] = v;
+        }
+      }
+      base += __popc(m);
+    }
+  }
+}
+
+template <typename T>
+fgb_status launch_dense_to_csr(fgb_ctx* ctx, ProxWork& w, const T* M, DevFactor& f, int* status) {
+  FGB_TRY(prox_work_reserve(ctx, w, (long)f.rows * f.cols, f.rows + f.cols + 2));
+  const int with_cols = f.t_rowptr ? 1 : 0;
+  const long warps = (long)f.rows + (with_cols ? f.cols : 0);
+  const int blocks = (int)((warps * 32 + 255) / 256);
+  int* rcnt = w.row_cnt;
+  int* ccnt = w.row_cnt + f.rows;
+  k_d2c_count_rc<T><<<blocks, 256, 0, ctx->stream>>>(M, f.rows, f.cols, rcnt, ccnt, with_cols);
+  FGB_LAUNCHED(ctx);
+  k_d2c_scan_rc<<<1, 1024, 0, ctx->stream>>>(rcnt, f.rows, ccnt, f.cols, f.rowptr, f.t_rowptr, with_cols, f.cap,
+                                             status);
+  FGB_LAUNCHED(ctx);
+  k_d2c_write_rc<T><<<blocks, 256, 0, ctx->stream>>>(M, f.rows, f.cols, f.rowptr, f.colind, (T*)f.val, f.t_rowptr,
+                                                     f.t_colind, (T*)f.t_val, f.cap, with_cols);
+  FGB_LAUNCHED(ctx);
   return FGB_OK;
 }
 
@@ -824,7 +951,7 @@ template fgb_status launch_prox<float>(fgb_ctx*, ProxWork&, const fgb_constraint
                                        int*);
 template fgb_status launch_prox<double>(fgb_ctx*, ProxWork&, const fgb_constraint&, double*, int, int,
                                         const double*, int*);
-template fgb_status launch_dense_to_csr<float>(fgb_ctx*, ProxWork&, const float*, DevFactor&);
-template fgb_status launch_dense_to_csr<double>(fgb_ctx*, ProxWork&, const double*, DevFactor&);
+template fgb_status launch_dense_to_csr<float>(fgb_ctx*, ProxWork&, const float*, DevFactor&, int*);
+template fgb_status launch_dense_to_csr<double>(fgb_ctx*, ProxWork&, const double*, DevFactor&, int*);
 
 }  // namespace fgb

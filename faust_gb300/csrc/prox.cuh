@@ -34,6 +34,8 @@ struct ProxWork {
   int* row_cnt = nullptr;            // rows+1
   void* supp = nullptr;              // device copy of a support (SUPP)
   size_t supp_bytes = 0;
+  void* heap = nullptr;              // heap of the tie replay when it does not fit on chip
+  long heap_cap = 0;
 };
 
 fgb_status prox_work_reserve(fgb_ctx* ctx, ProxWork& w, long elems, int rows);
@@ -47,10 +49,10 @@ fgb_status launch_prox(fgb_ctx* ctx, ProxWork& w, const fgb_constraint& c, T* M,
                        const T* supp_dev, int* d_status);
 
 // Queues dense -> CSR conversion of the non-zero entries of M into the
-// factor f (whose arrays must have capacity for every entry it may receive:
-// f.cap >= nonzeros); f.nnz is updated on the host only by the caller reading
-// rowptr[rows] back.  Also rebuilds the transpose CSR when f.t_* is set.
+// factor f (capacity f.cap; more entries set *status) and, when f.t_* is set,
+// the CSR of its transpose.  f.nnz is only known on the device afterwards
+// (rowptr[rows]).
 template <typename T>
-fgb_status launch_dense_to_csr(fgb_ctx* ctx, ProxWork& w, const T* M, DevFactor& f);
+fgb_status launch_dense_to_csr(fgb_ctx* ctx, ProxWork& w, const T* M, DevFactor& f, int* status);
 
 }  // namespace fgb
