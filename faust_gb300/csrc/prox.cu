@@ -301,6 +301,69 @@ __device__ void heap_adjust(HeapView h, int hole, int len, HNode v) {
   h.n[hole] = v;
 }
 
+// The same adjustment with a two-level lookahead: both children and all
+// their children are read in one batch of independent shared-memory loads,
+// so the descent takes one round trip per two levels.  The moves are exactly
+// those of heap_adjust.
+__host__ __device__ inline void heap_adjust2(HeapView h, int hole, int len, HNode v) {
+  const int top = hole;
+  const int lim = (len - 1) / 2;
+  int child = hole;
+  while (child < lim) {
+    const int r1 = 2 * (child + 1), l1 = r1 - 1;
+    const HNode nr = h.n[r1], nl = h.n[l1];
+    const bool rhas = r1 < lim, lhas = l1 < lim;
+    HNode rr, rl, lr, ll;
+    if (rhas) {
+      rr = h.n[2 * (r1 + 1)];
+      rl = h.n[2 * (r1 + 1) - 1];
+    }
+    if (lhas) {
+      lr = h.n[2 * (l1 + 1)];
+      ll = h.n[2 * (l1 + 1) - 1];
+    }
+    int c = r1;
+    HNode cn = nr;
+    bool chas = rhas;
+    HNode gr = rr, gl = rl;
+    if (nr.key > nl.key) {
+      c = l1;
+      cn = nl;
+      chas = lhas;
+      gr = lr;
+      gl = ll;
+    }
+    h.n[hole] = cn;
+    hole = c;
+    child = c;
+    if (!chas) break;
+    const int r2 = 2 * (c + 1);
+    int c2 = r2;
+    HNode c2n = gr;
+    if (gr.key > gl.key) {
+      c2 = r2 - 1;
+      c2n = gl;
+    }
+    h.n[hole] = c2n;
+    hole = c2;
+    child = c2;
+  }
+  if ((len & 1) == 0 && child == (len - 2) / 2) {
+    child = 2 * (child + 1);
+    h.n[hole] = h.n[child - 1];
+    hole = child - 1;
+  }
+  int parent = (hole - 1) / 2;
+  while (hole > top) {
+    const HNode pn = h.n[parent];
+    if (!(pn.key > v.key)) break;
+    h.n[hole] = pn;
+    hole = parent;
+    parent = (hole - 1) / 2;
+  }
+  h.n[hole] = v;
+}
+
 constexpr int HR_CHUNK = 8192;
 constexpr int HR_PER = HR_CHUNK / PX_THREADS;  // 32 entries per thread
 
@@ -320,7 +383,7 @@ __global__ void __launch_bounds__(PX_THREADS)
   if (threadIdx.x == 0 && k >= 2) {
     int parent = (k - 2) / 2;
     while (true) {
-      heap_adjust(h, parent, k, h.n[parent]);
+      heap_adjust2(h, parent, k, h.n[parent]);
       if (parent == 0) break;
       parent--;
     }
@@ -374,7 +437,7 @@ __global__ void __launch_bounds__(PX_THREADS)
       for (int q = 0; q < nc; ++q) {
         const HNode c = cand[q];
         if (c.key > top) {
-          heap_adjust(h, 0, k, c);
+          heap_adjust2(h, 0, k, c);
           top = h.n[0].key;
         }
       }
