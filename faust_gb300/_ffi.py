@@ -81,6 +81,7 @@ _SIGS = {
     "fgb_faust_factor_to_dense": (_I, [_P, _I, _P]),
     "fgb_faust_factor_to_csr": (_I, [_P, _I, _P, _P, _P]),
     "fgb_prox": (_I, [_P, _I, ctypes.POINTER(Constraint), _P]),
+    "fgb_prox_noalloc": (_I, [_P, _I, ctypes.POINTER(Constraint), _P, _P]),
     "fgb_palm_params_default": (_I, [ctypes.POINTER(PalmParams)]),
     "fgb_palm4msa2": (_I, [_P, _I, _P, _I, _I, _I, ctypes.POINTER(Constraint), ctypes.POINTER(PalmParams),
                            ctypes.POINTER(_P), ctypes.POINTER(_D), ctypes.POINTER(_P)]),

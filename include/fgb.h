@@ -153,6 +153,23 @@ typedef struct fgb_constraint {
  * (faust_prox.hpp:52-69), ties included.  F32 and F64. */
 fgb_status fgb_prox(fgb_ctx* ctx, fgb_dtype dtype, const fgb_constraint* cons, void* M);
 
+/* Same projection as fgb_prox, for callers that cannot allocate device
+ * memory: no cudaMalloc/cudaFree or allocating library call is made.  This
+ * entry point has no counterpart in the reference.  Its scratch memory is one
+ * fixed 6 MiB device array inside the library (every GPU that loads the
+ * library holds it until the process exits), which limits it to
+ * rows*cols <= 4194304, rows+cols <= 65536 and, for FGB_SP / FGB_SP_POS,
+ * k <= 65536 (larger sizes return FGB_ERR_INVALID_ARG).  M is a DEVICE
+ * matrix as in fgb_prox; for FGB_SUPP the support must be given in DEVICE
+ * memory through supp_dev (cons->supp is ignored).  The first call on a
+ * device looks up the array's device address: make that first call before
+ * any stream capture.  All calls share the array, so calls that overlap on
+ * the GPU (several streams or threads at once) race; the entry point
+ * clears what must start at zero and synchronises the context's stream
+ * before returning. */
+fgb_status fgb_prox_noalloc(fgb_ctx* ctx, fgb_dtype dtype, const fgb_constraint* cons, void* M,
+                            const void* supp_dev);
+
 /* ------------------------------------------------------------------ PALM4MSA */
 typedef struct fgb_palm_params {
   int nb_it;                 /* StoppingCriterion num_its (faust_StoppingCriterion.hpp:112-154) */
