@@ -392,6 +392,108 @@ def cpu_baseline_palm(its=5):
             "sample": "%d of %d iterations timed (%.2f s), scaled to the full run" % (its, PALM_ITS, dt)}
 
 
+# ---------------------------------------------------------------- batched PALM4MSA
+def batched_problem(rng, count=512):
+    """count instances, n = round16(exp(U[ln 64, ln 512])), target = P1 P2 P3 +
+    1e-3 N(0,1) with each Pi n x n with 4 distinct random columns per row,
+    N(0,1) values; FP32."""
+    from faust_gb300 import synth
+    ns = (np.round(np.exp(rng.uniform(np.log(64), np.log(512), size=count)) / 16) * 16).astype(int)
+    ns = np.clip(ns, 64, 512)
+    mats = []
+    for n in ns:
+        P = [synth.random_csr(int(n), int(n), 4, rng, np.float64) for _ in range(3)]
+        A = (P[0] @ (P[1] @ P[2].toarray())) + 1e-3 * rng.standard_normal((n, n))
+        mats.append(np.asarray(A, np.float32))
+    return ns, mats
+
+
+def run_batched(args, rank, world):
+    """512 independent palm4msa2 instances (splincol k=4, 4 factors, 100
+    iterations, FP32 with FP64 step-size norms) in one persistent launch;
+    value = instances per second (all ranks)."""
+    import torch
+    import faust_gb300 as fg
+    from faust_gb300 import fact
+    torch.cuda.set_device(rank % max(1, torch.cuda.device_count()))
+    rng = np.random.default_rng(4 + rank)
+    ns, mats = batched_problem(rng, args.batch_count)
+    ctx = fg.default_context(torch.cuda.current_device())
+    dev = [torch.from_numpy(np.ascontiguousarray(A.T)).cuda().t() for A in mats]
+    cons_by_n = {}
+    probs = []
+    for A, n in zip(dev, ns):
+        if n not in cons_by_n:
+            cons_by_n[n] = [fact.ConstraintInt("splincol", int(n), int(n), 4) for _ in range(4)]
+        probs.append((A, cons_by_n[n]))
+    params = fact.ParamsPalm4MSA(probs[0][1], 100, norm2_fp64=True)
+    for _ in range(args.warmup):
+        res = fact.palm4msa_batched(probs[:32], params, ctx=ctx, ctas_per_sm=args.ctas_per_sm)
+        for r in res:
+            r.faust.close()
+    torch.cuda.synchronize()
+    _barrier(world)
+    times = []
+    with ClockSampler(torch.cuda.current_device()) as clk:
+        for _ in range(args.steps):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            res = fact.palm4msa_batched(probs, params, ctx=ctx, ctas_per_sm=args.ctas_per_sm)
+            times.append(time.perf_counter() - t0)
+            bad = sum(1 for r in res if r.status)
+            for r in res:
+                r.faust.close()
+    step_s = _max_over_ranks(float(np.mean(times)), world)
+    # end to end: host matrices in, every factor back to host memory
+    t0 = time.perf_counter()
+    dev2 = [torch.from_numpy(np.ascontiguousarray(A.T)).cuda().t() for A in mats]
+    res = fact.palm4msa_batched([(A, c) for A, (_, c) in zip(dev2, probs)], params, ctx=ctx,
+                                ctas_per_sm=args.ctas_per_sm)
+    d2h = 0
+    for r in res:
+        for i in range(4):
+            f = r.faust.factors(i)
+            d2h += f.nnz * 8 + (f.shape[0] + 1) * 4
+        r.faust.close()
+    e2e_s = time.perf_counter() - t0
+    out = {
+        "metric": METRIC, "submetric": "batched palm4msa2 instances per second (one persistent launch)",
+        "value": round(len(mats) * world / step_s, 2), "unit": "instances/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(step_s * 1e3, 2), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32 (FP64 step-size norms)", "data": "synthetic (seeded)",
+        "config": {"workload": "%d palm4msa2 instances, n in [64, 512] log-uniform (multiples of 16), "
+                               "target P1P2P3 + 1e-3 noise, 4 factors splincol k=4, 100 iterations" % len(mats),
+                   "sum_n2": int(np.sum(ns.astype(np.int64) ** 2)), "failed_instances": bad,
+                   "ctas_per_sm": args.ctas_per_sm},
+        "e2e": {"value": round(len(mats) / e2e_s, 2), "unit": "instances/s",
+                "h2d_bytes_per_step": int(sum(A.nbytes for A in mats)), "d2h_bytes_per_step": int(d2h)},
+        "gpu_launches": 1,
+        "clocks": clk.summary(),
+    }
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        out["cpu_baseline"] = cpu_baseline_batched(ns, mats)
+    return out
+
+
+def cpu_baseline_batched(ns, mats, sample=16):
+    """The oracle on a sample of instances, one instance per host core."""
+    import concurrent.futures
+    import multiprocessing
+    from oracle import oracle as O
+    idx = np.random.default_rng(0).choice(len(mats), size=min(sample, len(mats)), replace=False)
+    threads = os.cpu_count() or 1
+    O.set_threads(1)
+    t0 = time.perf_counter()
+    with concurrent.futures.ThreadPoolExecutor(max_workers=threads) as ex:
+        list(ex.map(lambda i: O.palm4msa2(mats[i], [dict(kind=O.SPLINCOL, k=4, rows=int(ns[i]), cols=int(ns[i]))
+                                                    for _ in range(4)], 100, norm2_fp64=True), idx))
+    dt = time.perf_counter() - t0
+    scale = float(np.sum(ns.astype(np.float64) ** 2) / np.sum(ns[idx].astype(np.float64) ** 2))
+    return {"value": round(len(mats) / (dt * scale), 3), "unit": "instances/s", "cores": threads, "kind": "port",
+            "sample": "%d of %d instances on %d threads (%.1f s), scaled by sum n^2" % (len(idx), len(mats),
+                                                                                      threads, dt)}
+
+
 # ---------------------------------------------------------------- learned warm start
 def run_warmstart(args, rank, world):
     """Gaussian-kernel butterfly factorizations: plain palm4msa2 (200
@@ -493,7 +595,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="palm",
-                    choices=["palm", "csr_butterfly", "csr_random", "bsr", "warmstart"])
+                    choices=["palm", "batched", "csr_butterfly", "csr_random", "bsr", "warmstart"])
+    ap.add_argument("--batch-count", type=int, default=512)
+    ap.add_argument("--ctas-per-sm", type=int, default=2)
     ap.add_argument("--ws-train", type=int, default=20000)
     ap.add_argument("--ws-test", type=int, default=1024)
     ap.add_argument("--ws-epochs", type=int, default=20)
@@ -519,6 +623,8 @@ def main():
         out = run_palm(args, rank, world)
     elif args.workload == "warmstart":
         out = run_warmstart(args, rank, world)
+    elif args.workload == "batched":
+        out = run_batched(args, rank, world)
     else:
         out = run_faust_x(args, rank, world)
     if rank == 0:

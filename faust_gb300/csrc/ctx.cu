@@ -96,6 +96,8 @@ fgb_status fgb_ctx_destroy(fgb_ctx* ctx) {
   if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
   if (ctx->cancel_host) cudaFreeHost((void*)ctx->cancel_host);
   if (ctx->rand_dev) cudaFree(ctx->rand_dev);
+  if (ctx->x0_d) cudaFree(ctx->x0_d);
+  if (ctx->x0_f) cudaFree(ctx->x0_f);
   delete ctx;
   return FGB_OK;
 }

@@ -33,6 +33,9 @@ struct fgb_ctx {
   // cached on the device.
   int* rand_dev = nullptr;
   int rand_n = 0;
+  // the power-iteration start vector -1 + 2*rand()/RAND_MAX in FP64 and FP32
+  double* x0_d = nullptr;
+  float* x0_f = nullptr;
 };
 
 namespace fgb {

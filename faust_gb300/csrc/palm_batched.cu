@@ -166,8 +166,9 @@ __device__ __forceinline__ void pi_op(const Fac<T>* F, int lo, int hi, bool tall
 // TransformHelper::spectralNorm of F[lo..hi) by Faust::power_iteration; the
 // same steps as k_power_iteration (power.cu), on one block.
 template <typename T, typename TC>
-__device__ double b_spectral_norm(const Fac<T>* F, int lo, int hi, int max_iter, TC thr, const int* rnd, TC* vbuf,
+__device__ double b_spectral_norm(const Fac<T>* F, int lo, int hi, int max_iter, TC thr, const TC* x0, TC* vbuf,
                                   int maxn, TC* lane, int* st) {
+  __shared__ TC s_nrm, s_inv;
   if (hi <= lo) return 1.0;
   for (int i = lo; i < hi; ++i)
     if (F[i].rowptr[F[i].rows] == 0) return 0.0;
@@ -177,7 +178,7 @@ __device__ double b_spectral_norm(const Fac<T>* F, int lo, int hi, int max_iter,
   const int nops = 2 * (hi - lo);
   TC* bufs[3] = {vbuf, vbuf + maxn, vbuf + 2 * maxn};
   int xi = 0;
-  for (int i = threadIdx.x; i < n; i += BT) bufs[0][i] = addr(TC(-1), divr(mulr(TC(2), (TC)rnd[i]), (TC)RAND_MAX));
+  for (int i = threadIdx.x; i < n; i += BT) bufs[0][i] = x0[i];
   __syncthreads();
   TC lam_old = TC(1), lam = TC(0);
   int it = 0;
@@ -187,12 +188,18 @@ __device__ double b_spectral_norm(const Fac<T>* F, int lo, int hi, int max_iter,
     ++it;
     lam_old = lam;
     TC* x = bufs[xi];
-    const TC nrm = sqrtr(b_cdot<TC>(x, x, n, lane));
+    const TC ss = b_cdot<TC>(x, x, n, lane);
+    if (threadIdx.x == 0) {  // scalar FP64 work by one thread
+      s_nrm = sqrtr(ss);
+      s_inv = s_nrm == TC(0) ? TC(0) : divr(TC(1), s_nrm);
+    }
+    __syncthreads();
+    const TC nrm = s_nrm;
     if (nrm == TC(0)) {
       if (threadIdx.x == 0) *st = FGB_ERR_ZERO_NORM;
       return 0.0;
     }
-    const TC inv = divr(TC(1), nrm);
+    const TC inv = s_inv;
     for (int i = threadIdx.x; i < n; i += BT) x[i] = mulr(x[i], inv);
     __syncthreads();
     int si = xi, di = (xi + 1) % 3;
@@ -220,8 +227,14 @@ __device__ double b_spectral_norm(const Fac<T>* F, int lo, int hi, int max_iter,
     lam = b_cdot<TC>(x, res, n, lane);
     xi = si;
   }
-  const TC r = sqrtr(lam);
-  return (double)(r < TC(0) ? -r : r);
+  if (threadIdx.x == 0) {
+    const TC r = sqrtr(lam);
+    s_nrm = r < TC(0) ? -r : r;
+  }
+  __syncthreads();
+  const double result = (double)s_nrm;
+  __syncthreads();
+  return result;
 }
 
 // ------------------------------------------------------------------ projections
@@ -333,8 +346,14 @@ __device__ bool b_project(const Cons<T>& c, T* M, int rows, int cols, unsigned c
           lane[threadIdx.x] = acc;
           total = addr(total, bat_tree(lane));
         }
-        T scal = sqrtr(total);
-        if (scal != T(0)) scal = divr((T)c.s, scal);
+        __shared__ T s_scal;
+        if (threadIdx.x == 0) {
+          T scal = sqrtr(total);
+          if (scal != T(0)) scal = divr((T)c.s, scal);
+          s_scal = scal;
+        }
+        __syncthreads();
+        const T scal = s_scal;
         for (long e = threadIdx.x; e < len; e += BT) M[at(e)] = mulr(bpos(M[at(e)], pos), scal);
         __syncthreads();
       }
@@ -355,12 +374,18 @@ __device__ bool b_project(const Cons<T>& c, T* M, int rows, int cols, unsigned c
       lane[threadIdx.x] = acc;
       total = addr(total, bat_tree(lane));
     }
-    const T n = sqrtr(total);
+    __shared__ T s_n, s_inv2;
+    if (threadIdx.x == 0) {
+      s_n = sqrtr(total);
+      s_inv2 = s_n == T(0) ? T(0) : (T)__ddiv_rn(1.0, (double)s_n);
+    }
+    __syncthreads();
+    const T n = s_n;
     if (n == T(0)) {
       if (threadIdx.x == 0) *st = FGB_ERR_ZERO_NORM;
       return false;
     }
-    const T inv = (T)__ddiv_rn(1.0, (double)n);
+    const T inv = s_inv2;
     for (long i = threadIdx.x; i < N; i += BT) M[i] = mulr(M[i], inv);
     __syncthreads();
   }
@@ -479,7 +504,7 @@ __device__ bool b_dense_to_csr(const T* M, Fac<T>& f, int* cnt, int* st) {
 
 // ------------------------------------------------------------------ one instance
 template <typename T, typename TN>
-__device__ void run_instance(Inst<T>& I, const Slot<T>& W, const Params& P, const int* rnd, TN* vbuf, int maxn,
+__device__ void run_instance(Inst<T>& I, const Slot<T>& W, const Params& P, const TN* x0, TN* vbuf, int maxn,
                              T* lane, TN* lane_n) {
   const int J = I.J;
   Fac<T>* S = I.f;
@@ -516,25 +541,31 @@ __device__ void run_instance(Inst<T>& I, const Slot<T>& W, const Params& P, cons
       if (P.constant_step) {
         c = divr(T(1), (T)P.step_size);
       } else {
-        const double nR = b_spectral_norm<T, TN>(S, f + 1, J, P.norm2_max_iter, (TN)P.norm2_threshold, rnd, vbuf,
+        const double nR = b_spectral_norm<T, TN>(S, f + 1, J, P.norm2_max_iter, (TN)P.norm2_threshold, x0, vbuf,
                                                  maxn, lane_n, &st);
-        const double nL = b_spectral_norm<T, TN>(S, 0, f, P.norm2_max_iter, (TN)P.norm2_threshold, rnd, vbuf, maxn,
+        const double nL = b_spectral_norm<T, TN>(S, 0, f, P.norm2_max_iter, (TN)P.norm2_threshold, x0, vbuf, maxn,
                                                  lane_n, &st);
         __syncthreads();
         if (threadIdx.x == 0) {
           if (isnan(nR) || isnan(nL)) st = st ? st : FGB_ERR_NAN;
           if ((nR == 0.0 && (it > 0 || !r2l)) || (nL == 0.0 && (it > 0 || r2l))) st = st ? st : FGB_ERR_ZERO_NORM;
         }
-        const double tnR = (double)(T)nR, tnL = (double)(T)nL, l = (double)lam;
-        double cc = __dmul_rn(1.001, l);
-        cc = __dmul_rn(cc, l);
-        cc = __dmul_rn(cc, tnR);
-        cc = __dmul_rn(cc, tnR);
-        cc = __dmul_rn(cc, tnL);
-        cc = __dmul_rn(cc, tnL);
-        c = (T)cc;
+        if (threadIdx.x == 0) {
+          const double tnR = (double)(T)nR, tnL = (double)(T)nL, l = (double)lam;
+          double cc = __dmul_rn(1.001, l);
+          cc = __dmul_rn(cc, l);
+          cc = __dmul_rn(cc, tnR);
+          cc = __dmul_rn(cc, tnR);
+          cc = __dmul_rn(cc, tnL);
+          cc = __dmul_rn(cc, tnL);
+          sh_c = (T)cc;
+        }
+        __syncthreads();
+        c = sh_c;
       }
-      const T alpha = divr(lam, c);
+      if (threadIdx.x == 0) sh_alpha = divr(lam, c);
+      __syncthreads();
+      const T alpha = sh_alpha;
       __syncthreads();
       if (st) break;
       b_csr_to_dense(Sf, W.D);
@@ -655,7 +686,14 @@ __device__ void run_instance(Inst<T>& I, const Slot<T>& W, const Params& P, cons
         lane[threadIdx.x] = s2;
         ss = addr(ss, bat_tree(lane));
       }
-      const T nS = sqrtr(ss);
+      if (threadIdx.x == 0) {
+        sh_c = sqrtr(ss);
+        sh_alpha = (sh_c == T(0) || isnan(tr) || isnan(sh_c)) ? T(0) : divr(tr, mulr(sh_c, sh_c));
+      }
+      __syncthreads();
+      const T nS = sh_c;
+      const T lam_new = sh_alpha;
+      __syncthreads();
       if (nS == T(0)) {
         if (!P.no_lambda_error) {
           if (threadIdx.x == 0) st = FGB_ERR_ZERO_NORM;
@@ -667,7 +705,7 @@ __device__ void run_instance(Inst<T>& I, const Slot<T>& W, const Params& P, cons
           break;
         }
       } else {
-        lam = divr(tr, mulr(nS, nS));
+        lam = lam_new;
       }
     }
     __syncthreads();
@@ -677,13 +715,11 @@ __device__ void run_instance(Inst<T>& I, const Slot<T>& W, const Params& P, cons
     I.status = st;
     I.lambda = (double)lam;
   }
-  (void)sh_c;
-  (void)sh_alpha;
 }
 
 template <typename T, typename TN>
 __global__ void __launch_bounds__(BT) k_palm_batched(Inst<T>* insts, const int* order, int* queue, Slot<T>* slots,
-                                                     const __grid_constant__ Params P, const int* rnd, int maxn) {
+                                                     const __grid_constant__ Params P, const TN* x0, int maxn) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   TN* vbuf = reinterpret_cast<TN*>(smem_raw);  // 3 * maxn
   TN* lane_n = vbuf + 3 * (long)maxn;
@@ -696,7 +732,7 @@ __global__ void __launch_bounds__(BT) k_palm_batched(Inst<T>* insts, const int* 
     const int q = next;
     __syncthreads();
     if (q >= P.ninst) break;
-    run_instance<T, TN>(insts[order[q]], W, P, rnd, vbuf, maxn, lane, lane_n);
+    run_instance<T, TN>(insts[order[q]], W, P, x0, vbuf, maxn, lane, lane_n);
   }
 }
 
@@ -899,11 +935,11 @@ static fgb_status batched_impl(fgb_ctx* ctx, fgb_dtype dt, int nprob, const fgb_
     if (fp64n) {
       auto kern = k_palm_batched<T, double>;
       if (smem > 40 * 1024) s = cuda_check(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem), "attr");
-      if (s == FGB_OK) kern<<<nslots, BT, smem, ctx->stream>>>(d_inst, d_order, d_queue, d_slots, P, rnd, maxdim);
+      if (s == FGB_OK) kern<<<nslots, BT, smem, ctx->stream>>>(d_inst, d_order, d_queue, d_slots, P, ctx->x0_d, maxdim);
     } else {
       auto kern = k_palm_batched<T, float>;
       if (smem > 40 * 1024) s = cuda_check(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem), "attr");
-      if (s == FGB_OK) kern<<<nslots, BT, smem, ctx->stream>>>(d_inst, d_order, d_queue, d_slots, P, rnd, maxdim);
+      if (s == FGB_OK) kern<<<nslots, BT, smem, ctx->stream>>>(d_inst, d_order, d_queue, d_slots, P, ctx->x0_f, maxdim);
     }
     if (s == FGB_OK) {
       ctx->launches.fetch_add(1);

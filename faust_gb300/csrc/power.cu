@@ -61,10 +61,11 @@ struct PIStaged {
 template <typename TF, typename TC>
 __global__ void __launch_bounds__(PI_THREADS)
     k_power_iteration(const __grid_constant__ PIChain ca, const __grid_constant__ PIChain cb, int max_iter, TC thr,
-                      const int* __restrict__ rnd, PIOut* out, const __grid_constant__ PIPalm palm, int maxn,
+                      const TC* __restrict__ x0, PIOut* out, const __grid_constant__ PIPalm palm, int maxn,
                       int smem_bytes) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ PIStaged ops[PI_MAX_OPS];
+  __shared__ TC s_inv, s_nrm;
   TC* buf0 = reinterpret_cast<TC*>(smem_raw);
   TC* buf1 = buf0 + maxn;
   TC* buf2 = buf1 + maxn;
@@ -125,8 +126,7 @@ __global__ void __launch_bounds__(PI_THREADS)
     __syncthreads();
     TC* bufs[3] = {buf0, buf1, buf2};
     int xi = 0;
-    for (int i = threadIdx.x; i < n; i += blockDim.x)
-      bufs[0][i] = addr(TC(-1), divr(mulr(TC(2), (TC)rnd[i]), (TC)RAND_MAX));
+    for (int i = threadIdx.x; i < n; i += blockDim.x) bufs[0][i] = x0[i];
     __syncthreads();
     TC lam_old = TC(1), lam = TC(0);
     int it = 0;
@@ -136,12 +136,20 @@ __global__ void __launch_bounds__(PI_THREADS)
       ++it;
       lam_old = lam;
       TC* x = bufs[xi];
-      const TC nrm = sqrtr(block_cdot<TC>(x, x, n, lane));
+      // scalar FP64 work (sqrt, division) by one thread: GB300's FP64 pipe
+      // is narrow, 1024 redundant copies would saturate it
+      const TC ss = block_cdot<TC>(x, x, n, lane);
+      if (threadIdx.x == 0) {
+        s_nrm = sqrtr(ss);
+        s_inv = s_nrm == TC(0) ? TC(0) : divr(TC(1), s_nrm);
+      }
+      __syncthreads();
+      const TC nrm = s_nrm;
       if (nrm == TC(0)) {
         st = FGB_ERR_ZERO_NORM;
         break;
       }
-      const TC inv = divr(TC(1), nrm);
+      const TC inv = s_inv;
       for (int i = threadIdx.x; i < n; i += blockDim.x) x[i] = mulr(x[i], inv);
       __syncthreads();
       // products ping-pong between the two buffers other than x, which keeps
@@ -178,7 +186,7 @@ __global__ void __launch_bounds__(PI_THREADS)
         flag = 0;
       } else {
         flag = (it < max_iter) ? it : -1;
-        result = (double)absd(sqrtr(lam));
+        if (threadIdx.x == 0) result = (double)absd(sqrtr(lam));
       }
     }
   }
@@ -219,6 +227,14 @@ __global__ void __launch_bounds__(PI_THREADS)
   }
 }
 
+// -1 + (2*r)/RAND_MAX in each precision, the mapping of Eigen's Random().
+__global__ void k_start_vectors(int n, const int* __restrict__ rnd, double* __restrict__ xd, float* __restrict__ xf) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    xd[i] = __dadd_rn(-1.0, __ddiv_rn(__dmul_rn(2.0, (double)rnd[i]), (double)RAND_MAX));
+    xf[i] = __fadd_rn(-1.f, __fdiv_rn(__fmul_rn(2.f, (float)rnd[i]), (float)RAND_MAX));
+  }
+}
+
 fgb_status pi_rand_device(fgb_ctx* ctx, int n, const int** d_rand) {
   if (ctx->rand_n < n) {
     // glibc rand() after srand(418) = random()'s TYPE_3 generator with a
@@ -238,8 +254,18 @@ fgb_status pi_rand_device(fgb_ctx* ctx, int n, const int** d_rand) {
     if (ctx->rand_dev) cudaFree(ctx->rand_dev);
     ctx->rand_dev = nullptr;
     ctx->rand_n = 0;
+    if (ctx->x0_d) cudaFree(ctx->x0_d);
+    if (ctx->x0_f) cudaFree(ctx->x0_f);
+    ctx->x0_d = nullptr;
+    ctx->x0_f = nullptr;
     FGB_TRY(dmalloc(ctx, (void**)&ctx->rand_dev, sizeof(int) * n));
+    FGB_TRY(dmalloc(ctx, (void**)&ctx->x0_d, sizeof(double) * n));
+    FGB_TRY(dmalloc(ctx, (void**)&ctx->x0_f, sizeof(float) * n));
     FGB_CUDA(ctx, cudaMemcpy(ctx->rand_dev, h.data(), sizeof(int) * n, cudaMemcpyHostToDevice));
+    k_start_vectors<<<std::max(1, std::min((n + 255) / 256, 64)), 256, 0, ctx->stream>>>(n, ctx->rand_dev, ctx->x0_d,
+                                                                                        ctx->x0_f);
+    FGB_LAUNCHED(ctx);
+    FGB_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     ctx->rand_n = n;
   }
   *d_rand = ctx->rand_dev;
@@ -262,7 +288,9 @@ static fgb_status launch_pi_t(fgb_ctx* ctx, const PIChain& a, const PIChain& b, 
     FGB_CUDA(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     attr_set = smem;
   }
-  kern<<<2, PI_THREADS, smem, ctx->stream>>>(a, b, max_iter, (TC)thr, d_rand, d_out, palm, maxn, (int)smem);
+  const TC* x0 = sizeof(TC) == 8 ? (const TC*)(const void*)ctx->x0_d : (const TC*)(const void*)ctx->x0_f;
+  (void)d_rand;
+  kern<<<2, PI_THREADS, smem, ctx->stream>>>(a, b, max_iter, (TC)thr, x0, d_out, palm, maxn, (int)smem);
   FGB_LAUNCHED(ctx);
   return FGB_OK;
 }

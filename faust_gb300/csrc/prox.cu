@@ -543,8 +543,14 @@ __global__ void __launch_bounds__(PX_THREADS)
     lane[threadIdx.x] = acc;
     total = addr(total, lane_tree_256(lane));
   }
-  T scal = sqrtr(total);
-  if (scal != T(0)) scal = divr((T)s, scal);
+  __shared__ T s_scal;
+  if (threadIdx.x == 0) {
+    T scal = sqrtr(total);
+    if (scal != T(0)) scal = divr((T)s, scal);
+    s_scal = scal;
+  }
+  __syncthreads();
+  const T scal = s_scal;
   for (long e = threadIdx.x; e < len; e += blockDim.x) M[at(e)] = mulr(pos_adj(M[at(e)], pos), scal);
 }
 
