@@ -166,6 +166,12 @@ static int max_dim(const fgb_faust* F) {
 }  // namespace fgb
 
 fgb_faust::~fgb_faust() {
+  if (pool) {
+    for (auto& x : f) {
+      fgb::dfree(x.aux);
+      x = fgb::DevFactor();
+    }
+  }
   for (auto& x : f) fgb::free_factor(x);
   fgb::dfree(buf[0]);
   fgb::dfree(buf[1]);

@@ -6,6 +6,7 @@
 #include <cuda_bf16.h>
 
 #include <atomic>
+#include <memory>
 #include <cstdint>
 #include <cstdio>
 #include <string>
@@ -112,6 +113,9 @@ struct fgb_faust {
   size_t dxy_bytes = 0;
   // Device descriptor array for the fused chain kernel.
   void* chain_desc = nullptr;
+  // When set, the factor arrays are views into this shared device block
+  // (results of one batched call) and are released with its last owner.
+  std::shared_ptr<void> pool;
   ~fgb_faust();
 };
 

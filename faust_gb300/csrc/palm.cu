@@ -158,8 +158,15 @@ struct Palm {
   fgb_palm_params p;
   bool r2l = false;
   long long graph_nodes = 0;
+  // the step-size power iteration (two blocks) runs on a side stream beside
+  // the gradient products (whole grid) and joins before alpha is read
+  cudaStream_t side = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
 
   ~Palm() {
+    if (side) cudaStreamDestroy(side);
+    if (ev_fork) cudaEventDestroy(ev_fork);
+    if (ev_join) cudaEventDestroy(ev_join);
     for (auto& f : S) free_factor(f);
     for (auto* q : packed) dfree(q);
     for (auto* q : supp) dfree(q);
@@ -310,7 +317,7 @@ struct Palm {
     pp.alpha = alpha;
     const bool fp64 = sizeof(T) == 8 || p.norm2_fp64;
     return launch_power_iteration(ctx, sizeof(T) == 8 ? FGB_F64 : FGB_F32, fp64, a, b, p.norm2_max_iter,
-                                  p.norm2_threshold, rnd, pi, pp);
+                                  p.norm2_threshold, rnd, pi, pp, side);
   }
 
   fgb_status init_ite() {
@@ -329,7 +336,10 @@ struct Palm {
   }
 
   fgb_status update_fact(int f, int it) {
+    FGB_CUDA(ctx, cudaEventRecord(ev_fork, ctx->stream));
+    FGB_CUDA(ctx, cudaStreamWaitEvent(side, ev_fork, 0));
     FGB_TRY(step_size(f, it));
+    FGB_CUDA(ctx, cudaEventRecord(ev_join, side));
     const bool hasL = f > 0, hasR = f + 1 < J;
     const DevFactor& Sf = S[f];
     Epi<T> st;
@@ -393,6 +403,7 @@ struct Palm {
       for (int l = 0; l < f; ++l) ops.push_back({0, l});
     }
     if (ops.empty()) {
+      FGB_CUDA(ctx, cudaStreamWaitEvent(ctx->stream, ev_join, 0));
       k_d_minus<T><<<grid((long)Sf.rows * Sf.cols), 256, 0, ctx->stream>>>(D, E, (long)Sf.rows * Sf.cols, alpha);
       FGB_LAUNCHED(ctx);
     } else {
@@ -401,6 +412,7 @@ struct Palm {
         const bool last = q + 1 == ops.size();
         const DevFactor& F = S[ops[q].second];
         T* dst = last ? D : buf[cur ^ 1];
+        if (last) FGB_CUDA(ctx, cudaStreamWaitEvent(ctx->stream, ev_join, 0));
         if (ops[q].first == 0) {
           FGB_TRY(mul_SH(F, src, cols, dst, last ? eD : st));
           rows = F.cols;
@@ -475,6 +487,11 @@ struct Palm {
 
   fgb_status run() {
     if (p.nb_it <= 0) return FGB_OK;
+    if (!side) {
+      FGB_CUDA(ctx, cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking));
+      FGB_CUDA(ctx, cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming));
+      FGB_CUDA(ctx, cudaEventCreateWithFlags(&ev_join, cudaEventDisableTiming));
+    }
     // iteration 0 eagerly (its zero-norm rule differs), the rest as a graph
     FGB_TRY(iteration(0));
     int st = 0;

@@ -48,6 +48,7 @@ struct Inst {
   double lambda;  // in: initial lambda; out: final lambda
   Fac<T> f[MAXJ];
   Cons<T> c[MAXJ];
+  int nnz[MAXJ];  // out: entries of each factor
 };
 
 template <typename T>
@@ -65,7 +66,7 @@ struct Params {
   double norm2_threshold, step_size;
   long maxdim2;
   int ninst;
-  int pad;
+  int stage_elems;  // shared-memory staging area of a CTA, in elements of T
 };
 
 // ------------------------------------------------------------------ block ops
@@ -97,34 +98,72 @@ __device__ __forceinline__ T b_epi(int mode, T acc, const T* aux, long idx, T s)
   return acc;
 }
 
-// Y = S X   (S: rows x inner CSR, X: inner x ncols, Y: rows x ncols; lds = rows)
+// Shared-memory staging area of a CTA (elements of T).
 template <typename T>
-__device__ void b_spmm(const int* rp, const int* ci, const T* v, int rows, const T* X, int ldx, int ncols, T* Y,
-                       int mode, const T* aux, T s) {
-  const long n = (long)rows * ncols;
-  for (long idx = threadIdx.x; idx < n; idx += BT) {
-    const int i = (int)(idx % rows);
-    const long j = idx / rows;
-    T acc = T(0);
-    for (int p = rp[i]; p < rp[i + 1]; ++p) acc = fmad(v[p], X[ci[p] + j * ldx], acc);
-    Y[idx] = b_epi(mode, acc, aux, idx, s);
+struct Stage {
+  T* p;
+  int elems;
+};
+
+// Y = S X   (S: rows x inner CSR, X: inner x ncols, Y: rows x ncols; lds = rows).
+// Blocks of X's columns are staged in shared memory, so the gathers of one
+// output column read on-chip; each entry is still the sequential fma over the
+// row's stored entries.
+template <typename T>
+__device__ void b_spmm(const int* rp, const int* ci, const T* v, int rows, int inner, const T* X, int ldx, int ncols,
+                       T* Y, int mode, const T* aux, T s, Stage<T> sg) {
+  const int cb = max(1, min(ncols, sg.elems / max(1, inner)));
+  for (int j0 = 0; j0 < ncols; j0 += cb) {
+    const int nc = min(cb, ncols - j0);
+    const long ne = (long)inner * nc;
+    for (long e = threadIdx.x; e < ne; e += BT) {
+      const int r = (int)(e % inner);
+      const int c = (int)(e / inner);
+      sg.p[e] = X[r + (long)(j0 + c) * ldx];
+    }
+    __syncthreads();
+    const long no = (long)rows * nc;
+    for (long e = threadIdx.x; e < no; e += BT) {
+      const int i = (int)(e % rows);
+      const int c = (int)(e / rows);
+      const T* xs = sg.p + (long)c * inner;
+      T acc = T(0);
+      const int p1 = rp[i + 1];
+      for (int p = rp[i]; p < p1; ++p) acc = fmad(v[p], xs[ci[p]], acc);
+      const long idx = i + (long)(j0 + c) * rows;
+      Y[idx] = b_epi(mode, acc, aux, idx, s);
+    }
+    __syncthreads();
   }
-  __syncthreads();
 }
 
 // Y = X S^T given the CSR of S (srows rows): y[r, c] = sum over row c of S.
+// Blocks of X's rows (all xcols columns) are staged in shared memory.
 template <typename T>
-__device__ void b_dense_csrT(const T* X, int xrows, const int* rp, const int* ci, const T* v, int srows, T* Y,
-                             int mode, const T* aux, T s) {
-  const long n = (long)xrows * srows;
-  for (long idx = threadIdx.x; idx < n; idx += BT) {
-    const int r = (int)(idx % xrows);
-    const int c = (int)(idx / xrows);
-    T acc = T(0);
-    for (int p = rp[c]; p < rp[c + 1]; ++p) acc = fmad(v[p], X[r + (long)ci[p] * xrows], acc);
-    Y[idx] = b_epi(mode, acc, aux, idx, s);
+__device__ void b_dense_csrT(const T* X, int xrows, int xcols, const int* rp, const int* ci, const T* v, int srows,
+                             T* Y, int mode, const T* aux, T s, Stage<T> sg) {
+  const int rb = max(1, min(xrows, sg.elems / max(1, xcols)));
+  for (int r0 = 0; r0 < xrows; r0 += rb) {
+    const int nr = min(rb, xrows - r0);
+    const long ne = (long)nr * xcols;
+    for (long e = threadIdx.x; e < ne; e += BT) {
+      const int rl = (int)(e % nr);
+      const int col = (int)(e / nr);
+      sg.p[e] = X[r0 + rl + (long)col * xrows];
+    }
+    __syncthreads();
+    const long no = (long)nr * srows;
+    for (long e = threadIdx.x; e < no; e += BT) {
+      const int rl = (int)(e % nr);
+      const int c = (int)(e / nr);
+      T acc = T(0);
+      const int p1 = rp[c + 1];
+      for (int p = rp[c]; p < p1; ++p) acc = fmad(v[p], sg.p[rl + (long)ci[p] * nr], acc);
+      const long idx = r0 + rl + (long)c * xrows;
+      Y[idx] = b_epi(mode, acc, aux, idx, s);
+    }
+    __syncthreads();
   }
-  __syncthreads();
 }
 
 // Canonical sum of a[i]*b[i] over i < n (every thread gets the result).
@@ -276,42 +315,96 @@ __device__ void b_heap_adjust(unsigned long long* hk, int* hi, int hole, int len
   hi[hole] = vi;
 }
 
-// Per-line heap selection (std::partial_sort, |a| > |b|) of k entries.
+// The same adjustment on a heap whose entry j sits at hk[j * BT] (one heap
+// per thread, interleaved in shared memory).
+__device__ void b_heap_adjust_s(unsigned long long* hk, int* hi, int hole, int len, unsigned long long vk, int vi) {
+  const int top = hole;
+  int child = hole;
+  while (child < (len - 1) / 2) {
+    child = 2 * (child + 1);
+    if (hk[child * BT] > hk[(child - 1) * BT]) child--;
+    hk[hole * BT] = hk[child * BT];
+    hi[hole * BT] = hi[child * BT];
+    hole = child;
+  }
+  if ((len & 1) == 0 && child == (len - 2) / 2) {
+    child = 2 * (child + 1);
+    hk[hole * BT] = hk[(child - 1) * BT];
+    hi[hole * BT] = hi[(child - 1) * BT];
+    hole = child - 1;
+  }
+  int parent = (hole - 1) / 2;
+  while (hole > top && hk[parent * BT] > vk) {
+    hk[hole * BT] = hk[parent * BT];
+    hi[hole * BT] = hi[parent * BT];
+    hole = parent;
+    parent = (hole - 1) / 2;
+  }
+  hk[hole * BT] = vk;
+  hi[hole * BT] = vi;
+}
+
+// Per-line heap selection (std::partial_sort, |a| > |b|) of k entries, one
+// thread per line.  The heaps live in the staging area when they fit (else
+// in per-thread arrays); entries are read eight at a time.
 template <typename T>
 __device__ void b_line_topk(const T* M, int rows, int cols, bool by_col, int k, int pos, unsigned char* flags,
-                            unsigned char bit) {
+                            unsigned char bit, Stage<T> sg) {
   const int nl = by_col ? cols : rows, len = by_col ? rows : cols;
+  const long step = by_col ? 1 : rows;
+  const bool on_chip = (size_t)k * BT * 12 <= (size_t)sg.elems * sizeof(T);
+  unsigned long long* shk = reinterpret_cast<unsigned long long*>(sg.p) + threadIdx.x;
+  int* shi = reinterpret_cast<int*>(reinterpret_cast<unsigned long long*>(sg.p) + (size_t)k * BT) + threadIdx.x;
   for (int line = threadIdx.x; line < nl; line += BT) {
-    auto at = [&](int e) -> long { return by_col ? (long)line * rows + e : (long)e * rows + line; };
+    const long base = by_col ? (long)line * rows : line;
     if (k >= len) {
-      for (int e = 0; e < len; ++e) flags[at(e)] |= bit;
+      for (int e = 0; e < len; ++e) flags[base + e * step] |= bit;
       continue;
     }
-    unsigned long long hk[KMAX];
-    int hi[KMAX];
-    for (int e = 0; e < k; ++e) {
-      hk[e] = bkey(bpos(M[at(e)], pos));
-      hi[e] = e;
-    }
-    if (k >= 2) {
-      int parent = (k - 2) / 2;
-      while (true) {
-        b_heap_adjust(hk, hi, parent, k, hk[parent], hi[parent]);
-        if (parent == 0) break;
-        parent--;
+    if (on_chip) {
+      for (int e = 0; e < k; ++e) {
+        shk[e * BT] = bkey(bpos(M[base + e * step], pos));
+        shi[e * BT] = e;
       }
+      if (k >= 2)
+        for (int parent = (k - 2) / 2; parent >= 0; --parent)
+          b_heap_adjust_s(shk, shi, parent, k, shk[parent * BT], shi[parent * BT]);
+      int e = k;
+      for (; e + 8 <= len; e += 8) {
+        unsigned long long kk[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) kk[u] = bkey(bpos(M[base + (e + u) * step], pos));
+#pragma unroll
+        for (int u = 0; u < 8; ++u)
+          if (kk[u] > shk[0]) b_heap_adjust_s(shk, shi, 0, k, kk[u], e + u);
+      }
+      for (; e < len; ++e) {
+        const unsigned long long key = bkey(bpos(M[base + e * step], pos));
+        if (key > shk[0]) b_heap_adjust_s(shk, shi, 0, k, key, e);
+      }
+      for (int q = 0; q < k; ++q) flags[base + (long)shi[q * BT] * step] |= bit;
+    } else {
+      unsigned long long hk[KMAX];
+      int hi[KMAX];
+      for (int e = 0; e < k; ++e) {
+        hk[e] = bkey(bpos(M[base + e * step], pos));
+        hi[e] = e;
+      }
+      if (k >= 2)
+        for (int parent = (k - 2) / 2; parent >= 0; --parent) b_heap_adjust(hk, hi, parent, k, hk[parent], hi[parent]);
+      for (int e = k; e < len; ++e) {
+        const unsigned long long key = bkey(bpos(M[base + e * step], pos));
+        if (key > hk[0]) b_heap_adjust(hk, hi, 0, k, key, e);
+      }
+      for (int q = 0; q < k; ++q) flags[base + (long)hi[q] * step] |= bit;
     }
-    for (int e = k; e < len; ++e) {
-      const unsigned long long key = bkey(bpos(M[at(e)], pos));
-      if (key > hk[0]) b_heap_adjust(hk, hi, 0, k, key, e);
-    }
-    for (int e = 0; e < k; ++e) flags[at(hi[e])] |= bit;
   }
   __syncthreads();
 }
 
 template <typename T>
-__device__ bool b_project(const Cons<T>& c, T* M, int rows, int cols, unsigned char* flags, T* lane, int* st) {
+__device__ bool b_project(const Cons<T>& c, T* M, int rows, int cols, unsigned char* flags, T* lane, int* st,
+                          Stage<T> sg) {
   const long N = (long)rows * cols;
   int pos = c.pos;
   if (c.kind == FGB_SPCOL || c.kind == FGB_SPLIN || c.kind == FGB_SPLINCOL) {
@@ -319,8 +412,8 @@ __device__ bool b_project(const Cons<T>& c, T* M, int rows, int cols, unsigned c
     if (c.k <= 0) {
       b_zero(M, N);
     } else {
-      if (c.kind != FGB_SPLIN) b_line_topk(M, rows, cols, true, min(c.k, rows), pos, flags, 1);
-      if (c.kind != FGB_SPCOL) b_line_topk(M, rows, cols, false, min(c.k, cols), pos, flags, 2);
+      if (c.kind != FGB_SPLIN) b_line_topk(M, rows, cols, true, min(c.k, rows), pos, flags, 1, sg);
+      if (c.kind != FGB_SPCOL) b_line_topk(M, rows, cols, false, min(c.k, cols), pos, flags, 2, sg);
       for (long i = threadIdx.x; i < N; i += BT) {
         const T v = bpos(M[i], pos);
         M[i] = flags[i] ? v : T(0);
@@ -505,7 +598,7 @@ __device__ bool b_dense_to_csr(const T* M, Fac<T>& f, int* cnt, int* st) {
 // ------------------------------------------------------------------ one instance
 template <typename T, typename TN>
 __device__ void run_instance(Inst<T>& I, const Slot<T>& W, const Params& P, const TN* x0, TN* vbuf, int maxn,
-                             T* lane, TN* lane_n) {
+                             T* lane, TN* lane_n, Stage<T> sg) {
   const int J = I.J;
   Fac<T>* S = I.f;
   const bool r2l = P.r2l != 0;
@@ -524,13 +617,11 @@ __device__ void run_instance(Inst<T>& I, const Slot<T>& W, const Params& P, cons
       if (!r2l) {
         b_csr_to_dense(S[J - 1], packed[J - 2]);
         for (int i = J - 3; i >= 0; --i)
-          b_spmm<T>(S[i + 1].rowptr, S[i + 1].colind, S[i + 1].val, S[i + 1].rows, packed[i + 1], S[i + 1].cols, acols,
-                    packed[i], E_STORE, nullptr, T(0));
+          b_spmm<T>(S[i + 1].rowptr, S[i + 1].colind, S[i + 1].val, S[i + 1].rows, S[i + 1].cols, packed[i + 1], S[i + 1].cols, acols, packed[i], E_STORE, nullptr, T(0), sg);
       } else {
         b_csr_to_dense(S[0], packed[1]);
         for (int i = 2; i < J; ++i)
-          b_dense_csrT<T>(packed[i - 1], arows, S[i - 1].t_rowptr, S[i - 1].t_colind, S[i - 1].t_val, S[i - 1].cols,
-                          packed[i], E_STORE, nullptr, T(0));
+          b_dense_csrT<T>(packed[i - 1], arows, S[i - 1].rows, S[i - 1].t_rowptr, S[i - 1].t_colind, S[i - 1].t_val, S[i - 1].cols, packed[i], E_STORE, nullptr, T(0), sg);
       }
     }
     for (int step = 0; step < J; ++step) {
@@ -573,8 +664,7 @@ __device__ void run_instance(Inst<T>& I, const Slot<T>& W, const Params& P, cons
       int cur = 0;
       if (!r2l) {
         if (hasR)
-          b_spmm<T>(Sf.rowptr, Sf.colind, Sf.val, Sf.rows, packed[f], Sf.cols, acols, buf[cur], f == 0 ? E_LAMBDA : E_STORE,
-                    I.A, lam);
+          b_spmm<T>(Sf.rowptr, Sf.colind, Sf.val, Sf.rows, Sf.cols, packed[f], Sf.cols, acols, buf[cur], f == 0 ? E_LAMBDA : E_STORE, I.A, lam, sg);
         else if (f == 0) {
           for (long i = threadIdx.x; i < (long)arows * acols; i += BT) buf[cur][i] = subr(mulr(lam, W.D[i]), I.A[i]);
           __syncthreads();
@@ -582,15 +672,13 @@ __device__ void run_instance(Inst<T>& I, const Slot<T>& W, const Params& P, cons
           b_csr_to_dense(Sf, buf[cur]);
         }
         for (int l = f - 1; l >= 0; --l) {
-          b_spmm<T>(S[l].rowptr, S[l].colind, S[l].val, S[l].rows, buf[cur], S[l].cols, acols, buf[cur ^ 1],
-                    l == 0 ? E_LAMBDA : E_STORE, I.A, lam);
+          b_spmm<T>(S[l].rowptr, S[l].colind, S[l].val, S[l].rows, S[l].cols, buf[cur], S[l].cols, acols, buf[cur ^ 1], l == 0 ? E_LAMBDA : E_STORE, I.A, lam, sg);
           cur ^= 1;
         }
       } else {
         const int nR = J - 1 - f;
         if (hasL)
-          b_dense_csrT<T>(packed[f], arows, Sf.t_rowptr, Sf.t_colind, Sf.t_val, Sf.cols, buf[cur],
-                          nR == 0 ? E_LAMBDA : E_STORE, I.A, lam);
+          b_dense_csrT<T>(packed[f], arows, Sf.rows, Sf.t_rowptr, Sf.t_colind, Sf.t_val, Sf.cols, buf[cur], nR == 0 ? E_LAMBDA : E_STORE, I.A, lam, sg);
         else if (nR == 0) {
           for (long i = threadIdx.x; i < (long)arows * acols; i += BT) buf[cur][i] = subr(mulr(lam, W.D[i]), I.A[i]);
           __syncthreads();
@@ -598,8 +686,7 @@ __device__ void run_instance(Inst<T>& I, const Slot<T>& W, const Params& P, cons
           b_csr_to_dense(Sf, buf[cur]);
         }
         for (int l = f + 1; l < J; ++l) {
-          b_dense_csrT<T>(buf[cur], arows, S[l].t_rowptr, S[l].t_colind, S[l].t_val, S[l].cols, buf[cur ^ 1],
-                          l == J - 1 ? E_LAMBDA : E_STORE, I.A, lam);
+          b_dense_csrT<T>(buf[cur], arows, S[l].rows, S[l].t_rowptr, S[l].t_colind, S[l].t_val, S[l].cols, buf[cur ^ 1], l == J - 1 ? E_LAMBDA : E_STORE, I.A, lam, sg);
           cur ^= 1;
         }
       }
@@ -615,16 +702,14 @@ __device__ void run_instance(Inst<T>& I, const Slot<T>& W, const Params& P, cons
         auto left = [&](int l) {
           const bool last = ++q == nops;
           T* dst = last ? W.D : buf[cur ^ 1];
-          b_spmm<T>(S[l].t_rowptr, S[l].t_colind, S[l].t_val, S[l].cols, buf[cur], S[l].rows, cols, dst,
-                    last ? E_DMINUS : E_STORE, W.D, alpha);
+          b_spmm<T>(S[l].t_rowptr, S[l].t_colind, S[l].t_val, S[l].cols, S[l].rows, buf[cur], S[l].rows, cols, dst, last ? E_DMINUS : E_STORE, W.D, alpha, sg);
           rows = S[l].cols;
           if (!last) cur ^= 1;
         };
         auto right = [&](int l) {
           const bool last = ++q == nops;
           T* dst = last ? W.D : buf[cur ^ 1];
-          b_dense_csrT<T>(buf[cur], rows, S[l].rowptr, S[l].colind, S[l].val, S[l].rows, dst,
-                          last ? E_DMINUS : E_STORE, W.D, alpha);
+          b_dense_csrT<T>(buf[cur], rows, S[l].cols, S[l].rowptr, S[l].colind, S[l].val, S[l].rows, dst, last ? E_DMINUS : E_STORE, W.D, alpha, sg);
           cols = S[l].rows;
           if (!last) cur ^= 1;
         };
@@ -636,7 +721,7 @@ __device__ void run_instance(Inst<T>& I, const Slot<T>& W, const Params& P, cons
           for (int l = 0; l < f; ++l) left(l);
         }
       }
-      if (!b_project<T>(I.c[f], W.D, Sf.rows, Sf.cols, W.flags, lane, &st)) break;
+      if (!b_project<T>(I.c[f], W.D, Sf.rows, Sf.cols, W.flags, lane, &st, sg)) break;
       if (!b_dense_to_csr<T>(W.D, S[f], W.cnt, &st)) break;
     }
     __syncthreads();
@@ -655,19 +740,16 @@ __device__ void run_instance(Inst<T>& I, const Slot<T>& W, const Params& P, cons
         b_csr_to_dense(S[0], buf[0]);
         Smat = buf[0];
       } else if (reuse && !r2l && use_pR0) {
-        b_spmm<T>(S[0].rowptr, S[0].colind, S[0].val, S[0].rows, packed[0], S[0].cols, acols, buf[0], E_STORE, nullptr,
-                  T(0));
+        b_spmm<T>(S[0].rowptr, S[0].colind, S[0].val, S[0].rows, S[0].cols, packed[0], S[0].cols, acols, buf[0], E_STORE, nullptr, T(0), sg);
         Smat = buf[0];
       } else if (reuse && r2l && !use_pR0) {
-        b_dense_csrT<T>(packed[J - 1], arows, S[J - 1].t_rowptr, S[J - 1].t_colind, S[J - 1].t_val, S[J - 1].cols,
-                        buf[0], E_STORE, nullptr, T(0));
+        b_dense_csrT<T>(packed[J - 1], arows, S[J - 1].rows, S[J - 1].t_rowptr, S[J - 1].t_colind, S[J - 1].t_val, S[J - 1].cols, buf[0], E_STORE, nullptr, T(0), sg);
         Smat = buf[0];
       } else {
         int cur = 0;
         b_csr_to_dense(S[J - 1], buf[cur]);
         for (int l = J - 2; l >= 0; --l) {
-          b_spmm<T>(S[l].rowptr, S[l].colind, S[l].val, S[l].rows, buf[cur], S[l].cols, acols, buf[cur ^ 1], E_STORE,
-                    nullptr, T(0));
+          b_spmm<T>(S[l].rowptr, S[l].colind, S[l].val, S[l].rows, S[l].cols, buf[cur], S[l].cols, acols, buf[cur ^ 1], E_STORE, nullptr, T(0), sg);
           cur ^= 1;
         }
         Smat = buf[cur];
@@ -714,6 +796,7 @@ __device__ void run_instance(Inst<T>& I, const Slot<T>& W, const Params& P, cons
   if (threadIdx.x == 0) {
     I.status = st;
     I.lambda = (double)lam;
+    for (int f = 0; f < J; ++f) I.nnz[f] = S[f].rowptr[S[f].rows];
   }
 }
 
@@ -723,6 +806,9 @@ __global__ void __launch_bounds__(BT) k_palm_batched(Inst<T>* insts, const int* 
   extern __shared__ __align__(16) unsigned char smem_raw[];
   TN* vbuf = reinterpret_cast<TN*>(smem_raw);  // 3 * maxn
   TN* lane_n = vbuf + 3 * (long)maxn;
+  // staging area 16-byte aligned after the vectors
+  const size_t sg_off = ((3 * (size_t)maxn + BT) * sizeof(TN) + 15) & ~(size_t)15;
+  Stage<T> sg{reinterpret_cast<T*>(smem_raw + sg_off), P.stage_elems};
   __shared__ T lane[BT];
   __shared__ int next;
   const Slot<T> W = slots[blockIdx.x];
@@ -732,7 +818,7 @@ __global__ void __launch_bounds__(BT) k_palm_batched(Inst<T>* insts, const int* 
     const int q = next;
     __syncthreads();
     if (q >= P.ninst) break;
-    run_instance<T, TN>(insts[order[q]], W, P, x0, vbuf, maxn, lane, lane_n);
+    run_instance<T, TN>(insts[order[q]], W, P, x0, vbuf, maxn, lane, lane_n, sg);
   }
 }
 
@@ -776,7 +862,7 @@ static fgb_status batched_impl(fgb_ctx* ctx, fgb_dtype dt, int nprob, const fgb_
   FGB_CUDA(ctx, cudaSetDevice(ctx->device));
   const size_t es = sizeof(T);
   const long md2 = (long)maxdim * maxdim;
-  // slots
+  // slots (one device block for all of them)
   int per_sm = opts && opts->ctas_per_sm > 0 ? opts->ctas_per_sm : 2;
   int nslots = std::min(nprob, per_sm * ctx->sm_count);
   std::vector<void*> allocs;
@@ -785,23 +871,101 @@ static fgb_status batched_impl(fgb_ctx* ctx, fgb_dtype dt, int nprob, const fgb_
     if (s == FGB_OK) allocs.push_back(*q);
     return s;
   };
+  auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
   fgb_status s = FGB_OK;
   std::vector<Slot<T>> hs(nslots);
-  for (int i = 0; i < nslots && s == FGB_OK; ++i) {
-    s = alloc((void**)&hs[i].D, es * md2);
-    if (s == FGB_OK) s = alloc((void**)&hs[i].buf0, es * md2);
-    if (s == FGB_OK) s = alloc((void**)&hs[i].buf1, es * md2);
-    if (s == FGB_OK) s = alloc((void**)&hs[i].packed, es * md2 * std::max(1, maxJ));
-    if (s == FGB_OK) s = alloc((void**)&hs[i].flags, (size_t)md2);
-    if (s == FGB_OK) s = alloc((void**)&hs[i].cnt, sizeof(int) * (maxdim + 2));
-    if (s == FGB_OK) s = cuda_check(ctx, cudaMemsetAsync(hs[i].flags, 0, (size_t)md2, ctx->stream), "memset");
+  {
+    const size_t dense = al(es * md2);
+    const size_t slot_bytes = 3 * dense + al(es * md2 * std::max(1, maxJ)) + al((size_t)md2) +
+                              al(sizeof(int) * (maxdim + 2));
+    unsigned char* base = nullptr;
+    s = alloc((void**)&base, slot_bytes * nslots);
+    for (int i = 0; i < nslots && s == FGB_OK; ++i) {
+      unsigned char* q = base + slot_bytes * i;
+      hs[i].D = reinterpret_cast<T*>(q);
+      q += dense;
+      hs[i].buf0 = reinterpret_cast<T*>(q);
+      q += dense;
+      hs[i].buf1 = reinterpret_cast<T*>(q);
+      q += dense;
+      hs[i].packed = reinterpret_cast<T*>(q);
+      q += al(es * md2 * std::max(1, maxJ));
+      hs[i].flags = q;
+      q += al((size_t)md2);
+      hs[i].cnt = reinterpret_cast<int*>(q);
+    }
+    // the projections expect cleared flags
+    if (s == FGB_OK) s = cuda_check(ctx, cudaMemsetAsync(base, 0, slot_bytes * nslots, ctx->stream), "memset");
   }
-  // instances and their factors
+  // instances and their factors: every factor array of every instance in one
+  // device block, filled from one host image with a single copy
   std::vector<Inst<T>> hi(nprob);
   std::vector<std::vector<DevFactor>> facs(nprob);
   std::vector<std::pair<const void*, T*>> supp_cache;
-  std::vector<T> h;
   std::vector<std::pair<double, int>> cost(nprob);
+  // host CSR (and transpose) of every initial factor: the given dense
+  // matrix, or palm4msa2's default (zeros for the first factor updated,
+  // identity for the others)
+  struct HostCSR {
+    std::vector<int> rp, ci, trp, tci;
+    std::vector<T> vv, tvv;
+    long cap = 0;
+    size_t off = 0;
+  };
+  std::vector<std::vector<HostCSR>> hc(nprob);
+  size_t pool_bytes = 0;
+  for (int i = 0; i < nprob; ++i) {
+    const fgb_palm_problem& q = probs[i];
+    hc[i].resize(q.nfacts);
+    for (int f = 0; f < q.nfacts; ++f) {
+      const fgb_constraint& c = q.cons[f];
+      HostCSR& H = hc[i][f];
+      H.rp.assign(c.rows + 1, 0);
+      if (q.init_facts) {
+        const T* d = (const T*)q.init_facts[f];
+        for (int r = 0; r < c.rows; ++r) {
+          for (int col = 0; col < c.cols; ++col) {
+            const T v = d[(size_t)col * c.rows + r];
+            if (v != T(0)) {
+              H.ci.push_back(col);
+              H.vv.push_back(v);
+            }
+          }
+          H.rp[r + 1] = (int)H.ci.size();
+        }
+      } else {
+        const bool zero = p->is_update_way_R2L ? (f == q.nfacts - 1) : (f == 0);
+        for (int r = 0; r < c.rows; ++r) {
+          if (!zero && r < c.cols) {
+            H.ci.push_back(r);
+            H.vv.push_back(T(1));
+          }
+          H.rp[r + 1] = (int)H.ci.size();
+        }
+      }
+      H.trp.assign(c.cols + 1, 0);
+      H.tci.resize(H.ci.size());
+      H.tvv.resize(H.ci.size());
+      for (int col : H.ci) H.trp[col + 1]++;
+      for (int col = 0; col < c.cols; ++col) H.trp[col + 1] += H.trp[col];
+      std::vector<int> fill(H.trp.begin(), H.trp.end() - 1);
+      for (int r = 0; r < c.rows; ++r)
+        for (int pp = H.rp[r]; pp < H.rp[r + 1]; ++pp) {
+          const int slot = fill[H.ci[pp]]++;
+          H.tci[slot] = r;
+          H.tvv[slot] = H.vv[pp];
+        }
+      H.cap = std::max<long>(palm_factor_capacity(c), (long)H.ci.size());
+      H.off = pool_bytes;
+      pool_bytes += al(sizeof(int) * (c.rows + 1)) + al(sizeof(int) * (c.cols + 1)) + 2 * al(sizeof(int) * H.cap) +
+                    2 * al(es * H.cap);
+    }
+  }
+  unsigned char* pool = nullptr;
+  if (s == FGB_OK) s = dmalloc(ctx, (void**)&pool, std::max<size_t>(pool_bytes, 256));
+  std::shared_ptr<void> pool_owner;
+  if (s == FGB_OK) pool_owner = std::shared_ptr<void>(pool, [](void* q) { dfree(q); });
+  std::vector<unsigned char> img(pool_bytes, 0);
   for (int i = 0; i < nprob && s == FGB_OK; ++i) {
     const fgb_palm_problem& q = probs[i];
     Inst<T>& I = hi[i];
@@ -815,61 +979,30 @@ static fgb_status batched_impl(fgb_ctx* ctx, fgb_dtype dt, int nprob, const fgb_
     double cst = 0;
     for (int f = 0; f < q.nfacts && s == FGB_OK; ++f) {
       const fgb_constraint& c = q.cons[f];
+      HostCSR& H = hc[i][f];
       DevFactor& F = facs[i][f];
       F.format = FGB_CSR;
       F.rows = c.rows;
       F.cols = c.cols;
-      F.cap = (int)palm_factor_capacity(c);
-      h.assign((size_t)c.rows * c.cols, T(0));
-      if (q.init_facts) {
-        std::memcpy(h.data(), q.init_facts[f], es * h.size());
-      } else {
-        const bool zero = p->is_update_way_R2L ? (f == q.nfacts - 1) : (f == 0);
-        if (!zero)
-          for (int d = 0; d < std::min(c.rows, c.cols); ++d) h[(size_t)d * c.rows + d] = T(1);
-      }
-      // host CSR of the initial factor
-      std::vector<int> rp(c.rows + 1, 0), ci;
-      std::vector<T> vv;
-      for (int r = 0; r < c.rows; ++r) {
-        for (int col = 0; col < c.cols; ++col) {
-          const T v = h[(size_t)col * c.rows + r];
-          if (v != T(0)) {
-            ci.push_back(col);
-            vv.push_back(v);
-          }
-        }
-        rp[r + 1] = (int)ci.size();
-      }
-      F.cap = std::max<int>(F.cap, (int)ci.size());
-      F.nnz = (int)ci.size();
-      // transpose on the host (ordered by row)
-      std::vector<int> trp(c.cols + 1, 0), tci(ci.size());
-      std::vector<T> tvv(ci.size());
-      for (int col : ci) trp[col + 1]++;
-      for (int col = 0; col < c.cols; ++col) trp[col + 1] += trp[col];
-      std::vector<int> fill(trp.begin(), trp.end() - 1);
-      for (int r = 0; r < c.rows; ++r)
-        for (int pp = rp[r]; pp < rp[r + 1]; ++pp) {
-          const int slot = fill[ci[pp]]++;
-          tci[slot] = r;
-          tvv[slot] = vv[pp];
-        }
-      s = dmalloc(ctx, (void**)&F.rowptr, sizeof(int) * (c.rows + 1));
-      if (s == FGB_OK) s = dmalloc(ctx, (void**)&F.colind, sizeof(int) * F.cap);
-      if (s == FGB_OK) s = dmalloc(ctx, &F.val, es * F.cap);
-      if (s == FGB_OK) s = dmalloc(ctx, (void**)&F.t_rowptr, sizeof(int) * (c.cols + 1));
-      if (s == FGB_OK) s = dmalloc(ctx, (void**)&F.t_colind, sizeof(int) * F.cap);
-      if (s == FGB_OK) s = dmalloc(ctx, &F.t_val, es * F.cap);
-      if (s != FGB_OK) break;
-      cudaMemcpy(F.rowptr, rp.data(), sizeof(int) * rp.size(), cudaMemcpyHostToDevice);
-      cudaMemcpy(F.t_rowptr, trp.data(), sizeof(int) * trp.size(), cudaMemcpyHostToDevice);
-      if (!ci.empty()) {
-        cudaMemcpy(F.colind, ci.data(), sizeof(int) * ci.size(), cudaMemcpyHostToDevice);
-        cudaMemcpy(F.val, vv.data(), es * vv.size(), cudaMemcpyHostToDevice);
-        cudaMemcpy(F.t_colind, tci.data(), sizeof(int) * tci.size(), cudaMemcpyHostToDevice);
-        cudaMemcpy(F.t_val, tvv.data(), es * tvv.size(), cudaMemcpyHostToDevice);
-      }
+      F.cap = (int)H.cap;
+      F.nnz = (int)H.ci.size();
+      const long cap = H.cap;
+      const std::vector<int>&rp = H.rp, &ci = H.ci, &trp = H.trp, &tci = H.tci;
+      const std::vector<T>&vv = H.vv, &tvv = H.tvv;
+      // carve the pool and write the host image
+      size_t o = H.off;
+      auto place = [&](const void* src, size_t bytes, size_t room) {
+        if (bytes) std::memcpy(img.data() + o, src, bytes);
+        void* d = pool + o;
+        o += al(room);
+        return d;
+      };
+      F.rowptr = (int*)place(rp.data(), sizeof(int) * rp.size(), sizeof(int) * (c.rows + 1));
+      F.t_rowptr = (int*)place(trp.data(), sizeof(int) * trp.size(), sizeof(int) * (c.cols + 1));
+      F.colind = (int*)place(ci.data(), sizeof(int) * ci.size(), sizeof(int) * cap);
+      F.t_colind = (int*)place(tci.data(), sizeof(int) * tci.size(), sizeof(int) * cap);
+      F.val = place(vv.data(), es * vv.size(), es * cap);
+      F.t_val = place(tvv.data(), es * tvv.size(), es * cap);
       F.has_t = true;
       I.f[f] = Fac<T>{F.rows, F.cols, F.cap, 0, F.rowptr, F.colind, (T*)F.val, F.t_rowptr, F.t_colind, (T*)F.t_val};
       Cons<T>& C = I.c[f];
@@ -895,6 +1028,8 @@ static fgb_status batched_impl(fgb_ctx* ctx, fgb_dtype dt, int nprob, const fgb_
     }
     cost[i] = {-(cst * q.nfacts), i};
   }
+  if (s == FGB_OK && pool_bytes)
+    s = cuda_check(ctx, cudaMemcpy(pool, img.data(), pool_bytes, cudaMemcpyHostToDevice), "batched upload");
   if (s == FGB_OK) s = cuda_check(ctx, cudaGetLastError(), "batched upload");
   Inst<T>* d_inst = nullptr;
   Slot<T>* d_slots = nullptr;
@@ -931,14 +1066,24 @@ static fgb_status batched_impl(fgb_ctx* ctx, fgb_dtype dt, int nprob, const fgb_
     P.maxdim2 = md2;
     P.ninst = nprob;
     const bool fp64n = sizeof(T) == 8 || p->norm2_fp64;
-    const size_t smem = (3 * (size_t)maxdim + BT) * (fp64n ? 8 : 4);
+    // power-iteration vectors, their reduction lanes, then the staging area
+    // of the block products (a share of the SM's shared memory per CTA)
+    const size_t vec_bytes = ((3 * (size_t)maxdim + BT) * (fp64n ? 8 : 4) + 15) & ~(size_t)15;
+    const size_t per_cta = std::min<size_t>(ctx->smem_optin ? ctx->smem_optin : 227 * 1024,
+                                            (size_t)(228 * 1024) / per_sm - 2048);
+    const size_t stage_bytes = per_cta > vec_bytes + 8192 + 4096 ? per_cta - vec_bytes - 8192 : 4096;
+    P.stage_elems = (int)std::min<size_t>(stage_bytes / es, (size_t)md2);
+    if (P.stage_elems < maxdim)
+      s = fail(ctx, FGB_ERR_NOT_SUPPORTED, "batched palm4msa2: dimension %d too large for %d CTAs per SM", maxdim,
+               per_sm);
+    const size_t smem = vec_bytes + (size_t)P.stage_elems * es;
     if (fp64n) {
       auto kern = k_palm_batched<T, double>;
-      if (smem > 40 * 1024) s = cuda_check(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem), "attr");
+      s = cuda_check(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem), "attr");
       if (s == FGB_OK) kern<<<nslots, BT, smem, ctx->stream>>>(d_inst, d_order, d_queue, d_slots, P, ctx->x0_d, maxdim);
     } else {
       auto kern = k_palm_batched<T, float>;
-      if (smem > 40 * 1024) s = cuda_check(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem), "attr");
+      s = cuda_check(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem), "attr");
       if (s == FGB_OK) kern<<<nslots, BT, smem, ctx->stream>>>(d_inst, d_order, d_queue, d_slots, P, ctx->x0_f, maxdim);
     }
     if (s == FGB_OK) {
@@ -956,17 +1101,14 @@ static fgb_status batched_impl(fgb_ctx* ctx, fgb_dtype dt, int nprob, const fgb_
       F->ctx = ctx;
       F->dtype = dt;
       F->f = facs[i];
-      for (auto& f : F->f) {
-        int nnz = 0;
-        cudaMemcpy(&nnz, f.rowptr + f.rows, sizeof(int), cudaMemcpyDeviceToHost);
-        f.nnz = nnz;
-      }
+      F->pool = pool_owner;
+      for (int f = 0; f < (int)F->f.size(); ++f) F->f[f].nnz = hi[i].nnz[f];
       facs[i].clear();
       res[i].faust = F;
     }
   }
-  for (auto& v : facs)
-    for (auto& f : v) free_factor(f);
+  // factors not handed out are views into the pool (released with its owner)
+  facs.clear();
   for (void* q : allocs) dfree(q);
   return s;
 }

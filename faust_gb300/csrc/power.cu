@@ -274,7 +274,7 @@ fgb_status pi_rand_device(fgb_ctx* ctx, int n, const int** d_rand) {
 
 template <typename TF, typename TC>
 static fgb_status launch_pi_t(fgb_ctx* ctx, const PIChain& a, const PIChain& b, int max_iter, double thr,
-                              const int* d_rand, PIOut* d_out, const PIPalm& palm) {
+                              const int* d_rand, PIOut* d_out, const PIPalm& palm, cudaStream_t stream) {
   const int maxn = std::max(1, std::max(a.maxdim, b.maxdim));
   const size_t vec = (3 * (size_t)maxn + CR_LANES) * sizeof(TC);
   const size_t cap = std::min<size_t>(ctx->smem_optin > 4096 ? ctx->smem_optin - 4096 : 0, 220 * 1024);
@@ -290,18 +290,20 @@ static fgb_status launch_pi_t(fgb_ctx* ctx, const PIChain& a, const PIChain& b, 
   }
   const TC* x0 = sizeof(TC) == 8 ? (const TC*)(const void*)ctx->x0_d : (const TC*)(const void*)ctx->x0_f;
   (void)d_rand;
-  kern<<<2, PI_THREADS, smem, ctx->stream>>>(a, b, max_iter, (TC)thr, x0, d_out, palm, maxn, (int)smem);
+  kern<<<2, PI_THREADS, smem, stream>>>(a, b, max_iter, (TC)thr, x0, d_out, palm, maxn, (int)smem);
   FGB_LAUNCHED(ctx);
   return FGB_OK;
 }
 
 fgb_status launch_power_iteration(fgb_ctx* ctx, fgb_dtype tf, bool fp64, const PIChain& a, const PIChain& b,
-                                  int max_iter, double thr, const int* d_rand, PIOut* d_out, const PIPalm& palm) {
+                                  int max_iter, double thr, const int* d_rand, PIOut* d_out, const PIPalm& palm,
+                                  cudaStream_t stream) {
   if (a.nops > PI_MAX_OPS || b.nops > PI_MAX_OPS) return fail(ctx, FGB_ERR_NOT_SUPPORTED, "power iteration: chain too long");
-  if (tf == FGB_F64) return launch_pi_t<double, double>(ctx, a, b, max_iter, thr, d_rand, d_out, palm);
+  if (!stream) stream = ctx->stream;
+  if (tf == FGB_F64) return launch_pi_t<double, double>(ctx, a, b, max_iter, thr, d_rand, d_out, palm, stream);
   if (tf == FGB_F32) {
-    if (fp64) return launch_pi_t<float, double>(ctx, a, b, max_iter, thr, d_rand, d_out, palm);
-    return launch_pi_t<float, float>(ctx, a, b, max_iter, thr, d_rand, d_out, palm);
+    if (fp64) return launch_pi_t<float, double>(ctx, a, b, max_iter, thr, d_rand, d_out, palm, stream);
+    return launch_pi_t<float, float>(ctx, a, b, max_iter, thr, d_rand, d_out, palm, stream);
   }
   return fail(ctx, FGB_ERR_NOT_SUPPORTED, "power iteration: F32 or F64 factors");
 }

@@ -57,9 +57,11 @@ struct PIOut {
 void pi_chain_build(const DevFactor* F, int lo, int hi, PIChain& ch);
 
 // Queues the two-chain power iteration kernel (chains with n == 0 are
-// skipped).  TF: factor value type; norms computed in TC.
+// skipped) on `stream` (nullptr: the context's stream).  TF: factor value
+// type; norms computed in TC.
 fgb_status launch_power_iteration(fgb_ctx* ctx, fgb_dtype tf, bool fp64, const PIChain& a, const PIChain& b,
-                                  int max_iter, double thr, const int* d_rand, PIOut* d_out, const PIPalm& palm);
+                                  int max_iter, double thr, const int* d_rand, PIOut* d_out, const PIPalm& palm,
+                                  cudaStream_t stream = nullptr);
 
 // Raw glibc rand() values after srand(418), length n, in device memory,
 // cached per context size.

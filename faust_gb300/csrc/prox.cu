@@ -56,6 +56,7 @@ fgb_status prox_work_reserve(fgb_ctx* ctx, ProxWork& w, long elems, int rows) {
   FGB_CUDA(ctx, cudaMemsetAsync(w.hist, 0, sizeof(unsigned) * 2048, ctx->stream));
   w.cap_elems = elems;
   w.cap_rows = rows;
+  w.growable = 1;
   return FGB_OK;
 }
 
@@ -69,6 +70,10 @@ void prox_work_free(ProxWork& w) {
   dfree(w.row_cnt);
   dfree(w.supp);
   dfree(w.heap);
+  dfree(w.cand);
+  dfree(w.wbound);
+  dfree(w.wcount);
+  dfree(w.heap2);
   w = ProxWork();
 }
 
@@ -449,6 +454,415 @@ __global__ void __launch_bounds__(PX_THREADS)
     if (h.n[i].key == t) flags[h.n[i].idx] = 1;
 }
 
+// ------------------------------------------------------------------ tie replay with a parallel pre-filter
+// The same selection as k_heap_replay, split so that only the sequential
+// part stays on one SM:
+//
+//  1. k_rp_bounds (one block per window of the linear order): a lower bound
+//     of the k-th largest key of the window, from two 12-bit histograms.
+//  2. k_rp_filter (one block per window): an entry i >= k can enter the heap
+//     only if its key exceeds the heap top at its arrival, and that top is at
+//     least the k-th largest key of every earlier window and at least the
+//     initial top (the smallest of the first k keys).  Entries above the
+//     largest of those bounds are kept, in linear order, in the window's
+//     own slot range of the candidate array.
+//  3. k_rp_replay (one block): make_heap of the first k keys, level by level
+//     in parallel (subtrees of one level are disjoint, so the order of
+//     libstdc++'s loop does not matter among them), then one warp replays
+//     every candidate against the live top.  A replacement of the top runs
+//     __adjust_heap + __push_heap as a warp: the hole's path to a leaf
+//     (the preferred child of each node, the left one only when its key is
+//     strictly smaller) is found five levels per round from a ballot of the
+//     preferences of a 31-node subtree, and because keys grow along that
+//     path, the sift-up of the new key is one more ballot.
+//
+// Windows: [0, 2k), [2k, 4k), [4k, 8k), ... doubling up to wmax entries,
+// then wmax entries each.
+constexpr int RP_BLOCK = 512;
+constexpr int RP_BINS = 4096;
+constexpr int RP_STAGE = 2048;
+constexpr int RP_MAXWIN = 1024;
+
+// Entries of the heap's key array: node n at n + 1, padded so that the
+// two-level look-ahead of rp_insert (up to entry 4 * lim + 7) stays inside.
+__host__ __device__ inline long rp_key_len(long k) { return ((2 * k + 8) + 1) & ~1L; }
+
+__host__ __device__ inline void rp_window(long i, long N, long k, long wmax, long* lo, long* hi) {
+  long s = 0, len = 2 * k;
+  long j = 0;
+  while (j < i && len < wmax) {
+    s += len;
+    len = s < wmax ? s : wmax;
+    ++j;
+  }
+  if (j < i) s += (i - j) * len;
+  *lo = s < N ? s : N;
+  *hi = s + len < N ? s + len : N;
+}
+
+static long rp_wmax(long N, long k) {
+  long w = std::max(65536L, 2 * k);
+  w = std::max(w, (N + 511) / 512);
+  return (w + 255) / 256 * 256;
+}
+
+static int rp_window_count(long N, long k, long wmax) {
+  int n = 0;
+  long lo, hi;
+  do {
+    rp_window(n, N, k, wmax, &lo, &hi);
+    ++n;
+  } while (hi < N);
+  return n;
+}
+
+// Block-wide (RP_BLOCK threads): the bin of the need-th largest key of a
+// histogram with bins in increasing key order, and the count above it.
+__device__ void rp_find_bin(const unsigned* hist, long need, int* s_bin, long* s_above, long* s_warp) {
+  constexpr int PER = RP_BINS / RP_BLOCK;  // 8 bins per thread, thread 0 holds the top ones
+  const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+  long mine = 0;
+  for (int q = 0; q < PER; ++q) mine += hist[RP_BINS - 1 - (t * PER + q)];
+  long incl = mine;
+  for (int o = 1; o < 32; o <<= 1) {
+    const long y = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += y;
+  }
+  if (lane == 31) s_warp[warp] = incl;
+  __syncthreads();
+  if (t == 0) {
+    long run = 0;
+    for (int w = 0; w < RP_BLOCK / 32; ++w) {
+      const long x = s_warp[w];
+      s_warp[w] = run;
+      run += x;
+    }
+  }
+  __syncthreads();
+  const long before = s_warp[warp] + incl - mine;  // keys in higher bins than this thread's
+  if (before < need && before + mine >= need) {
+    long acc = before;
+    for (int q = 0; q < PER; ++q) {
+      const int b = RP_BINS - 1 - (t * PER + q);
+      if (acc + hist[b] >= need) {
+        *s_bin = b;
+        *s_above = acc;
+        break;
+      }
+      acc += hist[b];
+    }
+  }
+  __syncthreads();
+}
+
+// Warp-aggregated shared-memory histogram increment (every lane calls it).
+__device__ __forceinline__ void rp_hist_add(unsigned* hist, unsigned bin, bool valid) {
+  const unsigned key = valid ? bin : 0xffffffffu;
+  const unsigned same = __match_any_sync(0xffffffffu, key);
+  const int lane = threadIdx.x & 31;
+  if (valid && (__ffs(same) - 1) == lane) atomicAdd(&hist[bin], (unsigned)__popc(same));
+}
+
+template <typename T>
+__global__ void __launch_bounds__(RP_BLOCK)
+    k_rp_bounds(const T* __restrict__ M, long N, int pos, long k, long wmax, const TopkState* st,
+                unsigned long long* __restrict__ wb) {
+  if (st->sel_case != 2) return;
+  __shared__ unsigned hist[RP_BINS];
+  __shared__ int s_bin;
+  __shared__ long s_above, s_warp[RP_BLOCK / 32];
+  long lo, hi;
+  rp_window(blockIdx.x, N, k, wmax, &lo, &hi);
+  if (hi - lo < k) {
+    if (threadIdx.x == 0) wb[blockIdx.x] = 0;
+    return;
+  }
+  constexpr int KB = (int)sizeof(T) * 8;
+  constexpr int S1 = KB - 12, S2 = KB - 24;
+  unsigned long long bound = 0;
+  long need = k;
+  for (int pass = 0; pass < 2; ++pass) {
+    for (int i = threadIdx.x; i < RP_BINS; i += RP_BLOCK) hist[i] = 0;
+    if (threadIdx.x == 0) s_bin = 0;
+    __syncthreads();
+    for (long b0 = lo; b0 < hi; b0 += RP_BLOCK) {
+      const long i = b0 + threadIdx.x;
+      const bool in = i < hi;
+      const unsigned long long key = in ? mag_key(pos_adj(M[i], pos)) : 0ULL;
+      const bool take = in && (pass == 0 || (key >> S1) == (bound >> S1));
+      const unsigned bin = (unsigned)((pass == 0 ? key >> S1 : key >> S2) & (RP_BINS - 1));
+      rp_hist_add(hist, bin, take);
+    }
+    __syncthreads();
+    rp_find_bin(hist, need, &s_bin, &s_above, s_warp);
+    if (pass == 0) {
+      bound = (unsigned long long)s_bin << S1;
+      need -= s_above;
+    } else {
+      bound |= (unsigned long long)s_bin << S2;
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) wb[blockIdx.x] = bound;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(RP_BLOCK)
+    k_rp_filter(const T* __restrict__ M, long N, int pos, long k, long wmax, const TopkState* st,
+                const unsigned long long* __restrict__ wb, HNode* __restrict__ cand, int* __restrict__ wcnt) {
+  if (st->sel_case != 2) return;
+  constexpr int U = 8, NW = RP_BLOCK / 32;
+  __shared__ unsigned long long s_min[NW];
+  __shared__ unsigned long long s_bound;
+  __shared__ int s_cnt[U * NW];
+  __shared__ int s_total;
+  const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+  long lo, hi;
+  rp_window(blockIdx.x, N, k, wmax, &lo, &hi);
+  // initial top: the smallest of the first k keys
+  unsigned long long mn = ~0ULL;
+  for (long i = t; i < k; i += RP_BLOCK) {
+    const unsigned long long key = mag_key(pos_adj(M[i], pos));
+    mn = key < mn ? key : mn;
+  }
+  for (int o = 16; o >= 1; o >>= 1) {
+    const unsigned long long y = __shfl_xor_sync(0xffffffffu, mn, o);
+    mn = y < mn ? y : mn;
+  }
+  if (lane == 0) s_min[warp] = mn;
+  __syncthreads();
+  if (t == 0) {
+    unsigned long long b = ~0ULL;
+    for (int w = 0; w < NW; ++w) b = s_min[w] < b ? s_min[w] : b;
+    for (int w = 0; w < (int)blockIdx.x; ++w) b = wb[w] > b ? wb[w] : b;
+    s_bound = b;
+  }
+  __syncthreads();
+  const unsigned long long bound = s_bound;
+  const long start = lo > k ? lo : k;
+  int total = 0;
+  const unsigned lt = (1u << lane) - 1u;
+  for (long tb = start; tb < hi; tb += (long)U * RP_BLOCK) {
+    unsigned long long kk[U];
+    unsigned bal[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const long e = tb + (long)u * RP_BLOCK + t;
+      kk[u] = e < hi ? mag_key(pos_adj(M[e], pos)) : 0ULL;
+      bal[u] = __ballot_sync(0xffffffffu, e < hi && kk[u] > bound);
+      if (lane == 0) s_cnt[u * NW + warp] = __popc(bal[u]);
+    }
+    __syncthreads();
+    if (warp == 0) {
+      // exclusive scan of the U * NW counts in (u, warp) order: lane owns 4
+      int v[4], sum = 0;
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        v[q] = s_cnt[lane * 4 + q];
+        sum += v[q];
+      }
+      int incl = sum;
+      for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += y;
+      }
+      int run = incl - sum;
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        s_cnt[lane * 4 + q] = run;
+        run += v[q];
+      }
+      if (lane == 31) s_total = incl;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      if ((bal[u] >> lane) & 1u) {
+        const long e = tb + (long)u * RP_BLOCK + t;
+        const int o = total + s_cnt[u * NW + warp] + __popc(bal[u] & lt);
+        cand[lo + o] = HNode{kk[u], e};
+      }
+    }
+    total += s_total;
+    __syncthreads();
+  }
+  if (t == 0) wcnt[blockIdx.x] = total;
+}
+
+// libstdc++ __adjust_heap(first, hole, len, first[hole]) + __push_heap with
+// comp(a, b) = a.key > b.key, one thread, on the split heap (node n at
+// storage n + 1).
+__device__ void rp_adjust(unsigned long long* hk, long long* hidx, long hole, long lim, long half) {
+  const unsigned long long vk = hk[hole + 1];
+  const long long vi = hidx[hole + 1];
+  const long top = hole;
+  long child = hole;
+  while (child < lim) {
+    child = 2 * (child + 1);
+    if (hk[child + 1] > hk[child]) child--;
+    hk[hole + 1] = hk[child + 1];
+    hidx[hole + 1] = hidx[child + 1];
+    hole = child;
+  }
+  if (child == half) {
+    child = 2 * (child + 1);
+    hk[hole + 1] = hk[child];
+    hidx[hole + 1] = hidx[child];
+    hole = child - 1;
+  }
+  long parent = (hole - 1) / 2;
+  while (hole > top && hk[parent + 1] > vk) {
+    hk[hole + 1] = hk[parent + 1];
+    hidx[hole + 1] = hidx[parent + 1];
+    hole = parent;
+    parent = (hole - 1) / 2;
+  }
+  hk[hole + 1] = vk;
+  hidx[hole + 1] = vi;
+}
+
+// __pop_heap's replacement of the top by (vk, vi), one thread.  libstdc++
+// moves the hole from the top to a leaf along the preferred children (the
+// left one only when its key is strictly smaller) and then sifts vk up; along
+// that path keys never decrease, so the net effect is: every path node whose
+// key is <= vk moves up one level and vk takes the place of the last one
+// moved.  The walk therefore stops at the first preferred child above vk.
+// Two levels per step: the children and the four grandchildren of the hole
+// are read together (the key array is padded to 2 * len + 8 entries so the
+// look-ahead reads stay inside it).  Returns the new top key.
+__device__ __forceinline__ unsigned long long rp_insert(unsigned long long* hk, long long* hidx, long lim, long half,
+                                                        unsigned long long vk, long long vi) {
+  long hole = 0;
+  unsigned long long top = vk;
+  bool stop = false;
+  while (hole < lim) {
+    const ulonglong2 c2 = *reinterpret_cast<const ulonglong2*>(hk + 2 * hole + 2);
+    const ulonglong2 gl = *reinterpret_cast<const ulonglong2*>(hk + 4 * hole + 4);
+    const ulonglong2 gr = *reinterpret_cast<const ulonglong2*>(hk + 4 * hole + 6);
+    const bool left = c2.y > c2.x;
+    const unsigned long long ck = left ? c2.x : c2.y;
+    const long c = 2 * hole + 2 - (left ? 1 : 0);
+    if (ck > vk) {
+      stop = true;
+      break;
+    }
+    if (hole == 0) top = ck;
+    hk[hole + 1] = ck;
+    hidx[hole + 1] = hidx[c + 1];
+    hole = c;
+    if (c >= lim) break;
+    const ulonglong2 g = left ? gl : gr;
+    const bool l2 = g.y > g.x;
+    const unsigned long long gk = l2 ? g.x : g.y;
+    const long gc = 2 * c + 2 - (l2 ? 1 : 0);
+    if (gk > vk) {
+      stop = true;
+      break;
+    }
+    hk[c + 1] = gk;
+    hidx[c + 1] = hidx[gc + 1];
+    hole = gc;
+  }
+  if (!stop && hole == half) {
+    const unsigned long long ck = hk[2 * hole + 2];
+    if (!(ck > vk)) {
+      if (hole == 0) top = ck;
+      hk[hole + 1] = ck;
+      hidx[hole + 1] = hidx[2 * hole + 2];
+      hole = 2 * hole + 1;
+    }
+  }
+  hk[hole + 1] = vk;
+  hidx[hole + 1] = vi;
+  return top;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(PX_THREADS)
+    k_rp_replay(const T* __restrict__ M, long N, int pos, long k, long wmax, int nwin, TopkState* st,
+                unsigned char* __restrict__ flags, const HNode* __restrict__ cand, const int* __restrict__ wcnt,
+                unsigned long long* gk, long long* gi, int heap_in_smem) {
+  if (st->sel_case != 2) return;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ long s_off[RP_MAXWIN + 1];
+  __shared__ long s_lo[RP_MAXWIN];
+  HNode* stage = reinterpret_cast<HNode*>(smem_raw);  // 2 x RP_STAGE
+  unsigned long long* hk = heap_in_smem ? reinterpret_cast<unsigned long long*>(stage + 2 * RP_STAGE) : gk;
+  long long* hidx = heap_in_smem ? reinterpret_cast<long long*>(hk + rp_key_len(k)) : gi;
+  const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+  const long lim = (k - 1) / 2;
+  const long half = (k & 1) == 0 ? (k - 2) / 2 : -1;
+  for (long i = t; i < k; i += blockDim.x) {
+    hk[i + 1] = mag_key(pos_adj(M[i], pos));
+    hidx[i + 1] = i;
+  }
+  if (t == 0) {
+    long acc = 0;
+    for (int w = 0; w < nwin; ++w) {
+      long lo, hi;
+      rp_window(w, N, k, wmax, &lo, &hi);
+      s_off[w] = acc;
+      s_lo[w] = lo;
+      acc += wcnt[w];
+    }
+    s_off[nwin] = acc;
+  }
+  __syncthreads();
+  // make_heap, deepest parents first, one level at a time
+  if (k >= 2) {
+    const long lastp = (k - 2) / 2;
+    for (int L = 63 - __clzll(lastp + 1); L >= 0; --L) {
+      const long a = (1L << L) - 1, b = min((2L << L) - 2, lastp);
+      for (long n = a + t; n <= b; n += blockDim.x) rp_adjust(hk, hidx, n, lim, half);
+      __syncthreads();
+    }
+  }
+  const long total = s_off[nwin];
+  const long nsteps = (total + RP_STAGE - 1) / RP_STAGE;
+  auto stage_chunk = [&](long c, HNode* dst, int t0, int nthr) {
+    const long q0 = c * RP_STAGE;
+    const int cnt = (int)min((long)RP_STAGE, total - q0);
+    for (int j = t0; j < cnt; j += nthr) {
+      const long q = q0 + j;
+      int a = 0, b = nwin - 1;
+      while (a < b) {
+        const int mid = (a + b + 1) >> 1;
+        if (s_off[mid] <= q) a = mid;
+        else b = mid - 1;
+      }
+      dst[j] = cand[s_lo[a] + (q - s_off[a])];
+    }
+  };
+  if (nsteps > 0) stage_chunk(0, stage, t, blockDim.x);
+  __syncthreads();
+  unsigned long long top = hk[1];
+  for (long c = 0; c < nsteps; ++c) {
+    if (warp != 0) {
+      if (c + 1 < nsteps) stage_chunk(c + 1, stage + ((c + 1) & 1) * RP_STAGE, t - 32, blockDim.x - 32);
+    } else if (lane == 0) {
+      const HNode* buf = stage + (c & 1) * RP_STAGE;
+      const int cnt = (int)min((long)RP_STAGE, total - c * RP_STAGE);
+      int q = 0;
+      for (; q + 4 <= cnt; q += 4) {
+        HNode cn[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) cn[u] = buf[q + u];
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+          if (cn[u].key > top) top = rp_insert(hk, hidx, lim, half, cn[u].key, cn[u].idx);
+      }
+      for (; q < cnt; ++q) {
+        const HNode cn = buf[q];
+        if (cn.key > top) top = rp_insert(hk, hidx, lim, half, cn.key, cn.idx);
+      }
+    }
+    __syncthreads();
+  }
+  const unsigned long long tt = st->t;
+  for (long i = t; i < k; i += blockDim.x)
+    if (hk[i + 1] == tt) flags[hidx[i + 1]] = 1;
+}
+
 // ------------------------------------------------------------------ sp apply
 template <typename T>
 __global__ void k_sp_apply(T* __restrict__ M, long N, int pos, const TopkState* st, unsigned char* __restrict__ flags) {
@@ -748,6 +1162,63 @@ static fgb_status queue_normalize(fgb_ctx* ctx, ProxWork& w, T* M, long N, int* 
   return FGB_OK;
 }
 
+// Pre-filtered tie replay (k_rp_bounds, k_rp_filter, k_rp_replay); every
+// kernel returns at once unless the selection needs the heap order.
+template <typename T>
+static fgb_status queue_tie_replay(fgb_ctx* ctx, ProxWork& w, const T* M, long N, long k, int pos) {
+  const long wmax = rp_wmax(N, k);
+  const int nwin = rp_window_count(N, k, wmax);
+  if (nwin > RP_MAXWIN) return fail(ctx, FGB_ERR_NOT_SUPPORTED, "tie replay: %d windows", nwin);
+  if (w.cand_cap < N) {
+    dfree(w.cand);
+    dfree(w.wbound);
+    dfree(w.wcount);
+    w.cand = nullptr;
+    w.wbound = nullptr;
+    w.wcount = nullptr;
+    w.cand_cap = 0;
+    FGB_TRY(dmalloc(ctx, &w.cand, sizeof(HNode) * (size_t)N));
+    FGB_TRY(dmalloc(ctx, (void**)&w.wbound, sizeof(unsigned long long) * RP_MAXWIN));
+    FGB_TRY(dmalloc(ctx, (void**)&w.wcount, sizeof(int) * RP_MAXWIN));
+    w.cand_cap = N;
+  }
+  const long hkn = rp_key_len(k);  // key array (padded), then k + 2 positions
+  const size_t stage_bytes = 2 * (size_t)RP_STAGE * sizeof(HNode);
+  const size_t heap_bytes = sizeof(unsigned long long) * (size_t)hkn + sizeof(long long) * (size_t)(k + 2);
+  const size_t cap = std::min<size_t>(ctx->smem_optin > 24 * 1024 ? ctx->smem_optin - 24 * 1024 : 0, 200 * 1024);
+  const bool in_smem = stage_bytes + heap_bytes <= cap;
+  const size_t smem = stage_bytes + (in_smem ? heap_bytes : 0);
+  unsigned long long* gk = nullptr;
+  long long* gi = nullptr;
+  if (!in_smem) {
+    if (w.heap2_cap < k) {
+      dfree(w.heap2);
+      w.heap2 = nullptr;
+      w.heap2_cap = 0;
+      FGB_TRY(dmalloc(ctx, &w.heap2, heap_bytes));
+      w.heap2_cap = k;
+    }
+    gk = reinterpret_cast<unsigned long long*>(w.heap2);
+    gi = reinterpret_cast<long long*>(gk + hkn);
+  }
+  k_rp_bounds<T><<<nwin, RP_BLOCK, 0, ctx->stream>>>(M, N, pos, k, wmax, w.state, w.wbound);
+  FGB_LAUNCHED(ctx);
+  k_rp_filter<T><<<nwin, RP_BLOCK, 0, ctx->stream>>>(M, N, pos, k, wmax, w.state, w.wbound,
+                                                     reinterpret_cast<HNode*>(w.cand), w.wcount);
+  FGB_LAUNCHED(ctx);
+  auto kern = k_rp_replay<T>;
+  static thread_local size_t attr_set = 0;
+  if (smem > attr_set) {
+    FGB_CUDA(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    attr_set = smem;
+  }
+  kern<<<1, PX_THREADS, smem, ctx->stream>>>(M, N, pos, k, wmax, nwin, w.state, w.flags,
+                                             reinterpret_cast<const HNode*>(w.cand), w.wcount, gk, gi,
+                                             in_smem ? 1 : 0);
+  FGB_LAUNCHED(ctx);
+  return FGB_OK;
+}
+
 template <typename T>
 static fgb_status queue_sp(fgb_ctx* ctx, ProxWork& w, T* M, long N, long k, int pos, int* d_status) {
   k_topk_init<<<1, 1, 0, ctx->stream>>>(w.state, k);
@@ -772,34 +1243,38 @@ static fgb_status queue_sp(fgb_ctx* ctx, ProxWork& w, T* M, long N, long k, int 
   const int nch = (int)((N + chunk - 1) / chunk);
   k_tie_case<T><<<nch, PX_THREADS, 0, ctx->stream>>>(M, N, pos, chunk, w.state, w.chunk_cnt);
   FGB_LAUNCHED(ctx);
-  // candidates of one chunk, then the heap itself when it fits on chip;
-  // larger heaps live in the workspace
-  const size_t cand_bytes = (size_t)HR_CHUNK * sizeof(HNode);
-  const size_t heap_bytes = (size_t)k * sizeof(HNode);
-  const size_t cap = std::min<size_t>(ctx->smem_optin > 8192 ? ctx->smem_optin - 8192 : 0, 200 * 1024);
-  const bool use_smem = cand_bytes + heap_bytes <= cap;
-  size_t smem = use_smem ? cand_bytes + heap_bytes : cand_bytes;
-  HNode* gheap = nullptr;
-  if (!use_smem) {
-    if (w.heap_cap < k) {
-      dfree(w.heap);
-      w.heap = nullptr;
-      w.heap_cap = 0;
-      FGB_TRY(dmalloc(ctx, &w.heap, heap_bytes));
-      w.heap_cap = k;
+  if (w.growable) {
+    FGB_TRY(queue_tie_replay<T>(ctx, w, M, N, k, pos));
+  } else {
+    // candidates of one chunk, then the heap itself when it fits on chip;
+    // larger heaps live in the workspace
+    const size_t cand_bytes = (size_t)HR_CHUNK * sizeof(HNode);
+    const size_t heap_bytes = (size_t)k * sizeof(HNode);
+    const size_t cap = std::min<size_t>(ctx->smem_optin > 8192 ? ctx->smem_optin - 8192 : 0, 200 * 1024);
+    const bool use_smem = cand_bytes + heap_bytes <= cap;
+    size_t smem = use_smem ? cand_bytes + heap_bytes : cand_bytes;
+    HNode* gheap = nullptr;
+    if (!use_smem) {
+      if (w.heap_cap < k) {
+        dfree(w.heap);
+        w.heap = nullptr;
+        w.heap_cap = 0;
+        FGB_TRY(dmalloc(ctx, &w.heap, heap_bytes));
+        w.heap_cap = k;
+      }
+      gheap = reinterpret_cast<HNode*>(w.heap);
     }
-    gheap = reinterpret_cast<HNode*>(w.heap);
+    auto kern = k_heap_replay<T>;
+    // the kernel also has static shared arrays: opt in whenever the dynamic
+    // part approaches the default 48 KB limit (once per size, outside captures)
+    static thread_local size_t attr_set = 0;
+    if (smem > 40 * 1024 && smem > attr_set) {
+      FGB_CUDA(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+      attr_set = smem;
+    }
+    kern<<<1, PX_THREADS, smem, ctx->stream>>>(M, N, pos, (int)k, w.state, w.flags, gheap, use_smem ? 1 : 0);
+    FGB_LAUNCHED(ctx);
   }
-  auto kern = k_heap_replay<T>;
-  // the kernel also has static shared arrays: opt in whenever the dynamic
-  // part approaches the default 48 KB limit (once per size, outside captures)
-  static thread_local size_t attr_set = 0;
-  if (smem > 40 * 1024 && smem > attr_set) {
-    FGB_CUDA(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    attr_set = smem;
-  }
-  kern<<<1, PX_THREADS, smem, ctx->stream>>>(M, N, pos, (int)k, w.state, w.flags, gheap, use_smem ? 1 : 0);
-  FGB_LAUNCHED(ctx);
   k_sp_apply<T><<<g, PX_THREADS, 0, ctx->stream>>>(M, N, pos, w.state, w.flags);
   FGB_LAUNCHED(ctx);
   if (d_status) {

@@ -36,6 +36,15 @@ struct ProxWork {
   size_t supp_bytes = 0;
   void* heap = nullptr;              // heap of the tie replay when it does not fit on chip
   long heap_cap = 0;
+  // pre-filtered tie replay (allocated on first use, only in workspaces made
+  // by prox_work_reserve; a workspace built by hand keeps the one-block replay)
+  int growable = 0;
+  void* cand = nullptr;              // candidate (key, position) slots, one per entry
+  long cand_cap = 0;
+  unsigned long long* wbound = nullptr;  // per-window lower bounds of the k-th largest key
+  int* wcount = nullptr;             // per-window candidate counts
+  void* heap2 = nullptr;             // split heap (keys, positions) when it does not fit on chip
+  long heap2_cap = 0;
 };
 
 fgb_status prox_work_reserve(fgb_ctx* ctx, ProxWork& w, long elems, int rows);

@@ -62,6 +62,24 @@ def test_prox_sp_heap_order_case(oracle):
     assert found == 40
 
 
+@pytest.mark.parametrize("rows,cols,k,levels", [(1024, 1024, 2048, 6), (1024, 1024, 2048, 400),
+                                                 (512, 384, 30000, 50), (777, 301, 9000, 3)])
+def test_prox_sp_heap_order_large(oracle, rows, cols, k, levels):
+    """Large selections through the pre-filtered replay: 1M entries with
+    k = 2048 (heap on chip) and k = 30000 (heap in device memory), few or
+    many distinct magnitudes; bit-exact against std::partial_sort."""
+    rng = np.random.default_rng(rows + k + levels)
+    M = _tie_matrix(rng, rows, cols, levels)
+    # a few large entries late in the order force heap evictions of ties
+    tail = rng.integers(rows * cols // 2, rows * cols, size=64)
+    M.reshape(-1, order="F")[tail] = (levels + 1) / 8.0
+    for pos in (False, True):
+        c = fact.ConstraintInt("sp", rows, cols, k, normalized=False, pos=pos)
+        got = _gpu_prox(M, c)
+        ref = oracle.prox(oracle.SP, M, k=k, normalized=False, pos=pos)
+        assert np.array_equal(got, ref), pos
+
+
 @pytest.mark.parametrize("name,kind", [("spcol", 1), ("splin", 2), ("splincol", 3)])
 @pytest.mark.parametrize("seed", range(4))
 def test_prox_lines_bitexact(oracle, name, kind, seed):
