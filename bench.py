@@ -357,19 +357,23 @@ def palm_roofline(ctx, hbm, peak_kind):
     import scipy.sparse as sp
     S = sp.random(PALM_N, PALM_N, density=PALM_K / PALM_N ** 2, random_state=3, format="csr")
     S.sort_indices()
-    F = fg.Faust([S], ctx=ctx)
+    # one call = 40 back-to-back launches (one per factor), so host overhead
+    # between launches does not enter the per-launch time
+    nf = 40
+    F = fg.Faust([S] * nf, ctx=ctx)
     X = torch.randn((PALM_N, PALM_N), device="cuda", dtype=torch.float64).t()
     Y = torch.empty((PALM_N, PALM_N), device="cuda", dtype=torch.float64).t()
-    for _ in range(5):
+    for _ in range(3):
         F.matmul_device(X, Y, mode=1)
+    stream = torch.cuda.current_stream()
     s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    reps = 200
-    s.record()
-    for _ in range(reps):
+    calls = 10
+    s.record(stream)
+    for _ in range(calls):
         F.matmul_device(X, Y, mode=1)
-    e.record()
+    e.record(stream)
     torch.cuda.synchronize()
-    us = s.elapsed_time(e) * 1e3 / reps
+    us = s.elapsed_time(e) * 1e3 / (calls * nf)
     nbytes = 2 * PALM_N * PALM_N * 8 + S.nnz * 12 + (PALM_N + 1) * 4
     achieved = nbytes / (us * 1e-6) / 1e9
     F.close()

@@ -74,6 +74,7 @@ _SIGS = {
     "fgb_faust_destroy": (_I, [_P]),
     "fgb_faust_shape": (_I, [_P, ctypes.POINTER(_I), ctypes.POINTER(_I), ctypes.POINTER(_I)]),
     "fgb_faust_mul": (_I, [_P, _P, _I, _I, _P, _I, _I]),
+    "fgb_faust_mul_op": (_I, [_P, ctypes.c_char, _P, _I, _I, _P, _I, _I]),
     "fgb_faust_mul_host": (_I, [_P, _P, _I, _P]),
     "fgb_faust_spectral_norm": (_I, [_P, _I, _D, ctypes.POINTER(_D), ctypes.POINTER(_I)]),
     "fgb_faust_factor_info": (_I, [_P, _I, ctypes.POINTER(_I), ctypes.POINTER(_I), ctypes.POINTER(_I),
@@ -89,6 +90,9 @@ _SIGS = {
                                   ctypes.POINTER(PalmParams), ctypes.POINTER(_P), ctypes.POINTER(_D),
                                   ctypes.POINTER(_P)]),
     "fgb_rel_err": (_I, [_P, _P, _D, ctypes.POINTER(_D)]),
+    "fgb_hierarchical": (_I, [_P, _I, _P, _I, _I, _I, ctypes.POINTER(Constraint), ctypes.POINTER(Constraint),
+                              ctypes.POINTER(PalmParams), ctypes.POINTER(PalmParams), _I, ctypes.POINTER(_D),
+                              ctypes.POINTER(_P)]),
     "fgb_palm4msa2_batched": (_I, [_P, _I, _I, ctypes.POINTER(PalmProblem), ctypes.POINTER(PalmParams),
                                    ctypes.POINTER(BatchOpts), ctypes.POINTER(PalmResultC)]),
     # include/fgb_mlp.h

@@ -151,6 +151,58 @@ static fgb_status fused_desc(fgb_faust* F) {
   return FGB_OK;
 }
 
+// F^T X = S_J^T (... (S_1^T X)): the transposed factors applied first to last.
+static fgb_status mul_per_factor_t(fgb_faust* F, const void* X, int ldx, int ncols, void* Y, int ldy) {
+  fgb_ctx* ctx = F->ctx;
+  const int J = (int)F->f.size();
+  const size_t es = dtype_size(F->dtype);
+  int maxcols = 0;
+  for (auto& f : F->f) maxcols = std::max(maxcols, f.cols);
+  if (J > 1) {
+    size_t need = (size_t)maxcols * ncols * es;
+    if (F->buf_bytes < need) {
+      dfree(F->buf[0]);
+      dfree(F->buf[1]);
+      F->buf[0] = F->buf[1] = nullptr;
+      F->buf_bytes = 0;
+      FGB_TRY(dmalloc(ctx, &F->buf[0], need));
+      FGB_TRY(dmalloc(ctx, &F->buf[1], need));
+      F->buf_bytes = need;
+    }
+  }
+  const void* in = X;
+  int ldin = ldx;
+  for (int k = 0; k < J; ++k) {
+    const DevFactor& f = F->f[k];
+    void* out = (k == J - 1) ? Y : F->buf[k & 1];
+    int ldout = (k == J - 1) ? ldy : f.cols;
+    if (F->dtype == FGB_F64) {
+      FGB_TRY(launch_csr_spmm<double>(ctx, f.t_rowptr, f.t_colind, (const double*)f.t_val, f.cols, f.rows,
+                                      (const double*)in, ldin, ncols, (double*)out, ldout, Epi<double>()));
+    } else {
+      FGB_TRY(launch_csr_spmm<float>(ctx, f.t_rowptr, f.t_colind, (const float*)f.t_val, f.cols, f.rows,
+                                     (const float*)in, ldin, ncols, (float*)out, ldout, Epi<float>()));
+    }
+    in = out;
+    ldin = ldout;
+  }
+  return FGB_OK;
+}
+
+static fgb_status fused_desc_t(fgb_faust* F) {
+  if (F->chain_desc_t) return FGB_OK;
+  const size_t J = F->f.size();
+  std::vector<ChainDesc> h(J);
+  for (size_t i = 0; i < J; ++i) {
+    const DevFactor& f = F->f[J - 1 - i];
+    h[i] = ChainDesc{f.t_rowptr, f.t_colind, f.t_val, f.cols, f.rows};
+  }
+  FGB_TRY(dmalloc(F->ctx, &F->chain_desc_t, sizeof(ChainDesc) * J));
+  FGB_CUDA(F->ctx, cudaMemcpyAsync(F->chain_desc_t, h.data(), sizeof(ChainDesc) * J, cudaMemcpyHostToDevice,
+                                   F->ctx->stream));
+  return FGB_OK;
+}
+
 static bool all_csr(const fgb_faust* F) {
   for (auto& f : F->f)
     if (f.format != FGB_CSR) return false;
@@ -178,6 +230,7 @@ fgb_faust::~fgb_faust() {
   fgb::dfree(dx);
   fgb::dfree(dy);
   fgb::dfree(chain_desc);
+  fgb::dfree(chain_desc_t);
   if (hx) cudaFreeHost(hx);
   if (hy) cudaFreeHost(hy);
 }
@@ -256,6 +309,35 @@ fgb_status fgb_faust_mul(fgb_faust* F, const void* X, int ldx, int ncols, void* 
     return chain_fused(ctx, F->dtype, (const ChainDesc*)F->chain_desc, (int)F->f.size(), X, ldx, ncols, Y, ldy,
                        max_dim(F), false, nullptr);
   return mul_per_factor(F, X, ldx, ncols, Y, ldy);
+}
+
+fgb_status fgb_faust_mul_op(fgb_faust* F, char op, const void* X, int ldx, int ncols, void* Y, int ldy, int mode) {
+  if (!F) return FGB_ERR_INVALID_ARG;
+  if (op == 'N' || op == 'n') return fgb_faust_mul(F, X, ldx, ncols, Y, ldy, mode);
+  fgb_ctx* ctx = F->ctx;
+  if (op != 'T' && op != 't' && op != 'H' && op != 'h')
+    return fail(ctx, FGB_ERR_INVALID_ARG, "fgb_faust_mul_op: op must be N, T or H");
+  if (!X || !Y || ncols < 0) return fail(ctx, FGB_ERR_INVALID_ARG, "fgb_faust_mul_op: null operand");
+  if (ldx < F->f.front().rows || ldy < F->f.back().cols)
+    return fail(ctx, FGB_ERR_INVALID_ARG, "fgb_faust_mul_op: leading dimension smaller than the row count");
+  if (!all_csr(F)) return fail(ctx, FGB_ERR_NOT_SUPPORTED, "fgb_faust_mul_op: transposed products of CSR Fausts only");
+  if (ncols == 0) return FGB_OK;
+  FGB_CUDA(ctx, cudaSetDevice(ctx->device));
+  // real scalars: the adjoint is the transpose
+  for (auto& f : F->f)
+    if (!f.has_t) FGB_TRY(csr_build_transpose(ctx, F->dtype, f));
+  bool fits = false;
+  int maxd = max_dim(F);
+  if (mode != 1) {
+    FGB_TRY(fused_desc_t(F));
+    chain_fused(ctx, F->dtype, (const ChainDesc*)F->chain_desc_t, (int)F->f.size(), X, ldx, ncols, Y, ldy, maxd, true,
+                &fits);
+  }
+  if (mode == 2 && !fits) return fail(ctx, FGB_ERR_NOT_SUPPORTED, "fused chain: factors do not fit on chip");
+  if (fits && (mode == 2 || (mode == 0 && F->f.size() > 1)))
+    return chain_fused(ctx, F->dtype, (const ChainDesc*)F->chain_desc_t, (int)F->f.size(), X, ldx, ncols, Y, ldy,
+                       maxd, false, nullptr);
+  return mul_per_factor_t(F, X, ldx, ncols, Y, ldy);
 }
 
 fgb_status fgb_faust_mul_host(fgb_faust* F, const void* X, int ncols, void* Y) {

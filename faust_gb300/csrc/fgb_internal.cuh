@@ -111,8 +111,10 @@ struct fgb_faust {
   void* dx = nullptr;
   void* dy = nullptr;
   size_t dxy_bytes = 0;
-  // Device descriptor array for the fused chain kernel.
+  // Device descriptor arrays for the fused chain kernel (F, and F^T as the
+  // chain of transposed factors in reverse order).
   void* chain_desc = nullptr;
+  void* chain_desc_t = nullptr;
   // When set, the factor arrays are views into this shared device block
   // (results of one batched call) and are released with its last owner.
   std::shared_ptr<void> pool;

@@ -210,7 +210,7 @@ struct Palm {
 
   // ---------------------------------------------------------------- setup
   fgb_status setup(const T* A_dev, int rows, int cols, const fgb_constraint* cs, int nf, const fgb_palm_params& pp,
-                   const void* const* init_facts, double init_lambda) {
+                   const void* const* init_facts, double init_lambda, const DevFactor* init_dev = nullptr) {
     J = nf;
     p = pp;
     r2l = p.is_update_way_R2L != 0;
@@ -263,6 +263,32 @@ struct Palm {
     // Initial factors (faust_palm4msa2020.hpp:115-149): the first factor to
     // update is zero, the others identity; or the caller's init_facts.
     std::vector<T> h;
+    for (int i = 0; i < J && init_dev; ++i) {
+      // device-resident initial factors (CSR): densified, then the usual
+      // dense -> CSR of the factor (its transpose included)
+      DevFactor& f = S[i];
+      const DevFactor& g = init_dev[i];
+      if (g.rows != f.rows || g.cols != f.cols)
+        return fail(ctx, FGB_ERR_INVALID_ARG, "initial factor %d is %d x %d, the constraint %d x %d", i, g.rows, g.cols,
+                    f.rows, f.cols);
+      if (g.nnz > f.cap) {
+        dfree(f.colind);
+        dfree(f.val);
+        dfree(f.t_colind);
+        dfree(f.t_val);
+        f.cap = g.nnz;
+        FGB_TRY(dmalloc(ctx, (void**)&f.colind, sizeof(int) * f.cap));
+        FGB_TRY(dmalloc(ctx, &f.val, es * f.cap));
+        FGB_TRY(dmalloc(ctx, (void**)&f.t_colind, sizeof(int) * f.cap));
+        FGB_TRY(dmalloc(ctx, &f.t_val, es * f.cap));
+      }
+      FGB_TRY(launch_csr_to_dense<T>(ctx, g, D));
+      FGB_TRY(launch_dense_to_csr<T>(ctx, pw, D, f, status));
+    }
+    if (init_dev) {
+      FGB_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+      return FGB_OK;
+    }
     for (int i = 0; i < J; ++i) {
       DevFactor& f = S[i];
       h.assign((size_t)f.rows * f.cols, T(0));
@@ -627,6 +653,141 @@ static fgb_status palm_entry(fgb_ctx* ctx, fgb_dtype dt, const void* A_dev, int 
   return s;
 }
 
+// Reads the entry counts of factors left on the device by a finished run.
+static fgb_status read_nnz(fgb_ctx* ctx, std::vector<DevFactor>& S) {
+  for (auto& f : S) {
+    int nnz = 0;
+    FGB_CUDA(ctx, cudaMemcpy(&nnz, f.rowptr + f.rows, sizeof(int), cudaMemcpyDeviceToHost));
+    f.nnz = nnz;
+    f.has_t = true;
+  }
+  return FGB_OK;
+}
+
+// Faust::hierarchical (src/algorithm/factorization/faust_hierarchical.hpp:1-121),
+// 2020 version: step i splits the current residual (the last factor, or the
+// first when is_fact_side_left) in two by palm4msa2 with the constraints
+// (fac_i, res_i) from the default zero / identity start and lambda 1, the
+// global lambda is multiplied by that run's lambda, the two factors replace
+// the residual, and palm4msa2 then refines every factor against A starting
+// from them and from the global lambda.
+template <typename T>
+static fgb_status hier_impl(fgb_ctx* ctx, fgb_dtype dt, const void* A_host, int rows, int cols, int nsteps,
+                            const fgb_constraint* fac, const fgb_constraint* res, const fgb_palm_params* p2,
+                            const fgb_palm_params* pg, int left, double* lambda, fgb_faust** out) {
+  if (nsteps <= 0 || !fac || !res) return fail(ctx, FGB_ERR_INVALID_ARG, "hierarchical: no constraint");
+  const size_t es = sizeof(T);
+  T* A = nullptr;
+  T* dense = nullptr;
+  FGB_TRY(dmalloc(ctx, (void**)&A, es * (size_t)rows * cols));
+  fgb_status s = cuda_check(ctx, cudaMemcpy(A, A_host, es * (size_t)rows * cols, cudaMemcpyHostToDevice), "copy A");
+  cudaStream_t user = ctx->stream, ps = nullptr;
+  if (s == FGB_OK) s = cuda_check(ctx, cudaStreamCreateWithFlags(&ps, cudaStreamNonBlocking), "stream");
+  if (s == FGB_OK) ctx->stream = ps;
+  std::vector<DevFactor> S;
+  double glo_lambda = 1.0;
+  for (int i = 0; i < nsteps && s == FGB_OK; ++i) {
+    // the matrix split at this step
+    const T* Si = A;
+    int sr = rows, sc = cols;
+    if (i > 0) {
+      const DevFactor& r = left ? S.front() : S.back();
+      sr = r.rows;
+      sc = r.cols;
+      dfree(dense);
+      dense = nullptr;
+      s = dmalloc(ctx, (void**)&dense, es * (size_t)sr * sc);
+      if (s == FGB_OK) s = launch_csr_to_dense<T>(ctx, r, dense);
+      Si = dense;
+    }
+    if (s != FGB_OK) break;
+    const fgb_constraint lc[2] = {left ? res[i] : fac[i], left ? fac[i] : res[i]};
+    if (lc[0].rows != sr || lc[1].cols != sc || lc[0].cols != lc[1].rows) {
+      s = fail(ctx, FGB_ERR_INVALID_ARG, "hierarchical step %d: constraints %dx%d, %dx%d do not split %d x %d", i,
+               lc[0].rows, lc[0].cols, lc[1].rows, lc[1].cols, sr, sc);
+      break;
+    }
+    std::vector<DevFactor> two;
+    double lam_local = 1.0;
+    {
+      Palm<T> L;
+      L.ctx = ctx;
+      s = L.setup(Si, sr, sc, lc, 2, *p2, nullptr, 1.0);
+      if (s == FGB_OK) s = L.run();
+      T lt = T(1);
+      if (s == FGB_OK) s = cuda_check(ctx, cudaMemcpy(&lt, L.lam, sizeof(T), cudaMemcpyDeviceToHost), "lambda");
+      lam_local = (double)lt;
+      if (s == FGB_OK) {
+        two = L.S;
+        L.S.clear();
+        s = read_nnz(ctx, two);
+      }
+    }
+    if (s != FGB_OK) {
+      for (auto& f : two) free_factor(f);
+      break;
+    }
+    glo_lambda *= lam_local;
+    if (i > 0) {
+      if (left) {
+        free_factor(S.front());
+        S.erase(S.begin());
+      } else {
+        free_factor(S.back());
+        S.pop_back();
+      }
+    }
+    if (left)
+      S.insert(S.begin(), two.begin(), two.end());
+    else
+      S.insert(S.end(), two.begin(), two.end());
+    // constraints of the global run, in the order of the factors
+    std::vector<fgb_constraint> gc;
+    if (left) {
+      gc.push_back(res[i]);
+      for (int j = i; j >= 0; --j) gc.push_back(fac[j]);
+    } else {
+      for (int j = 0; j <= i; ++j) gc.push_back(fac[j]);
+      gc.push_back(res[i]);
+    }
+    {
+      Palm<T> G;
+      G.ctx = ctx;
+      s = G.setup(A, rows, cols, gc.data(), (int)gc.size(), *pg, nullptr, glo_lambda, S.data());
+      if (s == FGB_OK) s = G.run();
+      T lt = T(1);
+      if (s == FGB_OK) s = cuda_check(ctx, cudaMemcpy(&lt, G.lam, sizeof(T), cudaMemcpyDeviceToHost), "lambda");
+      if (s == FGB_OK) {
+        glo_lambda = (double)lt;
+        for (auto& f : S) free_factor(f);
+        S = G.S;
+        G.S.clear();
+        s = read_nnz(ctx, S);
+      }
+    }
+  }
+  if (ps) cudaStreamSynchronize(ps);
+  ctx->stream = user;
+  if (ps) cudaStreamDestroy(ps);
+  dfree(dense);
+  dfree(A);
+  if (s != FGB_OK) {
+    for (auto& f : S) free_factor(f);
+    return s;
+  }
+  if (lambda) *lambda = glo_lambda;
+  if (out) {
+    fgb_faust* F = new fgb_faust();
+    F->ctx = ctx;
+    F->dtype = dt;
+    F->f = S;
+    *out = F;
+  } else {
+    for (auto& f : S) free_factor(f);
+  }
+  return FGB_OK;
+}
+
 }  // namespace fgb
 
 using namespace fgb;
@@ -784,3 +945,18 @@ fgb_status fgb_rel_err(fgb_faust* F, const void* A_dev, double lambda, double* o
 }
 
 }  // extern "C"
+
+extern "C" fgb_status fgb_hierarchical(fgb_ctx* ctx, fgb_dtype dtype, const void* A, int rows, int cols, int nsteps,
+                                       const fgb_constraint* fac_cons, const fgb_constraint* res_cons,
+                                       const fgb_palm_params* params_2facts, const fgb_palm_params* params_global,
+                                       int is_fact_side_left, double* lambda, fgb_faust** out) {
+  if (!ctx || !A || !params_2facts || !params_global) return FGB_ERR_INVALID_ARG;
+  if (cudaSetDevice(ctx->device) != cudaSuccess) return fail(ctx, FGB_ERR_CUDA, "cudaSetDevice");
+  if (dtype == FGB_F64)
+    return hier_impl<double>(ctx, dtype, A, rows, cols, nsteps, fac_cons, res_cons, params_2facts, params_global,
+                             is_fact_side_left, lambda, out);
+  if (dtype == FGB_F32)
+    return hier_impl<float>(ctx, dtype, A, rows, cols, nsteps, fac_cons, res_cons, params_2facts, params_global,
+                            is_fact_side_left, lambda, out);
+  return fail(ctx, FGB_ERR_NOT_SUPPORTED, "hierarchical: F32 or F64");
+}

@@ -105,62 +105,233 @@ struct Stage {
   int elems;
 };
 
-// Y = S X   (S: rows x inner CSR, X: inner x ncols, Y: rows x ncols; lds = rows).
-// Blocks of X's columns are staged in shared memory, so the gathers of one
-// output column read on-chip; each entry is still the sequential fma over the
-// row's stored entries.
+
+// dst[r + c * ldd] = src[r + c * lds] for r < rows, c < cols (thread t takes
+// the entries t, t + BT, ... of the column-major order; four loads issued
+// before their stores).
 template <typename T>
-__device__ void b_spmm(const int* rp, const int* ci, const T* v, int rows, int inner, const T* X, int ldx, int ncols,
-                       T* Y, int mode, const T* aux, T s, Stage<T> sg) {
-  const int cb = max(1, min(ncols, sg.elems / max(1, inner)));
+__device__ __forceinline__ void b_copy(T* dst, int ldd, const T* src, long lds, int rows, int cols) {
+  const int dr = BT % rows, dc = BT / rows;
+  int r = (int)threadIdx.x % rows, c = (int)threadIdx.x / rows;
+  while (c < cols) {
+    int r1 = r + dr, c1 = c + dc;
+    if (r1 >= rows) {
+      r1 -= rows;
+      ++c1;
+    }
+    const T v0 = src[r + (long)c * lds];
+    const bool has1 = c1 < cols;
+    const T v1 = has1 ? src[r1 + (long)c1 * lds] : T(0);
+    dst[r + c * ldd] = v0;
+    if (has1) dst[r1 + c1 * ldd] = v1;
+    r = r1 + dr;
+    c = c1 + dc;
+    if (r >= rows) {
+      r -= rows;
+      ++c;
+    }
+  }
+}
+
+// A CSR matrix as seen by a block op: in global memory, or copied into the
+// staging area.
+template <typename T>
+struct Csr {
+  const int* rp;
+  const int* ci;
+  const T* v;
+};
+
+// Copies the CSR of a factor (nrows rows) to the front of the staging area
+// when it takes at most half of it, and shrinks sg to the rest.  The caller
+// synchronizes before the copy is read.
+template <typename T>
+__device__ Csr<T> b_stage_csr(const int* rp, const int* ci, const T* v, int nrows, Stage<T>& sg) {
+  const int nnz = rp[nrows];
+  const size_t vb = ((size_t)nnz * sizeof(T) + 15) & ~(size_t)15;
+  const size_t ib = ((size_t)(nrows + 1 + nnz) * sizeof(int) + 15) & ~(size_t)15;
+  if (vb + ib > (size_t)sg.elems * sizeof(T) / 2) return Csr<T>{rp, ci, v};
+  T* sv = sg.p;
+  int* srp = reinterpret_cast<int*>(reinterpret_cast<char*>(sg.p) + vb);
+  int* sci = srp + nrows + 1;
+  for (int i = threadIdx.x; i <= nrows; i += BT) srp[i] = rp[i];
+  for (int i = threadIdx.x; i < nnz; i += BT) {
+    sci[i] = ci[i];
+    sv[i] = v[i];
+  }
+  sg.p = reinterpret_cast<T*>(reinterpret_cast<char*>(sg.p) + vb + ib);
+  sg.elems -= (int)((vb + ib) / sizeof(T));
+  return Csr<T>{srp, sci, sv};
+}
+
+// sum over the stored entries p of row r of v[p] * x[ci[p] * stride], in order
+template <typename TA, typename TV, typename TX>
+__device__ __forceinline__ TA b_row_dot(const int* __restrict__ rp, const int* __restrict__ ci,
+                                        const TV* __restrict__ v, int r, const TX* __restrict__ x, int stride) {
+  TA acc = TA(0);
+  const int p1 = rp[r + 1];
+#pragma unroll 8
+  for (int p = rp[r]; p < p1; ++p) acc = fmad((TA)v[p], (TA)x[ci[p] * stride], acc);
+  return acc;
+}
+
+// 16 bytes of T from shared memory (G = 16 / sizeof(T) values).
+template <typename T>
+struct Vec16;
+template <>
+struct Vec16<float> {
+  static constexpr int G = 4;
+  __device__ static void load(const float* p, float* o) {
+    const float4 v = *reinterpret_cast<const float4*>(p);
+    o[0] = v.x;
+    o[1] = v.y;
+    o[2] = v.z;
+    o[3] = v.w;
+  }
+};
+template <>
+struct Vec16<double> {
+  static constexpr int G = 2;
+  __device__ static void load(const double* p, double* o) {
+    const double2 v = *reinterpret_cast<const double2*>(p);
+    o[0] = v.x;
+    o[1] = v.y;
+  }
+};
+
+// Y = S X   (S: rows x inner CSR, X: inner x ncols, Y: rows x ncols; lds = rows).
+// S and a block of X's columns are staged in shared memory, the block stored
+// row by row (stride sx) so that the G columns a thread owns are one 16-byte
+// read per stored entry; each output entry is the sequential fma over its
+// row's entries, G of them in flight per thread.
+template <typename T>
+__device__ __noinline__ void b_spmm(const int* rp, const int* ci, const T* v, int rows, int inner, const T* X, int ldx,
+                                   int ncols, T* Y, int mode, const T* aux, T s, Stage<T> sg) {
+  constexpr int G = Vec16<T>::G;
+  const Csr<T> S = b_stage_csr<T>(rp, ci, v, rows, sg);
+  // block width: a multiple of G, row stride padded off multiples of 32 words
+  int cb = sg.elems / max(1, inner) - G;
+  cb = max(G, min(cb, (ncols + G - 1) / G * G) / G * G);
   for (int j0 = 0; j0 < ncols; j0 += cb) {
     const int nc = min(cb, ncols - j0);
-    const long ne = (long)inner * nc;
-    for (long e = threadIdx.x; e < ne; e += BT) {
-      const int r = (int)(e % inner);
-      const int c = (int)(e / inner);
-      sg.p[e] = X[r + (long)(j0 + c) * ldx];
+    const int ncp = (nc + G - 1) / G * G;
+    const int sx = ncp + (((ncp * (int)sizeof(T)) % 128 == 0) ? G : 0);
+    // stage: st[k * sx + c] = X[k, j0 + c] (zero beyond ncols)
+    {
+      // eight loads in flight per thread before their stores
+      const int dk = BT % inner, dcol = BT / inner;
+      int k = (int)threadIdx.x % inner, c = (int)threadIdx.x / inner;
+      while (c < ncp) {
+        T vv[8];
+        int kk[8], cc[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+          kk[u] = k;
+          cc[u] = c;
+          vv[u] = c < nc ? X[k + (long)(j0 + c) * ldx] : T(0);
+          k += dk;
+          c += dcol;
+          if (k >= inner) {
+            k -= inner;
+            ++c;
+          }
+        }
+#pragma unroll
+        for (int u = 0; u < 8; ++u)
+          if (cc[u] < ncp) sg.p[kk[u] * sx + cc[u]] = vv[u];
+      }
     }
     __syncthreads();
-    const long no = (long)rows * nc;
-    for (long e = threadIdx.x; e < no; e += BT) {
-      const int i = (int)(e % rows);
-      const int c = (int)(e / rows);
-      const T* xs = sg.p + (long)c * inner;
-      T acc = T(0);
-      const int p1 = rp[i + 1];
-      for (int p = rp[i]; p < p1; ++p) acc = fmad(v[p], xs[ci[p]], acc);
-      const long idx = i + (long)(j0 + c) * rows;
-      Y[idx] = b_epi(mode, acc, aux, idx, s);
+    const int ng = ncp / G;
+    const int di = BT % rows, dg = BT / rows;
+    int i = (int)threadIdx.x % rows, g = (int)threadIdx.x / rows;
+    for (; g < ng; i += di, g += dg, (i >= rows ? (i -= rows, ++g) : 0)) {
+      T acc[G];
+#pragma unroll
+      for (int u = 0; u < G; ++u) acc[u] = T(0);
+      const int p1 = S.rp[i + 1];
+      for (int p = S.rp[i]; p < p1; ++p) {
+        const T val = S.v[p];
+        T xv[G];
+        Vec16<T>::load(sg.p + S.ci[p] * sx + g * G, xv);
+#pragma unroll
+        for (int u = 0; u < G; ++u) acc[u] = fmad(val, xv[u], acc[u]);
+      }
+#pragma unroll
+      for (int u = 0; u < G; ++u) {
+        const int c = g * G + u;
+        if (c < nc) {
+          const long idx = i + (long)(j0 + c) * rows;
+          Y[idx] = b_epi(mode, acc[u], aux, idx, s);
+        }
+      }
     }
     __syncthreads();
   }
 }
 
 // Y = X S^T given the CSR of S (srows rows): y[r, c] = sum over row c of S.
-// Blocks of X's rows (all xcols columns) are staged in shared memory.
+// S and a block of X's rows (all xcols columns, column-major with a row
+// stride padded to G) are staged in shared memory; a thread owns G
+// consecutive rows of one output column.
 template <typename T>
-__device__ void b_dense_csrT(const T* X, int xrows, int xcols, const int* rp, const int* ci, const T* v, int srows,
-                             T* Y, int mode, const T* aux, T s, Stage<T> sg) {
-  const int rb = max(1, min(xrows, sg.elems / max(1, xcols)));
+__device__ __noinline__ void b_dense_csrT(const T* X, int xrows, int xcols, const int* rp, const int* ci, const T* v,
+                                         int srows, T* Y, int mode, const T* aux, T s, Stage<T> sg) {
+  constexpr int G = Vec16<T>::G;
+  const Csr<T> S = b_stage_csr<T>(rp, ci, v, srows, sg);
+  int rb = sg.elems / max(1, xcols) - G;
+  rb = max(G, min(rb, (xrows + G - 1) / G * G) / G * G);
   for (int r0 = 0; r0 < xrows; r0 += rb) {
     const int nr = min(rb, xrows - r0);
-    const long ne = (long)nr * xcols;
-    for (long e = threadIdx.x; e < ne; e += BT) {
-      const int rl = (int)(e % nr);
-      const int col = (int)(e / nr);
-      sg.p[e] = X[r0 + rl + (long)col * xrows];
+    const int nrp = (nr + G - 1) / G * G;
+    {
+      // eight loads in flight per thread before their stores
+      const int dr = BT % nrp, dcol = BT / nrp;
+      int rl = (int)threadIdx.x % nrp, col = (int)threadIdx.x / nrp;
+      while (col < xcols) {
+        T vv[8];
+        int rr[8], cc[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+          rr[u] = rl;
+          cc[u] = col;
+          vv[u] = (col < xcols && rl < nr) ? X[r0 + rl + (long)col * xrows] : T(0);
+          rl += dr;
+          col += dcol;
+          if (rl >= nrp) {
+            rl -= nrp;
+            ++col;
+          }
+        }
+#pragma unroll
+        for (int u = 0; u < 8; ++u)
+          if (cc[u] < xcols) sg.p[rr[u] + cc[u] * nrp] = vv[u];
+      }
     }
     __syncthreads();
-    const long no = (long)nr * srows;
-    for (long e = threadIdx.x; e < no; e += BT) {
-      const int rl = (int)(e % nr);
-      const int c = (int)(e / nr);
-      T acc = T(0);
-      const int p1 = rp[c + 1];
-      for (int p = rp[c]; p < p1; ++p) acc = fmad(v[p], sg.p[rl + (long)ci[p] * nr], acc);
-      const long idx = r0 + rl + (long)c * xrows;
-      Y[idx] = b_epi(mode, acc, aux, idx, s);
+    const int ng = nrp / G;
+    const int dg = BT % ng, dc = BT / ng;
+    int g = (int)threadIdx.x % ng, c = (int)threadIdx.x / ng;
+    for (; c < srows; g += dg, c += dc, (g >= ng ? (g -= ng, ++c) : 0)) {
+      T acc[G];
+#pragma unroll
+      for (int u = 0; u < G; ++u) acc[u] = T(0);
+      const int p1 = S.rp[c + 1];
+      for (int p = S.rp[c]; p < p1; ++p) {
+        const T val = S.v[p];
+        T xv[G];
+        Vec16<T>::load(sg.p + S.ci[p] * nrp + g * G, xv);
+#pragma unroll
+        for (int u = 0; u < G; ++u) acc[u] = fmad(val, xv[u], acc[u]);
+      }
+#pragma unroll
+      for (int u = 0; u < G; ++u) {
+        const int rl = g * G + u;
+        if (rl < nr) {
+          const long idx = r0 + rl + (long)c * xrows;
+          Y[idx] = b_epi(mode, acc[u], aux, idx, s);
+        }
+      }
     }
     __syncthreads();
   }
@@ -205,7 +376,7 @@ __device__ __forceinline__ void pi_op(const Fac<T>* F, int lo, int hi, bool tall
 // TransformHelper::spectralNorm of F[lo..hi) by Faust::power_iteration; the
 // same steps as k_power_iteration (power.cu), on one block.
 template <typename T, typename TC>
-__device__ double b_spectral_norm(const Fac<T>* F, int lo, int hi, int max_iter, TC thr, const TC* x0, TC* vbuf,
+__device__ __noinline__ double b_spectral_norm(const Fac<T>* F, int lo, int hi, int max_iter, TC thr, const TC* x0, TC* vbuf,
                                   int maxn, TC* lane, int* st) {
   __shared__ TC s_nrm, s_inv;
   if (hi <= lo) return 1.0;
@@ -250,11 +421,7 @@ __device__ double b_spectral_norm(const Fac<T>* F, int lo, int hi, int max_iter,
       pi_op(F, lo, hi, tall, o, rp, ci, v, orow);
       const TC* src = bufs[si];
       TC* dst = bufs[di];
-      for (int r = threadIdx.x; r < orow; r += BT) {
-        TC acc = TC(0);
-        for (int p = rp[r]; p < rp[r + 1]; ++p) acc = fmad((TC)v[p], src[ci[p]], acc);
-        dst[r] = acc;
-      }
+      for (int r = threadIdx.x; r < orow; r += BT) dst[r] = b_row_dot<TC>(rp, ci, v, r, src, 1);
       __syncthreads();
       si = di;
       di = 3 - xi - si;
@@ -348,7 +515,7 @@ __device__ void b_heap_adjust_s(unsigned long long* hk, int* hi, int hole, int l
 // thread per line.  The heaps live in the staging area when they fit (else
 // in per-thread arrays); entries are read eight at a time.
 template <typename T>
-__device__ void b_line_topk(const T* M, int rows, int cols, bool by_col, int k, int pos, unsigned char* flags,
+__device__ __noinline__ void b_line_topk(const T* M, int rows, int cols, bool by_col, int k, int pos, unsigned char* flags,
                             unsigned char bit, Stage<T> sg) {
   const int nl = by_col ? cols : rows, len = by_col ? rows : cols;
   const long step = by_col ? 1 : rows;
@@ -403,7 +570,7 @@ __device__ void b_line_topk(const T* M, int rows, int cols, bool by_col, int k, 
 }
 
 template <typename T>
-__device__ bool b_project(const Cons<T>& c, T* M, int rows, int cols, unsigned char* flags, T* lane, int* st,
+__device__ __noinline__ bool b_project(const Cons<T>& c, T* M, int rows, int cols, unsigned char* flags, T* lane, int* st,
                           Stage<T> sg) {
   const long N = (long)rows * cols;
   int pos = c.pos;
@@ -487,7 +654,7 @@ __device__ bool b_project(const Cons<T>& c, T* M, int rows, int cols, unsigned c
 
 // dense -> CSR of the non-zero entries, then the transpose CSR.
 template <typename T>
-__device__ bool b_dense_to_csr(const T* M, Fac<T>& f, int* cnt, int* st) {
+__device__ __noinline__ bool b_dense_to_csr(const T* M, Fac<T>& f, int* cnt, int* st) {
   __shared__ int part[BT];
   const int rows = f.rows, cols = f.cols;
   for (int i = threadIdx.x; i < rows; i += BT) {
@@ -801,7 +968,7 @@ __device__ void run_instance(Inst<T>& I, const Slot<T>& W, const Params& P, cons
 }
 
 template <typename T, typename TN>
-__global__ void __launch_bounds__(BT) k_palm_batched(Inst<T>* insts, const int* order, int* queue, Slot<T>* slots,
+__global__ void __launch_bounds__(BT, 2) k_palm_batched(Inst<T>* insts, const int* order, int* queue, Slot<T>* slots,
                                                      const __grid_constant__ Params P, const TN* x0, int maxn) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   TN* vbuf = reinterpret_cast<TN*>(smem_raw);  // 3 * maxn
@@ -1072,8 +1239,10 @@ static fgb_status batched_impl(fgb_ctx* ctx, fgb_dtype dt, int nprob, const fgb_
     const size_t per_cta = std::min<size_t>(ctx->smem_optin ? ctx->smem_optin : 227 * 1024,
                                             (size_t)(228 * 1024) / per_sm - 2048);
     const size_t stage_bytes = per_cta > vec_bytes + 8192 + 4096 ? per_cta - vec_bytes - 8192 : 4096;
-    P.stage_elems = (int)std::min<size_t>(stage_bytes / es, (size_t)md2);
-    if (P.stage_elems < maxdim)
+    P.stage_elems = (int)std::min<size_t>(stage_bytes / es, std::max<size_t>((size_t)md2, 4 * (16 / es) * (size_t)maxdim));
+    // the block products need 2 * G * maxdim entries of the staging area
+    // after a factor's CSR (which takes at most half of it); G = 16 / sizeof(T)
+    if ((size_t)P.stage_elems < 4 * (16 / es) * (size_t)maxdim)
       s = fail(ctx, FGB_ERR_NOT_SUPPORTED, "batched palm4msa2: dimension %d too large for %d CTAs per SM", maxdim,
                per_sm);
     const size_t smem = vec_bytes + (size_t)P.stage_elems * es;

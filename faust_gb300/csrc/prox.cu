@@ -483,8 +483,9 @@ constexpr int RP_BINS = 4096;
 constexpr int RP_STAGE = 2048;
 constexpr int RP_MAXWIN = 1024;
 
-// Entries of the heap's key array: node n at n + 1, padded so that the
-// two-level look-ahead of rp_insert (up to entry 4 * lim + 7) stays inside.
+// Entries of each heap array (keys, positions): node n at n + 1, padded so
+// that reading the two children of any node below k (entries 2n + 2, 2n + 3)
+// and the two-level look-ahead of rp_insert (up to 4 * lim + 7) stay inside.
 __host__ __device__ inline long rp_key_len(long k) { return ((2 * k + 8) + 1) & ~1L; }
 
 __host__ __device__ inline void rp_window(long i, long N, long k, long wmax, long* lo, long* hi) {
@@ -692,11 +693,11 @@ __global__ void __launch_bounds__(RP_BLOCK)
 // libstdc++ __adjust_heap(first, hole, len, first[hole]) + __push_heap with
 // comp(a, b) = a.key > b.key, one thread, on the split heap (node n at
 // storage n + 1).
-__device__ void rp_adjust(unsigned long long* hk, long long* hidx, long hole, long lim, long half) {
+__device__ void rp_adjust(unsigned long long* hk, unsigned* hidx, int hole, int lim, int half) {
   const unsigned long long vk = hk[hole + 1];
-  const long long vi = hidx[hole + 1];
-  const long top = hole;
-  long child = hole;
+  const unsigned vi = hidx[hole + 1];
+  const int top = hole;
+  int child = hole;
   while (child < lim) {
     child = 2 * (child + 1);
     if (hk[child + 1] > hk[child]) child--;
@@ -710,7 +711,7 @@ __device__ void rp_adjust(unsigned long long* hk, long long* hidx, long hole, lo
     hidx[hole + 1] = hidx[child];
     hole = child - 1;
   }
-  long parent = (hole - 1) / 2;
+  int parent = (hole - 1) / 2;
   while (hole > top && hk[parent + 1] > vk) {
     hk[hole + 1] = hk[parent + 1];
     hidx[hole + 1] = hidx[parent + 1];
@@ -730,9 +731,9 @@ __device__ void rp_adjust(unsigned long long* hk, long long* hidx, long hole, lo
 // Two levels per step: the children and the four grandchildren of the hole
 // are read together (the key array is padded to 2 * len + 8 entries so the
 // look-ahead reads stay inside it).  Returns the new top key.
-__device__ __forceinline__ unsigned long long rp_insert(unsigned long long* hk, long long* hidx, long lim, long half,
-                                                        unsigned long long vk, long long vi) {
-  long hole = 0;
+__device__ __forceinline__ unsigned long long rp_insert(unsigned long long* hk, unsigned* hidx, int lim, int half,
+                                                        unsigned long long vk, unsigned vi) {
+  int hole = 0;
   unsigned long long top = vk;
   bool stop = false;
   while (hole < lim) {
@@ -741,7 +742,7 @@ __device__ __forceinline__ unsigned long long rp_insert(unsigned long long* hk, 
     const ulonglong2 gr = *reinterpret_cast<const ulonglong2*>(hk + 4 * hole + 6);
     const bool left = c2.y > c2.x;
     const unsigned long long ck = left ? c2.x : c2.y;
-    const long c = 2 * hole + 2 - (left ? 1 : 0);
+    const int c = 2 * hole + 2 - (left ? 1 : 0);
     if (ck > vk) {
       stop = true;
       break;
@@ -751,10 +752,9 @@ __device__ __forceinline__ unsigned long long rp_insert(unsigned long long* hk, 
     hidx[hole + 1] = hidx[c + 1];
     hole = c;
     if (c >= lim) break;
-    const ulonglong2 g = left ? gl : gr;
-    const bool l2 = g.y > g.x;
-    const unsigned long long gk = l2 ? g.x : g.y;
-    const long gc = 2 * c + 2 - (l2 ? 1 : 0);
+    const bool l2 = left ? (gl.y > gl.x) : (gr.y > gr.x);
+    const unsigned long long gk = left ? (l2 ? gl.x : gl.y) : (l2 ? gr.x : gr.y);
+    const int gc = 2 * c + 2 - (l2 ? 1 : 0);
     if (gk > vk) {
       stop = true;
       break;
@@ -777,24 +777,122 @@ __device__ __forceinline__ unsigned long long rp_insert(unsigned long long* hk, 
   return top;
 }
 
-template <typename T>
+// Replays the candidates buf[0..cnt) against the heap with one warp, several
+// replacements in flight.  A replacement (rp_insert's walk, one level per
+// step) reads the children of its hole and writes the hole; if every
+// replacement in flight is at least two levels below the next one, the
+// levels they touch never overlap, so each step advances all of them at once
+// (lane = one replacement).  A candidate is taken only once the previous one
+// has passed level 1, when the top it is compared with is final; the result
+// is the sequential replay's.  On return nothing is in flight and top is the
+// heap's top key.
+__device__ __forceinline__ void rp_pipeline(const HNode* buf, int cnt, unsigned long long* hk, unsigned* hidx,
+                                            int lim, int half, unsigned long long& top) {
+  const unsigned FULL = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  bool act = false;
+  int hole = 0;
+  unsigned long long vk = 0;
+  unsigned vi = 0;
+  // replacements start on even steps only (the previous one is then two
+  // levels down) and take lanes round robin: a replacement lasts at most one
+  // step per heap level (< 32 for k < 2^31), so a lane is free again after
+  // 32 starts
+  int next_lane = 0;
+  int drain = 0;  // steps left once the candidates are used up
+  // a window of 32 candidates in registers, one per lane; wmask = not yet passed
+  int q0 = 0;
+  unsigned long long wk = lane < cnt ? buf[lane].key : 0ULL;
+  unsigned wi = lane < cnt ? (unsigned)buf[lane].idx : 0u;
+  unsigned wmask = __ballot_sync(FULL, lane < cnt);
+  for (int step = 0;; ++step) {
+    if ((step & 1) == 0 && drain == 0) {
+      unsigned m = wmask & __ballot_sync(FULL, wk > top);
+      while (!m) {
+        q0 += 32;
+        if (q0 >= cnt) break;
+        const int i = q0 + lane;
+        wk = i < cnt ? buf[i].key : 0ULL;
+        wi = i < cnt ? (unsigned)buf[i].idx : 0u;
+        wmask = __ballot_sync(FULL, i < cnt);
+        m = wmask & __ballot_sync(FULL, wk > top);
+      }
+      if (m) {
+        const int src = __ffs(m) - 1;
+        wmask &= ~((2u << src) - 1u);
+        const unsigned long long nk = __shfl_sync(FULL, wk, src);
+        const unsigned ni = __shfl_sync(FULL, wi, src);
+        if (lane == next_lane) {
+          act = true;
+          hole = 0;
+          vk = nk;
+          vi = ni;
+        }
+        next_lane = (next_lane + 1) & 31;
+      } else {
+        wmask = 0;
+        drain = 33;
+      }
+    }
+    if (drain && --drain == 0) break;
+    // one level for every replacement in flight, without branches: the
+    // children of any node below k lie inside the padded arrays
+    {
+      const int h = act ? hole : 0;
+      const ulonglong2 c2 = *reinterpret_cast<const ulonglong2*>(hk + 2 * h + 2);
+      const uint2 i2 = *reinterpret_cast<const uint2*>(hidx + 2 * h + 2);
+      const bool two = h < lim, one = h == half;
+      const bool left = one || (two && c2.y > c2.x);
+      const unsigned long long ck = left ? c2.x : c2.y;
+      const unsigned cidx = left ? i2.x : i2.y;
+      const bool move = (two || one) && !(ck > vk);
+      const int c = 2 * h + 2 - (left ? 1 : 0);
+      const bool leaf = c >= lim && c != half;
+      if (act) {
+        hk[h + 1] = move ? ck : vk;
+        hidx[h + 1] = move ? cidx : vi;
+      }
+      if (act && move && leaf) {
+        hk[c + 1] = vk;
+        hidx[c + 1] = vi;
+      }
+      act = act && move && !leaf;
+      hole = c;
+    }
+    __syncwarp();
+    top = hk[1];
+  }
+}
+
+// HEAP_SMEM: the heap is in shared memory after the staging buffers (the
+// compiler then addresses it as shared memory); else in gk / gi.  Positions
+// are 32-bit (the host takes this path only for fewer than 2^32 entries).
+template <typename T, bool HEAP_SMEM>
 __global__ void __launch_bounds__(PX_THREADS)
     k_rp_replay(const T* __restrict__ M, long N, int pos, long k, long wmax, int nwin, TopkState* st,
                 unsigned char* __restrict__ flags, const HNode* __restrict__ cand, const int* __restrict__ wcnt,
-                unsigned long long* gk, long long* gi, int heap_in_smem) {
+                unsigned long long* gk, unsigned* gi) {
   if (st->sel_case != 2) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ long s_off[RP_MAXWIN + 1];
   __shared__ long s_lo[RP_MAXWIN];
   HNode* stage = reinterpret_cast<HNode*>(smem_raw);  // 2 x RP_STAGE
-  unsigned long long* hk = heap_in_smem ? reinterpret_cast<unsigned long long*>(stage + 2 * RP_STAGE) : gk;
-  long long* hidx = heap_in_smem ? reinterpret_cast<long long*>(hk + rp_key_len(k)) : gi;
+  unsigned long long* hk;
+  unsigned* hidx;
+  if (HEAP_SMEM) {
+    hk = reinterpret_cast<unsigned long long*>(smem_raw + 2 * RP_STAGE * sizeof(HNode));
+    hidx = reinterpret_cast<unsigned*>(smem_raw + 2 * RP_STAGE * sizeof(HNode) +
+                                       sizeof(unsigned long long) * rp_key_len(k));
+  } else {
+    hk = gk;
+    hidx = gi;
+  }
   const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
-  const long lim = (k - 1) / 2;
-  const long half = (k & 1) == 0 ? (k - 2) / 2 : -1;
-  for (long i = t; i < k; i += blockDim.x) {
+  const int lim = (int)((k - 1) / 2);
+  const int half = (k & 1) == 0 ? (int)((k - 2) / 2) : -1;
+  for (int i = t; i < (int)k; i += blockDim.x) {
     hk[i + 1] = mag_key(pos_adj(M[i], pos));
-    hidx[i + 1] = i;
+    hidx[i + 1] = (unsigned)i;
   }
   if (t == 0) {
     long acc = 0;
@@ -810,10 +908,10 @@ __global__ void __launch_bounds__(PX_THREADS)
   __syncthreads();
   // make_heap, deepest parents first, one level at a time
   if (k >= 2) {
-    const long lastp = (k - 2) / 2;
-    for (int L = 63 - __clzll(lastp + 1); L >= 0; --L) {
-      const long a = (1L << L) - 1, b = min((2L << L) - 2, lastp);
-      for (long n = a + t; n <= b; n += blockDim.x) rp_adjust(hk, hidx, n, lim, half);
+    const int lastp = (int)((k - 2) / 2);
+    for (int L = 31 - __clz(lastp + 1); L >= 0; --L) {
+      const int a = (1 << L) - 1, b = min((2 << L) - 2, lastp);
+      for (int n = a + t; n <= b; n += blockDim.x) rp_adjust(hk, hidx, n, lim, half);
       __syncthreads();
     }
   }
@@ -839,27 +937,14 @@ __global__ void __launch_bounds__(PX_THREADS)
   for (long c = 0; c < nsteps; ++c) {
     if (warp != 0) {
       if (c + 1 < nsteps) stage_chunk(c + 1, stage + ((c + 1) & 1) * RP_STAGE, t - 32, blockDim.x - 32);
-    } else if (lane == 0) {
-      const HNode* buf = stage + (c & 1) * RP_STAGE;
-      const int cnt = (int)min((long)RP_STAGE, total - c * RP_STAGE);
-      int q = 0;
-      for (; q + 4 <= cnt; q += 4) {
-        HNode cn[4];
-#pragma unroll
-        for (int u = 0; u < 4; ++u) cn[u] = buf[q + u];
-#pragma unroll
-        for (int u = 0; u < 4; ++u)
-          if (cn[u].key > top) top = rp_insert(hk, hidx, lim, half, cn[u].key, cn[u].idx);
-      }
-      for (; q < cnt; ++q) {
-        const HNode cn = buf[q];
-        if (cn.key > top) top = rp_insert(hk, hidx, lim, half, cn.key, cn.idx);
-      }
+    } else {
+      rp_pipeline(stage + (c & 1) * RP_STAGE, (int)min((long)RP_STAGE, total - c * RP_STAGE), hk, hidx, lim, half,
+                  top);
     }
     __syncthreads();
   }
   const unsigned long long tt = st->t;
-  for (long i = t; i < k; i += blockDim.x)
+  for (int i = t; i < (int)k; i += blockDim.x)
     if (hk[i + 1] == tt) flags[hidx[i + 1]] = 1;
 }
 
@@ -1184,12 +1269,12 @@ static fgb_status queue_tie_replay(fgb_ctx* ctx, ProxWork& w, const T* M, long N
   }
   const long hkn = rp_key_len(k);  // key array (padded), then k + 2 positions
   const size_t stage_bytes = 2 * (size_t)RP_STAGE * sizeof(HNode);
-  const size_t heap_bytes = sizeof(unsigned long long) * (size_t)hkn + sizeof(long long) * (size_t)(k + 2);
+  const size_t heap_bytes = (sizeof(unsigned long long) + sizeof(unsigned)) * (size_t)hkn;
   const size_t cap = std::min<size_t>(ctx->smem_optin > 24 * 1024 ? ctx->smem_optin - 24 * 1024 : 0, 200 * 1024);
   const bool in_smem = stage_bytes + heap_bytes <= cap;
   const size_t smem = stage_bytes + (in_smem ? heap_bytes : 0);
   unsigned long long* gk = nullptr;
-  long long* gi = nullptr;
+  unsigned* gi = nullptr;
   if (!in_smem) {
     if (w.heap2_cap < k) {
       dfree(w.heap2);
@@ -1199,22 +1284,21 @@ static fgb_status queue_tie_replay(fgb_ctx* ctx, ProxWork& w, const T* M, long N
       w.heap2_cap = k;
     }
     gk = reinterpret_cast<unsigned long long*>(w.heap2);
-    gi = reinterpret_cast<long long*>(gk + hkn);
+    gi = reinterpret_cast<unsigned*>(gk + hkn);
   }
   k_rp_bounds<T><<<nwin, RP_BLOCK, 0, ctx->stream>>>(M, N, pos, k, wmax, w.state, w.wbound);
   FGB_LAUNCHED(ctx);
   k_rp_filter<T><<<nwin, RP_BLOCK, 0, ctx->stream>>>(M, N, pos, k, wmax, w.state, w.wbound,
                                                      reinterpret_cast<HNode*>(w.cand), w.wcount);
   FGB_LAUNCHED(ctx);
-  auto kern = k_rp_replay<T>;
-  static thread_local size_t attr_set = 0;
-  if (smem > attr_set) {
+  auto kern = in_smem ? k_rp_replay<T, true> : k_rp_replay<T, false>;
+  static thread_local size_t attr_set[2] = {0, 0};
+  if (smem > attr_set[in_smem]) {
     FGB_CUDA(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    attr_set = smem;
+    attr_set[in_smem] = smem;
   }
   kern<<<1, PX_THREADS, smem, ctx->stream>>>(M, N, pos, k, wmax, nwin, w.state, w.flags,
-                                             reinterpret_cast<const HNode*>(w.cand), w.wcount, gk, gi,
-                                             in_smem ? 1 : 0);
+                                             reinterpret_cast<const HNode*>(w.cand), w.wcount, gk, gi);
   FGB_LAUNCHED(ctx);
   return FGB_OK;
 }
@@ -1243,7 +1327,7 @@ static fgb_status queue_sp(fgb_ctx* ctx, ProxWork& w, T* M, long N, long k, int 
   const int nch = (int)((N + chunk - 1) / chunk);
   k_tie_case<T><<<nch, PX_THREADS, 0, ctx->stream>>>(M, N, pos, chunk, w.state, w.chunk_cnt);
   FGB_LAUNCHED(ctx);
-  if (w.growable) {
+  if (w.growable && N < (1L << 32) - 1) {
     FGB_TRY(queue_tie_replay<T>(ctx, w, M, N, k, pos));
   } else {
     // candidates of one chunk, then the heap itself when it fits on chip;

@@ -156,6 +156,58 @@ def palm4msa(M, constraints, params=None, ret_lambda=True, ctx=None):
     return PalmResult(F, lam.value)
 
 
+class ParamsHierarchical:
+    """pyfaust.factparams.ParamsHierarchical: fact_constraints[i] and
+    res_constraints[i] split the residual at step i; stop_crit1 (iterations
+    of each two-factor palm4msa2), stop_crit2 (iterations of each global
+    palm4msa2); the rest as ParamsPalm4MSA."""
+
+    def __init__(self, fact_constraints, res_constraints, stop_crit1, stop_crit2, is_update_way_R2L=False,
+                 init_lambda=1.0, step_size=1e-16, constant_step_size=False, is_fact_side_left=False,
+                 packing_RL=True, no_normalization=False, no_lambda=False, norm2_max_iter=100,
+                 norm2_threshold=1e-6, norm2_fp64=False):
+        if len(fact_constraints) != len(res_constraints):
+            raise ValueError("fact_constraints and res_constraints must have the same length")
+        self.fact_constraints = list(fact_constraints)
+        self.res_constraints = list(res_constraints)
+        self.is_fact_side_left = is_fact_side_left
+
+        def mk(its):
+            return ParamsPalm4MSA([], int(its), is_update_way_R2L=is_update_way_R2L, init_lambda=init_lambda,
+                                  step_size=step_size, constant_step_size=constant_step_size, packing_RL=packing_RL,
+                                  no_normalization=no_normalization, no_lambda=no_lambda,
+                                  norm2_max_iter=norm2_max_iter, norm2_threshold=norm2_threshold,
+                                  norm2_fp64=norm2_fp64)
+        self.params_2facts = mk(stop_crit1)
+        self.params_global = mk(stop_crit2)
+
+
+def hierarchical(M, p, ret_lambda=True, ctx=None):
+    """hierarchical (2020 backend) on the GPU: Faust::hierarchical.  M: numpy
+    array (host).  Returns a PalmResult (faust with len(fact_constraints) + 1
+    factors, lambda_)."""
+    ctx = ctx or default_context()
+    dtype = np.dtype(M.dtype)
+    if dtype not in (np.float32, np.float64):
+        dtype = np.dtype(np.float64)
+    Mc = np.asfortranarray(M, dtype=dtype)
+    rows, cols = Mc.shape
+    n = len(p.fact_constraints)
+    keep = []
+    fc = (_ffi.Constraint * n)()
+    rc = (_ffi.Constraint * n)()
+    for i in range(n):
+        fc[i] = p.fact_constraints[i]._c(dtype, keep)
+        rc[i] = p.res_constraints[i]._c(dtype, keep)
+    p2, pg = p.params_2facts._c(), p.params_global._c()
+    lam = ctypes.c_double(1.0)
+    h = ctypes.c_void_p()
+    check(_ffi.lib().fgb_hierarchical(ctx.handle, _ffi.F64 if dtype == np.float64 else _ffi.F32, Mc.ctypes.data, rows,
+                                      cols, n, fc, rc, ctypes.byref(p2), ctypes.byref(pg), int(p.is_fact_side_left),
+                                      ctypes.byref(lam), ctypes.byref(h)), ctx.handle)
+    return PalmResult(Faust._from_handle(h, ctx, dtype), lam.value)
+
+
 def palm4msa_batched(problems, params, ctx=None, ctas_per_sm=0):
     """Runs many palm4msa2 instances in one persistent launch.
 

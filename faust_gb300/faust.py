@@ -200,6 +200,25 @@ class Faust:
               self.ctx.handle)
         return Y
 
+    def matmul_op_device(self, op, X, Y=None, mode=0):
+        """Y = op(F) X on the device with op in 'N', 'T', 'H' (H = T for real
+        scalars): Transform::multiply(X, op).  Column-major CUDA tensors."""
+        import torch
+        op = op.upper()
+        if op == "N":
+            return self.matmul_device(X, Y, mode)
+        rows_in, rows_out, ncols = self.shape[0], self.shape[1], X.shape[1]
+        if X.shape[0] != rows_in:
+            raise ValueError("dimensions do not match: %s(F) with F %s @ %s" % (op, self.shape, tuple(X.shape)))
+        Xc = X if _is_colmajor(X) else X.t().contiguous().t()
+        if Y is None:
+            Y = torch.empty((ncols, rows_out), dtype=X.dtype, device=X.device).t()
+        elif not _is_colmajor(Y):
+            raise ValueError("Y must be column-major")
+        check(_ffi.lib().fgb_faust_mul_op(self.handle, op.encode(), Xc.data_ptr(), _ld(Xc), ncols, Y.data_ptr(),
+                                          _ld(Y), int(mode)), self.ctx.handle)
+        return Y
+
     def norm(self, ord=2, max_iter=100, threshold=1e-6):
         """2-norm by FP64 power iteration (TransformHelper::spectralNorm)."""
         if ord != 2:

@@ -102,6 +102,14 @@ fgb_status fgb_faust_shape(const fgb_faust* F, int* rows, int* cols, int* nfacto
  * with FGB_ERR_NOT_SUPPORTED when the chain does not fit on chip). */
 fgb_status fgb_faust_mul(fgb_faust* F, const void* X, int ldx, int ncols, void* Y, int ldy, int mode);
 
+// Y = op(F) X with op 'N' (as fgb_faust_mul), 'T' or 'H' (the adjoint; the
+// transpose for real scalars): F^T X = S_J^T (... (S_1^T X)), X of
+// rows(F) x ncols (ld >= rows(F)), Y of cols(F) x ncols.  CSR Fausts only;
+// the factors' transposes are built on first use.  Replaces
+// Transform<FPP,Cpu>::multiply(const MatDense&, char opThis)
+// (CPU/faust_Transform.hpp:1754-1773, the 'T' / 'H' branches).
+fgb_status fgb_faust_mul_op(fgb_faust* F, char op, const void* X, int ldx, int ncols, void* Y, int ldy, int mode);
+
 /* Y = F X with X, Y in HOST memory: copy in, product, copy out, synchronous.
  * Replaces TransformHelper<FPP,Cpu>::multiply(const FPP* A, int A_ncols,
  * FPP* C) (CPU/faust_TransformHelper.hpp:406-433) and
@@ -202,6 +210,21 @@ fgb_status fgb_palm4msa2(fgb_ctx* ctx, fgb_dtype dtype, const void* A, int rows,
 fgb_status fgb_palm4msa2_device(fgb_ctx* ctx, fgb_dtype dtype, const void* A_dev, int rows, int cols, int nfacts,
                                 const fgb_constraint* cons, const fgb_palm_params* params,
                                 const void* const* init_facts, double* lambda, fgb_faust** out);
+
+/* hierarchical (2020) factorization: Faust::hierarchical
+ * (src/algorithm/factorization/faust_hierarchical.hpp:1-121, .h:6-24).
+ * Step i = 0..nsteps-1 splits the current residual (the last factor, or the
+ * first when is_fact_side_left) by palm4msa2 with constraints
+ * (fac_cons[i], res_cons[i]) -- (res_cons[i], fac_cons[i]) on the left side --
+ * and params_2facts (zero / identity start, lambda 1); the global lambda is
+ * multiplied by that lambda; then palm4msa2 with params_global refines all
+ * factors against A from the current factors and the global lambda.  A: rows
+ * x cols column-major in HOST memory.  The result has nsteps + 1 factors;
+ * lambda receives the final global lambda.  F32 and F64. */
+fgb_status fgb_hierarchical(fgb_ctx* ctx, fgb_dtype dtype, const void* A, int rows, int cols, int nsteps,
+                            const fgb_constraint* fac_cons, const fgb_constraint* res_cons,
+                            const fgb_palm_params* params_2facts, const fgb_palm_params* params_global,
+                            int is_fact_side_left, double* lambda, fgb_faust** out);
 
 /* ------------------------------------------------------------------ batched PALM4MSA
  * Many independent palm4msa2 instances (uneven sizes) in ONE persistent

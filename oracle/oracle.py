@@ -203,3 +203,42 @@ def rel_err(A, facts, lam):
     _check(lib().orc_rel_err_f64(_p(Af), A.shape[0], A.shape[1], len(facts), _p(cd), _p(fl), ctypes.c_double(lam),
                                  ctypes.byref(out)))
     return out.value
+
+
+def hierarchical(A, fac_cons, res_cons, its_2facts, its_global, is_fact_side_left=False, is_update_way_R2L=False,
+                 **palm_kw):
+    """Faust::hierarchical, 2020 version (src/algorithm/factorization/
+    faust_hierarchical.hpp:1-121), composed from this oracle's palm4msa2.
+
+    Step i splits the current residual (last factor, or first on the left
+    side) with the constraints (fac_i, res_i) -- (res_i, fac_i) on the left --
+    from the default start and lambda 1 (:42-97); the global lambda is
+    multiplied by the local one (:99); the two factors replace the residual
+    (:101-111); palm4msa2 refines all factors against A from them and the
+    global lambda, with the constraints fac_0..fac_i, res_i in factor order
+    (:114-121).  Returns (dense factors, lambda)."""
+    A = np.asfortranarray(A)
+    S = None
+    glo = 1.0
+    for i in range(len(fac_cons)):
+        if i == 0:
+            Si = A
+        else:
+            Si = np.asfortranarray(S[0] if is_fact_side_left else S[-1])
+        lc = [res_cons[i], fac_cons[i]] if is_fact_side_left else [fac_cons[i], res_cons[i]]
+        two, lam, _ = palm4msa2(Si, lc, its_2facts, is_update_way_R2L=is_update_way_R2L, init_lambda=1.0, **palm_kw)
+        glo *= lam
+        if i == 0:
+            S = list(two)
+        elif is_fact_side_left:
+            S = list(two) + S[1:]
+        else:
+            S = S[:-1] + list(two)
+        if is_fact_side_left:
+            gc = [res_cons[i]] + [fac_cons[j] for j in range(i, -1, -1)]
+        else:
+            gc = [fac_cons[j] for j in range(i + 1)] + [res_cons[i]]
+        S, glo, _ = palm4msa2(A, gc, its_global, is_update_way_R2L=is_update_way_R2L, init_facts=S,
+                              init_lambda=glo, **palm_kw)
+        S = list(S)
+    return S, glo

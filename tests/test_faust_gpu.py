@@ -67,6 +67,35 @@ def test_csr_chain_ragged(fgb, oracle, dtype, ncols):
         assert np.array_equal(Y, ref)
 
 
+@pytest.mark.parametrize("dtype", [np.float32, np.float64])
+@pytest.mark.parametrize("ncols", [1, 5, 64])
+def test_csr_chain_transposed(fgb, oracle, dtype, ncols):
+    """F^T X (op 'T' and 'H') against the oracle chain of the transposed
+    factors in reverse order, per-factor and fused paths, ragged shapes."""
+    rng = np.random.default_rng(100 + ncols)
+    dims = [64, 100, 37, 250, 64]
+    facs = []
+    for a, b in zip(dims[:-1], dims[1:]):
+        m = synth.random_csr(a, b, min(4, b), rng, dtype).tolil()
+        m[a // 2, :] = 0
+        facs.append(m.tocsr())
+    X = synth.dense_colmajor(dims[0], ncols, rng, dtype)
+    F = fgb.Faust(facs, dtype=dtype)
+    tfacs = []
+    for f in reversed(facs):
+        t = f.T.tocsr()
+        t.sort_indices()
+        tfacs.append(t)
+    ref = oracle.chain_mul(tfacs, X)
+    for op in ("T", "H"):
+        for mode in (0, 1):
+            Y = _to_np(F.matmul_op_device(op, _colmajor_cuda(X), mode=mode))
+            assert Y.shape == (dims[-1], ncols)
+            assert np.array_equal(Y, ref), (op, mode)
+    Xn = synth.dense_colmajor(dims[-1], ncols, rng, dtype)
+    assert np.array_equal(_to_np(F.matmul_op_device("N", _colmajor_cuda(Xn))), oracle.chain_mul(facs, Xn))
+
+
 def test_csr_butterfly_fp32_bitexact(fgb, oracle):
     rng = np.random.default_rng(13)
     facs = synth.butterfly_faust_factors(10, rng, np.float32)

@@ -233,3 +233,40 @@ def test_palm_fixture_config_compared_palm2(oracle):
     facts2, lam2, _ = oracle.palm4msa2(data, cons, 200, packing_RL=False, norm2_threshold=1e-15,
                                        norm2_max_iter=1000)
     assert lam2 == lam and all(np.array_equal(a, b) for a, b in zip(facts, facts2))
+
+
+# ---------------------------------------------------------------- hierarchical
+def _wht_cons(oracle, n):
+    d = 2 ** n
+    fc = [dict(kind=oracle.SPLINCOL, k=2, rows=d, cols=d) for _ in range(n - 1)]
+    rc = [dict(kind=oracle.SPLINCOL, k=d // 2 ** (i + 1), rows=d, cols=d) for i in range(n - 1)]
+    return fc, rc
+
+
+@pytest.mark.parametrize("n", [4, 5])
+def test_hierarchical_wht_factorizes_hadamard(oracle, n):
+    """pyfaust's ParamsHierarchicalWHT (factparams.py:1605-1638: splincol k=2
+    factors, residuals splincol d/2^(i+1), 30 iterations each, R2L, no
+    packing): the Hadamard matrix comes out exactly as n butterfly-like
+    factors with 2 entries per row and column."""
+    d = 2 ** n
+    A = synth.hadamard(d).astype(np.float64)
+    fc, rc = _wht_cons(oracle, n)
+    S, lam = oracle.hierarchical(A, fc, rc, 30, 30, is_update_way_R2L=True, packing_RL=False)
+    assert len(S) == n
+    for f in S:
+        assert _nnz_rows(f).max() <= 2 and np.count_nonzero(f) == 2 * d
+    assert oracle.rel_err(A, S, lam) < 1e-12
+
+
+def test_hierarchical_left_side_shapes(oracle):
+    """is_fact_side_left: the residual is split on the left; factor shapes
+    and the global constraint order follow faust_hierarchical.hpp:101-121."""
+    rng = np.random.default_rng(5)
+    A = rng.standard_normal((40, 24))
+    fc = [dict(kind=oracle.SP, k=60, rows=24, cols=24), dict(kind=oracle.SP, k=60, rows=32, cols=24)]
+    rc = [dict(kind=oracle.SP, k=400, rows=40, cols=24), dict(kind=oracle.SP, k=300, rows=40, cols=32)]
+    S, lam = oracle.hierarchical(A, fc, rc, 10, 10, is_fact_side_left=True)
+    assert [f.shape for f in S] == [(40, 32), (32, 24), (24, 24)]
+    assert np.count_nonzero(S[0]) <= 300 and np.count_nonzero(S[1]) <= 60 and np.count_nonzero(S[2]) <= 60
+    assert 0 < oracle.rel_err(A, S, lam) < 1

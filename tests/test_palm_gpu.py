@@ -261,3 +261,44 @@ def test_palm_batched_butterfly_supp(oracle):
         assert r.lambda_ == lam_o
         for i in range(6):
             assert np.array_equal(r.faust.factors(i).toarray().astype(np.float32), facts_o[i])
+
+
+# ---------------------------------------------------------------- hierarchical
+def _dense_factors(F):
+    return [F.factors(i).toarray() for i in range(F.numfactors())]
+
+
+def test_hierarchical_wht_bitexact(oracle):
+    """hierarchical with pyfaust's ParamsHierarchicalWHT on the 32 x 32
+    Hadamard matrix: factors and lambda equal to the oracle's composition of
+    palm4msa2 runs, and the factorization is exact."""
+    n, d = 5, 32
+    A = synth.hadamard(d).astype(np.float64)
+    fc = [fact.ConstraintInt("splincol", d, d, 2) for _ in range(n - 1)]
+    rc = [fact.ConstraintInt("splincol", d, d, d // 2 ** (i + 1)) for i in range(n - 1)]
+    p = fact.ParamsHierarchical(fc, rc, 30, 30, is_update_way_R2L=True, packing_RL=False)
+    res = fact.hierarchical(A, p)
+    got = _dense_factors(res.faust)
+    ref, lam = oracle.hierarchical(A, [c.oracle_dict() for c in fc], [c.oracle_dict() for c in rc], 30, 30,
+                                   is_update_way_R2L=True, packing_RL=False)
+    assert res.lambda_ == lam
+    assert len(got) == len(ref) and all(np.array_equal(a, b) for a, b in zip(got, ref))
+    assert oracle.rel_err(A, got, res.lambda_) < 1e-12
+    res.faust.close()
+
+
+@pytest.mark.parametrize("dtype", [np.float64, np.float32])
+def test_hierarchical_left_side_sp_bitexact(oracle, dtype):
+    rng = np.random.default_rng(5)
+    A = rng.standard_normal((40, 24)).astype(dtype)
+    fc = [fact.ConstraintInt("sp", 24, 24, 60), fact.ConstraintInt("sp", 32, 24, 60)]
+    rc = [fact.ConstraintInt("sp", 40, 24, 400), fact.ConstraintInt("sp", 40, 32, 300)]
+    p = fact.ParamsHierarchical(fc, rc, 10, 10, is_fact_side_left=True, norm2_fp64=dtype == np.float32)
+    res = fact.hierarchical(A, p)
+    got = _dense_factors(res.faust)
+    ref, lam = oracle.hierarchical(A, [c.oracle_dict() for c in fc], [c.oracle_dict() for c in rc], 10, 10,
+                                   is_fact_side_left=True, norm2_fp64=dtype == np.float32)
+    assert [g.shape for g in got] == [(40, 32), (32, 24), (24, 24)]
+    assert np.float64(res.lambda_) == np.float64(lam)
+    assert all(np.array_equal(a, b) for a, b in zip(got, ref))
+    res.faust.close()
