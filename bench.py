@@ -325,7 +325,7 @@ def run_palm(args, rank, world):
         r.faust.close()
     e2e_s = float(np.median(e2e))
     hbm, tflops, peak_kind = _peaks()
-    roof = palm_roofline(ctx, hbm, peak_kind)
+    roof, roof_spmm = palm_roofline(ctx, hbm, peak_kind)
     out = {
         "metric": METRIC, "submetric": "palm4msa2 FP64 time to the plain 200-iteration relative error (s per run)",
         "value": round(step_s, 5), "unit": "s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
@@ -336,6 +336,7 @@ def run_palm(args, rank, world):
                    "l2": "flushed (256 MB write) before every timed run", "rel_err": err.value,
                    "lambda": res.lambda_},
         "roofline": roof,
+        "roofline_spmm": roof_spmm,
         "e2e": {"value": round(e2e_s, 5), "unit": "s", "h2d_bytes_per_step": int(H.nbytes),
                 "d2h_bytes_per_step": int(d2h)},
         "gpu_launches": int(launches),
@@ -346,26 +347,41 @@ def run_palm(args, rank, world):
     return out
 
 
+def fp64_peak(ctx):
+    """Scalar FP64 FMA throughput of the device in TFLOP/s, measured in this
+    run (fgb_probe_fp64_fma: dependent-FMA loops on every SM)."""
+    import ctypes
+    from faust_gb300 import _ffi
+    out = ctypes.c_double()
+    _ffi.check(_ffi.lib().fgb_probe_fp64_fma(ctx.handle, ctypes.byref(out)), ctx.handle)
+    return out.value / 1e12
+
+
 def palm_roofline(ctx, hbm, peak_kind):
-    """The sparse x dense product of the PALM gradient chain (k_csr_spmm on a
-    1024 x 1024 FP64 factor with 2048 entries times a dense 1024 x 1024
-    block), timed alone with CUDA events over repeated launches."""
+    """Rooflines of the two FP64 kernels that bound the PALM run, each timed
+    alone with CUDA events: the power iteration (one CTA per chain; a
+    9-factor chain of the run's shape) against one SM's share of the FP64 FMA
+    peak, and the sparse x dense product of the gradient chain (k_csr_spmm,
+    1024 x 1024 FP64 factor with 2048 entries times a 1024 x 1024 block, 40
+    back-to-back launches per call) against the device FP64 FMA peak.  Both
+    work on L2-resident data: the scalar FP64 pipe, not HBM, bounds them."""
+    import ctypes
     import torch
     import faust_gb300 as fg
-    from faust_gb300 import synth
-    rng = np.random.default_rng(3)
     import scipy.sparse as sp
+    from faust_gb300 import _ffi
+    peak = fp64_peak(ctx)
+    sm_count = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
+    stream = torch.cuda.current_stream()
     S = sp.random(PALM_N, PALM_N, density=PALM_K / PALM_N ** 2, random_state=3, format="csr")
     S.sort_indices()
-    # one call = 40 back-to-back launches (one per factor), so host overhead
-    # between launches does not enter the per-launch time
+    # --- k_csr_spmm
     nf = 40
     F = fg.Faust([S] * nf, ctx=ctx)
     X = torch.randn((PALM_N, PALM_N), device="cuda", dtype=torch.float64).t()
     Y = torch.empty((PALM_N, PALM_N), device="cuda", dtype=torch.float64).t()
     for _ in range(3):
         F.matmul_device(X, Y, mode=1)
-    stream = torch.cuda.current_stream()
     s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     calls = 10
     s.record(stream)
@@ -374,14 +390,41 @@ def palm_roofline(ctx, hbm, peak_kind):
     e.record(stream)
     torch.cuda.synchronize()
     us = s.elapsed_time(e) * 1e3 / (calls * nf)
-    nbytes = 2 * PALM_N * PALM_N * 8 + S.nnz * 12 + (PALM_N + 1) * 4
-    achieved = nbytes / (us * 1e-6) / 1e9
     F.close()
-    return {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
-            "frac": round(achieved / hbm, 4), "traffic": None, "peak_kind": peak_kind,
-            "kernel": "k_csr_spmm (PALM gradient product, 1024^2 FP64, 2048 nnz)",
-            "algorithmic_bytes_per_launch": int(nbytes), "us_per_launch": round(us, 3),
-            "note": "operands are L2-resident (16 MB), so achieved can exceed HBM bandwidth"}
+    flops = 2.0 * S.nnz * PALM_N
+    spmm = {"bound": "fp64", "achieved": round(flops / (us * 1e-6) / 1e12, 4), "peak": round(peak, 4),
+            "unit": "TFLOP/s", "frac": round(flops / (us * 1e-6) / 1e12 / peak, 4),
+            "traffic": 8465408, "traffic_note": "dram bytes of one launch, ncu capture with cold L2",
+            "peak_kind": "measured in this run (FP64 FMA loop on all SMs)",
+            "kernel": "k_csr_spmm (PALM gradient product, 1024^2 FP64 factor with 2048 entries x 1024^2 block)",
+            "algorithmic_flops_per_launch": int(flops), "us_per_launch": round(us, 3)}
+    # --- power iteration on one 9-factor chain (one CTA)
+    G = fg.Faust([S] * 9, ctx=ctx)
+    out, flag = ctypes.c_double(), ctypes.c_int()
+
+    def norm():
+        _ffi.check(_ffi.lib().fgb_faust_spectral_norm(G.handle, 100, 0.0, ctypes.byref(out), ctypes.byref(flag)),
+                   ctx.handle)
+    norm()
+    reps = 3
+    s.record(stream)
+    for _ in range(reps):
+        norm()
+    e.record(stream)
+    torch.cuda.synchronize()
+    pi_us = s.elapsed_time(e) * 1e3 / reps
+    G.close()
+    its = 100 if flag.value < 0 else max(1, flag.value)
+    # per iteration: F F^H x over 18 products (2 flops per entry) and two
+    # length-n dot products
+    pi_flops = its * (18 * 2.0 * S.nnz + 4.0 * PALM_N)
+    sm_peak = peak / sm_count
+    pi = {"bound": "fp64", "achieved": round(pi_flops / (pi_us * 1e-6) / 1e12, 5), "peak": round(sm_peak, 5),
+          "unit": "TFLOP/s", "frac": round(pi_flops / (pi_us * 1e-6) / 1e12 / sm_peak, 4), "traffic": None,
+          "peak_kind": "one SM's share of the FP64 FMA peak measured in this run",
+          "kernel": "k_power_iteration (one CTA per chain; 9-factor chain, %d iterations)" % its,
+          "algorithmic_flops_per_launch": int(pi_flops), "us_per_launch": round(pi_us, 1)}
+    return pi, spmm
 
 
 def cpu_baseline_palm(its=5):

@@ -95,6 +95,8 @@ _SIGS = {
                               ctypes.POINTER(_P)]),
     "fgb_palm4msa2_batched": (_I, [_P, _I, _I, ctypes.POINTER(PalmProblem), ctypes.POINTER(PalmParams),
                                    ctypes.POINTER(BatchOpts), ctypes.POINTER(PalmResultC)]),
+    # include/fgb_diag.h
+    "fgb_probe_fp64_fma": (_I, [_P, ctypes.POINTER(_D)]),
     # include/fgb_mlp.h
     "fgb_gemm_bf16": (_I, [_P, _I, _I, _I, _P, ctypes.c_long, _P, ctypes.c_long, _P, ctypes.c_long, _I, _P, _I, _I,
                            _P]),

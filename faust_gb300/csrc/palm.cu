@@ -162,11 +162,27 @@ struct Palm {
   // the gradient products (whole grid) and joins before alpha is read
   cudaStream_t side = nullptr;
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+  // The chains not yet touched by the current sweep (R_f = S[f+1..J) left to
+  // right, L_f = S[0..f) right to left) only hold factors of the previous
+  // iteration: their J norms are computed in one launch at the start of the
+  // iteration, on a second side stream; each update then iterates only its
+  // other chain.
+  bool hoist = false;
+  cudaStream_t side2 = nullptr;
+  cudaEvent_t ev_it = nullptr, ev_old = nullptr;
+  PIChain* d_old_chains = nullptr;
+  PIOut* pi_old = nullptr;
+  int old_maxn = 0;
 
   ~Palm() {
     if (side) cudaStreamDestroy(side);
     if (ev_fork) cudaEventDestroy(ev_fork);
     if (ev_join) cudaEventDestroy(ev_join);
+    if (side2) cudaStreamDestroy(side2);
+    if (ev_it) cudaEventDestroy(ev_it);
+    if (ev_old) cudaEventDestroy(ev_old);
+    dfree(d_old_chains);
+    dfree(pi_old);
     for (auto& f : S) free_factor(f);
     for (auto* q : packed) dfree(q);
     for (auto* q : supp) dfree(q);
@@ -323,16 +339,28 @@ struct Palm {
   // ---------------------------------------------------------------- one iteration
   fgb_status step_size(int f, int it) {
     PIChain a, b;
+    PIPalm pp;
+    std::memset(&pp, 0, sizeof(pp));
     if (p.constant_step_size) {
       std::memset(&a, 0, sizeof(a));
       std::memset(&b, 0, sizeof(b));
       a.empty = b.empty = 1;
+    } else if (hoist) {
+      // only the chain the sweep has already updated; the other norm comes
+      // from the launch at the start of the iteration
+      std::memset(&b, 0, sizeof(b));
+      b.empty = 1;
+      if (!r2l)
+        pi_chain_build(S.data(), 0, f, a);  // L
+      else
+        pi_chain_build(S.data(), f + 1, J, a);  // R
+      pp.ext_norm = &pi_old->norm[f];
+      pp.ext_is_r = r2l ? 0 : 1;
+      FGB_CUDA(ctx, cudaStreamWaitEvent(side, ev_old, 0));
     } else {
       pi_chain_build(S.data(), f + 1, J, a);  // R
       pi_chain_build(S.data(), 0, f, b);      // L
     }
-    PIPalm pp;
-    std::memset(&pp, 0, sizeof(pp));
     pp.enabled = 1;
     pp.it = it;
     pp.r2l = r2l ? 1 : 0;
@@ -499,15 +527,29 @@ struct Palm {
   }
 
   fgb_status iteration(int it) {
+    if (hoist) {
+      FGB_CUDA(ctx, cudaEventRecord(ev_it, ctx->stream));
+      FGB_CUDA(ctx, cudaStreamWaitEvent(side2, ev_it, 0));
+      const bool fp64 = sizeof(T) == 8 || p.norm2_fp64;
+      FGB_TRY(launch_power_iteration_many(ctx, sizeof(T) == 8 ? FGB_F64 : FGB_F32, fp64, d_old_chains, J, old_maxn,
+                                          p.norm2_max_iter, p.norm2_threshold, pi_old, side2));
+      FGB_CUDA(ctx, cudaEventRecord(ev_old, side2));
+    }
     FGB_TRY(init_ite());
     for (int s = 0; s < J; ++s) FGB_TRY(update_fact(r2l ? J - 1 - s : s, it));
     if (!p.no_lambda) FGB_TRY(update_lambda());
     return FGB_OK;
   }
 
+  // the run's status word, then the power iterations' (zero or NaN norms)
   fgb_status read_status(int* st) {
-    FGB_CUDA(ctx, cudaMemcpyAsync(st, status, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    int h[3] = {0, 0, 0};
+    FGB_CUDA(ctx, cudaMemcpyAsync(&h[0], status, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    FGB_CUDA(ctx, cudaMemcpyAsync(&h[1], &pi->status, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    if (pi_old)
+      FGB_CUDA(ctx, cudaMemcpyAsync(&h[2], &pi_old->status, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
     FGB_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    *st = h[0] ? h[0] : (h[1] ? h[1] : h[2]);
     return FGB_OK;
   }
 
@@ -517,6 +559,30 @@ struct Palm {
       FGB_CUDA(ctx, cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking));
       FGB_CUDA(ctx, cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming));
       FGB_CUDA(ctx, cudaEventCreateWithFlags(&ev_join, cudaEventDisableTiming));
+    }
+    hoist = !p.constant_step_size && J >= 2 && J <= PI_MAX_CHAINS && !getenv("FGB_NO_PI_HOIST");
+    if (hoist && !d_old_chains) {
+      // chain f: the factors the sweep reaches after f (their buffers do not
+      // move during the run, so the descriptors are built once)
+      std::vector<PIChain> h(J);
+      old_maxn = 1;
+      for (int f = 0; f < J; ++f) {
+        if (!r2l)
+          pi_chain_build(S.data(), f + 1, J, h[f]);
+        else
+          pi_chain_build(S.data(), 0, f, h[f]);
+        if (h[f].nops > PI_MAX_OPS) hoist = false;
+        old_maxn = std::max(old_maxn, h[f].maxdim);
+      }
+      if (hoist) {
+        FGB_TRY(dmalloc(ctx, (void**)&d_old_chains, sizeof(PIChain) * J));
+        FGB_TRY(dmalloc(ctx, (void**)&pi_old, sizeof(PIOut)));
+        FGB_CUDA(ctx, cudaMemcpy(d_old_chains, h.data(), sizeof(PIChain) * J, cudaMemcpyHostToDevice));
+        FGB_CUDA(ctx, cudaMemset(pi_old, 0, sizeof(PIOut)));
+        FGB_CUDA(ctx, cudaStreamCreateWithFlags(&side2, cudaStreamNonBlocking));
+        FGB_CUDA(ctx, cudaEventCreateWithFlags(&ev_it, cudaEventDisableTiming));
+        FGB_CUDA(ctx, cudaEventCreateWithFlags(&ev_old, cudaEventDisableTiming));
+      }
     }
     // iteration 0 eagerly (its zero-norm rule differs), the rest as a graph
     FGB_TRY(iteration(0));

@@ -60,9 +60,9 @@ struct PIStaged {
 
 template <typename TF, typename TC>
 __global__ void __launch_bounds__(PI_THREADS)
-    k_power_iteration(const __grid_constant__ PIChain ca, const __grid_constant__ PIChain cb, int max_iter, TC thr,
-                      const TC* __restrict__ x0, PIOut* out, const __grid_constant__ PIPalm palm, int maxn,
-                      int smem_bytes) {
+    k_power_iteration(const __grid_constant__ PIChain ca, const __grid_constant__ PIChain cb,
+                      const PIChain* __restrict__ dchains, int max_iter, TC thr, const TC* __restrict__ x0, PIOut* out,
+                      const __grid_constant__ PIPalm palm, int maxn, int smem_bytes) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ PIStaged ops[PI_MAX_OPS];
   __shared__ TC s_inv, s_nrm;
@@ -72,7 +72,7 @@ __global__ void __launch_bounds__(PI_THREADS)
   TC* lane = buf2 + maxn;
   unsigned char* pool = reinterpret_cast<unsigned char*>(lane + CR_LANES);
   const long pool_bytes = smem_bytes - (long)(pool - smem_raw);
-  const PIChain& ch = (blockIdx.x == 0) ? ca : cb;
+  const PIChain& ch = dchains ? dchains[blockIdx.x] : ((blockIdx.x == 0) ? ca : cb);
   double result = 1.0;
   int flag = 0;
   int st = 0;
@@ -207,7 +207,9 @@ __global__ void __launch_bounds__(PI_THREADS)
         if (palm.constant_step) {
           cv = divr(TF(1), (TF)palm.step_size);
         } else {
-          const double nR = out->norm[0], nL = out->norm[1];
+          const double own = out->norm[0];
+          const double nR = palm.ext_norm ? (palm.ext_is_r ? *palm.ext_norm : own) : out->norm[0];
+          const double nL = palm.ext_norm ? (palm.ext_is_r ? own : *palm.ext_norm) : out->norm[1];
           if (isnan(nR) || isnan(nL)) atomicCAS(&out->status, 0, (int)FGB_ERR_NAN);
           if ((nR == 0.0 && (palm.it > 0 || !palm.r2l)) || (nL == 0.0 && (palm.it > 0 || palm.r2l)))
             atomicCAS(&out->status, 0, (int)FGB_ERR_ZERO_NORM);
@@ -290,7 +292,8 @@ static fgb_status launch_pi_t(fgb_ctx* ctx, const PIChain& a, const PIChain& b, 
   }
   const TC* x0 = sizeof(TC) == 8 ? (const TC*)(const void*)ctx->x0_d : (const TC*)(const void*)ctx->x0_f;
   (void)d_rand;
-  kern<<<2, PI_THREADS, smem, stream>>>(a, b, max_iter, (TC)thr, x0, d_out, palm, maxn, (int)smem);
+  kern<<<palm.ext_norm ? 1 : 2, PI_THREADS, smem, stream>>>(a, b, nullptr, max_iter, (TC)thr, x0, d_out, palm, maxn,
+                                                            (int)smem);
   FGB_LAUNCHED(ctx);
   return FGB_OK;
 }
@@ -304,6 +307,46 @@ fgb_status launch_power_iteration(fgb_ctx* ctx, fgb_dtype tf, bool fp64, const P
   if (tf == FGB_F32) {
     if (fp64) return launch_pi_t<float, double>(ctx, a, b, max_iter, thr, d_rand, d_out, palm, stream);
     return launch_pi_t<float, float>(ctx, a, b, max_iter, thr, d_rand, d_out, palm, stream);
+  }
+  return fail(ctx, FGB_ERR_NOT_SUPPORTED, "power iteration: F32 or F64 factors");
+}
+
+template <typename TF, typename TC>
+static fgb_status launch_pi_many_t(fgb_ctx* ctx, const PIChain* d_chains, int nchains, int maxn, int max_iter,
+                                   double thr, PIOut* d_out, cudaStream_t stream) {
+  maxn = std::max(1, maxn);
+  const size_t vec = (3 * (size_t)maxn + CR_LANES) * sizeof(TC);
+  const size_t cap = std::min<size_t>(ctx->smem_optin > 4096 ? ctx->smem_optin - 4096 : 0, 220 * 1024);
+  if (vec > cap)
+    return fail(ctx, FGB_ERR_NOT_SUPPORTED, "power iteration: vector of %d entries does not fit on chip", maxn);
+  const size_t smem = cap;
+  auto kern = k_power_iteration<TF, TC>;
+  static thread_local size_t attr_set = 0;
+  if (smem > attr_set) {
+    FGB_CUDA(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    attr_set = smem;
+  }
+  const TC* x0 = sizeof(TC) == 8 ? (const TC*)(const void*)ctx->x0_d : (const TC*)(const void*)ctx->x0_f;
+  PIChain none;
+  std::memset(&none, 0, sizeof(none));
+  none.empty = 1;
+  PIPalm palm;
+  std::memset(&palm, 0, sizeof(palm));
+  kern<<<nchains, PI_THREADS, smem, stream>>>(none, none, d_chains, max_iter, (TC)thr, x0, d_out, palm, maxn,
+                                              (int)smem);
+  FGB_LAUNCHED(ctx);
+  return FGB_OK;
+}
+
+fgb_status launch_power_iteration_many(fgb_ctx* ctx, fgb_dtype tf, bool fp64, const PIChain* d_chains, int nchains,
+                                       int maxn, int max_iter, double thr, PIOut* d_out, cudaStream_t stream) {
+  if (nchains <= 0 || nchains > PI_MAX_CHAINS)
+    return fail(ctx, FGB_ERR_NOT_SUPPORTED, "power iteration: %d chains", nchains);
+  if (!stream) stream = ctx->stream;
+  if (tf == FGB_F64) return launch_pi_many_t<double, double>(ctx, d_chains, nchains, maxn, max_iter, thr, d_out, stream);
+  if (tf == FGB_F32) {
+    if (fp64) return launch_pi_many_t<float, double>(ctx, d_chains, nchains, maxn, max_iter, thr, d_out, stream);
+    return launch_pi_many_t<float, float>(ctx, d_chains, nchains, maxn, max_iter, thr, d_out, stream);
   }
   return fail(ctx, FGB_ERR_NOT_SUPPORTED, "power iteration: F32 or F64 factors");
 }

@@ -9,6 +9,7 @@ namespace fgb {
 
 constexpr int PI_MAX_OPS = 64;
 constexpr int PI_THREADS = 1024;
+constexpr int PI_MAX_CHAINS = 64;
 
 // One sparse product y = S x (or S^H x through the transpose's CSR).
 struct PIOp {
@@ -43,11 +44,18 @@ struct PIPalm {
   const void* lambda;  // FPP device scalar
   void* c;             // FPP device scalar
   void* alpha;         // FPP device scalar
+  // When set, one of the two norms was computed earlier (a chain of factors
+  // that the current sweep has not touched yet): ext_norm points to it and
+  // the launch has one block, whose chain gives the other norm.  ext_is_r:
+  // the external norm is ||R|| (left-to-right sweep) or ||L|| (right to left).
+  const double* ext_norm;
+  int ext_is_r;
+  int pad;
 };
 
 struct PIOut {
-  double norm[2];
-  int flag[2];
+  double norm[PI_MAX_CHAINS];
+  int flag[PI_MAX_CHAINS];
   int status;        // fgb_status of the first failure (0 = ok)
   unsigned done;     // blocks finished (reset by the last one)
 };
@@ -62,6 +70,12 @@ void pi_chain_build(const DevFactor* F, int lo, int hi, PIChain& ch);
 fgb_status launch_power_iteration(fgb_ctx* ctx, fgb_dtype tf, bool fp64, const PIChain& a, const PIChain& b,
                                   int max_iter, double thr, const int* d_rand, PIOut* d_out, const PIPalm& palm,
                                   cudaStream_t stream = nullptr);
+
+// Norms of nchains chains described in DEVICE memory (one block each, no
+// step-size epilogue) into d_out->norm[0..nchains); maxn: the longest vector
+// of any chain.
+fgb_status launch_power_iteration_many(fgb_ctx* ctx, fgb_dtype tf, bool fp64, const PIChain* d_chains, int nchains,
+                                       int maxn, int max_iter, double thr, PIOut* d_out, cudaStream_t stream);
 
 // Raw glibc rand() values after srand(418), length n, in device memory,
 // cached per context size.
