@@ -58,6 +58,37 @@ struct PIStaged {
   int pad;
 };
 
+// The stored entries of one row of one product, held in registers ahead of
+// its use (the first PI_PF of them; longer rows read the rest in place).
+constexpr int PI_PF = 4;
+template <typename TF>
+struct PIRow {
+  int b, e;
+  int c[PI_PF];
+  TF v[PI_PF];
+};
+
+template <typename TF>
+__device__ __forceinline__ void pi_rowptr(const PIStaged& op, int r, int& b, int& e) {
+  if (r < op.rows) {
+    b = op.rp[r];
+    e = op.rp[r + 1];
+  } else {
+    b = e = 0;
+  }
+}
+
+template <typename TF>
+__device__ __forceinline__ void pi_entries(const PIStaged& op, PIRow<TF>& R) {
+  const TF* v = reinterpret_cast<const TF*>(op.v);
+#pragma unroll
+  for (int u = 0; u < PI_PF; ++u)
+    if (R.b + u < R.e) {
+      R.c[u] = op.ci[R.b + u];
+      R.v[u] = v[R.b + u];
+    }
+}
+
 template <typename TF, typename TC>
 __global__ void __launch_bounds__(PI_THREADS)
     k_power_iteration(const __grid_constant__ PIChain ca, const __grid_constant__ PIChain cb,
@@ -128,6 +159,19 @@ __global__ void __launch_bounds__(PI_THREADS)
     int xi = 0;
     for (int i = threadIdx.x; i < n; i += blockDim.x) bufs[0][i] = x0[i];
     __syncthreads();
+    // Software pipeline over the products (the same sequence every
+    // iteration): while product o is computed, a thread reads the row
+    // pointers of its first row of product o + 3 and the entries of that row
+    // of product o + 1, so the L2 latency of the products not staged on chip
+    // overlaps the work of the products before them.
+    const int nops = ch.nops;
+    const int r0 = threadIdx.x;
+    PIRow<TF> P0, P1;
+    int b2, e2, b3, e3;
+    pi_rowptr<TF>(ops[0], r0, P0.b, P0.e);
+    pi_entries<TF>(ops[0], P0);
+    pi_rowptr<TF>(ops[1 % nops], r0, P1.b, P1.e);
+    pi_rowptr<TF>(ops[2 % nops], r0, b2, e2);
     TC lam_old = TC(1), lam = TC(0);
     int it = 0;
     bool zero_vec = false;
@@ -155,18 +199,34 @@ __global__ void __launch_bounds__(PI_THREADS)
       // products ping-pong between the two buffers other than x, which keeps
       // the normalised vector for the dot product
       int si = xi, di = (xi + 1) % 3;
-      for (int o = 0; o < ch.nops; ++o) {
+      for (int o = 0; o < nops; ++o) {
         const PIStaged op = ops[o];
         const TF* __restrict__ val = reinterpret_cast<const TF*>(op.v);
         const TC* src = bufs[si];
         TC* dst = bufs[di];
-        for (int r = threadIdx.x; r < op.rows; r += blockDim.x) {
+        // issue the loads for later products
+        pi_rowptr<TF>(ops[(o + 3) % nops], r0, b3, e3);
+        pi_entries<TF>(ops[(o + 1) % nops], P1);
+        if (r0 < op.rows) {
+          TC acc = TC(0);
+#pragma unroll
+          for (int u = 0; u < PI_PF; ++u)
+            if (P0.b + u < P0.e) acc = fmad((TC)P0.v[u], src[P0.c[u]], acc);
+          for (int p = P0.b + PI_PF; p < P0.e; ++p) acc = fmad((TC)val[p], src[op.ci[p]], acc);
+          dst[r0] = acc;
+        }
+        for (int r = r0 + blockDim.x; r < op.rows; r += blockDim.x) {
           TC acc = TC(0);
           const int p1 = op.rp[r + 1];
           for (int p = op.rp[r]; p < p1; ++p) acc = fmad((TC)val[p], src[op.ci[p]], acc);
           dst[r] = acc;
         }
         __syncthreads();
+        P0 = P1;
+        P1.b = b2;
+        P1.e = e2;
+        b2 = b3;
+        e2 = e3;
         si = di;
         di = 3 - xi - si;
       }
