@@ -50,8 +50,8 @@ struct Shared {
 
 __global__ void __launch_bounds__(THREADS, 1)
     k_bsr_tc(const __grid_constant__ CUtensorMap tmX, const __grid_constant__ CUtensorMap tmB,
-             const int* __restrict__ browptr, const int* __restrict__ bcolind, int nbr, int mtiles,
-             __nv_bfloat16* __restrict__ Y, long ldy, int* __restrict__ err) {
+             const int* __restrict__ browptr, const int* __restrict__ bcolind, int nbr, int nnzb, int stage_idx,
+             int mtiles, __nv_bfloat16* __restrict__ Y, long ldy, int* __restrict__ err) {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   // stage buffers start at a 1024-byte boundary (128-byte swizzle atoms)
   unsigned char* base = reinterpret_cast<unsigned char*>(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
@@ -76,6 +76,19 @@ __global__ void __launch_bounds__(THREADS, 1)
                  "r"((uint32_t)TMEM_COLS));
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
   }
+  // The block structure (row pointers, block columns) is read by every role
+  // for every item: kept in shared memory when it fits, so no role waits on
+  // a global load between items.
+  const int* rp = browptr;
+  const int* cix = bcolind;
+  if (stage_idx) {
+    int* s_rp = reinterpret_cast<int*>(base + STAGES * STAGE_BYTES + ((sizeof(Shared) + 15) & ~(size_t)15));
+    int* s_ci = s_rp + ((nbr + 1 + 3) & ~3);
+    for (int i = threadIdx.x; i <= nbr; i += THREADS) s_rp[i] = browptr[i];
+    for (int i = threadIdx.x; i < nnzb; i += THREADS) s_ci[i] = bcolind[i];
+    rp = s_rp;
+    cix = s_ci;
+  }
   fence_before();
   __syncthreads();
   fence_after();
@@ -93,9 +106,9 @@ __global__ void __launch_bounds__(THREADS, 1)
     for (int u = 0; u < STAGES; ++u) pend[u] = -1;
     for (long it = blockIdx.x; it < items && waited_ok; it += gridDim.x) {
       const int mt = (int)(it / nbr), br = (int)(it % nbr);
-      const int p0 = browptr[br], p1 = browptr[br + 1];
+      const int p0 = rp[br], p1 = rp[br + 1];
       for (int pb = p0; pb < p1 && waited_ok; pb += 32) {
-        const int mine = (pb + lane < p1) ? bcolind[pb + lane] : 0;
+        const int mine = (pb + lane < p1) ? cix[pb + lane] : 0;
         const int nb = min(32, p1 - pb);
         for (int q = 0; q < nb; ++q) {
           const int bc = __shfl_sync(0xffffffffu, mine, q);
@@ -142,7 +155,7 @@ __global__ void __launch_bounds__(THREADS, 1)
       bool ok = true;
       for (long it = blockIdx.x; it < items && ok; it += gridDim.x) {
         const int br = (int)(it % nbr);
-        const int p0 = browptr[br], p1 = browptr[br + 1];
+        const int p0 = rp[br], p1 = rp[br + 1];
         if (p1 == p0) continue;  // empty block row: the epilogue writes zeros
         if (!mbar_wait(&sh->acc_empty[a], aph ^ 1u, abort_flag)) {
           ok = false;
@@ -188,7 +201,7 @@ __global__ void __launch_bounds__(THREADS, 1)
     bool ok = true;
     for (long it = blockIdx.x; it < items && ok; it += gridDim.x) {
       const int mt = (int)(it / nbr), br = (int)(it % nbr);
-      const int p0 = browptr[br], p1 = browptr[br + 1];
+      const int p0 = rp[br], p1 = rp[br + 1];
       const long j = (long)mt * TM + q * 32 + lane;
       uint4* dst = reinterpret_cast<uint4*>(Y + j * ldy + (long)br * BLK);
       if (p1 == p0) {
@@ -302,8 +315,12 @@ fgb_status launch_bsr_tc(fgb_ctx* ctx, const DevFactor& f, const __nv_bfloat16* 
   if (f.bm != 64 || f.bn != 64 || f.nnz == 0) return FGB_OK;
   if (ncols % tc::TM || ldx % 8 || ldy % 8) return FGB_OK;
   if (((uintptr_t)X & 15) || ((uintptr_t)Y & 15)) return FGB_OK;
-  const size_t smem = tc::STAGES * tc::STAGE_BYTES + sizeof(tc::Shared) + 1024;
-  if (smem > ctx->smem_optin) return FGB_OK;
+  const int nbr = f.rows / tc::BLK, mtiles = ncols / tc::TM;
+  const size_t base_smem = tc::STAGES * tc::STAGE_BYTES + ((sizeof(tc::Shared) + 15) & ~(size_t)15) + 1024;
+  if (base_smem > ctx->smem_optin) return FGB_OK;
+  const size_t idx_bytes = sizeof(int) * ((size_t)((nbr + 1 + 3) & ~3) + (size_t)f.nnz);
+  const bool stage_idx = base_smem + idx_bytes <= ctx->smem_optin;
+  const size_t smem = base_smem + (stage_idx ? idx_bytes : 0);
   const __nv_bfloat16* blocks = (const __nv_bfloat16*)f.aux;
   if (!blocks) return FGB_OK;
   CUtensorMap mx, mb;
@@ -314,15 +331,15 @@ fgb_status launch_bsr_tc(fgb_ctx* ctx, const DevFactor& f, const __nv_bfloat16* 
     FGB_TRY(dmalloc(ctx, (void**)&g_err, sizeof(int)));
     FGB_CUDA(ctx, cudaMemset(g_err, 0, sizeof(int)));
   }
-  static bool attr = false;
-  if (!attr) {
+  static size_t attr = 0;
+  if (smem > attr) {
     FGB_CUDA(ctx, cudaFuncSetAttribute(tc::k_bsr_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    attr = true;
+    attr = smem;
   }
-  const int nbr = f.rows / tc::BLK, mtiles = ncols / tc::TM;
   const long items = (long)nbr * mtiles;
   const int grid = (int)std::min<long>(items, ctx->sm_count);
-  tc::k_bsr_tc<<<grid, tc::THREADS, smem, ctx->stream>>>(mx, mb, f.rowptr, f.colind, nbr, mtiles, Y, (long)ldy, g_err);
+  tc::k_bsr_tc<<<grid, tc::THREADS, smem, ctx->stream>>>(mx, mb, f.rowptr, f.colind, nbr, f.nnz, stage_idx ? 1 : 0,
+                                                         mtiles, Y, (long)ldy, g_err);
   FGB_LAUNCHED(ctx);
   *taken = true;
   return FGB_OK;

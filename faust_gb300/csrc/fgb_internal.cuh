@@ -145,14 +145,26 @@ __device__ __forceinline__ double divr(double a, double b) { return __ddiv_rn(a,
 __device__ __forceinline__ float sqrtr(float a) { return __fsqrt_rn(a); }
 __device__ __forceinline__ double sqrtr(double a) { return __dsqrt_rn(a); }
 
-// Tree over 256 lane partials held in shared memory `lane` (256 threads call).
+// Pairwise tree over 256 lane partials held in shared memory `lane` (every
+// thread of the block calls; blocks of at least 32 threads): level s adds
+// lane t + s into lane t for t < s, s = 128, 64, ..., 1.  One warp evaluates
+// it -- the three upper levels in registers (lane t of the warp holds the
+// partials t, t + 32, t + 64, t + 96 of level 128), the five lower ones by
+// shuffles -- with the same additions in the same association as the
+// level-by-level form.  lane[0] carries the result to the block.
 template <typename T>
 __device__ __forceinline__ T lane_tree_256(T* lane) {
-  const int t = threadIdx.x;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    const int t = threadIdx.x;
+    const T a0 = addr(lane[t], lane[t + 128]);
+    const T a1 = addr(lane[t + 32], lane[t + 160]);
+    const T a2 = addr(lane[t + 64], lane[t + 192]);
+    const T a3 = addr(lane[t + 96], lane[t + 224]);
+    T c = addr(addr(a0, a2), addr(a1, a3));
 #pragma unroll
-  for (int s = CR_LANES / 2; s >= 1; s >>= 1) {
-    __syncthreads();
-    if (t < s) lane[t] = addr(lane[t], lane[t + s]);
+    for (int s = 16; s >= 1; s >>= 1) c = addr(c, __shfl_down_sync(0xffffffffu, c, s));
+    if (t == 0) lane[0] = c;
   }
   __syncthreads();
   T r = lane[0];
