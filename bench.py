@@ -180,9 +180,11 @@ def run_faust_x(args, rank, world):
     W.setup(ctx)
     fused = False
     if W.name != "bsr":
-        # decide which path automatic mode takes: fused when it fits
-        from ctypes import c_int
-        fused = len(W.facs) > 1
+        # the path automatic mode takes: the fused chain when the
+        # intermediates would not stay in L2 (a quarter of it), else one launch
+        # per factor
+        l2 = torch.cuda.get_device_properties(torch.cuda.current_device()).L2_cache_size
+        fused = len(W.facs) > 1 and W.n * W.ncols * np.dtype(W.np_dtype).itemsize > l2 // 4
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
     for _ in range(args.warmup):
         W.step()
@@ -215,7 +217,28 @@ def run_faust_x(args, rank, world):
     e2e_ms = float(np.median(e2e)) * 1e3
     hbm, tflops, peak_kind = _peaks()
     kb = W.kernel_bytes(fused)
-    achieved = kb / (step_ms / 1e3 / (1 if fused else len(W.factor_bytes()))) / 1e9
+    launch_s = step_ms / 1e3 / (1 if fused else len(W.factor_bytes()))
+    achieved = kb / launch_s / 1e9
+    if W.name == "csr_random":
+        # FP64 on L2-resident operands: the scalar FP64 pipe bounds the
+        # per-factor products (10 dependent FMAs per entry)
+        peak = fp64_peak(ctx)
+        fl = W.flops / len(W.facs)
+        roof = {"bound": "fp64", "achieved": round(fl / launch_s / 1e12, 4), "peak": round(peak, 4),
+                "unit": "TFLOP/s", "frac": round(fl / launch_s / 1e12 / peak, 4), "traffic": None,
+                "peak_kind": "measured in this run (FP64 FMA loop on all SMs)",
+                "kernel": "k_csr_chain_fused" if fused else "k_csr_spmm",
+                "algorithmic_flops_per_launch": int(fl), "algorithmic_bytes_per_launch": int(kb)}
+    elif W.name == "bsr":
+        fl = W.flops / len(W.bsr)
+        roof = {"bound": "tensor", "achieved": round(fl / launch_s / 1e12, 1), "peak": tflops, "unit": "TFLOP/s",
+                "frac": round(fl / launch_s / 1e12 / tflops, 4), "traffic": 255876096,
+                "traffic_note": "dram read + write bytes of one launch, ncu capture", "peak_kind": peak_kind,
+                "kernel": "k_bsr_tc", "algorithmic_flops_per_launch": int(fl), "algorithmic_bytes_per_launch": int(kb)}
+    else:
+        roof = {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
+                "frac": round(achieved / hbm, 4), "traffic": None, "peak_kind": peak_kind,
+                "kernel": "k_csr_chain_fused" if fused else "k_csr_spmm", "algorithmic_bytes_per_launch": int(kb)}
     value = W.step_bytes * world / (step_ms / 1e3) / 1e9
     out = {
         "metric": METRIC, "submetric": "Faust.X effective GB/s (per-factor algorithmic bytes / step time)",
@@ -224,10 +247,7 @@ def run_faust_x(args, rank, world):
         "dtype": W.dtype, "data": "synthetic (seeded)",
         "config": {"workload": W.name, "desc": W.desc, "l2": "flushed (256 MB write) before every timed step",
                    "path": "fused chain kernel" if fused else "one launch per factor"},
-        "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
-                     "frac": round(achieved / hbm, 4), "traffic": None, "peak_kind": peak_kind,
-                     "kernel": "k_csr_chain_fused" if fused else "k_csr_spmm / k_bsr",
-                     "algorithmic_bytes_per_launch": int(kb)},
+        "roofline": roof,
         "e2e": {"value": round(W.step_bytes / (e2e_ms / 1e3) / 1e9, 2), "unit": "GB/s",
                 "ms_per_step": round(e2e_ms, 3),
                 "h2d_bytes_per_step": int(W.n * W.ncols * W.es), "d2h_bytes_per_step": int(W.n * W.ncols * W.es)},

@@ -203,6 +203,18 @@ static fgb_status fused_desc_t(fgb_faust* F) {
   return FGB_OK;
 }
 
+// Automatic mode: the fused chain saves the intermediate products' trips
+// through memory, which only matters when they would leave L2; when every
+// intermediate fits in L2 the per-factor launches (whole grid per factor,
+// more rows in flight) are faster.  Threshold: a quarter of the L2.
+static bool fused_pays(const fgb_faust* F, int ncols) {
+  int dev = F->ctx->device, l2 = 0;
+  cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, dev);
+  size_t maxrows = 0;
+  for (auto& f : F->f) maxrows = std::max(maxrows, (size_t)std::max(f.rows, f.cols));
+  return maxrows * (size_t)ncols * dtype_size(F->dtype) > (size_t)std::max(l2, 1) / 4;
+}
+
 static bool all_csr(const fgb_faust* F) {
   for (auto& f : F->f)
     if (f.format != FGB_CSR) return false;
@@ -305,7 +317,7 @@ fgb_status fgb_faust_mul(fgb_faust* F, const void* X, int ldx, int ncols, void* 
   }
   if (mode == 2 && !fits)
     return fail(ctx, FGB_ERR_NOT_SUPPORTED, "fused chain: factors do not fit on chip (or not CSR)");
-  if (fits && (mode == 2 || (mode == 0 && F->f.size() > 1)))
+  if (fits && (mode == 2 || (mode == 0 && F->f.size() > 1 && fused_pays(F, ncols))))
     return chain_fused(ctx, F->dtype, (const ChainDesc*)F->chain_desc, (int)F->f.size(), X, ldx, ncols, Y, ldy,
                        max_dim(F), false, nullptr);
   return mul_per_factor(F, X, ldx, ncols, Y, ldy);
@@ -334,7 +346,7 @@ fgb_status fgb_faust_mul_op(fgb_faust* F, char op, const void* X, int ldx, int n
                 &fits);
   }
   if (mode == 2 && !fits) return fail(ctx, FGB_ERR_NOT_SUPPORTED, "fused chain: factors do not fit on chip");
-  if (fits && (mode == 2 || (mode == 0 && F->f.size() > 1)))
+  if (fits && (mode == 2 || (mode == 0 && F->f.size() > 1 && fused_pays(F, ncols))))
     return chain_fused(ctx, F->dtype, (const ChainDesc*)F->chain_desc_t, (int)F->f.size(), X, ldx, ncols, Y, ldy,
                        maxd, false, nullptr);
   return mul_per_factor_t(F, X, ldx, ncols, Y, ldy);
