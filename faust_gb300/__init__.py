@@ -5,7 +5,9 @@ Python API (mirrors pyfaust):
   Faust(factors)            device-resident product of CSR / BSR factors
   F @ X                     Faust x dense (host arrays or CUDA tensors)
   F.norm(2)                 FP64 power-iteration 2-norm
+  F.save(path) / Faust.load(path)  MAT5 'faust_factors' files
   fact.palm4msa(M, cons, params)   palm4msa2 on the GPU
+  fact.hierarchical(M, params)     hierarchical factorization (PALM chain)
   proj.sp / splincol / ...  constraint descriptions
 """
 from . import _ffi

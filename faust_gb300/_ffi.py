@@ -81,6 +81,7 @@ _SIGS = {
                                    ctypes.POINTER(_I)]),
     "fgb_faust_factor_to_dense": (_I, [_P, _I, _P]),
     "fgb_faust_factor_to_csr": (_I, [_P, _I, _P, _P, _P]),
+    "fgb_faust_factor_to_bsr": (_I, [_P, _I, _P, _P, _P]),
     "fgb_prox": (_I, [_P, _I, ctypes.POINTER(Constraint), _P]),
     "fgb_prox_noalloc": (_I, [_P, _I, ctypes.POINTER(Constraint), _P, _P]),
     "fgb_palm_params_default": (_I, [ctypes.POINTER(PalmParams)]),

@@ -420,6 +420,22 @@ fgb_status fgb_faust_factor_to_csr(fgb_faust* F, int i, int* host_rowptr, int* h
   return FGB_OK;
 }
 
+fgb_status fgb_faust_factor_to_bsr(fgb_faust* F, int i, int* host_browptr, int* host_bcolind, void* host_blocks) {
+  if (!F || i < 0 || i >= (int)F->f.size()) return FGB_ERR_INVALID_ARG;
+  fgb_ctx* ctx = F->ctx;
+  const DevFactor& f = F->f[i];
+  if (f.format != FGB_BSR) return fail(ctx, FGB_ERR_NOT_SUPPORTED, "factor is not BSR");
+  FGB_CUDA(ctx, cudaSetDevice(ctx->device));
+  FGB_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  FGB_CUDA(ctx, cudaMemcpy(host_browptr, f.rowptr, sizeof(int) * (f.rows / f.bm + 1), cudaMemcpyDeviceToHost));
+  if (f.nnz) {
+    FGB_CUDA(ctx, cudaMemcpy(host_bcolind, f.colind, sizeof(int) * f.nnz, cudaMemcpyDeviceToHost));
+    FGB_CUDA(ctx, cudaMemcpy(host_blocks, f.val, dtype_size(F->dtype) * (size_t)f.nnz * f.bm * f.bn,
+                             cudaMemcpyDeviceToHost));
+  }
+  return FGB_OK;
+}
+
 fgb_status fgb_faust_factor_to_dense(fgb_faust* F, int i, void* host_dense) {
   if (!F || i < 0 || i >= (int)F->f.size() || !host_dense) return FGB_ERR_INVALID_ARG;
   fgb_ctx* ctx = F->ctx;

@@ -241,6 +241,36 @@ class Faust:
               self.ctx.handle)
         return sp.csr_matrix((v[:nnz.value], ci[:nnz.value], rp), shape=(r.value, c.value))
 
+    def bsr_factor(self, i):
+        """Factor i of a BF16 Faust as a BSRFactor (copied to host)."""
+        fmt, r, c, nb = ctypes.c_int(), ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        check(_ffi.lib().fgb_faust_factor_info(self.handle, int(i), ctypes.byref(fmt), ctypes.byref(r),
+                                               ctypes.byref(c), ctypes.byref(nb)), self.ctx.handle)
+        if fmt.value != _ffi.BSR:
+            raise ValueError("factor %d is not BSR" % i)
+        brow = np.zeros(r.value // 64 + 1, np.int32)
+        bcol = np.zeros(max(1, nb.value), np.int32)
+        blocks = np.zeros((max(1, nb.value), 64, 64), np.uint16)  # [j][c][r]: column-major blocks
+        check(_ffi.lib().fgb_faust_factor_to_bsr(self.handle, int(i), brow.ctypes.data, bcol.ctypes.data,
+                                                 blocks.ctypes.data), self.ctx.handle)
+        n = nb.value
+        return BSRFactor(r.value, c.value, brow, bcol[:n], blocks[:n].transpose(0, 2, 1))
+
+    def save(self, filepath, format="Matlab"):
+        """Writes the Faust as a MAT5 file (Faust.save / Transform::save_mat_file,
+        faust_Transform.hpp:434-475): variable 'faust_factors', a 1 x J cell."""
+        if format != "Matlab":
+            raise ValueError("only the Matlab (.mat) format is supported")
+        from . import matio
+        matio.save(self, filepath)
+
+    @staticmethod
+    def load(filepath, ctx=None):
+        """Reads a Faust from a .mat file (Transform::read_from_mat_file,
+        faust_Transform.hpp:481-514)."""
+        from . import matio
+        return matio.load(filepath, ctx)
+
     def toarray(self):
         """Full product: F applied to the identity."""
         return self @ np.eye(self.shape[1], dtype=self.dtype)

@@ -128,6 +128,10 @@ fgb_status fgb_faust_spectral_norm(fgb_faust* F, int max_iter, double threshold,
 fgb_status fgb_faust_factor_info(const fgb_faust* F, int i, int* format, int* rows, int* cols, int* nnz);
 fgb_status fgb_faust_factor_to_dense(fgb_faust* F, int i, void* host_dense);
 fgb_status fgb_faust_factor_to_csr(fgb_faust* F, int i, int* host_rowptr, int* host_colind, void* host_values);
+/* BSR factor i copied to host as stored: browptr[rows/bm + 1], bcolind[nblocks]
+ * and nblocks column-major bm x bn blocks (MatBSR's layout, faust_MatBSR.h:41-145;
+ * read back by the .mat writer, MatBSR::toMatIOVar, faust_MatBSR.hpp:387-470). */
+fgb_status fgb_faust_factor_to_bsr(fgb_faust* F, int i, int* host_browptr, int* host_bcolind, void* host_blocks);
 
 /* ------------------------------------------------------------------ projections
  * Constraint kinds: ConstraintName (faust_ConstraintGeneric.h:49-70). */

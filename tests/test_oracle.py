@@ -259,6 +259,33 @@ def test_hierarchical_wht_factorizes_hadamard(oracle, n):
     assert oracle.rel_err(A, S, lam) < 1e-12
 
 
+def _hadamard32_config(oracle):
+    """The hierarchical configuration of the reference's Hadamard tests
+    (misc/config_file/mat/config_HADAMARD_32.mat, extracted by
+    tests/golden/make_golden.py) as oracle constraint dicts."""
+    import json
+    with open(os.path.join(GOLDEN, "config_HADAMARD_32_params.json")) as f:
+        p = json.load(f)
+    kinds = {"sp": oracle.SP, "spcol": oracle.SPCOL, "splin": oracle.SPLIN, "splincol": oracle.SPLINCOL}
+    fc, rc = [[dict(kind=kinds[c[0]], k=c[1], rows=c[2], cols=c[3]) for c in row] for row in p["cons"]]
+    return p, fc, rc
+
+
+def test_hierarchical_hadamard32_reference_config(oracle):
+    """config_HADAMARD_32.mat equals pyfaust's WHT parameters for n = 5, and
+    with it (update_way 1 = right-to-left, faust_init_from_matio_params.hpp:142-148)
+    the 32 x 32 Hadamard matrix factorizes exactly into nfacts factors."""
+    p, fc, rc = _hadamard32_config(oracle)
+    assert (p["nfacts"], p["nrow"], p["ncol"]) == (5, 32, 32)
+    assert (fc, rc) == _wht_cons(oracle, 5)
+    A = synth.hadamard(p["nrow"]).astype(np.float64)
+    S, lam = oracle.hierarchical(A, fc, rc, p["niter1"], p["niter2"],
+                                 is_update_way_R2L=bool(p["update_way"]), packing_RL=False)
+    assert len(S) == p["nfacts"]
+    assert all(np.count_nonzero(f) == 2 * 32 for f in S)
+    assert oracle.rel_err(A, S, lam) < 1e-12
+
+
 def test_hierarchical_left_side_shapes(oracle):
     """is_fact_side_left: the residual is split on the left; factor shapes
     and the global constraint order follow faust_hierarchical.hpp:101-121."""

@@ -288,6 +288,29 @@ def test_hierarchical_wht_bitexact(oracle):
 
 
 @pytest.mark.parametrize("dtype", [np.float64, np.float32])
+def test_hierarchical_hadamard32_reference_config(oracle, dtype):
+    """The reference's Hadamard test configuration (config_HADAMARD_32.mat,
+    committed as JSON): factors and lambda equal the oracle's in double and
+    float, and the float factorization is exact to float rounding."""
+    import json
+    with open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden",
+                           "config_HADAMARD_32_params.json")) as f:
+        p = json.load(f)
+    fc, rc = [[fact.ConstraintInt(c[0], c[2], c[3], c[1]) for c in row] for row in p["cons"]]
+    A = synth.hadamard(p["nrow"]).astype(dtype)
+    r2l = bool(p["update_way"])
+    res = fact.hierarchical(A, fact.ParamsHierarchical(fc, rc, p["niter1"], p["niter2"],
+                                                       is_update_way_R2L=r2l, packing_RL=False))
+    got = _dense_factors(res.faust)
+    ref, lam = oracle.hierarchical(A, [c.oracle_dict() for c in fc], [c.oracle_dict() for c in rc],
+                                   p["niter1"], p["niter2"], is_update_way_R2L=r2l, packing_RL=False)
+    assert np.float64(res.lambda_) == np.float64(lam)
+    assert len(got) == p["nfacts"] and all(np.array_equal(a, b) for a, b in zip(got, ref))
+    assert oracle.rel_err(A, got, res.lambda_) < (1e-12 if dtype == np.float64 else 1e-5)
+    res.faust.close()
+
+
+@pytest.mark.parametrize("dtype", [np.float64, np.float32])
 def test_hierarchical_left_side_sp_bitexact(oracle, dtype):
     rng = np.random.default_rng(5)
     A = rng.standard_normal((40, 24)).astype(dtype)
