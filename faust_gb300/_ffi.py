@@ -15,6 +15,7 @@ STATUS_NAMES = {0: "OK", 1: "INVALID_ARG", 2: "OOM", 3: "CUDA", 4: "NAN", 5: "ZE
                 7: "TIMEOUT", 8: "NOT_SUPPORTED"}
 F32, F64, BF16 = 0, 1, 2
 CSR, BSR = 0, 1
+ORDER_DEFAULT_L2R, ORDER_DYNPROG = 0, 5
 # Constraint kinds (fgb_cons_kind).
 SP, SPCOL, SPLIN, SPLINCOL, NORMCOL, NORMLIN, SUPP, SP_POS = range(8)
 
@@ -75,6 +76,9 @@ _SIGS = {
     "fgb_faust_shape": (_I, [_P, ctypes.POINTER(_I), ctypes.POINTER(_I), ctypes.POINTER(_I)]),
     "fgb_faust_mul": (_I, [_P, _P, _I, _I, _P, _I, _I]),
     "fgb_faust_mul_op": (_I, [_P, ctypes.c_char, _P, _I, _I, _P, _I, _I]),
+    "fgb_faust_product": (_I, [_P, ctypes.c_char, _I, _P, _I]),
+    "fgb_faust_mul_dynprog": (_I, [_P, ctypes.c_char, _P, _I, _I, _P, _I]),
+    "fgb_dynprog_plan": (_I, [_I, _P, _P, _P, _P, ctypes.c_char, _P]),
     "fgb_faust_mul_host": (_I, [_P, _P, _I, _P]),
     "fgb_faust_spectral_norm": (_I, [_P, _I, _D, ctypes.POINTER(_D), ctypes.POINTER(_I)]),
     "fgb_faust_factor_info": (_I, [_P, _I, ctypes.POINTER(_I), ctypes.POINTER(_I), ctypes.POINTER(_I),

@@ -243,6 +243,7 @@ fgb_faust::~fgb_faust() {
   fgb::dfree(dy);
   fgb::dfree(chain_desc);
   fgb::dfree(chain_desc_t);
+  fgb::dfree(pws);
   if (hx) cudaFreeHost(hx);
   if (hy) cudaFreeHost(hy);
 }

@@ -115,6 +115,9 @@ struct fgb_faust {
   // chain of transposed factors in reverse order).
   void* chain_desc = nullptr;
   void* chain_desc_t = nullptr;
+  // Workspace of the dense product (intermediates and dense images).
+  void* pws = nullptr;
+  size_t pws_bytes = 0;
   // When set, the factor arrays are views into this shared device block
   // (results of one batched call) and are released with its last owner.
   std::shared_ptr<void> pool;

@@ -94,6 +94,34 @@ class BSRFactor:
         return int(self.bcolind.size)
 
 
+def _order_code(order):
+    codes = {"DEFAULT_L2R": _ffi.ORDER_DEFAULT_L2R, "DYNPROG": _ffi.ORDER_DYNPROG}
+    if isinstance(order, str):
+        if order.upper() not in codes:
+            raise ValueError("order must be DEFAULT_L2R or DYNPROG")
+        return codes[order.upper()]
+    return int(order)
+
+
+def _torch_dtype(dt):
+    import torch
+    return {np.dtype(np.float32): torch.float32, np.dtype(np.float64): torch.float64}[np.dtype(dt)]
+
+
+def dynprog_plan(leaves, op="N"):
+    """Split table of the library's DYNPROG (host code, no device):
+    leaves = [(rows, cols, nnz, is_dense)]; returns {(i, j): k}."""
+    n = len(leaves)
+    a = np.asarray(leaves, np.int64).reshape(n, 4)
+    rows, cols, nnz, dense = (np.ascontiguousarray(a[:, q], np.int32) for q in range(4))
+    split = np.zeros(n * n, np.int32)
+    rc = _ffi.lib().fgb_dynprog_plan(n, rows.ctypes.data, cols.ctypes.data, nnz.ctypes.data, dense.ctypes.data,
+                                     op.upper().encode(), split.ctypes.data)
+    if rc != 0:
+        raise ValueError("fgb_dynprog_plan failed (%d)" % rc)
+    return {(i, j): int(split[i * n + j]) for i in range(n) for j in range(i + 1, n)}
+
+
 def _is_colmajor(T):
     rows, cols = T.shape
     return (T.stride(0) == 1 or rows == 1) and (cols == 1 or T.stride(1) >= rows)
@@ -219,6 +247,39 @@ class Faust:
                                           _ld(Y), int(mode)), self.ctx.handle)
         return Y
 
+    def product_device(self, op="N", order="DEFAULT_L2R", Y=None):
+        """Dense op(F) on the device (TransformHelper::get_product): order
+        'DEFAULT_L2R' (Transform::get_product) or 'DYNPROG' (dynprog_multiply).
+        Returns a column-major CUDA tensor."""
+        import torch
+        op = op.upper()
+        code = _order_code(order)
+        rows, cols = self.shape if op == "N" else self.shape[::-1]
+        if Y is None:
+            Y = torch.empty((cols, rows), dtype=_torch_dtype(self.dtype), device="cuda:%d" % self.ctx.device).t()
+        elif not _is_colmajor(Y) or tuple(Y.shape) != (rows, cols):
+            raise ValueError("Y must be a column-major %d x %d tensor" % (rows, cols))
+        check(_ffi.lib().fgb_faust_product(self.handle, op.encode(), code, Y.data_ptr(), _ld(Y)), self.ctx.handle)
+        return Y
+
+    def matmul_dynprog_device(self, X, op="N", Y=None):
+        """Y = op(F) X with the product order chosen by DYNPROG
+        (TransformHelper::multiply with mul_order_opt_mode DYNPROG)."""
+        import torch
+        op = op.upper()
+        rows_in, rows_out = (self.shape[1], self.shape[0]) if op == "N" else self.shape
+        if X.shape[0] != rows_in:
+            raise ValueError("dimensions do not match: %s(F) with F %s @ %s" % (op, self.shape, tuple(X.shape)))
+        Xc = X if _is_colmajor(X) else X.t().contiguous().t()
+        ncols = X.shape[1]
+        if Y is None:
+            Y = torch.empty((ncols, rows_out), dtype=X.dtype, device=X.device).t()
+        elif not _is_colmajor(Y):
+            raise ValueError("Y must be column-major")
+        check(_ffi.lib().fgb_faust_mul_dynprog(self.handle, op.encode(), Xc.data_ptr(), _ld(Xc), ncols, Y.data_ptr(),
+                                               _ld(Y)), self.ctx.handle)
+        return Y
+
     def norm(self, ord=2, max_iter=100, threshold=1e-6):
         """2-norm by FP64 power iteration (TransformHelper::spectralNorm)."""
         if ord != 2:
@@ -271,9 +332,14 @@ class Faust:
         from . import matio
         return matio.load(filepath, ctx)
 
-    def toarray(self):
-        """Full product: F applied to the identity."""
-        return self @ np.eye(self.shape[1], dtype=self.dtype)
+    def toarray(self, order="DEFAULT_L2R"):
+        """Full product as a host array (pyfaust Faust.toarray: get_product).
+        BF16 BSR Fausts: F applied to the identity."""
+        if self.dtype_code == _ffi.BF16:
+            return self @ np.eye(self.shape[1], dtype=self.dtype)
+        Y = self.product_device("N", order)
+        self.ctx.synchronize()
+        return Y.cpu().numpy()
 
     def close(self):
         if getattr(self, "handle", None):

@@ -110,6 +110,31 @@ fgb_status fgb_faust_mul(fgb_faust* F, const void* X, int ldx, int ncols, void* 
 // (CPU/faust_Transform.hpp:1754-1773, the 'T' / 'H' branches).
 fgb_status fgb_faust_mul_op(fgb_faust* F, char op, const void* X, int ldx, int ncols, void* Y, int ldy, int mode);
 
+/* Product orders: the values of FaustMulMode (CPU/faust_prod_opt.h:12-60)
+ * that the device path runs. */
+enum { FGB_ORDER_DEFAULT_L2R = 0, FGB_ORDER_DYNPROG = 5 };
+
+/* Y = op(F) as a dense column-major matrix on the device (ldy >= its rows),
+ * TransformHelper<FPP,Cpu>::get_product(mul_order_opt_mode)
+ * (CPU/faust_TransformHelper.hpp:1132-1178):
+ *   FGB_ORDER_DEFAULT_L2R  Transform::get_product (CPU/faust_Transform.hpp:598-656)
+ *   FGB_ORDER_DYNPROG      dynprog_multiply (faust_prod_opt_gen.hpp:80-202)
+ * op 'N', 'T' or 'H' ('H' = 'T' for real scalars).  CSR Fausts only. */
+fgb_status fgb_faust_product(fgb_faust* F, char op, int order, void* Y, int ldy);
+
+/* Y = op(F) X in the DYNPROG order, X dense (device, column-major) as the
+ * last operand of the chain: TransformHelper::multiply(const MatDense&) with
+ * mul_order_opt_mode == DYNPROG (CPU/faust_TransformHelper.hpp:373-379). */
+fgb_status fgb_faust_mul_dynprog(fgb_faust* F, char op, const void* X, int ldx, int ncols, void* Y, int ldy);
+
+/* Host-only: the DYNPROG split table for a chain of n leaves (stored rows,
+ * cols, nonzeros, is_dense per leaf; op 'N' or 'T').  split[i*n + j] = k
+ * for i < j means the product of leaves i..j is (i..k)(k+1..j); other cells
+ * are -1.  The cost model is the reference's (CPU/faust_prod_opt.cpp:1-80,
+ * faust_prod_opt_gen.hpp:113-190) in 32-bit two's complement arithmetic. */
+fgb_status fgb_dynprog_plan(int n, const int* rows, const int* cols, const int* nnz, const int* is_dense, char op,
+                            int* split);
+
 /* Y = F X with X, Y in HOST memory: copy in, product, copy out, synchronous.
  * Replaces TransformHelper<FPP,Cpu>::multiply(const FPP* A, int A_ncols,
  * FPP* C) (CPU/faust_TransformHelper.hpp:406-433) and

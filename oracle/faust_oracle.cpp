@@ -868,6 +868,60 @@ static int chain_mul_impl(int nfac, const int* dims, const int* rowptr, const in
   })
 }
 
+// Pairwise products of the dense Faust product (dynprog_multiply_rec,
+// faust_prod_opt_gen.hpp:8-79): Y = S X with S one CSR matrix, Y = X S^T
+// given the CSR of S, and dense x dense with a sequential fma over k
+// ascending from +0 (every entry; no fma past the inner dimension).
+template <typename T>
+static int spmm_impl(int rows, int cols, const int* rowptr, const int* colind, const T* val, const T* X, int ncols,
+                     T* Y) {
+  ORC_TRY({
+    Csr<T> S;
+    S.rows = rows;
+    S.cols = cols;
+    S.rowptr.assign(rowptr, rowptr + rows + 1);
+    S.colind.assign(colind, colind + S.rowptr[rows]);
+    S.val.assign(val, val + S.rowptr[rows]);
+    Dense<T> M(cols, ncols);
+    std::memcpy(M.a.data(), X, sizeof(T) * M.a.size());
+    Dense<T> R = spmm(S, M);
+    std::memcpy(Y, R.a.data(), sizeof(T) * R.a.size());
+  })
+}
+
+template <typename T>
+static int dense_csrT_impl(int xrows, const T* X, int srows, int scols, const int* rowptr, const int* colind,
+                           const T* val, T* Y) {
+  ORC_TRY({
+    Csr<T> S;
+    S.rows = srows;
+    S.cols = scols;
+    S.rowptr.assign(rowptr, rowptr + srows + 1);
+    S.colind.assign(colind, colind + S.rowptr[srows]);
+    S.val.assign(val, val + S.rowptr[srows]);
+    Dense<T> M(xrows, scols);
+    std::memcpy(M.a.data(), X, sizeof(T) * M.a.size());
+    Dense<T> R = dense_times_csrT(M, S);
+    std::memcpy(Y, R.a.data(), sizeof(T) * R.a.size());
+  })
+}
+
+template <typename T>
+static void gemm_seq(int m, int n, int k, const T* A, const T* B, T* C) {
+#pragma omp parallel for schedule(static)
+  for (int q = 0; q < n; ++q)
+    for (int r = 0; r < m; ++r) {
+      T acc = T(0);
+      for (int p = 0; p < k; ++p) acc = fma_(A[(size_t)p * m + r], B[(size_t)q * k + p], acc);
+      C[(size_t)q * m + r] = acc;
+    }
+}
+
+template <typename T>
+static int gemm_seq_impl(int m, int n, int k, const T* A, const T* B, T* C) {
+  ORC_TRY({ gemm_seq(m, n, k, A, B, C); })
+}
+
 template <typename T>
 static std::vector<Cons<T>> unpack_cons(int J, const int* ikind, const long* ik, const double* s, const int* flags,
                                         const int* cdims, const T* supp_concat) {
@@ -951,6 +1005,29 @@ int orc_chain_mul_f64(int nfac, const int* dims, const int* rowptr, const int* c
 int orc_chain_mul_f32(int nfac, const int* dims, const int* rowptr, const int* colind, const float* val,
                       const float* X, int xrows, int ncols, float* Y) {
   return chain_mul_impl<float>(nfac, dims, rowptr, colind, val, X, xrows, ncols, Y);
+}
+
+int orc_spmm_f64(int rows, int cols, const int* rp, const int* ci, const double* v, const double* X, int ncols,
+                 double* Y) {
+  return spmm_impl<double>(rows, cols, rp, ci, v, X, ncols, Y);
+}
+int orc_spmm_f32(int rows, int cols, const int* rp, const int* ci, const float* v, const float* X, int ncols,
+                 float* Y) {
+  return spmm_impl<float>(rows, cols, rp, ci, v, X, ncols, Y);
+}
+int orc_dense_csrT_f64(int xrows, const double* X, int srows, int scols, const int* rp, const int* ci,
+                       const double* v, double* Y) {
+  return dense_csrT_impl<double>(xrows, X, srows, scols, rp, ci, v, Y);
+}
+int orc_dense_csrT_f32(int xrows, const float* X, int srows, int scols, const int* rp, const int* ci, const float* v,
+                       float* Y) {
+  return dense_csrT_impl<float>(xrows, X, srows, scols, rp, ci, v, Y);
+}
+int orc_gemm_seq_f64(int m, int n, int k, const double* A, const double* B, double* C) {
+  return gemm_seq_impl<double>(m, n, k, A, B, C);
+}
+int orc_gemm_seq_f32(int m, int n, int k, const float* A, const float* B, float* C) {
+  return gemm_seq_impl<float>(m, n, k, A, B, C);
 }
 
 int orc_bsr_mul_f64(int m, int n, int bm, int bn, const int* browptr, const int* bcolind, const double* blocks,

@@ -242,3 +242,158 @@ def hierarchical(A, fac_cons, res_cons, its_2facts, its_global, is_fact_side_lef
                               init_lambda=glo, **palm_kw)
         S = list(S)
     return S, glo
+
+
+# ---------------------------------------------------------------- dense product
+def _csr(S):
+    import scipy.sparse as sps
+    S = sps.csr_matrix(S)
+    S.sort_indices()
+    return S
+
+
+def _csr_op(S, op):
+    """CSR of op(S); a transposed row lists entries by increasing original row."""
+    return _csr(S) if op == "N" else _csr(_csr(S).T)
+
+
+def _spmm(S, X):
+    S = _csr(S)
+    X = np.asfortranarray(X, dtype=S.dtype)
+    Y = np.zeros((S.shape[0], X.shape[1]), S.dtype, order="F")
+    fn = lib().orc_spmm_f64 if S.dtype == np.float64 else lib().orc_spmm_f32
+    rp, ci = S.indptr.astype(np.int32), S.indices.astype(np.int32)
+    _check(fn(S.shape[0], S.shape[1], _p(rp), _p(ci), _p(np.ascontiguousarray(S.data)), _p(X), X.shape[1], _p(Y)))
+    return Y
+
+
+def _dense_csrT(X, S):
+    """Y = X S^T given the CSR of S: y[r, c] = sequential fma over row c of S."""
+    S = _csr(S)
+    X = np.asfortranarray(X, dtype=S.dtype)
+    Y = np.zeros((X.shape[0], S.shape[0]), S.dtype, order="F")
+    fn = lib().orc_dense_csrT_f64 if S.dtype == np.float64 else lib().orc_dense_csrT_f32
+    rp, ci = S.indptr.astype(np.int32), S.indices.astype(np.int32)
+    _check(fn(X.shape[0], _p(X), S.shape[0], S.shape[1], _p(rp), _p(ci), _p(np.ascontiguousarray(S.data)), _p(Y)))
+    return Y
+
+
+def _gemm_seq(A, B):
+    A = np.asfortranarray(A)
+    B = np.asfortranarray(B, dtype=A.dtype)
+    C = np.zeros((A.shape[0], B.shape[1]), A.dtype, order="F")
+    fn = lib().orc_gemm_seq_f64 if A.dtype == np.float64 else lib().orc_gemm_seq_f32
+    _check(fn(A.shape[0], B.shape[1], A.shape[1], _p(A), _p(B), _p(C)))
+    return C
+
+
+def _w32(v):
+    """C int arithmetic of the reference's cost model: two's complement wrap."""
+    v &= 0xFFFFFFFF
+    return v - (1 << 32) if v >= (1 << 31) else v
+
+
+def _div32(a, b):
+    if b == 0:
+        return 0
+    q = abs(a) // abs(b)
+    return q if (a >= 0) == (b > 0) else -q  # C division truncates toward zero
+
+
+def dynprog_splits(leaves, op):
+    """Split table of dynprog_multiply (src/faust_linear_operator/
+    faust_prod_opt_gen.hpp:113-190) over the cost model of
+    CPU/faust_prod_opt.cpp:1-80.  leaves: list of (rows, cols, nnz, dense)
+    with stored dimensions.  Returns {(i, j): k}: leaves i..j multiply as
+    (i..k)(k+1..j); k is the first minimiser (strict <)."""
+    n = len(leaves)
+    INT_MAX = 2 ** 31 - 1
+    c = {(i, i): 0 for i in range(n)}
+    split = {}
+    tr = op != "N"
+    for p in range(1, n):
+        for i in range(n - p):
+            j = p + i
+            li, lj = leaves[i], leaves[j]
+            best, arg = INT_MAX, None
+            for k in range(i, j):
+                rf_init = k + 1 == j
+                cost = _w32(c[(i, k)] + c[(k + 1, j)])
+                mf_ncols = leaves[k][1]
+                if li[3] and lj[3]:
+                    add = _w32(_w32(li[0] * mf_ncols) * (lj[0] if tr and rf_init else lj[1]))
+                elif li[3]:
+                    add = _w32((mf_ncols if tr and k == i else li[0]) * lj[2])
+                elif lj[3]:
+                    add = _w32(li[2] * (lj[0] if tr and rf_init else lj[1]))
+                else:
+                    add = _div32(_w32(li[2] * lj[2]), li[1] if tr else li[0])
+                cost = _w32(cost + add)
+                if cost < best:
+                    best, arg = cost, k
+            c[(i, j)] = best
+            split[(i, j)] = i if arg is None else arg
+    return split
+
+
+def faust_product(factors, op="N", order=0, X=None):
+    """Dense product of a Faust of CSR factors (TESTING ONLY).
+
+    X None: TransformHelper::get_product (CPU/faust_TransformHelper.hpp:
+    1132-1178); order 0 (DEFAULT_L2R) = Transform::get_product
+    (CPU/faust_Transform.hpp:598-656): dense image of the last factor of
+    op(F), then sparse x dense products right to left; order 5 (DYNPROG) =
+    dynprog_multiply.  X given: op(F) X in the DYNPROG order
+    (TransformHelper::multiply, CPU/faust_TransformHelper.hpp:373-379).
+    Pairwise products: sparse x sparse = S x dense image; sparse x dense;
+    dense x sparse through the CSR of the right operand's transpose; dense x
+    dense with a sequential fma over k."""
+    op = "N" if op in ("N", "n") else "T"
+    facs = [_csr(f) for f in factors]
+    J = len(facs)
+    G = facs if op == "N" else facs[::-1]
+    if X is None and (order == 0 or J == 1):
+        if J == 1:
+            return np.asfortranarray(_csr_op(G[0], op).toarray())
+        cur = np.asfortranarray(_csr_op(G[-1], op).toarray())
+        for q in range(J - 2, -1, -1):
+            cur = _spmm(_csr_op(G[q], op), cur)
+        return cur
+    if order != 5:
+        raise ValueError("only DEFAULT_L2R (0) and DYNPROG (5)")
+    leaves = [(g.shape[0], g.shape[1], g.nnz, False) for g in G]
+    ops = [op] * J
+    data = list(G)
+    last_op = op
+    if X is not None:
+        X = np.asfortranarray(X, dtype=facs[0].dtype)
+        leaves.append((X.shape[0], X.shape[1], _w32(X.shape[0] * X.shape[1]), True))
+        data.append(X)
+        last_op = "N"
+    n = len(leaves)
+    split = dynprog_splits(leaves, op)
+
+    def mult(L, opl, R, opr):
+        lsp, rsp = not isinstance(L, np.ndarray), not isinstance(R, np.ndarray)
+        if lsp:
+            A = _csr_op(L, opl)
+            D = np.asfortranarray(_csr_op(R, opr).toarray()) if rsp else R
+            return _spmm(A, D)
+        if rsp:
+            return _dense_csrT(L, _csr_op(R, "T" if opr == "N" else "N"))
+        return _gemm_seq(L, R)
+
+    def rec(i, j):
+        if i == j:
+            return data[i]
+        if j - i == 1:
+            return mult(data[i], op, data[j], op if j < n - 1 else last_op)
+        k = split[(i, j)]
+        p1, p2 = rec(i, k), rec(k + 1, j)
+        opl = op if i == k else "N"
+        opr = (last_op if j == n - 1 else op) if k + 1 == j else "N"
+        return mult(p1, opl, p2, opr)
+
+    if n == 1:
+        return _spmm(_csr_op(data[0], op), X)
+    return rec(0, n - 1)

@@ -5,6 +5,8 @@ GPU and oracle follow the same floating-point operation order.  The top-k
 inputs include heavy ties, where the heap order of std::partial_sort
 decides which entries stay.
 """
+import os
+
 import numpy as np
 import pytest
 
