@@ -15,6 +15,8 @@ One JSON line is printed by rank 0.  Workloads (all inputs seeded, synthetic):
                  X 1024 x 512
   bsr            4 BSR factors 16384^2, 64x64 BF16 blocks, 8 blocks per block
                  row, times X 16384 x 4096 BF16 (FP32 accumulation)
+  product        dense product (get_product, DEFAULT_L2R) of the 12 CSR
+                 butterfly factors 4096^2, FP32 (the csr_butterfly Faust)
 --impl reference times the CPU restatement of the reference algorithm
 (oracle/, all host threads) on a bounded sample of the same workload; the
 reference itself cannot be compiled here (it needs Eigen 3.4).
@@ -282,6 +284,141 @@ def cpu_baseline_faust_x(W, sample_cols=None):
     bytes_ = sum(b + 2 * W.n * cols * es for b in W.factor_bytes())
     return {"value": round(bytes_ / dt / 1e9, 3), "unit": "GB/s", "cores": threads, "kind": "port",
             "sample": "%d of %d columns of X, %d repetitions" % (cols, W.ncols, reps)}
+
+
+# ---------------------------------------------------------------- dense product
+PROD_N, PROD_J = 4096, 12
+
+
+def _product_faust(rng):
+    from faust_gb300 import synth
+    return synth.butterfly_faust_factors(PROD_J, rng, np.float32)
+
+
+def _product_bytes(facs, es):
+    """Algorithmic bytes of get_product in the default order: the dense image
+    of the last factor (one write), then per applied factor one read of its
+    input, one write of its output and its CSR arrays."""
+    n = facs[0].shape[0]
+    plane = n * facs[-1].shape[1] * es
+    fb = [f.nnz * (es + 4) + (f.shape[0] + 1) * 4 for f in facs[:-1]]
+    per_factor = plane + sum(b + 2 * plane for b in fb)
+    chain_launch = 2 * plane + sum(fb)  # the fused chain: image in, product out, factors
+    return per_factor, chain_launch
+
+
+def run_product(args, rank, world):
+    import torch
+    import faust_gb300 as fg
+    torch.cuda.set_device(rank % max(1, torch.cuda.device_count()))
+    rng = np.random.default_rng(2024)
+    facs = _product_faust(rng)
+    stream = torch.cuda.current_stream()
+    ctx = fg.Context(torch.cuda.current_device(), stream=stream.cuda_stream)
+    F = fg.Faust(facs, ctx=ctx)
+    n = PROD_N
+    Y = torch.empty((n, n), dtype=torch.float32, device="cuda").t()
+    es = 4
+    step_bytes, chain_bytes = _product_bytes(facs, es)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    for _ in range(args.warmup):
+        F.product_device("N", "DEFAULT_L2R", Y=Y)
+    torch.cuda.synchronize()
+    _barrier(world)
+    times = []
+    launches0 = ctx.kernel_launches()
+    with ClockSampler(torch.cuda.current_device()) as clk:
+        for _ in range(args.steps):
+            flush.zero_()
+            s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            s.record(stream)
+            F.product_device("N", "DEFAULT_L2R", Y=Y)
+            e.record(stream)
+            times.append((s, e))
+        torch.cuda.synchronize()
+    launches = ctx.kernel_launches() - launches0
+    step_ms = _max_over_ranks(float(np.mean([a.elapsed_time(b) for a, b in times])), world)
+    # the dominant kernel alone on the same operands: the fused chain of the
+    # first 11 factors applied to the dense image of the last one
+    F11 = fg.Faust(facs[:-1], ctx=ctx)
+    img = torch.from_numpy(np.ascontiguousarray(facs[-1].toarray().T)).cuda().t()
+    Y2 = torch.empty_like(Y)
+    for _ in range(3):
+        F11.matmul_device(img, Y2)
+    ch = []
+    for _ in range(max(3, args.steps)):
+        flush.zero_()
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s.record(stream)
+        F11.matmul_device(img, Y2)
+        e.record(stream)
+        ch.append((s, e))
+    torch.cuda.synchronize()
+    chain_ms = float(np.mean([a.elapsed_time(b) for a, b in ch]))
+    # DYNPROG order (right-to-left leaf pairs for equal-cost butterflies);
+    # its first call also builds the factors' transposes, so warm up first
+    for _ in range(3):
+        F.product_device("N", "DYNPROG", Y=Y2)
+    dp = []
+    for _ in range(max(3, args.steps)):
+        flush.zero_()
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s.record(stream)
+        F.product_device("N", "DYNPROG", Y=Y2)
+        e.record(stream)
+        dp.append((s, e))
+    torch.cuda.synchronize()
+    dyn_ms = float(np.mean([a.elapsed_time(b) for a, b in dp]))
+    # end to end through the public API: toarray() = product + copy to host
+    F.toarray()
+    e2e = []
+    for _ in range(max(3, min(args.steps, 10))):
+        t0 = time.perf_counter()
+        F.toarray()
+        e2e.append(time.perf_counter() - t0)
+    e2e_ms = float(np.median(e2e)) * 1e3
+    hbm, _, peak_kind = _peaks()
+    achieved = chain_bytes / (chain_ms / 1e3) / 1e9
+    out = {
+        "metric": METRIC, "submetric": "Faust dense product effective GB/s (per-factor algorithmic bytes / step time)",
+        "value": round(step_bytes * world / (step_ms / 1e3) / 1e9, 2), "unit": "GB/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(step_ms, 4), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+        "config": {"workload": "product", "desc": "get_product (DEFAULT_L2R) of 12 CSR butterfly factors 4096^2 "
+                   "(2 nnz/row) FP32 -> dense 4096x4096", "l2": "flushed (256 MB write) before every timed step",
+                   "path": "dense image of the last factor + fused chain of the other 11",
+                   "dynprog_ms_per_step": round(dyn_ms, 4)},
+        "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
+                     "frac": round(achieved / hbm, 4), "traffic": None, "peak_kind": peak_kind,
+                     "kernel": "k_csr_chain_fused", "kernel_ms": round(chain_ms, 4),
+                     "algorithmic_bytes_per_launch": int(chain_bytes)},
+        "e2e": {"value": round(step_bytes / (e2e_ms / 1e3) / 1e9, 2), "unit": "GB/s", "ms_per_step": round(e2e_ms, 3),
+                "h2d_bytes_per_step": 0, "d2h_bytes_per_step": int(n * n * es)},
+        "gpu_launches": int(launches),
+        "clocks": clk.summary(),
+    }
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        out["cpu_baseline"] = cpu_baseline_product(facs)
+    F11.close()
+    F.close()
+    return out
+
+
+def cpu_baseline_product(facs, budget_s=3.0):
+    from oracle import oracle as O
+    threads = os.cpu_count() or 1
+    O.set_threads(threads)
+    step_bytes, _ = _product_bytes(facs, 4)
+    t0 = time.perf_counter()
+    reps = 0
+    while True:
+        O.faust_product(facs, "N", 0)
+        reps += 1
+        if time.perf_counter() - t0 > budget_s:
+            break
+    dt = (time.perf_counter() - t0) / reps
+    return {"value": round(step_bytes / dt / 1e9, 3), "unit": "GB/s", "cores": threads, "kind": "port",
+            "sample": "the whole product, %d repetitions" % reps}
 
 
 # ---------------------------------------------------------------- PALM4MSA
@@ -662,7 +799,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="palm",
-                    choices=["palm", "batched", "csr_butterfly", "csr_random", "bsr", "warmstart"])
+                    choices=["palm", "batched", "csr_butterfly", "csr_random", "bsr", "warmstart", "product"])
     ap.add_argument("--batch-count", type=int, default=512)
     ap.add_argument("--ctas-per-sm", type=int, default=2)
     ap.add_argument("--ws-train", type=int, default=20000)
@@ -692,6 +829,8 @@ def main():
         out = run_warmstart(args, rank, world)
     elif args.workload == "batched":
         out = run_batched(args, rank, world)
+    elif args.workload == "product":
+        out = run_product(args, rank, world)
     else:
         out = run_faust_x(args, rank, world)
     if rank == 0:
@@ -715,6 +854,17 @@ def reference_arm(args, world):
                                        "power-iteration tol 1e-8 (max 100), FP64"},
                 "cpu_baseline": cb,
                 "e2e": {"value": v, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+    if args.workload == "product":
+        facs = _product_faust(rng)
+        vals = [cpu_baseline_product(facs) for _ in range(max(1, args.steps))]
+        v = float(np.median([x["value"] for x in vals]))
+        cb = dict(vals[0])
+        cb["value"] = v
+        return {"impl": "reference", "metric": METRIC, "value": v, "unit": "GB/s", "n_gpus": world,
+                "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
+                "config": {"workload": "product"}, "cpu_baseline": cb,
+                "e2e": {"value": v, "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
     class _W:
         pass

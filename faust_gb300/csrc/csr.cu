@@ -135,6 +135,10 @@ fgb_status launch_csr_spmm(fgb_ctx* ctx, const int* rowptr, const int* colind, c
   // the GPU; small problems (PALM blocks) gather straight from L2.
   if (staged <= 96 * 1024 && tiles >= ctx->sm_count)
     return launch_spmm_tc<T, TC, true>(ctx, rowptr, colind, val, rows, inner, X, ldx, ncols, Y, ldy, epi);
+  // Half-width tiles when a full one does not fit (e.g. 4096 FP32 rows): the
+  // gathers still come from shared memory instead of dependent L2 round trips.
+  if (staged / 2 <= 96 * 1024 && 2 * tiles >= 4L * ctx->sm_count)
+    return launch_spmm_tc<T, TC / 2, true>(ctx, rowptr, colind, val, rows, inner, X, ldx, ncols, Y, ldy, epi);
   return launch_spmm_tc<T, TC / 2, false>(ctx, rowptr, colind, val, rows, inner, X, ldx, ncols, Y, ldy, epi);
 }
 

@@ -227,6 +227,57 @@ static int max_dim(const fgb_faust* F) {
   return m;
 }
 
+// The first nfac factors of op(F)'s product order applied to X, right to
+// left: G_0 ... G_{nfac-1} X with G_q = S_q (op N) or S_{J-1-q}^T (op T).
+// Automatic mode as in fgb_faust_mul: the fused chain when it fits on chip
+// and the intermediates would leave L2, else one launch per factor.
+fgb_status faust_apply_prefix(fgb_faust* F, char op, int nfac, const void* X, int ldx, int ncols, void* Y, int ldy) {
+  fgb_ctx* ctx = F->ctx;
+  const int J = (int)F->f.size();
+  const bool tr = op != 'N';
+  if (nfac <= 0 || nfac > J) return fail(ctx, FGB_ERR_INVALID_ARG, "faust_apply_prefix: bad factor count");
+  const int maxd = max_dim(F);
+  bool fits = false;
+  FGB_TRY(tr ? fused_desc_t(F) : fused_desc(F));
+  const ChainDesc* d = (const ChainDesc*)(tr ? F->chain_desc_t : F->chain_desc);
+  chain_fused(ctx, F->dtype, d, nfac, X, ldx, ncols, Y, ldy, maxd, true, &fits);
+  if (fits && nfac > 1 && fused_pays(F, ncols))
+    return chain_fused(ctx, F->dtype, d, nfac, X, ldx, ncols, Y, ldy, maxd, false, nullptr);
+  const size_t es = dtype_size(F->dtype);
+  if (nfac > 1) {
+    size_t need = (size_t)maxd * ncols * es;
+    if (F->buf_bytes < need) {
+      dfree(F->buf[0]);
+      dfree(F->buf[1]);
+      F->buf[0] = F->buf[1] = nullptr;
+      F->buf_bytes = 0;
+      FGB_TRY(dmalloc(ctx, &F->buf[0], need));
+      FGB_TRY(dmalloc(ctx, &F->buf[1], need));
+      F->buf_bytes = need;
+    }
+  }
+  const void* in = X;
+  int ldin = ldx;
+  for (int q = nfac - 1; q >= 0; --q) {
+    const DevFactor& f = F->f[tr ? J - 1 - q : q];
+    const int* rp = tr ? f.t_rowptr : f.rowptr;
+    const int* ci = tr ? f.t_colind : f.colind;
+    const void* v = tr ? f.t_val : f.val;
+    const int rows = tr ? f.cols : f.rows, inner = tr ? f.rows : f.cols;
+    void* out = (q == 0) ? Y : F->buf[(nfac - 1 - q) & 1];
+    const int ldout = (q == 0) ? ldy : std::max(1, rows);
+    if (F->dtype == FGB_F64)
+      FGB_TRY(launch_csr_spmm<double>(ctx, rp, ci, (const double*)v, rows, inner, (const double*)in, ldin, ncols,
+                                      (double*)out, ldout, Epi<double>()));
+    else
+      FGB_TRY(launch_csr_spmm<float>(ctx, rp, ci, (const float*)v, rows, inner, (const float*)in, ldin, ncols,
+                                     (float*)out, ldout, Epi<float>()));
+    in = out;
+    ldin = ldout;
+  }
+  return FGB_OK;
+}
+
 }  // namespace fgb
 
 fgb_faust::~fgb_faust() {

@@ -195,5 +195,8 @@ __device__ T block_cdot(const T* a, const T* b, long n, T* lane) {
 
 // Kernel helpers defined in the .cu files.
 fgb_status csr_build_transpose(fgb_ctx* ctx, fgb_dtype dt, DevFactor& f);
+// G_0 ... G_{nfac-1} X for the first nfac factors of op(F)'s product order
+// (G_q = S_q, or S_{J-1-q}^T for op T, whose transposes must exist); faust.cu.
+fgb_status faust_apply_prefix(fgb_faust* F, char op, int nfac, const void* X, int ldx, int ncols, void* Y, int ldy);
 
 }  // namespace fgb

@@ -335,6 +335,35 @@ static fgb_status ensure_ws(fgb_faust* F, size_t bytes) {
   return FGB_OK;
 }
 
+// Transform::get_product (CPU/faust_Transform.hpp:598-656): the dense image
+// of the last factor of op(F)'s product order, then the other J-1 factors
+// applied to it right to left (one fused launch when the intermediates would
+// leave L2, as for Faust x dense).
+template <typename T>
+static fgb_status run_default(fgb_faust* F, char op, void* Y, int ldy) {
+  fgb_ctx* ctx = F->ctx;
+  const int J = (int)F->f.size();
+  const DevFactor& last = op == 'N' ? F->f[J - 1] : F->f[0];
+  DevFactor img = last;
+  if (op != 'N') {
+    img.rowptr = last.t_rowptr;
+    img.colind = last.t_colind;
+    img.val = last.t_val;
+    img.rows = last.cols;
+    img.cols = last.rows;
+  }
+  if (J == 1 && ldy == std::max(1, img.rows)) return launch_csr_to_dense<T>(ctx, img, (T*)Y);
+  FGB_TRY(ensure_ws(F, sizeof(T) * std::max<size_t>(32, (size_t)img.rows * img.cols)));
+  T* im = (T*)F->pws;
+  FGB_TRY(launch_csr_to_dense<T>(ctx, img, im));
+  if (J == 1) {
+    FGB_CUDA(ctx, cudaMemcpy2DAsync(Y, sizeof(T) * ldy, im, sizeof(T) * img.rows, sizeof(T) * img.rows, img.cols,
+                                    cudaMemcpyDeviceToDevice, ctx->stream));
+    return FGB_OK;
+  }
+  return faust_apply_prefix(F, op, J - 1, im, std::max(1, img.rows), img.cols, Y, ldy);
+}
+
 template <typename T>
 static fgb_status run_dynprog(fgb_faust* F, char op, const void* X, int ldx, int ncols, void* Y, int ldy) {
   fgb_ctx* ctx = F->ctx;
@@ -378,59 +407,20 @@ static fgb_status run_dynprog(fgb_faust* F, char op, const void* X, int ldx, int
     dense.push_back(l.f ? 0 : 1);
   }
   dynprog_splits(pr.n, rows.data(), cols.data(), nnz.data(), dense.data(), op, pr.split);
+  // A plan that splits off the leftmost leaf at every level is the
+  // right-to-left chain: the same products in the same order as the default
+  // path, which runs them as one fused launch where that pays.
+  bool r2l = true;
+  for (int i = 0; i + 2 < pr.n; ++i) r2l = r2l && pr.split[(size_t)i * pr.n + pr.n - 1] == i;
+  if (r2l) {
+    if (!X) return run_default<T>(F, op, Y, ldy);
+    return faust_apply_prefix(F, op, J, X, ldx, ncols, Y, ldy);
+  }
   FGB_TRY(ensure_ws(F, sizeof(T) * std::max<size_t>(32, dynprog_ws_elems(pr.n, pr.leaves, pr.split, op,
                                                                               pr.last_op))));
   pr.ws = (T*)F->pws;
   PNode root;
   return pr.rec(0, pr.n - 1, true, root);
-}
-
-// Transform::get_product (CPU/faust_Transform.hpp:598-656).
-template <typename T>
-static fgb_status run_default(fgb_faust* F, char op, void* Y, int ldy) {
-  fgb_ctx* ctx = F->ctx;
-  const int J = (int)F->f.size();
-  const Epi<T> epi;
-  auto fac = [&](int q) -> const DevFactor& { return F->f[op == 'N' ? q : J - 1 - q]; };
-  // op(F) = G0 G1 ... G[J-1] with G = op(S) in product order
-  const DevFactor& last = fac(J - 1);
-  const int out_rows = op == 'N' ? F->f.front().rows : F->f.back().cols;
-  const int ncols = op == 'N' ? last.cols : last.rows;
-  int maxr = 0;
-  for (int q = 0; q < J; ++q) maxr = std::max(maxr, op == 'N' ? fac(q).rows : fac(q).cols);
-  const size_t plane = ((size_t)maxr * ncols + 31) & ~size_t(31);
-  FGB_TRY(ensure_ws(F, sizeof(T) * std::max<size_t>(32, 2 * plane)));
-  T* buf[2] = {(T*)F->pws, (T*)F->pws + plane};
-  // dense image of op(G[J-1])
-  DevFactor img = last;
-  if (op != 'N') {
-    img.rowptr = last.t_rowptr;
-    img.colind = last.t_colind;
-    img.val = last.t_val;
-    img.rows = last.cols;
-    img.cols = last.rows;
-  }
-  T* cur = (J == 1) ? (T*)nullptr : buf[0];
-  if (J == 1) {
-    if (ldy == img.rows) return launch_csr_to_dense<T>(ctx, img, (T*)Y);
-    FGB_TRY(launch_csr_to_dense<T>(ctx, img, buf[0]));
-    FGB_CUDA(ctx, cudaMemcpy2DAsync(Y, sizeof(T) * ldy, buf[0], sizeof(T) * img.rows, sizeof(T) * img.rows, img.cols,
-                                    cudaMemcpyDeviceToDevice, ctx->stream));
-    return FGB_OK;
-  }
-  FGB_TRY(launch_csr_to_dense<T>(ctx, img, cur));
-  int cur_rows = img.rows;
-  for (int q = J - 2; q >= 0; --q) {
-    const CsrView a = csr_op(fac(q), op);
-    T* dst = q == 0 ? (T*)Y : buf[(J - 2 - q + 1) & 1];
-    const int ldd = q == 0 ? ldy : std::max(1, a.rows);
-    FGB_TRY(launch_csr_spmm<T>(ctx, a.rp, a.ci, (const T*)a.v, a.rows, a.cols, cur, std::max(1, cur_rows), ncols, dst,
-                               ldd, epi));
-    cur = dst;
-    cur_rows = a.rows;
-  }
-  (void)out_rows;
-  return FGB_OK;
 }
 
 static bool product_ok(fgb_faust* F, char& op) {
