@@ -237,7 +237,11 @@ fgb_status faust_apply_prefix(fgb_faust* F, char op, int nfac, const void* X, in
   const bool tr = op != 'N';
   if (nfac <= 0 || nfac > J) return fail(ctx, FGB_ERR_INVALID_ARG, "faust_apply_prefix: bad factor count");
   const int maxd = max_dim(F);
-  bool fits = false;
+  bool fits = false, ran = false;
+  if (nfac > 1) {
+    FGB_TRY(bfly_chain(F, op, nfac, X, ldx, ncols, Y, ldy, false, &ran));
+    if (ran) return FGB_OK;
+  }
   FGB_TRY(tr ? fused_desc_t(F) : fused_desc(F));
   const ChainDesc* d = (const ChainDesc*)(tr ? F->chain_desc_t : F->chain_desc);
   chain_fused(ctx, F->dtype, d, nfac, X, ldx, ncols, Y, ldy, maxd, true, &fits);
@@ -362,6 +366,12 @@ fgb_status fgb_faust_mul(fgb_faust* F, const void* X, int ldx, int ncols, void* 
   FGB_CUDA(ctx, cudaSetDevice(ctx->device));
   const bool csr = all_csr(F);
   bool fits = false;
+  if (csr && (mode == 0 || mode == 3)) {
+    bool ran = false;
+    if (mode == 3 || F->f.size() > 1) FGB_TRY(bfly_chain(F, 'N', (int)F->f.size(), X, ldx, ncols, Y, ldy, mode == 3, &ran));
+    if (ran) return FGB_OK;
+    if (mode == 3) return fail(ctx, FGB_ERR_NOT_SUPPORTED, "butterfly chain: not every factor is a butterfly factor");
+  }
   if (csr && mode != 1) {
     FGB_TRY(fused_desc(F));
     chain_fused(ctx, F->dtype, (const ChainDesc*)F->chain_desc, (int)F->f.size(), X, ldx, ncols, Y, ldy, max_dim(F),
@@ -392,6 +402,12 @@ fgb_status fgb_faust_mul_op(fgb_faust* F, char op, const void* X, int ldx, int n
     if (!f.has_t) FGB_TRY(csr_build_transpose(ctx, F->dtype, f));
   bool fits = false;
   int maxd = max_dim(F);
+  if (mode == 0 || mode == 3) {
+    bool ran = false;
+    if (mode == 3 || F->f.size() > 1) FGB_TRY(bfly_chain(F, 'T', (int)F->f.size(), X, ldx, ncols, Y, ldy, mode == 3, &ran));
+    if (ran) return FGB_OK;
+    if (mode == 3) return fail(ctx, FGB_ERR_NOT_SUPPORTED, "butterfly chain: not every factor is a butterfly factor");
+  }
   if (mode != 1) {
     FGB_TRY(fused_desc_t(F));
     chain_fused(ctx, F->dtype, (const ChainDesc*)F->chain_desc_t, (int)F->f.size(), X, ldx, ncols, Y, ldy, maxd, true,

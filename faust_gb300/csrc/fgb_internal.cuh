@@ -93,6 +93,9 @@ struct DevFactor {
   bool has_t = false;
   // BSR: row-major copy of the blocks for the tensor-core kernel.
   void* aux = nullptr;
+  // Butterfly support (stride of the entries r & ~h, r | h in every row),
+  // 0 when the factor is not one, -1 until checked on the device.
+  int bfly = -1;
 };
 
 }  // namespace fgb
@@ -198,5 +201,9 @@ fgb_status csr_build_transpose(fgb_ctx* ctx, fgb_dtype dt, DevFactor& f);
 // G_0 ... G_{nfac-1} X for the first nfac factors of op(F)'s product order
 // (G_q = S_q, or S_{J-1-q}^T for op T, whose transposes must exist); faust.cu.
 fgb_status faust_apply_prefix(fgb_faust* F, char op, int nfac, const void* X, int ldx, int ncols, void* Y, int ldy);
+// The same product with the butterfly chain kernel when every factor has a
+// butterfly support (bfly.cu); *ran = false when it does not apply.
+fgb_status bfly_chain(fgb_faust* F, char op, int nfac, const void* X, int ldx, int ncols, void* Y, int ldy,
+                      bool force, bool* ran);
 
 }  // namespace fgb

@@ -99,7 +99,10 @@ fgb_status fgb_faust_shape(const fgb_faust* F, int* rows, int* cols, int* nfacto
  * (faust_MatBSR_gpu.cpp.in:108-140).  X and Y must not overlap.  BF16 Fausts
  * take BF16 X and produce BF16 Y with FP32 accumulation.
  * mode: 0 = automatic, 1 = one launch per factor, 2 = fused chain (fails
- * with FGB_ERR_NOT_SUPPORTED when the chain does not fit on chip). */
+ * with FGB_ERR_NOT_SUPPORTED when the chain does not fit on chip), 3 = the
+ * butterfly chain kernel (fails unless every factor has a butterfly support:
+ * entries r & ~h, r | h in row r, faust_butterfly.hpp:459-492).  Automatic
+ * mode takes the butterfly kernel for butterfly chains with enough columns. */
 fgb_status fgb_faust_mul(fgb_faust* F, const void* X, int ldx, int ncols, void* Y, int ldy, int mode);
 
 // Y = op(F) X with op 'N' (as fgb_faust_mul), 'T' or 'H' (the adjoint; the

@@ -106,6 +106,60 @@ def test_csr_butterfly_fp32_bitexact(fgb, oracle):
         assert np.array_equal(_to_np(F.matmul_device(_colmajor_cuda(X), mode=mode)), ref)
 
 
+def _bfly_perm_factors(nf, order, rng, dtype):
+    """Butterfly factors of size 2^nf applied with strides in a given order
+    (repeats allowed): factor q has stride 2^order[q]."""
+    import scipy.sparse as sp
+    n = 1 << nf
+    r = np.arange(n)
+    out = []
+    for b in order:
+        h = 1 << b
+        cols = np.stack([r & ~h, r | h], axis=1).ravel().astype(np.int32)
+        vals = rng.standard_normal(2 * n).astype(dtype)
+        out.append(sp.csr_matrix((vals, cols, np.arange(0, 2 * n + 1, 2, dtype=np.int32)), shape=(n, n)))
+    return out
+
+
+@pytest.mark.parametrize("dtype", [np.float32, np.float64])
+@pytest.mark.parametrize("nf,ncols", [(4, 7), (7, 130), (10, 1000), (12, 301)])
+def test_butterfly_kernel_bitexact(fgb, oracle, dtype, nf, ncols):
+    """The butterfly chain kernel (mode 3) against the oracle's CSR chain,
+    for F and F^T, ragged column counts."""
+    rng = np.random.default_rng(nf * 100 + ncols)
+    facs = synth.butterfly_faust_factors(nf, rng, dtype)
+    F = fgb.Faust(facs, dtype=dtype)
+    X = synth.dense_colmajor(1 << nf, ncols, rng, dtype)
+    assert np.array_equal(_to_np(F.matmul_device(_colmajor_cuda(X), mode=3)), oracle.chain_mul(facs, X))
+    assert np.array_equal(_to_np(F.matmul_device(_colmajor_cuda(X), mode=0)), oracle.chain_mul(facs, X))
+    ref_t = oracle.chain_mul([f.T.tocsr() for f in facs[::-1]], X)
+    assert np.array_equal(_to_np(F.matmul_op_device("T", _colmajor_cuda(X), mode=3)), ref_t)
+    F.close()
+
+
+@pytest.mark.parametrize("dtype", [np.float32, np.float64])
+def test_butterfly_kernel_shuffled_and_repeated_strides(fgb, oracle, dtype):
+    """Strides in any order, repeated strides and chains whose length is not
+    a multiple of the pass size."""
+    rng = np.random.default_rng(3)
+    for order in ([0, 5, 3, 3, 9, 1, 2, 2, 2, 8, 7], [9, 9], [4], [1, 0, 1, 0, 1]):
+        facs = _bfly_perm_factors(10, order, rng, dtype)
+        F = fgb.Faust(facs, dtype=dtype)
+        X = synth.dense_colmajor(1024, 97, rng, dtype)
+        assert np.array_equal(_to_np(F.matmul_device(_colmajor_cuda(X), mode=3)), oracle.chain_mul(facs, X)), order
+        F.close()
+
+
+def test_butterfly_kernel_rejects_other_supports(fgb):
+    rng = np.random.default_rng(4)
+    facs = [synth.random_csr(64, 64, 2, rng) for _ in range(3)]
+    F = fgb.Faust(facs)
+    X = _colmajor_cuda(synth.dense_colmajor(64, 8, rng))
+    with pytest.raises(Exception):
+        F.matmul_device(X, mode=3)
+    F.close()
+
+
 def test_csr_butterfly_config3b_column_subset(fgb, oracle):
     """Full size (12 factors of 4096^2, X 4096 x 8192 FP32): columns of Y
     depend only on the same columns of X, so a column subset is checked
