@@ -25,7 +25,7 @@
 namespace fgb {
 
 constexpr int BF_MAXS = 64;   // factors per chain
-constexpr int BF_G = 3;       // strides per pass (FP32); FP64 uses 2
+constexpr int BF_G = 3;       // largest number of strides per pass the plan holds
 constexpr int BF_THREADS = 256;
 
 struct BflyPlan {
@@ -76,57 +76,113 @@ __device__ __forceinline__ void st_row(T* p, const T (&x)[TC]) {
   }
 }
 
+// 16-byte row slot of matrix row r in the shared tile: the low three bits
+// are XORed with higher ones so that the rows one warp touches in a pass
+// (r = base + j * 2^b for consecutive orbit bases) fall in distinct bank
+// groups whatever the pass strides are.
+__device__ __forceinline__ int bf_slot(int r) { return r ^ (((r >> 3) ^ (r >> 6) ^ (r >> 9) ^ (r >> 12)) & 7); }
+
+// Rows of orbit o in pass ps: o with a zero inserted at every orbit stride,
+// plus every subset of the strides.
+template <int G>
+__device__ __forceinline__ void bf_rows(const BflyPlan& p, int ps, int o, int (&row)[1 << G]) {
+  const int g = p.pass_g[ps];
+  int bit[G];
+#pragma unroll
+  for (int b = 0; b < G; ++b) bit[b] = b < g ? p.pass_bit[ps][b] : 0;
+  int base = o;
+#pragma unroll
+  for (int b = 0; b < G; ++b)
+    if (b < g) base = ((base & ~(bit[b] - 1)) << 1) | (base & (bit[b] - 1));
+#pragma unroll
+  for (int k = 0; k < (1 << G); ++k) {
+    int r = base;
+#pragma unroll
+    for (int b = 0; b < G; ++b)
+      if ((k >> b) & 1) r += bit[b];
+    row[k] = r;
+  }
+}
+
+// The values of every factor of pass ps for the rows of one orbit.
+template <typename T, int G>
+__device__ __forceinline__ void bf_load_vals(const BflyPlan& p, int ps, const int (&row)[1 << G],
+                                             typename V2<T>::type (&v)[G][1 << G]) {
+  using T2 = typename V2<T>::type;
+  const int g = p.pass_g[ps], ns = p.pass_n[ps], first = p.pass_first[ps];
+#pragma unroll
+  for (int s = 0; s < G; ++s) {
+    const T2* vs = reinterpret_cast<const T2*>(p.val[first + (s < ns ? s : 0)]);
+#pragma unroll
+    for (int k = 0; k < (1 << G); ++k)
+      if (s < ns && k < (1 << g)) v[s][k] = __ldg(vs + row[k]);
+  }
+}
+
+// One block per column tile of TC columns; 256 threads.  Each thread walks
+// its (pass, orbit) items in order and loads the values of its next item
+// before working on the current one, so the L2 latency of the values
+// overlaps the shared-memory work (also across the pass barrier: values do
+// not depend on the tile).
 template <typename T, int TC, int G>
-__global__ void __launch_bounds__(BF_THREADS, 2)
+__global__ void __launch_bounds__(BF_THREADS, sizeof(T) == 4 ? 3 : 2)
     k_bfly_chain(const __grid_constant__ BflyPlan p, const T* __restrict__ X, int ldx, int ncols, T* __restrict__ Y,
                  int ldy) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  T* tile = reinterpret_cast<T*>(smem_raw);  // n x TC, row-major
+  T* tile = reinterpret_cast<T*>(smem_raw);  // n slots of TC values
   using T2 = typename V2<T>::type;
   const int n = p.n;
   const int j0 = blockIdx.x * TC;
-  for (int r = threadIdx.x; r < n; r += blockDim.x) {
+  const int tid = threadIdx.x;
+  // first item's values in flight while the tile is staged
+  int nps = 0;
+  while (nps < p.npasses && tid >= (n >> p.pass_g[nps])) ++nps;
+  int nrow[1 << G];
+  T2 vn[G][1 << G];
+  if (nps < p.npasses) {
+    bf_rows<G>(p, nps, tid, nrow);
+    bf_load_vals<T, G>(p, nps, nrow, vn);
+  }
+  for (int r = tid; r < n; r += blockDim.x) {
     T x[TC];
 #pragma unroll
     for (int t = 0; t < TC; ++t) x[t] = (j0 + t < ncols) ? X[r + (long)(j0 + t) * ldx] : T(0);
-    st_row<T, TC>(tile + (long)r * TC, x);
+    st_row<T, TC>(tile + (long)bf_slot(r) * TC, x);
   }
   __syncthreads();
   for (int ps = 0; ps < p.npasses; ++ps) {
     const int g = p.pass_g[ps], first = p.pass_first[ps], ns = p.pass_n[ps];
     const bool last = ps + 1 == p.npasses;
+    const int orbits = n >> g;
     int bit[G];
 #pragma unroll
     for (int b = 0; b < G; ++b) bit[b] = b < g ? p.pass_bit[ps][b] : 0;
-    const int orbits = n >> g;
-    for (int o = threadIdx.x; o < orbits; o += blockDim.x) {
-      // base: o with a zero inserted at every orbit stride (ascending)
-      int base = o;
-#pragma unroll
-      for (int b = 0; b < G; ++b)
-        if (b < g) base = ((base & ~(bit[b] - 1)) << 1) | (base & (bit[b] - 1));
+    for (int o = tid; o < orbits; o += blockDim.x) {
       int row[1 << G];
-#pragma unroll
-      for (int k = 0; k < (1 << G); ++k) {
-        int r = base;
-#pragma unroll
-        for (int b = 0; b < G; ++b)
-          if ((k >> b) & 1) r += bit[b];
-        row[k] = r;
-      }
-      // every value this orbit needs in this pass, issued before any use
       T2 v[G][1 << G];
 #pragma unroll
-      for (int s = 0; s < G; ++s) {
-        const T2* vs = reinterpret_cast<const T2*>(p.val[first + (s < ns ? s : 0)]);
+      for (int k = 0; k < (1 << G); ++k) row[k] = nrow[k];
 #pragma unroll
-        for (int k = 0; k < (1 << G); ++k)
-          if (s < ns && k < (1 << g)) v[s][k] = __ldg(vs + row[k]);
+      for (int s = 0; s < G; ++s)
+#pragma unroll
+        for (int k = 0; k < (1 << G); ++k) v[s][k] = vn[s][k];
+      // next item: the next orbit of this pass, else the first of a later pass
+      {
+        int qo = o + blockDim.x, qp = ps;
+        if (qo >= orbits) {
+          qp = ps + 1;
+          qo = tid;
+          while (qp < p.npasses && tid >= (n >> p.pass_g[qp])) ++qp;
+        }
+        if (qp < p.npasses) {
+          bf_rows<G>(p, qp, qo, nrow);
+          bf_load_vals<T, G>(p, qp, nrow, vn);
+        }
       }
       T xs[1 << G][TC];
 #pragma unroll
       for (int k = 0; k < (1 << G); ++k)
-        if (k < (1 << g)) ld_row<T, TC>(tile + (long)row[k] * TC, xs[k]);
+        if (k < (1 << g)) ld_row<T, TC>(tile + (long)bf_slot(row[k]) * TC, xs[k]);
 #pragma unroll
       for (int s = 0; s < G; ++s) {
         if (s >= ns) break;
@@ -158,7 +214,7 @@ __global__ void __launch_bounds__(BF_THREADS, 2)
       } else {
 #pragma unroll
         for (int k = 0; k < (1 << G); ++k)
-          if (k < (1 << g)) st_row<T, TC>(tile + (long)row[k] * TC, xs[k]);
+          if (k < (1 << g)) st_row<T, TC>(tile + (long)bf_slot(row[k]) * TC, xs[k]);
       }
     }
     if (!last) __syncthreads();
@@ -297,7 +353,7 @@ fgb_status bfly_chain(fgb_faust* F, char op, int nfac, const void* X, int ldx, i
   if (!force && tiles < ctx->sm_count) return FGB_OK;
   *ran = true;
   if (F->dtype == FGB_F32)
-    return launch_bfly<float, 4, 3>(F, op, nfac, (const float*)X, ldx, ncols, (float*)Y, ldy);
+    return launch_bfly<float, 4, 2>(F, op, nfac, (const float*)X, ldx, ncols, (float*)Y, ldy);
   return launch_bfly<double, 2, 2>(F, op, nfac, (const double*)X, ldx, ncols, (double*)Y, ldy);
 }
 
