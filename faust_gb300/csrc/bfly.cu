@@ -25,7 +25,7 @@
 namespace fgb {
 
 constexpr int BF_MAXS = 64;   // factors per chain
-constexpr int BF_G = 3;       // largest number of strides per pass the plan holds
+constexpr int BF_G = 3;       // stride slots per pass in the plan (two are used)
 constexpr int BF_THREADS = 256;
 
 struct BflyPlan {
@@ -34,6 +34,7 @@ struct BflyPlan {
   int stride[BF_MAXS];
   int pass_first[BF_MAXS], pass_n[BF_MAXS], pass_g[BF_MAXS];
   int pass_bit[BF_MAXS][BF_G];  // orbit strides of the pass, ascending
+  int step_bit[BF_MAXS];        // index of step s's stride among its pass's strides
 };
 
 template <typename T>
@@ -76,74 +77,84 @@ __device__ __forceinline__ void st_row(T* p, const T (&x)[TC]) {
   }
 }
 
-// 16-byte row slot of matrix row r in the shared tile: the low three bits
-// are XORed with higher ones so that the rows one warp touches in a pass
-// (r = base + j * 2^b for consecutive orbit bases) fall in distinct bank
-// groups whatever the pass strides are.
-__device__ __forceinline__ int bf_slot(int r) { return r ^ (((r >> 3) ^ (r >> 6) ^ (r >> 9) ^ (r >> 12)) & 7); }
+// 16-byte row slot of matrix row r in the shared tile.  Its low three bits
+// are XORed with (r3, r4, r3 ^ r4), so that the eight rows one quarter-warp
+// touches (eight consecutive orbits, same position in the orbit) land in
+// distinct bank groups for every pass stride pair of n = 4096 except
+// (1, 8), a lone 2, and (2, 2^j) with j >= 4, which are 2-way.
+__device__ __forceinline__ int bf_slot(int r) { return r ^ ((0x3650 >> (((r >> 3) & 3) << 2)) & 7); }
 
-// Rows of orbit o in pass ps: o with a zero inserted at every orbit stride,
-// plus every subset of the strides.
-template <int G>
-__device__ __forceinline__ void bf_rows(const BflyPlan& p, int ps, int o, int (&row)[1 << G]) {
-  const int g = p.pass_g[ps];
-  int bit[G];
-#pragma unroll
-  for (int b = 0; b < G; ++b) bit[b] = b < g ? p.pass_bit[ps][b] : 0;
-  int base = o;
-#pragma unroll
-  for (int b = 0; b < G; ++b)
-    if (b < g) base = ((base & ~(bit[b] - 1)) << 1) | (base & (bit[b] - 1));
-#pragma unroll
-  for (int k = 0; k < (1 << G); ++k) {
-    int r = base;
-#pragma unroll
-    for (int b = 0; b < G; ++b)
-      if ((k >> b) & 1) r += bit[b];
-    row[k] = r;
-  }
-}
+// One orbit of a pass with two strides (rows base, +b0, +b1, +b0+b1) or one
+// stride (rows base, +b0), and the values of the pass's factors on its rows.
+template <typename T>
+struct BfItem {
+  int row[4];
+  typename V2<T>::type v[2][4];
+};
 
-// The values of every factor of pass ps for the rows of one orbit.
-template <typename T, int G>
-__device__ __forceinline__ void bf_load_vals(const BflyPlan& p, int ps, const int (&row)[1 << G],
-                                             typename V2<T>::type (&v)[G][1 << G]) {
+template <typename T>
+__device__ __forceinline__ void bf_item(const BflyPlan& p, int ps, int o, BfItem<T>& it) {
   using T2 = typename V2<T>::type;
   const int g = p.pass_g[ps], ns = p.pass_n[ps], first = p.pass_first[ps];
+  const int b0 = p.pass_bit[ps][0], b1 = p.pass_bit[ps][1];
+  int base = ((o & ~(b0 - 1)) << 1) | (o & (b0 - 1));
+  if (g == 2) base = ((base & ~(b1 - 1)) << 1) | (base & (b1 - 1));
+  it.row[0] = base;
+  it.row[1] = base + b0;
+  it.row[2] = base + b1;
+  it.row[3] = base + b0 + b1;
+  const T2* v0 = reinterpret_cast<const T2*>(p.val[first]);
+  const T2* v1 = reinterpret_cast<const T2*>(p.val[first + (ns > 1 ? 1 : 0)]);
+  if (g == 2) {
 #pragma unroll
-  for (int s = 0; s < G; ++s) {
-    const T2* vs = reinterpret_cast<const T2*>(p.val[first + (s < ns ? s : 0)]);
+    for (int k = 0; k < 4; ++k) it.v[0][k] = __ldg(v0 + it.row[k]);
 #pragma unroll
-    for (int k = 0; k < (1 << G); ++k)
-      if (s < ns && k < (1 << g)) v[s][k] = __ldg(vs + row[k]);
+    for (int k = 0; k < 4; ++k) it.v[1][k] = __ldg(v1 + it.row[k]);
+  } else {
+    it.v[0][0] = __ldg(v0 + it.row[0]);
+    it.v[0][1] = __ldg(v0 + it.row[1]);
+    if (ns > 1) {
+      it.v[1][0] = __ldg(v1 + it.row[0]);
+      it.v[1][1] = __ldg(v1 + it.row[1]);
+    }
   }
 }
 
-// One block per column tile of TC columns; 256 threads.  Each thread walks
-// its (pass, orbit) items in order and loads the values of its next item
-// before working on the current one, so the L2 latency of the values
-// overlaps the shared-memory work (also across the pass barrier: values do
-// not depend on the tile).
-template <typename T, int TC, int G>
+// One factor on the rows of an orbit: pairs (k, k | 2^b) of local rows.
+template <typename T, int TC, int B>
+__device__ __forceinline__ void bf_stage(T (&xs)[4][TC], const typename V2<T>::type (&v)[4]) {
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    if ((k >> B) & 1) continue;
+    const int k1 = k | (1 << B);
+#pragma unroll
+    for (int t = 0; t < TC; ++t) {
+      const T a = xs[k][t], c = xs[k1][t];
+      xs[k][t] = fmad(v[k].y, c, fmad(v[k].x, a, T(0)));
+      xs[k1][t] = fmad(v[k1].y, c, fmad(v[k1].x, a, T(0)));
+    }
+  }
+}
+
+// One block per column tile of TC columns, BF_THREADS threads, two strides
+// per pass.  Each thread walks its (pass, orbit) items in order and loads the
+// values of its next item before working on the current one, so their L2
+// latency overlaps the shared-memory work (also across the pass barrier:
+// values do not depend on the tile).
+template <typename T, int TC>
 __global__ void __launch_bounds__(BF_THREADS, sizeof(T) == 4 ? 3 : 2)
     k_bfly_chain(const __grid_constant__ BflyPlan p, const T* __restrict__ X, int ldx, int ncols, T* __restrict__ Y,
                  int ldy) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T* tile = reinterpret_cast<T*>(smem_raw);  // n slots of TC values
-  using T2 = typename V2<T>::type;
   const int n = p.n;
   const int j0 = blockIdx.x * TC;
   const int tid = threadIdx.x;
-  // first item's values in flight while the tile is staged
   int nps = 0;
   while (nps < p.npasses && tid >= (n >> p.pass_g[nps])) ++nps;
-  int nrow[1 << G];
-  T2 vn[G][1 << G];
-  if (nps < p.npasses) {
-    bf_rows<G>(p, nps, tid, nrow);
-    bf_load_vals<T, G>(p, nps, nrow, vn);
-  }
-  for (int r = tid; r < n; r += blockDim.x) {
+  BfItem<T> nx;
+  if (nps < p.npasses) bf_item<T>(p, nps, tid, nx);
+  for (int r = tid; r < n; r += BF_THREADS) {
     T x[TC];
 #pragma unroll
     for (int t = 0; t < TC; ++t) x[t] = (j0 + t < ncols) ? X[r + (long)(j0 + t) * ldx] : T(0);
@@ -151,70 +162,59 @@ __global__ void __launch_bounds__(BF_THREADS, sizeof(T) == 4 ? 3 : 2)
   }
   __syncthreads();
   for (int ps = 0; ps < p.npasses; ++ps) {
-    const int g = p.pass_g[ps], first = p.pass_first[ps], ns = p.pass_n[ps];
+    const int g = p.pass_g[ps], ns = p.pass_n[ps], first = p.pass_first[ps];
     const bool last = ps + 1 == p.npasses;
     const int orbits = n >> g;
-    int bit[G];
-#pragma unroll
-    for (int b = 0; b < G; ++b) bit[b] = b < g ? p.pass_bit[ps][b] : 0;
-    for (int o = tid; o < orbits; o += blockDim.x) {
-      int row[1 << G];
-      T2 v[G][1 << G];
-#pragma unroll
-      for (int k = 0; k < (1 << G); ++k) row[k] = nrow[k];
-#pragma unroll
-      for (int s = 0; s < G; ++s)
-#pragma unroll
-        for (int k = 0; k < (1 << G); ++k) v[s][k] = vn[s][k];
-      // next item: the next orbit of this pass, else the first of a later pass
+    const int sb0 = p.step_bit[first], sb1 = p.step_bit[first + (ns > 1 ? 1 : 0)];
+    for (int o = tid; o < orbits; o += BF_THREADS) {
+      const BfItem<T> it = nx;
       {
-        int qo = o + blockDim.x, qp = ps;
+        int qo = o + BF_THREADS, qp = ps;
         if (qo >= orbits) {
           qp = ps + 1;
           qo = tid;
           while (qp < p.npasses && tid >= (n >> p.pass_g[qp])) ++qp;
         }
-        if (qp < p.npasses) {
-          bf_rows<G>(p, qp, qo, nrow);
-          bf_load_vals<T, G>(p, qp, nrow, vn);
-        }
+        if (qp < p.npasses) bf_item<T>(p, qp, qo, nx);
       }
-      T xs[1 << G][TC];
+      T xs[4][TC];
+      if (g == 2) {
 #pragma unroll
-      for (int k = 0; k < (1 << G); ++k)
-        if (k < (1 << g)) ld_row<T, TC>(tile + (long)bf_slot(row[k]) * TC, xs[k]);
+        for (int k = 0; k < 4; ++k) ld_row<T, TC>(tile + (long)bf_slot(it.row[k]) * TC, xs[k]);
+        if (sb0 == 0) bf_stage<T, TC, 0>(xs, it.v[0]);
+        else bf_stage<T, TC, 1>(xs, it.v[0]);
+        if (ns > 1) {
+          if (sb1 == 0) bf_stage<T, TC, 0>(xs, it.v[1]);
+          else bf_stage<T, TC, 1>(xs, it.v[1]);
+        }
+      } else {
+        // one stride: local rows 0 and 1 only
 #pragma unroll
-      for (int s = 0; s < G; ++s) {
-        if (s >= ns) break;
-        const int h = p.stride[first + s];
+        for (int k = 0; k < 2; ++k) ld_row<T, TC>(tile + (long)bf_slot(it.row[k]) * TC, xs[k]);
 #pragma unroll
-        for (int b = 0; b < G; ++b) {
-          if (b >= g || bit[b] != h) continue;
+        for (int s = 0; s < 2; ++s) {
+          if (s >= ns) break;
 #pragma unroll
-          for (int k = 0; k < (1 << G); ++k) {
-            if (((k >> b) & 1) || k >= (1 << g)) continue;
-            const int k1 = k | (1 << b);
-#pragma unroll
-            for (int t = 0; t < TC; ++t) {
-              const T a = xs[k][t], c = xs[k1][t];
-              xs[k][t] = fmad(v[s][k].y, c, fmad(v[s][k].x, a, T(0)));
-              xs[k1][t] = fmad(v[s][k1].y, c, fmad(v[s][k1].x, a, T(0)));
-            }
+          for (int t = 0; t < TC; ++t) {
+            const T a = xs[0][t], c = xs[1][t];
+            xs[0][t] = fmad(it.v[s][0].y, c, fmad(it.v[s][0].x, a, T(0)));
+            xs[1][t] = fmad(it.v[s][1].y, c, fmad(it.v[s][1].x, a, T(0)));
           }
         }
       }
+      const int kn = g == 2 ? 4 : 2;
       if (last) {
 #pragma unroll
-        for (int k = 0; k < (1 << G); ++k) {
-          if (k >= (1 << g)) continue;
+        for (int k = 0; k < 4; ++k) {
+          if (k >= kn) continue;
 #pragma unroll
           for (int t = 0; t < TC; ++t)
-            if (j0 + t < ncols) Y[row[k] + (long)(j0 + t) * ldy] = xs[k][t];
+            if (j0 + t < ncols) Y[it.row[k] + (long)(j0 + t) * ldy] = xs[k][t];
         }
       } else {
 #pragma unroll
-        for (int k = 0; k < (1 << G); ++k)
-          if (k < (1 << g)) st_row<T, TC>(tile + (long)bf_slot(row[k]) * TC, xs[k]);
+        for (int k = 0; k < 4; ++k)
+          if (k < kn) st_row<T, TC>(tile + (long)bf_slot(it.row[k]) * TC, xs[k]);
       }
     }
     if (!last) __syncthreads();
@@ -275,7 +275,8 @@ static fgb_status bfly_detect(fgb_faust* F) {
   return FGB_OK;
 }
 
-template <typename T, int G>
+// Passes of at most two consecutive factors (application order) with at most
+// two distinct strides.
 static void build_plan(fgb_faust* F, char op, int nfac, BflyPlan& p) {
   const int J = (int)F->f.size();
   p.n = F->f[0].rows;
@@ -290,32 +291,28 @@ static void build_plan(fgb_faust* F, char op, int nfac, BflyPlan& p) {
   p.npasses = 0;
   for (int s = 0; s < nfac;) {
     const int ps = p.npasses++;
-    int bits[BF_G], nb = 0, cnt = 0;
-    while (s < nfac && cnt < G) {
-      bool have = false;
-      for (int b = 0; b < nb; ++b) have = have || bits[b] == p.stride[s];
-      if (!have) {
-        if (nb == G) break;
-        bits[nb++] = p.stride[s];
-      }
-      ++cnt;
-      ++s;
-    }
-    std::sort(bits, bits + nb);
-    p.pass_first[ps] = s - cnt;
+    const int cnt = (s + 1 < nfac) ? 2 : 1;
+    int bits[2] = {p.stride[s], cnt > 1 ? p.stride[s + 1] : 0};
+    int nb = (cnt > 1 && bits[1] != bits[0]) ? 2 : 1;
+    if (nb == 2 && bits[1] < bits[0]) std::swap(bits[0], bits[1]);
+    p.pass_first[ps] = s;
     p.pass_n[ps] = cnt;
     p.pass_g[ps] = nb;
-    for (int b = 0; b < BF_G; ++b) p.pass_bit[ps][b] = b < nb ? bits[b] : 0;
+    p.pass_bit[ps][0] = bits[0];
+    p.pass_bit[ps][1] = nb == 2 ? bits[1] : 0;
+    p.pass_bit[ps][2] = 0;
+    for (int u = 0; u < cnt; ++u) p.step_bit[s + u] = p.stride[s + u] == bits[0] ? 0 : 1;
+    s += cnt;
   }
 }
 
-template <typename T, int TC, int G>
+template <typename T, int TC>
 static fgb_status launch_bfly(fgb_faust* F, char op, int nfac, const T* X, int ldx, int ncols, T* Y, int ldy) {
   fgb_ctx* ctx = F->ctx;
   BflyPlan p;
-  build_plan<T, G>(F, op, nfac, p);
+  build_plan(F, op, nfac, p);
   const size_t smem = (size_t)p.n * TC * sizeof(T);
-  auto kern = k_bfly_chain<T, TC, G>;
+  auto kern = k_bfly_chain<T, TC>;
   if (smem > 48 * 1024)
     FGB_CUDA(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   const int tiles = (ncols + TC - 1) / TC;
@@ -353,8 +350,8 @@ fgb_status bfly_chain(fgb_faust* F, char op, int nfac, const void* X, int ldx, i
   if (!force && tiles < ctx->sm_count) return FGB_OK;
   *ran = true;
   if (F->dtype == FGB_F32)
-    return launch_bfly<float, 4, 2>(F, op, nfac, (const float*)X, ldx, ncols, (float*)Y, ldy);
-  return launch_bfly<double, 2, 2>(F, op, nfac, (const double*)X, ldx, ncols, (double*)Y, ldy);
+    return launch_bfly<float, 4>(F, op, nfac, (const float*)X, ldx, ncols, (float*)Y, ldy);
+  return launch_bfly<double, 2>(F, op, nfac, (const double*)X, ldx, ncols, (double*)Y, ldy);
 }
 
 }  // namespace fgb
