@@ -122,7 +122,7 @@ def _bfly_perm_factors(nf, order, rng, dtype):
 
 
 @pytest.mark.parametrize("dtype", [np.float32, np.float64])
-@pytest.mark.parametrize("nf,ncols", [(4, 7), (7, 130), (10, 1000), (12, 301)])
+@pytest.mark.parametrize("nf,ncols", [(4, 7), (7, 130), (10, 1000), (12, 301), (10, 1301), (11, 2500)])
 def test_butterfly_kernel_bitexact(fgb, oracle, dtype, nf, ncols):
     """The butterfly chain kernel (mode 3) against the oracle's CSR chain,
     for F and F^T, ragged column counts."""
