@@ -243,8 +243,10 @@ def run_faust_x(args, rank, world):
                 "traffic_note": "dram read + write bytes of one launch, ncu capture", "peak_kind": peak_kind,
                 "kernel": "k_bsr_tc", "algorithmic_flops_per_launch": int(fl), "algorithmic_bytes_per_launch": int(kb)}
     else:
+        # dram read + write bytes of one launch from one ncu capture (the butterfly chain)
+        traffic = 217178624 if bfly else None
         roof = {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
-                "frac": round(achieved / hbm, 4), "traffic": None, "peak_kind": peak_kind,
+                "frac": round(achieved / hbm, 4), "traffic": traffic, "peak_kind": peak_kind,
                 "kernel": chain_kernel if fused else "k_csr_spmm", "algorithmic_bytes_per_launch": int(kb)}
     value = W.step_bytes * world / (step_ms / 1e3) / 1e9
     out = {
