@@ -32,9 +32,11 @@ __device__ __forceinline__ T epi_apply(const Epi<T>& e, T acc, long i, long j, T
 
 // Launch helpers (csr.cu).
 // Y = S X  (S: rows x inner CSR; X: inner x ncols; Y: rows x ncols).
+// max_row: longest row of S if known (rows of 16 or more entries run in a
+// separate warp-per-row kernel), -1 when unknown.
 template <typename T>
 fgb_status launch_csr_spmm(fgb_ctx* ctx, const int* rowptr, const int* colind, const T* val, int rows, int inner,
-                           const T* X, int ldx, int ncols, T* Y, int ldy, const Epi<T>& epi);
+                           const T* X, int ldx, int ncols, T* Y, int ldy, const Epi<T>& epi, int max_row = -1);
 // Y = X S^T given the CSR of S (S: srows x scols; X: xrows x scols; Y: xrows x srows).
 template <typename T>
 fgb_status launch_dense_csrT(fgb_ctx* ctx, const T* X, int ldx, int xrows, const int* rowptr, const int* colind,

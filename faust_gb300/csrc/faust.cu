@@ -53,6 +53,15 @@ static fgb_status upload_factor(fgb_ctx* ctx, fgb_dtype dt, const fgb_factor_des
     FGB_CUDA(ctx, cudaMemcpyAsync(f.val, d.values, es * nval, cudaMemcpyHostToDevice, ctx->stream));
   }
   if (d.format == FGB_BSR) FGB_TRY(bsr_tc_prepare(ctx, f));
+  if (d.format == FGB_CSR) {
+    // longest row and column: products skip the long-row kernel without them
+    std::vector<int> cc(std::max(1, d.cols), 0);
+    int mr = 0, mc = 0;
+    for (int r = 0; r < d.rows; ++r) mr = std::max(mr, d.rowptr[r + 1] - d.rowptr[r]);
+    for (int p = 0; p < d.nnz; ++p) mc = std::max(mc, ++cc[d.colind[p]]);
+    f.max_row = mr;
+    f.max_col = mc;
+  }
   return FGB_OK;
 }
 
@@ -129,10 +138,10 @@ static fgb_status mul_per_factor(fgb_faust* F, const void* X, int ldx, int ncols
       FGB_TRY(launch_bsr_spmm(ctx, f, (const __nv_bfloat16*)in, ldin, ncols, (__nv_bfloat16*)out, ldout));
     } else if (F->dtype == FGB_F64) {
       FGB_TRY(launch_csr_spmm<double>(ctx, f.rowptr, f.colind, (const double*)f.val, f.rows, f.cols,
-                                      (const double*)in, ldin, ncols, (double*)out, ldout, Epi<double>()));
+                                      (const double*)in, ldin, ncols, (double*)out, ldout, Epi<double>(), f.max_row));
     } else {
       FGB_TRY(launch_csr_spmm<float>(ctx, f.rowptr, f.colind, (const float*)f.val, f.rows, f.cols,
-                                     (const float*)in, ldin, ncols, (float*)out, ldout, Epi<float>()));
+                                     (const float*)in, ldin, ncols, (float*)out, ldout, Epi<float>(), f.max_row));
     }
     in = out;
     ldin = ldout;
@@ -178,10 +187,10 @@ static fgb_status mul_per_factor_t(fgb_faust* F, const void* X, int ldx, int nco
     int ldout = (k == J - 1) ? ldy : f.cols;
     if (F->dtype == FGB_F64) {
       FGB_TRY(launch_csr_spmm<double>(ctx, f.t_rowptr, f.t_colind, (const double*)f.t_val, f.cols, f.rows,
-                                      (const double*)in, ldin, ncols, (double*)out, ldout, Epi<double>()));
+                                      (const double*)in, ldin, ncols, (double*)out, ldout, Epi<double>(), f.max_col));
     } else {
       FGB_TRY(launch_csr_spmm<float>(ctx, f.t_rowptr, f.t_colind, (const float*)f.t_val, f.cols, f.rows,
-                                     (const float*)in, ldin, ncols, (float*)out, ldout, Epi<float>()));
+                                     (const float*)in, ldin, ncols, (float*)out, ldout, Epi<float>(), f.max_col));
     }
     in = out;
     ldin = ldout;
@@ -270,12 +279,13 @@ fgb_status faust_apply_prefix(fgb_faust* F, char op, int nfac, const void* X, in
     const int rows = tr ? f.cols : f.rows, inner = tr ? f.rows : f.cols;
     void* out = (q == 0) ? Y : F->buf[(nfac - 1 - q) & 1];
     const int ldout = (q == 0) ? ldy : std::max(1, rows);
+    const int ml = tr ? f.max_col : f.max_row;
     if (F->dtype == FGB_F64)
       FGB_TRY(launch_csr_spmm<double>(ctx, rp, ci, (const double*)v, rows, inner, (const double*)in, ldin, ncols,
-                                      (double*)out, ldout, Epi<double>()));
+                                      (double*)out, ldout, Epi<double>(), ml));
     else
       FGB_TRY(launch_csr_spmm<float>(ctx, rp, ci, (const float*)v, rows, inner, (const float*)in, ldin, ncols,
-                                     (float*)out, ldout, Epi<float>()));
+                                     (float*)out, ldout, Epi<float>(), ml));
     in = out;
     ldin = ldout;
   }

@@ -96,6 +96,8 @@ struct DevFactor {
   // Butterfly support (stride of the entries r & ~h, r | h in every row),
   // 0 when the factor is not one, -1 until checked on the device.
   int bfly = -1;
+  // Longest row / column (entries), -1 when not known on the host.
+  int max_row = -1, max_col = -1;
 };
 
 }  // namespace fgb
