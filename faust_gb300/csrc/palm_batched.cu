@@ -15,6 +15,7 @@
 #include <vector>
 
 #include "fgb_internal.cuh"
+#include "pirow.cuh"
 
 namespace fgb {
 namespace bat {
@@ -162,17 +163,6 @@ __device__ Csr<T> b_stage_csr(const int* rp, const int* ci, const T* v, int nrow
   sg.p = reinterpret_cast<T*>(reinterpret_cast<char*>(sg.p) + vb + ib);
   sg.elems -= (int)((vb + ib) / sizeof(T));
   return Csr<T>{srp, sci, sv};
-}
-
-// sum over the stored entries p of row r of v[p] * x[ci[p] * stride], in order
-template <typename TA, typename TV, typename TX>
-__device__ __forceinline__ TA b_row_dot(const int* __restrict__ rp, const int* __restrict__ ci,
-                                        const TV* __restrict__ v, int r, const TX* __restrict__ x, int stride) {
-  TA acc = TA(0);
-  const int p1 = rp[r + 1];
-#pragma unroll 8
-  for (int p = rp[r]; p < p1; ++p) acc = fmad((TA)v[p], (TA)x[ci[p] * stride], acc);
-  return acc;
 }
 
 // 16 bytes of T from shared memory (G = 16 / sizeof(T) values).
@@ -421,7 +411,8 @@ __device__ __noinline__ double b_spectral_norm(const Fac<T>* F, int lo, int hi, 
       pi_op(F, lo, hi, tall, o, rp, ci, v, orow);
       const TC* src = bufs[si];
       TC* dst = bufs[di];
-      for (int r = threadIdx.x; r < orow; r += BT) dst[r] = b_row_dot<TC>(rp, ci, v, r, src, 1);
+      // the power iteration's row order (pirow.cuh): long rows in chunks
+      for (int r = threadIdx.x; r < orow; r += BT) dst[r] = pi_row_thread<TC, T>(ci, v, rp[r], rp[r + 1], src);
       __syncthreads();
       si = di;
       di = 3 - xi - si;

@@ -7,6 +7,7 @@
 #include <cstring>
 #include <vector>
 
+#include "pirow.cuh"
 #include "power.cuh"
 
 namespace fgb {
@@ -35,6 +36,11 @@ void pi_chain_build(const DevFactor* F, int lo, int hi, PIChain& ch) {
     for (int i = hi - 1; i >= lo; --i) ch.ops[ch.nops++] = fwd(i);
   }
 }
+
+// static shared memory of k_power_iteration (op table, scalars, long-row list)
+// plus slack, kept out of the dynamic allocation
+constexpr int PI_LONG_CAP = 1024;
+constexpr size_t PI_STATIC_SMEM = 8192;
 
 template <typename T>
 __device__ __forceinline__ T absd(T x) {
@@ -97,6 +103,10 @@ __global__ void __launch_bounds__(PI_THREADS)
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ PIStaged ops[PI_MAX_OPS];
   __shared__ TC s_inv, s_nrm;
+  // rows of more than PI_CHUNK entries of the current product, done one
+  // warp each after the thread-per-row pass (two counters, used alternately)
+  __shared__ int s_long[PI_LONG_CAP];
+  __shared__ int s_nlong[2];
   TC* buf0 = reinterpret_cast<TC*>(smem_raw);
   TC* buf1 = buf0 + maxn;
   TC* buf2 = buf1 + maxn;
@@ -175,6 +185,9 @@ __global__ void __launch_bounds__(PI_THREADS)
     TC lam_old = TC(1), lam = TC(0);
     int it = 0;
     bool zero_vec = false;
+    if (threadIdx.x == 0) s_nlong[0] = s_nlong[1] = 0;
+    int gop = 0;  // products done (selects the long-row counter)
+    const int wlane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
     const TC athr = absd(thr);
     while ((absd(subr(lam_old, lam)) > athr || absd(lam) <= athr) && it < max_iter) {
       ++it;
@@ -207,21 +220,46 @@ __global__ void __launch_bounds__(PI_THREADS)
         // issue the loads for later products
         pi_rowptr<TF>(ops[(o + 3) % nops], r0, b3, e3);
         pi_entries<TF>(ops[(o + 1) % nops], P1);
+        int* const nlong = &s_nlong[gop & 1];
+        auto defer = [&](int r, int b, int e) {
+          const int slot = atomicAdd(nlong, 1);
+          if (slot < PI_LONG_CAP) s_long[slot] = r;
+          else dst[r] = pi_row_thread<TC, TF>(op.ci, val, b, e, src);  // list full: same order, one thread
+        };
         if (r0 < op.rows) {
-          TC acc = TC(0);
+          if (P0.e - P0.b > PI_CHUNK) {
+            defer(r0, P0.b, P0.e);
+          } else {
+            TC acc = TC(0);
 #pragma unroll
-          for (int u = 0; u < PI_PF; ++u)
-            if (P0.b + u < P0.e) acc = fmad((TC)P0.v[u], src[P0.c[u]], acc);
-          for (int p = P0.b + PI_PF; p < P0.e; ++p) acc = fmad((TC)val[p], src[op.ci[p]], acc);
-          dst[r0] = acc;
+            for (int u = 0; u < PI_PF; ++u)
+              if (P0.b + u < P0.e) acc = fmad((TC)P0.v[u], src[P0.c[u]], acc);
+            for (int p = P0.b + PI_PF; p < P0.e; ++p) acc = fmad((TC)val[p], src[op.ci[p]], acc);
+            dst[r0] = acc;
+          }
         }
         for (int r = r0 + blockDim.x; r < op.rows; r += blockDim.x) {
+          const int p0 = op.rp[r], p1 = op.rp[r + 1];
+          if (p1 - p0 > PI_CHUNK) {
+            defer(r, p0, p1);
+            continue;
+          }
           TC acc = TC(0);
-          const int p1 = op.rp[r + 1];
-          for (int p = op.rp[r]; p < p1; ++p) acc = fmad((TC)val[p], src[op.ci[p]], acc);
+          for (int p = p0; p < p1; ++p) acc = fmad((TC)val[p], src[op.ci[p]], acc);
           dst[r] = acc;
         }
         __syncthreads();
+        {
+          const int nl = min(*nlong, PI_LONG_CAP);
+          if (threadIdx.x == 0) s_nlong[(gop + 1) & 1] = 0;
+          for (int q = warp; q < nl; q += nwarps) {
+            const int r = s_long[q];
+            const TC v = pi_row_warp<TC, TF>(op.ci, val, op.rp[r], op.rp[r + 1], src, wlane);
+            if (wlane == 0) dst[r] = v;
+          }
+          if (nl) __syncthreads();
+          ++gop;
+        }
         P0 = P1;
         P1.b = b2;
         P1.e = e2;
@@ -339,7 +377,8 @@ static fgb_status launch_pi_t(fgb_ctx* ctx, const PIChain& a, const PIChain& b, 
                               const int* d_rand, PIOut* d_out, const PIPalm& palm, cudaStream_t stream) {
   const int maxn = std::max(1, std::max(a.maxdim, b.maxdim));
   const size_t vec = (3 * (size_t)maxn + CR_LANES) * sizeof(TC);
-  const size_t cap = std::min<size_t>(ctx->smem_optin > 4096 ? ctx->smem_optin - 4096 : 0, 220 * 1024);
+  const size_t cap = std::min<size_t>(ctx->smem_optin > PI_STATIC_SMEM ? ctx->smem_optin - PI_STATIC_SMEM : 0,
+                                      216 * 1024);
   if (vec > cap)
     return fail(ctx, FGB_ERR_NOT_SUPPORTED, "power iteration: vector of %d entries does not fit on chip", maxn);
   // the rest of shared memory stages the chain's CSR arrays
@@ -376,7 +415,8 @@ static fgb_status launch_pi_many_t(fgb_ctx* ctx, const PIChain* d_chains, int nc
                                    double thr, PIOut* d_out, cudaStream_t stream) {
   maxn = std::max(1, maxn);
   const size_t vec = (3 * (size_t)maxn + CR_LANES) * sizeof(TC);
-  const size_t cap = std::min<size_t>(ctx->smem_optin > 4096 ? ctx->smem_optin - 4096 : 0, 220 * 1024);
+  const size_t cap = std::min<size_t>(ctx->smem_optin > PI_STATIC_SMEM ? ctx->smem_optin - PI_STATIC_SMEM : 0,
+                                      216 * 1024);
   if (vec > cap)
     return fail(ctx, FGB_ERR_NOT_SUPPORTED, "power iteration: vector of %d entries does not fit on chip", maxn);
   const size_t smem = cap;

@@ -30,7 +30,9 @@
 //   * every product entry  y = sum_p a_p * x_p  is a sequential fused
 //     multiply-add over the sparse operand's entries in stored order
 //     (rows sorted by column; transposed products walk the transpose's CSR,
-//     i.e. in increasing original row), starting from +0;
+//     i.e. in increasing original row), starting from +0; inside the power
+//     iteration, rows of more than 16 entries are summed as 16-entry chunks
+//     combined by a pairwise tree (pi_row_dot below);
 //   * every reduction (sum of squares, dot product) over N values in
 //     column-major linear order uses 256 lanes inside chunks of 65536 values:
 //     lane t accumulates (by fma) the values whose chunk offset is = t mod 256,
@@ -211,6 +213,45 @@ static Dense<T> dense_times_csrT(const Dense<T>& X, const Csr<T>& S) {
     }
   }
   return Y;
+}
+
+// Sparse matrix times a vector inside the power iteration.  Each entry runs
+// over the row's stored entries in order, cut into chunks of PI_CHUNK: each
+// chunk is a sequential fma from +0 and the chunk partials P_0 .. P_{M-1}
+// are added by the recursive-halving pairwise tree (at stride s = 1, 2, 4,
+// ...: Q_l += Q_{l+s} for l = 0 mod 2s, l + s < M).  A row of at most
+// PI_CHUNK entries is the plain sequential fma.  With a single right-hand
+// column there is no other parallelism in a long row, and the chunks let a
+// GPU warp run it as independent short chains.
+static const int PI_CHUNK = 16;
+
+template <typename T>
+static T pi_row_dot(const T* val, const int* colind, int p0, int p1, const T* x) {
+  const int L = p1 - p0;
+  if (L <= PI_CHUNK) {
+    T acc = T(0);
+    for (int p = p0; p < p1; ++p) acc = fma_(val[p], x[colind[p]], acc);
+    return acc;
+  }
+  const int M = (L + PI_CHUNK - 1) / PI_CHUNK;
+  std::vector<T> Q(M);
+  for (int m = 0; m < M; ++m) {
+    T acc = T(0);
+    const int e = std::min(p1, p0 + (m + 1) * PI_CHUNK);
+    for (int p = p0 + m * PI_CHUNK; p < e; ++p) acc = fma_(val[p], x[colind[p]], acc);
+    Q[m] = acc;
+  }
+  for (int st = 1; st < M; st *= 2)
+    for (int l = 0; l + st < M; l += 2 * st) Q[l] = Q[l] + Q[l + st];
+  return Q[0];
+}
+
+template <typename T>
+static std::vector<T> pi_spmv(const Csr<T>& S, const std::vector<T>& x) {
+  std::vector<T> y(S.rows);
+  for (int i = 0; i < S.rows; ++i) y[i] = pi_row_dot(S.val.data(), S.colind.data(), S.rowptr[i], S.rowptr[i + 1],
+                                                     x.data());
+  return y;
 }
 
 // A factor together with the CSR of its transpose (built once per factor).
@@ -476,12 +517,9 @@ struct ChainOp {
 
 template <typename T>
 static std::vector<T> apply_chain_vec(const ChainOp<T>& A, const std::vector<T>& x) {
-  Dense<T> v(A.n, 1);
-  v.a = x;
-  for (auto& op : A.ops) {
-    v = op.second ? spmm_H(*op.first, v) : spmm(op.first->S, v);
-  }
-  return v.a;
+  std::vector<T> v = x;
+  for (auto& op : A.ops) v = pi_spmv(op.second ? op.first->St : op.first->S, v);
+  return v;
 }
 
 // Faust::power_iteration (faust_linear_algebra.hpp:806-899).
@@ -1028,6 +1066,20 @@ int orc_gemm_seq_f64(int m, int n, int k, const double* A, const double* B, doub
 }
 int orc_gemm_seq_f32(int m, int n, int k, const float* A, const float* B, float* C) {
   return gemm_seq_impl<float>(m, n, k, A, B, C);
+}
+
+int orc_pi_spmv_f64(int rows, int cols, const int* rp, const int* ci, const double* v, const double* x, double* y) {
+  ORC_TRY({
+    Csr<double> S;
+    S.rows = rows;
+    S.cols = cols;
+    S.rowptr.assign(rp, rp + rows + 1);
+    S.colind.assign(ci, ci + S.rowptr[rows]);
+    S.val.assign(v, v + S.rowptr[rows]);
+    std::vector<double> xv(x, x + cols);
+    std::vector<double> yv = pi_spmv(S, xv);
+    std::memcpy(y, yv.data(), sizeof(double) * rows);
+  })
 }
 
 int orc_bsr_mul_f64(int m, int n, int bm, int bn, const int* browptr, const int* bcolind, const double* blocks,

@@ -91,6 +91,18 @@ def chain_mul(factors, X):
     return Y
 
 
+def pi_spmv(S, x):
+    """y = S x with the power iteration's row order (16-entry chunks, pairwise
+    tree over the chunk partials), FP64."""
+    S = _csr(S).astype(np.float64)
+    x = np.ascontiguousarray(x, np.float64).ravel()
+    y = np.zeros(S.shape[0], np.float64)
+    rp, ci = S.indptr.astype(np.int32), S.indices.astype(np.int32)
+    _check(lib().orc_pi_spmv_f64(S.shape[0], S.shape[1], _p(rp), _p(ci), _p(np.ascontiguousarray(S.data)), _p(x),
+                                 _p(y)))
+    return y
+
+
 def bsr_mul_f64(m, n, bm, bn, browptr, bcolind, blocks, X):
     """Y = B X in FP64 (BSRMat::mul); blocks is (bnnz, bm*bn) column-major per block."""
     Xf = np.asfortranarray(X, dtype=np.float64)

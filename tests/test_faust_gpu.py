@@ -228,6 +228,28 @@ def test_spectral_norm_matches_oracle(fgb, oracle):
     assert got == ref
 
 
+@pytest.mark.parametrize("shape", [(1024, 1024), (700, 900)])
+def test_spectral_norm_long_rows_matches_oracle(fgb, oracle, shape):
+    """Rows and columns far longer than the 16-entry chunk of the power
+    iteration's row order (up to 1000 entries: several rounds of 32 chunks),
+    square and rectangular chains: the norm equals the oracle's bit for bit."""
+    import scipy.sparse as sp
+    rng = np.random.default_rng(22)
+    m, n = shape
+    facs = []
+    for (r, c) in [(m, n), (n, n), (n, m)]:
+        A = synth.random_csr(r, c, 3, rng).tolil()
+        for i in rng.choice(r, 12, replace=False):
+            cols = rng.choice(c, int(rng.integers(17, min(c, 1000))), replace=False)
+            A[i, cols] = rng.standard_normal(len(cols))
+        facs.append(sp.csr_matrix(A))
+    F = fgb.Faust(facs)
+    got = F.norm(2, max_iter=100, threshold=1e-12)
+    ref, _ = oracle.spectral_norm(facs, max_iter=100, thr=1e-12)
+    assert got == ref
+    F.close()
+
+
 def test_invalid_factor_is_rejected(fgb):
     import scipy.sparse as sp
     m = sp.csr_matrix(np.eye(4))

@@ -297,3 +297,51 @@ def test_hierarchical_left_side_shapes(oracle):
     assert [f.shape for f in S] == [(40, 32), (32, 24), (24, 24)]
     assert np.count_nonzero(S[0]) <= 300 and np.count_nonzero(S[1]) <= 60 and np.count_nonzero(S[2]) <= 60
     assert 0 < oracle.rel_err(A, S, lam) < 1
+
+
+def _fma(a, b, c):
+    from fractions import Fraction
+    return float(Fraction(a) * Fraction(b) + Fraction(c))
+
+
+def _row_value(vals, xs, chunk=16):
+    """Independent restatement of the canonical row order: 16-entry chunks
+    of sequential fma from +0, partials added by the recursive-halving tree."""
+    parts = []
+    for m in range(0, len(vals), chunk):
+        acc = 0.0
+        for v, x in zip(vals[m:m + chunk], xs[m:m + chunk]):
+            acc = _fma(v, x, acc)
+        parts.append(acc)
+    s = 1
+    while s < len(parts):
+        for l in range(0, len(parts) - s, 2 * s):
+            parts[l] = parts[l] + parts[l + s]
+        s *= 2
+    return parts[0] if parts else 0.0
+
+
+def test_pi_row_order_chunked_tree(oracle):
+    """The power iteration's sparse-row products follow the chunked tree
+    order (rows of 1..200 entries, including lengths around the 16-entry
+    chunk and the powers of two of the tree); plain products stay sequential."""
+    import scipy.sparse as sps
+    rng = np.random.default_rng(17)
+    lens = [1, 2, 15, 16, 17, 31, 32, 33, 48, 63, 64, 65, 100, 127, 128, 129, 200]
+    ncol = 256
+    rows, cols, vals = [], [], []
+    for i, L in enumerate(lens):
+        c = np.sort(rng.choice(ncol, L, replace=False))
+        rows += [i] * L
+        cols += list(c)
+        vals += list(rng.standard_normal(L) * 10.0 ** rng.integers(-3, 4, L))
+    S = sps.csr_matrix((vals, (rows, cols)), shape=(len(lens), ncol))
+    S.sort_indices()
+    x = rng.standard_normal((ncol, 1))
+    got = oracle.pi_spmv(S, x[:, 0])
+    seq = oracle.chain_mul([S], x)[:, 0]
+    for i in range(len(lens)):
+        p0, p1 = S.indptr[i], S.indptr[i + 1]
+        vals, xs = list(S.data[p0:p1]), [x[c, 0] for c in S.indices[p0:p1]]
+        assert got[i] == _row_value(vals, xs), lens[i]
+        assert seq[i] == _row_value(vals, xs, chunk=1 << 30), lens[i]
