@@ -6,6 +6,7 @@
 #include <climits>
 
 #include "csr.cuh"
+#include "rowdot.cuh"
 
 namespace fgb {
 
@@ -88,7 +89,7 @@ __global__ void __launch_bounds__(SPMM_THREADS)
 #pragma unroll
     for (int t = 0; t < TC; ++t) acc[t] = T(0);
     const int p0 = rowptr[i], p1 = rowptr[i + 1];
-    if (p1 - p0 >= long_row) continue;  // k_csr_spmm_long writes this row
+    if (p1 - p0 >= long_row) continue;  // k_csr_spmm_long writes this row (chunked order)
     for (int p = p0; p < p1; ++p) {
       const T v = val[p];
       const int c = colind[p];
@@ -108,74 +109,45 @@ __global__ void __launch_bounds__(SPMM_THREADS)
   }
 }
 
-// Rows with at least SPMM_LONG_ROW entries: one warp per (row, 32 columns),
-// lanes along the columns, so that every FMA instruction of the row's chains
-// has 32 active lanes (GB300 issues one FP64 FMA warp instruction per 64
-// cycles per scheduler whatever the number of active lanes, so a long row
-// left to one lane of a thread-per-row warp costs 32 times its share).
-// Each entry (i, j) is still the sequential fma over row i in stored order.
-// Block: 4 warps, 4 rows x 32 columns; warps of short rows move on at once,
-// and long rows next to each other land in different warps.
-constexpr int SPMM_LONG_ROW = 16;
-
-// Sequential fma over the stored entries p0..p1-1 of one sparse row, from
-// +0, one output per lane; GATHER(lane, c) is the dense value the lane
-// multiplies with entry column c.  Entries come 32 at a time, one per lane
-// (coalesced), and every gather of a full 32-entry block is issued before
-// its dependent FMAs; the next block's entries are loaded before the current
-// block's FMAs.  The last partial block goes in groups of four, so at most
-// three predicated-off FMAs are issued per row (GB300 issues one FP64 FMA
-// warp instruction per 64 cycles per scheduler, predicated or not).
-template <typename T, typename Gather>
-__device__ __forceinline__ T chain_32(const T* __restrict__ val, const int* __restrict__ colind, int p0, int p1,
-                                      int lane, Gather gather) {
-  const unsigned FULL = 0xffffffffu;
-  T acc = T(0);
-  T vl = p0 + lane < p1 ? __ldg(val + p0 + lane) : T(0);
-  int cl = p0 + lane < p1 ? __ldg(colind + p0 + lane) : 0;
-  int pb = p0;
-  for (; pb + 32 <= p1; pb += 32) {
-    T x[32];
-#pragma unroll
-    for (int u = 0; u < 32; ++u) x[u] = gather(__shfl_sync(FULL, cl, u));
-    const T vcur = vl;
-    const int q = pb + 32 + lane;
-    vl = q < p1 ? __ldg(val + q) : T(0);
-    cl = q < p1 ? __ldg(colind + q) : 0;
-#pragma unroll
-    for (int u = 0; u < 32; ++u) acc = fmad(__shfl_sync(FULL, vcur, u), x[u], acc);
-  }
-  const int n = p1 - pb;
-  for (int u0 = 0; u0 < n; u0 += 4) {
-    T x[4];
-#pragma unroll
-    for (int u = 0; u < 4; ++u) {
-      const int c = __shfl_sync(FULL, cl, (u0 + u) & 31);
-      x[u] = u0 + u < n ? gather(c) : T(0);
-    }
-#pragma unroll
-    for (int u = 0; u < 4; ++u) {
-      const T v = __shfl_sync(FULL, vl, (u0 + u) & 31);
-      if (u0 + u < n) acc = fmad(v, x[u], acc);
-    }
-  }
-  return acc;
-}
-
+// Rows of more than ROW_CHUNK entries: one block of 8 warps per (row, 32
+// columns), lanes along the columns, the row's chunk groups split over the
+// warps (rowdot.cuh), so every FP64 FMA instruction has 32 active lanes and
+// a row of L entries takes about L / 8 dependent steps instead of L.
 template <typename T>
-__global__ void __launch_bounds__(128)
+__global__ void __launch_bounds__(256)
     k_csr_spmm_long(const int* __restrict__ rowptr, const int* __restrict__ colind, const T* __restrict__ val,
                     int rows, const T* __restrict__ X, int ldx, int ncols, T* __restrict__ Y, int ldy, Epi<T> epi) {
+  __shared__ T roots[ROW_GROUPS * 32];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const long j = (long)blockIdx.x * 32 + lane;
   const bool okj = j < ncols;
   const T* __restrict__ xcol = X + (okj ? j : 0) * (long)ldx;
-  for (int i = blockIdx.y * 4 + warp; i < rows; i += gridDim.y * 4) {
+  for (int i = blockIdx.y; i < rows; i += gridDim.y) {
     const int p0 = rowptr[i], p1 = rowptr[i + 1];
-    if (p1 - p0 < SPMM_LONG_ROW) continue;
-    const T s = epi.scal ? *epi.scal : T(0);
-    const T acc = chain_32<T>(val, colind, p0, p1, lane, [&](int c) { return __ldg(xcol + c); });
-    if (okj) Y[i + j * (long)ldy] = epi_apply(epi, acc, i, j, s);
+    if (p1 - p0 <= ROW_CHUNK) continue;
+    const T v = row_block_long<T, 8>(val, colind, p0, p1, [&](int c) { return __ldg(xcol + c); }, roots, lane, warp);
+    if (warp == 0 && okj) Y[i + j * (long)ldy] = epi_apply(epi, v, i, j, epi.scal ? *epi.scal : T(0));
+  }
+}
+
+// X S^T for rows c of S with more than ROW_CHUNK entries: lanes along the rows
+// of X, the row's chunk groups split over 8 warps.
+template <typename T>
+__global__ void __launch_bounds__(256)
+    k_dense_csrT_long(const T* __restrict__ X, int ldx, int xrows, const int* __restrict__ rowptr,
+                      const int* __restrict__ colind, const T* __restrict__ val, int srows, T* __restrict__ Y, int ldy,
+                      Epi<T> epi) {
+  __shared__ T roots[ROW_GROUPS * 32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int r = blockIdx.x * 32 + lane;
+  const bool okr = r < xrows;
+  const T* __restrict__ xr = X + (okr ? r : 0);
+  for (int c = blockIdx.y; c < srows; c += gridDim.y) {
+    const int p0 = rowptr[c], p1 = rowptr[c + 1];
+    if (p1 - p0 <= ROW_CHUNK) continue;
+    const T v = row_block_long<T, 8>(val, colind, p0, p1, [&](int k) { return __ldg(xr + (long)k * ldx); }, roots,
+                                     lane, warp);
+    if (warp == 0 && okr) Y[r + (long)c * ldy] = epi_apply(epi, v, r, c, epi.scal ? *epi.scal : T(0));
   }
 }
 
@@ -207,12 +179,13 @@ fgb_status launch_csr_spmm(fgb_ctx* ctx, const int* rowptr, const int* colind, c
   constexpr int TC = 16 / sizeof(T) * 2;  // 8 floats or 4 doubles per thread
   const size_t staged = (size_t)inner * TC * sizeof(T);
   const long tiles = (ncols + TC - 1) / TC;
-  // long rows (known absent when max_row < SPMM_LONG_ROW) go to their own kernel
-  const bool has_long = max_row < 0 || max_row >= SPMM_LONG_ROW;
-  const int long_row = has_long ? SPMM_LONG_ROW : INT_MAX;
+  // rows of more than ROW_CHUNK entries (known absent when max_row is) go to
+  // their own kernel
+  const bool has_long = max_row < 0 || max_row > ROW_CHUNK;
+  const int long_row = has_long ? ROW_CHUNK + 1 : INT_MAX;
   if (has_long) {
-    dim3 g((unsigned)((ncols + 31) / 32), (unsigned)std::min((rows + 3) / 4, 64));
-    k_csr_spmm_long<T><<<g, 128, 0, ctx->stream>>>(rowptr, colind, val, rows, X, ldx, ncols, Y, ldy, epi);
+    dim3 g((unsigned)((ncols + 31) / 32), (unsigned)std::min(rows, 64));
+    k_csr_spmm_long<T><<<g, 256, 0, ctx->stream>>>(rowptr, colind, val, rows, X, ldx, ncols, Y, ldy, epi);
     FGB_LAUNCHED(ctx);
   }
   // Stage when the tile fits comfortably and there are enough tiles to fill
@@ -239,29 +212,24 @@ __global__ void __launch_bounds__(SPMM_THREADS)
   const int c = blockIdx.x;
   const int p0 = rowptr[c], p1 = rowptr[c + 1];
   const T s = epi.scal ? *epi.scal : T(0);
-  const int lane = threadIdx.x & 31;
-  if (p1 - p0 < 16) {
-    for (int r = blockIdx.y * blockDim.x + threadIdx.x; r < xrows; r += gridDim.y * blockDim.x) {
-      T acc = T(0);
-      for (int p = p0; p < p1; ++p) acc = fmad(__ldg(val + p), __ldg(X + r + (long)__ldg(colind + p) * ldx), acc);
-      Y[r + (long)c * ldy] = epi_apply(epi, acc, r, c, s);
-    }
-    return;
-  }
-  // long rows: whole warps walk the row loop together (the chain shuffles)
-  for (int rb = blockIdx.y * blockDim.x + (threadIdx.x & ~31); rb < xrows; rb += gridDim.y * blockDim.x) {
-    const int r = rb + lane;
-    const T* __restrict__ xr = X + (r < xrows ? r : 0);
-    const T acc = chain_32<T>(val, colind, p0, p1, lane, [&](int cc) { return __ldg(xr + (long)cc * ldx); });
-    if (r < xrows) Y[r + (long)c * ldy] = epi_apply(epi, acc, r, c, s);
+  if (p1 - p0 > ROW_CHUNK) return;  // k_dense_csrT_long writes this column (chunked order)
+  for (int r = blockIdx.y * blockDim.x + threadIdx.x; r < xrows; r += gridDim.y * blockDim.x) {
+    T acc = T(0);
+    for (int p = p0; p < p1; ++p) acc = fmad(__ldg(val + p), __ldg(X + r + (long)__ldg(colind + p) * ldx), acc);
+    Y[r + (long)c * ldy] = epi_apply(epi, acc, r, c, s);
   }
 }
 
 template <typename T>
 fgb_status launch_dense_csrT(fgb_ctx* ctx, const T* X, int ldx, int xrows, const int* rowptr, const int* colind,
-                             const T* val, int srows, int scols, T* Y, int ldy, const Epi<T>& epi) {
+                             const T* val, int srows, int scols, T* Y, int ldy, const Epi<T>& epi, int max_row) {
   (void)scols;
   if (srows == 0 || xrows == 0) return FGB_OK;
+  if (max_row < 0 || max_row > ROW_CHUNK) {
+    dim3 g((unsigned)((xrows + 31) / 32), (unsigned)std::min(srows, 64));
+    k_dense_csrT_long<T><<<g, 256, 0, ctx->stream>>>(X, ldx, xrows, rowptr, colind, val, srows, Y, ldy, epi);
+    FGB_LAUNCHED(ctx);
+  }
   // Two warps per block: the blocks of one output column (same chain length
   // for every thread) spread over many SMs, whose FP64 pipes (one warp
   // instruction per 64 cycles per scheduler on GB300) bound long columns.
@@ -531,9 +499,9 @@ template fgb_status launch_csr_spmm<float>(fgb_ctx*, const int*, const int*, con
 template fgb_status launch_csr_spmm<double>(fgb_ctx*, const int*, const int*, const double*, int, int, const double*,
                                             int, int, double*, int, const Epi<double>&, int);
 template fgb_status launch_dense_csrT<float>(fgb_ctx*, const float*, int, int, const int*, const int*, const float*,
-                                             int, int, float*, int, const Epi<float>&);
+                                             int, int, float*, int, const Epi<float>&, int);
 template fgb_status launch_dense_csrT<double>(fgb_ctx*, const double*, int, int, const int*, const int*,
-                                              const double*, int, int, double*, int, const Epi<double>&);
+                                              const double*, int, int, double*, int, const Epi<double>&, int);
 template fgb_status launch_csr_to_dense<float>(fgb_ctx*, const DevFactor&, float*);
 template fgb_status launch_csr_to_dense<double>(fgb_ctx*, const DevFactor&, double*);
 

@@ -1,8 +1,10 @@
 // csr.cuh — CSR x dense kernels shared by the Faust product and PALM.
 //
-// Every output entry is a sequential fused multiply-add over the sparse
-// operand's entries in stored order, starting from +0 (the order the oracle
-// restates), so results are bit-identical to the CPU restatement.
+// Every output entry follows the canonical row order of rowdot.cuh (a
+// sequential fused multiply-add over the sparse operand's entries in stored
+// order from +0 for rows of at most 16 entries; 16-entry chunks combined by a
+// pairwise tree beyond), the order the oracle restates, so results are
+// bit-identical to the CPU restatement.
 #pragma once
 
 #include "fgb_internal.cuh"
@@ -32,15 +34,15 @@ __device__ __forceinline__ T epi_apply(const Epi<T>& e, T acc, long i, long j, T
 
 // Launch helpers (csr.cu).
 // Y = S X  (S: rows x inner CSR; X: inner x ncols; Y: rows x ncols).
-// max_row: longest row of S if known (rows of 16 or more entries run in a
-// separate warp-per-row kernel), -1 when unknown.
+// max_row: longest row of S if known (rows of more than 16 entries run in a
+// separate kernel), -1 when unknown.
 template <typename T>
 fgb_status launch_csr_spmm(fgb_ctx* ctx, const int* rowptr, const int* colind, const T* val, int rows, int inner,
                            const T* X, int ldx, int ncols, T* Y, int ldy, const Epi<T>& epi, int max_row = -1);
 // Y = X S^T given the CSR of S (S: srows x scols; X: xrows x scols; Y: xrows x srows).
 template <typename T>
 fgb_status launch_dense_csrT(fgb_ctx* ctx, const T* X, int ldx, int xrows, const int* rowptr, const int* colind,
-                             const T* val, int srows, int scols, T* Y, int ldy, const Epi<T>& epi);
+                             const T* val, int srows, int scols, T* Y, int ldy, const Epi<T>& epi, int max_row = -1);
 // Dense column-major (ld = rows) image of a CSR factor.
 template <typename T>
 fgb_status launch_csr_to_dense(fgb_ctx* ctx, const DevFactor& f, T* out);

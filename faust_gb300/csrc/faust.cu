@@ -224,6 +224,18 @@ static bool fused_pays(const fgb_faust* F, int ncols) {
   return maxrows * (size_t)ncols * dtype_size(F->dtype) > (size_t)std::max(l2, 1) / 4;
 }
 
+// The fused chain kernel sums each row in one sequential chain, the canonical
+// order only for rows of at most ROW_CHUNK (16) entries: it runs only when
+// every factor is known to have no longer row (columns for the transposed
+// chain).
+static bool rows_short(const fgb_faust* F, bool transposed) {
+  for (auto& f : F->f) {
+    const int m = transposed ? f.max_col : f.max_row;
+    if (m < 0 || m > 16) return false;
+  }
+  return true;
+}
+
 static bool all_csr(const fgb_faust* F) {
   for (auto& f : F->f)
     if (f.format != FGB_CSR) return false;
@@ -251,11 +263,13 @@ fgb_status faust_apply_prefix(fgb_faust* F, char op, int nfac, const void* X, in
     FGB_TRY(bfly_chain(F, op, nfac, X, ldx, ncols, Y, ldy, false, &ran));
     if (ran) return FGB_OK;
   }
-  FGB_TRY(tr ? fused_desc_t(F) : fused_desc(F));
-  const ChainDesc* d = (const ChainDesc*)(tr ? F->chain_desc_t : F->chain_desc);
-  chain_fused(ctx, F->dtype, d, nfac, X, ldx, ncols, Y, ldy, maxd, true, &fits);
-  if (fits && nfac > 1 && fused_pays(F, ncols))
-    return chain_fused(ctx, F->dtype, d, nfac, X, ldx, ncols, Y, ldy, maxd, false, nullptr);
+  if (rows_short(F, tr)) {
+    FGB_TRY(tr ? fused_desc_t(F) : fused_desc(F));
+    const ChainDesc* d = (const ChainDesc*)(tr ? F->chain_desc_t : F->chain_desc);
+    chain_fused(ctx, F->dtype, d, nfac, X, ldx, ncols, Y, ldy, maxd, true, &fits);
+    if (fits && nfac > 1 && fused_pays(F, ncols))
+      return chain_fused(ctx, F->dtype, d, nfac, X, ldx, ncols, Y, ldy, maxd, false, nullptr);
+  }
   const size_t es = dtype_size(F->dtype);
   if (nfac > 1) {
     size_t need = (size_t)maxd * ncols * es;
@@ -382,13 +396,14 @@ fgb_status fgb_faust_mul(fgb_faust* F, const void* X, int ldx, int ncols, void* 
     if (ran) return FGB_OK;
     if (mode == 3) return fail(ctx, FGB_ERR_NOT_SUPPORTED, "butterfly chain: not every factor is a butterfly factor");
   }
-  if (csr && mode != 1) {
+  if (csr && mode != 1 && rows_short(F, false)) {
     FGB_TRY(fused_desc(F));
     chain_fused(ctx, F->dtype, (const ChainDesc*)F->chain_desc, (int)F->f.size(), X, ldx, ncols, Y, ldy, max_dim(F),
                 true, &fits);
   }
   if (mode == 2 && !fits)
-    return fail(ctx, FGB_ERR_NOT_SUPPORTED, "fused chain: factors do not fit on chip (or not CSR)");
+    return fail(ctx, FGB_ERR_NOT_SUPPORTED,
+                "fused chain: factors do not fit on chip, are not CSR or have rows of more than 16 entries");
   if (fits && (mode == 2 || (mode == 0 && F->f.size() > 1 && fused_pays(F, ncols))))
     return chain_fused(ctx, F->dtype, (const ChainDesc*)F->chain_desc, (int)F->f.size(), X, ldx, ncols, Y, ldy,
                        max_dim(F), false, nullptr);
@@ -418,7 +433,7 @@ fgb_status fgb_faust_mul_op(fgb_faust* F, char op, const void* X, int ldx, int n
     if (ran) return FGB_OK;
     if (mode == 3) return fail(ctx, FGB_ERR_NOT_SUPPORTED, "butterfly chain: not every factor is a butterfly factor");
   }
-  if (mode != 1) {
+  if (mode != 1 && rows_short(F, true)) {
     FGB_TRY(fused_desc_t(F));
     chain_fused(ctx, F->dtype, (const ChainDesc*)F->chain_desc_t, (int)F->f.size(), X, ldx, ncols, Y, ldy, maxd, true,
                 &fits);

@@ -15,7 +15,7 @@
 #include <vector>
 
 #include "fgb_internal.cuh"
-#include "pirow.cuh"
+#include "rowdot.cuh"
 
 namespace fgb {
 namespace bat {
@@ -193,7 +193,8 @@ struct Vec16<double> {
 // S and a block of X's columns are staged in shared memory, the block stored
 // row by row (stride sx) so that the G columns a thread owns are one 16-byte
 // read per stored entry; each output entry is the sequential fma over its
-// row's entries, G of them in flight per thread.
+// row's entries (rows of more than 16 entries: the chunked order of
+// rowdot.cuh), G of them in flight per thread.
 template <typename T>
 __device__ __noinline__ void b_spmm(const int* rp, const int* ci, const T* v, int rows, int inner, const T* X, int ldx,
                                    int ncols, T* Y, int mode, const T* aux, T s, Stage<T> sg) {
@@ -239,13 +240,19 @@ __device__ __noinline__ void b_spmm(const int* rp, const int* ci, const T* v, in
       T acc[G];
 #pragma unroll
       for (int u = 0; u < G; ++u) acc[u] = T(0);
-      const int p1 = S.rp[i + 1];
-      for (int p = S.rp[i]; p < p1; ++p) {
-        const T val = S.v[p];
-        T xv[G];
-        Vec16<T>::load(sg.p + S.ci[p] * sx + g * G, xv);
+      const int p0 = S.rp[i], p1 = S.rp[i + 1];
+      if (p1 - p0 > ROW_CHUNK) {
+        // rows of more than ROW_CHUNK entries: the chunked order of rowdot.cuh
+        row_long_g<T, G, 10>(S.ci, S.v, p0, p1, sg.p + g * G, sx,
+                             [](const T* q, T (&o)[G]) { Vec16<T>::load(q, o); }, acc);
+      } else {
+        for (int p = p0; p < p1; ++p) {
+          const T val = S.v[p];
+          T xv[G];
+          Vec16<T>::load(sg.p + S.ci[p] * sx + g * G, xv);
 #pragma unroll
-        for (int u = 0; u < G; ++u) acc[u] = fmad(val, xv[u], acc[u]);
+          for (int u = 0; u < G; ++u) acc[u] = fmad(val, xv[u], acc[u]);
+        }
       }
 #pragma unroll
       for (int u = 0; u < G; ++u) {
@@ -306,13 +313,19 @@ __device__ __noinline__ void b_dense_csrT(const T* X, int xrows, int xcols, cons
       T acc[G];
 #pragma unroll
       for (int u = 0; u < G; ++u) acc[u] = T(0);
-      const int p1 = S.rp[c + 1];
-      for (int p = S.rp[c]; p < p1; ++p) {
-        const T val = S.v[p];
-        T xv[G];
-        Vec16<T>::load(sg.p + S.ci[p] * nrp + g * G, xv);
+      const int p0 = S.rp[c], p1 = S.rp[c + 1];
+      if (p1 - p0 > ROW_CHUNK) {
+        // rows of more than ROW_CHUNK entries: the chunked order of rowdot.cuh
+        row_long_g<T, G, 10>(S.ci, S.v, p0, p1, sg.p + g * G, nrp,
+                             [](const T* q, T (&o)[G]) { Vec16<T>::load(q, o); }, acc);
+      } else {
+        for (int p = p0; p < p1; ++p) {
+          const T val = S.v[p];
+          T xv[G];
+          Vec16<T>::load(sg.p + S.ci[p] * nrp + g * G, xv);
 #pragma unroll
-        for (int u = 0; u < G; ++u) acc[u] = fmad(val, xv[u], acc[u]);
+          for (int u = 0; u < G; ++u) acc[u] = fmad(val, xv[u], acc[u]);
+        }
       }
 #pragma unroll
       for (int u = 0; u < G; ++u) {
@@ -411,8 +424,18 @@ __device__ __noinline__ double b_spectral_norm(const Fac<T>* F, int lo, int hi, 
       pi_op(F, lo, hi, tall, o, rp, ci, v, orow);
       const TC* src = bufs[si];
       TC* dst = bufs[di];
-      // the power iteration's row order (pirow.cuh): long rows in chunks
-      for (int r = threadIdx.x; r < orow; r += BT) dst[r] = pi_row_thread<TC, T>(ci, v, rp[r], rp[r + 1], src);
+      // the power iteration's row order (rowdot.cuh): long rows in chunks
+      for (int r = threadIdx.x; r < orow; r += BT) {
+        const int p0 = rp[r], p1 = rp[r + 1];
+        if (p1 - p0 > ROW_CHUNK) {
+          dst[r] = row_thread_long_inl<TC, T, 10>(ci, v, p0, p1, src, 1);
+        } else {
+          TC acc = TC(0);
+#pragma unroll 4
+          for (int p = p0; p < p1; ++p) acc = fmad((TC)v[p], src[ci[p]], acc);
+          dst[r] = acc;
+        }
+      }
       __syncthreads();
       si = di;
       di = 3 - xi - si;

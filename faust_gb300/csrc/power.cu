@@ -7,7 +7,7 @@
 #include <cstring>
 #include <vector>
 
-#include "pirow.cuh"
+#include "rowdot.cuh"
 #include "power.cuh"
 
 namespace fgb {
@@ -37,10 +37,9 @@ void pi_chain_build(const DevFactor* F, int lo, int hi, PIChain& ch) {
   }
 }
 
-// static shared memory of k_power_iteration (op table, scalars, long-row list)
+// static shared memory of k_power_iteration (op table, scalars, counters)
 // plus slack, kept out of the dynamic allocation
-constexpr int PI_LONG_CAP = 1024;
-constexpr size_t PI_STATIC_SMEM = 8192;
+constexpr size_t PI_STATIC_SMEM = 4096;
 
 template <typename T>
 __device__ __forceinline__ T absd(T x) {
@@ -104,14 +103,15 @@ __global__ void __launch_bounds__(PI_THREADS)
   __shared__ PIStaged ops[PI_MAX_OPS];
   __shared__ TC s_inv, s_nrm;
   // rows of more than PI_CHUNK entries of the current product, done one
-  // warp each after the thread-per-row pass (two counters, used alternately)
-  __shared__ int s_long[PI_LONG_CAP];
+  // warp each after the thread-per-row pass (list in the dynamic area, room
+  // for every row; two counters, used alternately)
   __shared__ int s_nlong[2];
   TC* buf0 = reinterpret_cast<TC*>(smem_raw);
   TC* buf1 = buf0 + maxn;
   TC* buf2 = buf1 + maxn;
   TC* lane = buf2 + maxn;
-  unsigned char* pool = reinterpret_cast<unsigned char*>(lane + CR_LANES);
+  int* s_long = reinterpret_cast<int*>(lane + CR_LANES);
+  unsigned char* pool = reinterpret_cast<unsigned char*>(s_long) + ((long)maxn * 4 + 15) / 16 * 16;
   const long pool_bytes = smem_bytes - (long)(pool - smem_raw);
   const PIChain& ch = dchains ? dchains[blockIdx.x] : ((blockIdx.x == 0) ? ca : cb);
   double result = 1.0;
@@ -221,14 +221,9 @@ __global__ void __launch_bounds__(PI_THREADS)
         pi_rowptr<TF>(ops[(o + 3) % nops], r0, b3, e3);
         pi_entries<TF>(ops[(o + 1) % nops], P1);
         int* const nlong = &s_nlong[gop & 1];
-        auto defer = [&](int r, int b, int e) {
-          const int slot = atomicAdd(nlong, 1);
-          if (slot < PI_LONG_CAP) s_long[slot] = r;
-          else dst[r] = pi_row_thread<TC, TF>(op.ci, val, b, e, src);  // list full: same order, one thread
-        };
         if (r0 < op.rows) {
           if (P0.e - P0.b > PI_CHUNK) {
-            defer(r0, P0.b, P0.e);
+            s_long[atomicAdd(nlong, 1)] = r0;
           } else {
             TC acc = TC(0);
 #pragma unroll
@@ -241,7 +236,7 @@ __global__ void __launch_bounds__(PI_THREADS)
         for (int r = r0 + blockDim.x; r < op.rows; r += blockDim.x) {
           const int p0 = op.rp[r], p1 = op.rp[r + 1];
           if (p1 - p0 > PI_CHUNK) {
-            defer(r, p0, p1);
+            s_long[atomicAdd(nlong, 1)] = r;
             continue;
           }
           TC acc = TC(0);
@@ -250,7 +245,7 @@ __global__ void __launch_bounds__(PI_THREADS)
         }
         __syncthreads();
         {
-          const int nl = min(*nlong, PI_LONG_CAP);
+          const int nl = *nlong;
           if (threadIdx.x == 0) s_nlong[(gop + 1) & 1] = 0;
           for (int q = warp; q < nl; q += nwarps) {
             const int r = s_long[q];
@@ -376,7 +371,7 @@ template <typename TF, typename TC>
 static fgb_status launch_pi_t(fgb_ctx* ctx, const PIChain& a, const PIChain& b, int max_iter, double thr,
                               const int* d_rand, PIOut* d_out, const PIPalm& palm, cudaStream_t stream) {
   const int maxn = std::max(1, std::max(a.maxdim, b.maxdim));
-  const size_t vec = (3 * (size_t)maxn + CR_LANES) * sizeof(TC);
+  const size_t vec = (3 * (size_t)maxn + CR_LANES) * sizeof(TC) + ((size_t)maxn * 4 + 15) / 16 * 16;
   const size_t cap = std::min<size_t>(ctx->smem_optin > PI_STATIC_SMEM ? ctx->smem_optin - PI_STATIC_SMEM : 0,
                                       216 * 1024);
   if (vec > cap)
@@ -414,7 +409,7 @@ template <typename TF, typename TC>
 static fgb_status launch_pi_many_t(fgb_ctx* ctx, const PIChain* d_chains, int nchains, int maxn, int max_iter,
                                    double thr, PIOut* d_out, cudaStream_t stream) {
   maxn = std::max(1, maxn);
-  const size_t vec = (3 * (size_t)maxn + CR_LANES) * sizeof(TC);
+  const size_t vec = (3 * (size_t)maxn + CR_LANES) * sizeof(TC) + ((size_t)maxn * 4 + 15) / 16 * 16;
   const size_t cap = std::min<size_t>(ctx->smem_optin > PI_STATIC_SMEM ? ctx->smem_optin - PI_STATIC_SMEM : 0,
                                       216 * 1024);
   if (vec > cap)

@@ -27,12 +27,12 @@
 // Floating-point operation order.  Eigen's summation order cannot be restated
 // without Eigen, so this restatement fixes one explicit order and the CUDA
 // kernels follow the same order, giving bit-identical FP64/FP32 results:
-//   * every product entry  y = sum_p a_p * x_p  is a sequential fused
-//     multiply-add over the sparse operand's entries in stored order
-//     (rows sorted by column; transposed products walk the transpose's CSR,
-//     i.e. in increasing original row), starting from +0; inside the power
-//     iteration, rows of more than 16 entries are summed as 16-entry chunks
-//     combined by a pairwise tree (pi_row_dot below);
+//   * every product entry  y = sum_p a_p * x_p  runs over the sparse
+//     operand's entries in stored order (rows sorted by column; transposed
+//     products walk the transpose's CSR, i.e. in increasing original row):
+//     chunks of 16 entries are sequential fused multiply-adds from +0 and
+//     the chunk partials are added by a pairwise tree (row_dot below), so a
+//     row of at most 16 entries is one sequential fma chain;
 //   * every reduction (sum of squares, dot product) over N values in
 //     column-major linear order uses 256 lanes inside chunks of 65536 values:
 //     lane t accumulates (by fma) the values whose chunk offset is = t mod 256,
@@ -179,7 +179,40 @@ static inline float fma_(float a, float b, float c) { return std::fmaf(a, b, c);
 static inline double fma_(double a, double b, double c) { return std::fma(a, b, c); }
 
 // ---------------------------------------------------------------- products
-// Y = S * X.  y[i,j] = sequential fma over row i of S (faust_MatSparse.hpp:253-254).
+// The value of one sparse row times a dense vector, the sum over the row's
+// stored entries p of val[p] * x(colind[p]) (faust_MatSparse.hpp:253-254 sums
+// them in order).  Canonical order: the entries in stored order are cut into
+// chunks of ROW_CHUNK; each chunk is a sequential fma from +0; the chunk
+// partials P_0 .. P_{M-1} are added by the recursive-halving pairwise tree
+// (at stride s = 1, 2, 4, ...: Q_l += Q_{l+s} for l = 0 mod 2s, l + s < M).
+// A row of at most ROW_CHUNK entries is the plain sequential fma.  On GB300
+// one FP64 FMA warp instruction issues every 64 cycles per scheduler, so a
+// long row summed in order would be a chain of 64-cycle steps; the chunks
+// let the GPU split it over warps and combine by the same tree.
+static const int ROW_CHUNK = 16;
+
+template <typename T, typename G>
+static T row_dot(const T* val, const int* colind, int p0, int p1, const G& x) {
+  const int L = p1 - p0;
+  if (L <= ROW_CHUNK) {
+    T acc = T(0);
+    for (int p = p0; p < p1; ++p) acc = fma_(val[p], x(colind[p]), acc);
+    return acc;
+  }
+  const int M = (L + ROW_CHUNK - 1) / ROW_CHUNK;
+  std::vector<T> Q(M);
+  for (int m = 0; m < M; ++m) {
+    T acc = T(0);
+    const int e = std::min(p1, p0 + (m + 1) * ROW_CHUNK);
+    for (int p = p0 + m * ROW_CHUNK; p < e; ++p) acc = fma_(val[p], x(colind[p]), acc);
+    Q[m] = acc;
+  }
+  for (int st = 1; st < M; st *= 2)
+    for (int l = 0; l + st < M; l += 2 * st) Q[l] = Q[l] + Q[l + st];
+  return Q[0];
+}
+
+// Y = S * X: y[i,j] = row_dot of row i of S with column j of X.
 template <typename T>
 static Dense<T> spmm(const Csr<T>& S, const Dense<T>& X) {
   if (S.cols != X.rows) throw Error(ERR_INVALID, "spmm: dimension mismatch");
@@ -188,16 +221,13 @@ static Dense<T> spmm(const Csr<T>& S, const Dense<T>& X) {
   for (int j = 0; j < X.cols; ++j) {
     const T* x = &X.a[(size_t)j * X.rows];
     T* y = &Y.a[(size_t)j * Y.rows];
-    for (int i = 0; i < S.rows; ++i) {
-      T acc = T(0);
-      for (int p = S.rowptr[i]; p < S.rowptr[i + 1]; ++p) acc = fma_(S.val[p], x[S.colind[p]], acc);
-      y[i] = acc;
-    }
+    for (int i = 0; i < S.rows; ++i)
+      y[i] = row_dot(S.val.data(), S.colind.data(), S.rowptr[i], S.rowptr[i + 1], [&](int c) { return x[c]; });
   }
   return Y;
 }
 
-// Y = X * S^T given the CSR of S: y[r, c] = sum over row c of S of v * x[r, col].
+// Y = X * S^T given the CSR of S: y[r, c] = row_dot of row c of S with row r of X.
 template <typename T>
 static Dense<T> dense_times_csrT(const Dense<T>& X, const Csr<T>& S) {
   if (X.cols != S.cols) throw Error(ERR_INVALID, "dense_times_csrT: dimension mismatch");
@@ -205,52 +235,19 @@ static Dense<T> dense_times_csrT(const Dense<T>& X, const Csr<T>& S) {
 #pragma omp parallel for schedule(static)
   for (int c = 0; c < S.rows; ++c) {
     T* y = &Y.a[(size_t)c * Y.rows];
-    for (int r = 0; r < X.rows; ++r) {
-      T acc = T(0);
-      for (int p = S.rowptr[c]; p < S.rowptr[c + 1]; ++p)
-        acc = fma_(S.val[p], X.a[(size_t)S.colind[p] * X.rows + r], acc);
-      y[r] = acc;
-    }
+    for (int r = 0; r < X.rows; ++r)
+      y[r] = row_dot(S.val.data(), S.colind.data(), S.rowptr[c], S.rowptr[c + 1],
+                     [&](int k) { return X.a[(size_t)k * X.rows + r]; });
   }
   return Y;
 }
 
-// Sparse matrix times a vector inside the power iteration.  Each entry runs
-// over the row's stored entries in order, cut into chunks of PI_CHUNK: each
-// chunk is a sequential fma from +0 and the chunk partials P_0 .. P_{M-1}
-// are added by the recursive-halving pairwise tree (at stride s = 1, 2, 4,
-// ...: Q_l += Q_{l+s} for l = 0 mod 2s, l + s < M).  A row of at most
-// PI_CHUNK entries is the plain sequential fma.  With a single right-hand
-// column there is no other parallelism in a long row, and the chunks let a
-// GPU warp run it as independent short chains.
-static const int PI_CHUNK = 16;
-
-template <typename T>
-static T pi_row_dot(const T* val, const int* colind, int p0, int p1, const T* x) {
-  const int L = p1 - p0;
-  if (L <= PI_CHUNK) {
-    T acc = T(0);
-    for (int p = p0; p < p1; ++p) acc = fma_(val[p], x[colind[p]], acc);
-    return acc;
-  }
-  const int M = (L + PI_CHUNK - 1) / PI_CHUNK;
-  std::vector<T> Q(M);
-  for (int m = 0; m < M; ++m) {
-    T acc = T(0);
-    const int e = std::min(p1, p0 + (m + 1) * PI_CHUNK);
-    for (int p = p0 + m * PI_CHUNK; p < e; ++p) acc = fma_(val[p], x[colind[p]], acc);
-    Q[m] = acc;
-  }
-  for (int st = 1; st < M; st *= 2)
-    for (int l = 0; l + st < M; l += 2 * st) Q[l] = Q[l] + Q[l + st];
-  return Q[0];
-}
-
+// Sparse matrix times a vector (the power iteration): the same row order.
 template <typename T>
 static std::vector<T> pi_spmv(const Csr<T>& S, const std::vector<T>& x) {
   std::vector<T> y(S.rows);
-  for (int i = 0; i < S.rows; ++i) y[i] = pi_row_dot(S.val.data(), S.colind.data(), S.rowptr[i], S.rowptr[i + 1],
-                                                     x.data());
+  for (int i = 0; i < S.rows; ++i)
+    y[i] = row_dot(S.val.data(), S.colind.data(), S.rowptr[i], S.rowptr[i + 1], [&](int c) { return x[c]; });
   return y;
 }
 
@@ -459,7 +456,7 @@ struct Cons {
 // faust_ConstraintInt.hpp:203-230, faust_ConstraintFPP.hpp:152-167).
 // The result becomes the new factor; a dense prox image is kept as a full CSR
 // (every entry), which yields the same products as a dense factor under the
-// sequential fma order, so the dense/sparse output rule of prox_*_gen
+// canonical row order, so the dense/sparse output rule of prox_*_gen
 // (faust_prox_gen.hpp) does not change any value.
 template <typename T>
 static void project(const Cons<T>& c, Dense<T>& D) {

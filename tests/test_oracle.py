@@ -321,10 +321,10 @@ def _row_value(vals, xs, chunk=16):
     return parts[0] if parts else 0.0
 
 
-def test_pi_row_order_chunked_tree(oracle):
-    """The power iteration's sparse-row products follow the chunked tree
-    order (rows of 1..200 entries, including lengths around the 16-entry
-    chunk and the powers of two of the tree); plain products stay sequential."""
+def test_row_order_chunked_tree(oracle):
+    """Sparse-row products (chain products and the power iteration's) follow
+    the chunked tree order: rows of 1..200 entries, including lengths around
+    the 16-entry chunk and the powers of two of the tree."""
     import scipy.sparse as sps
     rng = np.random.default_rng(17)
     lens = [1, 2, 15, 16, 17, 31, 32, 33, 48, 63, 64, 65, 100, 127, 128, 129, 200]
@@ -344,4 +344,4 @@ def test_pi_row_order_chunked_tree(oracle):
         p0, p1 = S.indptr[i], S.indptr[i + 1]
         vals, xs = list(S.data[p0:p1]), [x[c, 0] for c in S.indices[p0:p1]]
         assert got[i] == _row_value(vals, xs), lens[i]
-        assert seq[i] == _row_value(vals, xs, chunk=1 << 30), lens[i]
+        assert seq[i] == got[i], lens[i]
