@@ -113,20 +113,38 @@ __global__ void __launch_bounds__(SPMM_THREADS)
 // columns), lanes along the columns, the row's chunk groups split over the
 // warps (rowdot.cuh), so every FP64 FMA instruction has 32 active lanes and
 // a row of L entries takes about L / 8 dependent steps instead of L.
+// The long rows among rows y, y + ny, y + 2 ny, ... (up to 256 per pass,
+// found by all threads at once) into a shared list; returns their number.
+__device__ __forceinline__ int long_rows_scan(const int* __restrict__ rowptr, int rows, int i0, int stride, int* list,
+                                              int* cnt) {
+  if (threadIdx.x == 0) *cnt = 0;
+  __syncthreads();
+  const int i = i0 + (int)threadIdx.x * stride;
+  if (i < rows && rowptr[i + 1] - rowptr[i] > ROW_CHUNK) list[atomicAdd(cnt, 1)] = i;
+  __syncthreads();
+  return *cnt;
+}
+
 template <typename T>
 __global__ void __launch_bounds__(256)
     k_csr_spmm_long(const int* __restrict__ rowptr, const int* __restrict__ colind, const T* __restrict__ val,
                     int rows, const T* __restrict__ X, int ldx, int ncols, T* __restrict__ Y, int ldy, Epi<T> epi) {
   __shared__ T roots[ROW_GROUPS * 32];
+  __shared__ int list[256], cnt;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const long j = (long)blockIdx.x * 32 + lane;
   const bool okj = j < ncols;
   const T* __restrict__ xcol = X + (okj ? j : 0) * (long)ldx;
-  for (int i = blockIdx.y; i < rows; i += gridDim.y) {
-    const int p0 = rowptr[i], p1 = rowptr[i + 1];
-    if (p1 - p0 <= ROW_CHUNK) continue;
-    const T v = row_block_long<T, 8>(val, colind, p0, p1, [&](int c) { return __ldg(xcol + c); }, roots, lane, warp);
-    if (warp == 0 && okj) Y[i + j * (long)ldy] = epi_apply(epi, v, i, j, epi.scal ? *epi.scal : T(0));
+  // rows y + gridDim.y * t, 256 of them per pass
+  for (int i0 = blockIdx.y; i0 < rows; i0 += gridDim.y * 256) {
+    const int nl = long_rows_scan(rowptr, rows, i0, gridDim.y, list, &cnt);
+    for (int q = 0; q < nl; ++q) {
+      const int i = list[q];
+      const T v = row_block_long<T, 8>(val, colind, rowptr[i], rowptr[i + 1], [&](int c) { return __ldg(xcol + c); },
+                                       roots, lane, warp);
+      if (warp == 0 && okj) Y[i + j * (long)ldy] = epi_apply(epi, v, i, j, epi.scal ? *epi.scal : T(0));
+    }
+    __syncthreads();
   }
 }
 
@@ -138,16 +156,20 @@ __global__ void __launch_bounds__(256)
                       const int* __restrict__ colind, const T* __restrict__ val, int srows, T* __restrict__ Y, int ldy,
                       Epi<T> epi) {
   __shared__ T roots[ROW_GROUPS * 32];
+  __shared__ int list[256], cnt;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int r = blockIdx.x * 32 + lane;
   const bool okr = r < xrows;
   const T* __restrict__ xr = X + (okr ? r : 0);
-  for (int c = blockIdx.y; c < srows; c += gridDim.y) {
-    const int p0 = rowptr[c], p1 = rowptr[c + 1];
-    if (p1 - p0 <= ROW_CHUNK) continue;
-    const T v = row_block_long<T, 8>(val, colind, p0, p1, [&](int k) { return __ldg(xr + (long)k * ldx); }, roots,
-                                     lane, warp);
-    if (warp == 0 && okr) Y[r + (long)c * ldy] = epi_apply(epi, v, r, c, epi.scal ? *epi.scal : T(0));
+  for (int c0 = blockIdx.y; c0 < srows; c0 += gridDim.y * 256) {
+    const int nl = long_rows_scan(rowptr, srows, c0, gridDim.y, list, &cnt);
+    for (int q = 0; q < nl; ++q) {
+      const int c = list[q];
+      const T v = row_block_long<T, 8>(val, colind, rowptr[c], rowptr[c + 1],
+                                       [&](int k) { return __ldg(xr + (long)k * ldx); }, roots, lane, warp);
+      if (warp == 0 && okr) Y[r + (long)c * ldy] = epi_apply(epi, v, r, c, epi.scal ? *epi.scal : T(0));
+    }
+    __syncthreads();
   }
 }
 
@@ -184,7 +206,7 @@ fgb_status launch_csr_spmm(fgb_ctx* ctx, const int* rowptr, const int* colind, c
   const bool has_long = max_row < 0 || max_row > ROW_CHUNK;
   const int long_row = has_long ? ROW_CHUNK + 1 : INT_MAX;
   if (has_long) {
-    dim3 g((unsigned)((ncols + 31) / 32), (unsigned)std::min(rows, 64));
+    dim3 g((unsigned)((ncols + 31) / 32), (unsigned)std::min((rows + 255) / 256 * 4, 16));
     k_csr_spmm_long<T><<<g, 256, 0, ctx->stream>>>(rowptr, colind, val, rows, X, ldx, ncols, Y, ldy, epi);
     FGB_LAUNCHED(ctx);
   }
@@ -226,7 +248,7 @@ fgb_status launch_dense_csrT(fgb_ctx* ctx, const T* X, int ldx, int xrows, const
   (void)scols;
   if (srows == 0 || xrows == 0) return FGB_OK;
   if (max_row < 0 || max_row > ROW_CHUNK) {
-    dim3 g((unsigned)((xrows + 31) / 32), (unsigned)std::min(srows, 64));
+    dim3 g((unsigned)((xrows + 31) / 32), (unsigned)std::min((srows + 255) / 256 * 4, 16));
     k_dense_csrT_long<T><<<g, 256, 0, ctx->stream>>>(X, ldx, xrows, rowptr, colind, val, srows, Y, ldy, epi);
     FGB_LAUNCHED(ctx);
   }
