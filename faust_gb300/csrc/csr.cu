@@ -252,13 +252,10 @@ fgb_status launch_dense_csrT(fgb_ctx* ctx, const T* X, int ldx, int xrows, const
     k_dense_csrT_long<T><<<g, 256, 0, ctx->stream>>>(X, ldx, xrows, rowptr, colind, val, srows, Y, ldy, epi);
     FGB_LAUNCHED(ctx);
   }
-  // Two warps per block: the blocks of one output column (same chain length
-  // for every thread) spread over many SMs, whose FP64 pipes (one warp
-  // instruction per 64 cycles per scheduler on GB300) bound long columns.
-  constexpr int DT = 64;
-  const int rblocks = std::max(1, std::min((xrows + DT - 1) / DT, 65535));
+  // rows of at most ROW_CHUNK entries: one block per output column
+  int rblocks = std::max(1, std::min((xrows + SPMM_THREADS - 1) / SPMM_THREADS, 8));
   dim3 grid(srows, rblocks);
-  k_dense_csrT<T><<<grid, DT, 0, ctx->stream>>>(X, ldx, xrows, rowptr, colind, val, srows, Y, ldy, epi);
+  k_dense_csrT<T><<<grid, SPMM_THREADS, 0, ctx->stream>>>(X, ldx, xrows, rowptr, colind, val, srows, Y, ldy, epi);
   FGB_LAUNCHED(ctx);
   return FGB_OK;
 }
