@@ -27,6 +27,7 @@
 namespace fgb {
 
 constexpr int PX_THREADS = 256;
+constexpr int RS_MAX_PASSES = 6;  // passes of the single-launch radix select
 constexpr int LINE_KMAX = 64;
 
 __device__ __forceinline__ unsigned long long mag_key(double v) {
@@ -54,6 +55,8 @@ fgb_status prox_work_reserve(fgb_ctx* ctx, ProxWork& w, long elems, int rows) {
   FGB_TRY(dmalloc(ctx, (void**)&w.row_cnt, sizeof(int) * (rows + 2)));
   FGB_CUDA(ctx, cudaMemsetAsync(w.flags, 0, (size_t)std::max(1L, elems), ctx->stream));
   FGB_CUDA(ctx, cudaMemsetAsync(w.hist, 0, sizeof(unsigned) * 2048, ctx->stream));
+  FGB_TRY(dmalloc(ctx, (void**)&w.hist_passes, sizeof(unsigned) * (RS_MAX_PASSES * 2048 + 2)));
+  FGB_CUDA(ctx, cudaMemsetAsync(w.hist_passes, 0, sizeof(unsigned) * (RS_MAX_PASSES * 2048 + 2), ctx->stream));
   w.cap_elems = elems;
   w.cap_rows = rows;
   w.growable = 1;
@@ -63,6 +66,8 @@ fgb_status prox_work_reserve(fgb_ctx* ctx, ProxWork& w, long elems, int rows) {
 void prox_work_free(ProxWork& w) {
   dfree(w.state);
   dfree(w.hist);
+  dfree(w.hist_passes);
+  w.hist_passes = nullptr;
   dfree(w.flags);
   dfree(w.chunk_cnt);
   dfree(w.partials);
@@ -142,6 +147,159 @@ __global__ void __launch_bounds__(PX_THREADS)
     if (L < 0 && lane == 0) st->status = FGB_ERR_INVALID_ARG;
   }
   if (threadIdx.x == 0) st->blocks_done = 0;
+}
+
+// ------------------------------------------------------------------ radix select, one launch
+// All the passes of the radix select in one cooperative launch: per pass,
+// every block histograms its share of the keys that match the prefix, adds
+// its bins to the pass's global histogram, waits at a grid barrier, and then
+// every block reads the histogram and picks the bucket itself (the same
+// choice everywhere), so only one barrier per pass is needed.  Histogram p-1
+// is cleared by block 0 after barrier p, the last one at the start of the
+// next call.  The barrier wait is bounded: on time-out the state's status is
+// set to FGB_ERR_TIMEOUT.
+__device__ __forceinline__ bool rs_grid_barrier(unsigned* bar, unsigned nblocks, int* s_ok) {
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    bool ok = true;
+    volatile unsigned* gen = bar + 1;
+    const unsigned g0 = *gen;
+    __threadfence();
+    if (atomicAdd(&bar[0], 1u) == nblocks - 1) {
+      bar[0] = 0;
+      __threadfence();
+      atomicAdd(&bar[1], 1u);
+    } else {
+      long spins = 0;
+      while (*gen == g0) {
+        if (++spins > (1L << 21)) {
+          ok = false;
+          break;
+        }
+        __nanosleep(64);
+      }
+    }
+    __threadfence();
+    *s_ok = ok;
+  }
+  __syncthreads();
+  return *s_ok != 0;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(PX_THREADS)
+    k_radix_select(const T* __restrict__ M, long N, int pos, int npass, TopkState* st, unsigned* hists) {
+  __shared__ unsigned sh[2048];
+  __shared__ unsigned long long s_prefix, s_mask;
+  __shared__ long long s_krem, s_G, s_E;
+  __shared__ int s_ok, s_bad;
+  __shared__ unsigned long long s_wsum[PX_THREADS / 32];
+  unsigned* bar = hists + RS_MAX_PASSES * 2048;
+  const int shifts8[6] = {52, 41, 30, 19, 8, 0}, bits8[6] = {11, 11, 11, 11, 11, 8};
+  const int shifts4[3] = {20, 9, 0}, bits4[3] = {11, 11, 9};
+  if (threadIdx.x == 0) {
+    s_prefix = 0;
+    s_mask = 0;
+    s_krem = st->k_rem;
+    s_G = 0;
+    s_E = 0;
+    s_bad = 0;
+  }
+  if (blockIdx.x == 0)
+    for (int i = threadIdx.x; i < 2048; i += blockDim.x) hists[(npass - 1) * 2048 + i] = 0;
+  bool timed_out = false;
+  for (int p = 0; p < npass; ++p) {
+    const int shift = sizeof(T) == 8 ? shifts8[p] : shifts4[p];
+    const int bits = sizeof(T) == 8 ? bits8[p] : bits4[p];
+    const int nb = 1 << bits;
+    unsigned* hist = hists + p * 2048;
+    for (int i = threadIdx.x; i < nb; i += blockDim.x) sh[i] = 0;
+    __syncthreads();
+    const unsigned long long prefix = s_prefix, mask = s_mask;
+    {
+      // eight keys per thread in flight before their (rare after pass 0) atomics
+      const long stride = (long)gridDim.x * blockDim.x;
+      long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+      for (; i + 7 * stride < N; i += 8 * stride) {
+        unsigned long long key[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) key[u] = mag_key(pos_adj(M[i + u * stride], pos));
+#pragma unroll
+        for (int u = 0; u < 8; ++u)
+          if ((key[u] & mask) == prefix) atomicAdd(&sh[(key[u] >> shift) & (nb - 1)], 1u);
+      }
+      for (; i < N; i += stride) {
+        const unsigned long long key = mag_key(pos_adj(M[i], pos));
+        if ((key & mask) == prefix) atomicAdd(&sh[(key >> shift) & (nb - 1)], 1u);
+      }
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < nb; i += blockDim.x)
+      if (sh[i]) atomicAdd(&hist[i], sh[i]);
+    __threadfence();
+    if (!rs_grid_barrier(bar, gridDim.x, &s_ok)) timed_out = true;
+    if (p > 0 && blockIdx.x == 0)
+      for (int i = threadIdx.x; i < 2048; i += blockDim.x) hists[(p - 1) * 2048 + i] = 0;
+    for (int i = threadIdx.x; i < nb; i += blockDim.x) sh[i] = __ldcg(&hist[i]);
+    __syncthreads();
+    // the bucket holding the k_rem-th largest key (every block alike):
+    // thread t owns bins nb-1-t*per .. nb-per-t*per (descending), a block
+    // scan of their sums finds the owner, which walks its bins
+    {
+      const int per = nb / PX_THREADS;  // 8, 2 or 1
+      const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+      unsigned long long sum = 0;
+      for (int j = 0; j < per; ++j) sum += sh[nb - 1 - (t * per + j)];
+      unsigned long long incl = sum;
+      for (int o = 1; o < 32; o <<= 1) {
+        const unsigned long long y = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += y;
+      }
+      if (lane == 31) s_wsum[warp] = incl;
+      __syncthreads();
+      if (warp == 0) {
+        unsigned long long w = lane < PX_THREADS / 32 ? s_wsum[lane] : 0;
+        for (int o = 1; o < 32; o <<= 1) {
+          const unsigned long long y = __shfl_up_sync(0xffffffffu, w, o);
+          if (lane >= o) w += y;
+        }
+        if (lane < PX_THREADS / 32) s_wsum[lane] = w;  // inclusive warp totals
+      }
+      __syncthreads();
+      incl += warp ? s_wsum[warp - 1] : 0ULL;
+      const unsigned long long excl = incl - sum;
+      const long long krem = s_krem;
+      const long long total = (long long)s_wsum[PX_THREADS / 32 - 1];
+      __syncthreads();  // everyone has read s_krem before the owner updates it
+      if ((long long)excl < krem && krem <= (long long)incl) {
+        unsigned long long cum = excl;
+        for (int j = 0; j < per; ++j) {
+          const int b = nb - 1 - (t * per + j);
+          const unsigned long long h = sh[b];
+          if ((long long)(cum + h) >= krem) {
+            s_G += (long long)cum;
+            s_krem = krem - (long long)cum;
+            s_prefix = prefix | ((unsigned long long)b << shift);
+            s_mask = mask | ((unsigned long long)(nb - 1) << shift);
+            s_E = (long long)h;
+            break;
+          }
+          cum += h;
+        }
+      }
+      if (t == 0 && total < krem) s_bad = 1;
+    }
+    __syncthreads();
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    st->prefix = s_prefix;
+    st->mask = s_mask;
+    st->k_rem = s_krem;
+    st->G = s_G;
+    st->E = s_E;
+    if (s_bad) atomicCAS(&st->status, 0, (int)FGB_ERR_INVALID_ARG);
+  }
+  if (timed_out && threadIdx.x == 0) atomicCAS(&st->status, 0, (int)FGB_ERR_TIMEOUT);
 }
 
 // ------------------------------------------------------------------ tie case
@@ -1308,7 +1466,30 @@ static fgb_status queue_sp(fgb_ctx* ctx, ProxWork& w, T* M, long N, long k, int 
   k_topk_init<<<1, 1, 0, ctx->stream>>>(w.state, k);
   FGB_LAUNCHED(ctx);
   const int g = grid_for(ctx, N);
-  if (sizeof(T) == 8) {
+  if (w.hist_passes) {
+    // every pass in one cooperative launch (blocks co-resident for the barrier)
+    static thread_local int coop_blocks[2] = {0, 0};
+    int& nb = coop_blocks[sizeof(T) == 8];
+    if (!nb) {
+      int per_sm = 0;
+      FGB_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_radix_select<T>, PX_THREADS, 0));
+      nb = std::max(1, std::min(per_sm, 2)) * ctx->sm_count;
+    }
+    const int grid = (int)std::min<long>(nb, std::max(1L, (N + PX_THREADS - 1) / PX_THREADS));
+    const int npass = sizeof(T) == 8 ? 6 : 3;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(PX_THREADS);
+    cfg.stream = ctx->stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    const T* Mc = M;
+    FGB_CUDA(ctx, cudaLaunchKernelEx(&cfg, k_radix_select<T>, Mc, N, pos, npass, w.state, w.hist_passes));
+    FGB_LAUNCHED(ctx);
+  } else if (sizeof(T) == 8) {
     const int shifts[6] = {52, 41, 30, 19, 8, 0};
     const int bits[6] = {11, 11, 11, 11, 11, 8};
     for (int p = 0; p < 6; ++p) {

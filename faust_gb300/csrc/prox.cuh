@@ -45,6 +45,9 @@ struct ProxWork {
   int* wcount = nullptr;             // per-window candidate counts
   void* heap2 = nullptr;             // split heap (keys, positions) when it does not fit on chip
   long heap2_cap = 0;
+  // single-launch radix select (workspaces made by prox_work_reserve): one
+  // 2048-bin histogram per pass, then the grid barrier's two words
+  unsigned* hist_passes = nullptr;
 };
 
 fgb_status prox_work_reserve(fgb_ctx* ctx, ProxWork& w, long elems, int rows);
