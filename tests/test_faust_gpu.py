@@ -228,6 +228,43 @@ def test_spectral_norm_matches_oracle(fgb, oracle):
     assert got == ref
 
 
+def _long_row_factors(rng, dims, dtype, lengths):
+    """CSR factors with a few rows of the given lengths (beyond the 16-entry
+    chunk, past 256 entries = one chunk group round of 8 warps, past 4096 =
+    several rounds of 64 chunk groups) on top of 3 random entries per row."""
+    import scipy.sparse as sp
+    facs = []
+    for q in range(len(dims) - 1):
+        r, c = dims[q], dims[q + 1]
+        A = synth.random_csr(r, c, 3, rng, dtype).tolil()
+        rows = rng.choice(r, len(lengths), replace=False)
+        for i, L in zip(rows, lengths):
+            L = min(L, c)
+            cols = rng.choice(c, L, replace=False)
+            A[i, cols] = rng.standard_normal(L).astype(dtype)
+        facs.append(sp.csr_matrix(A, dtype=dtype))
+    return facs
+
+
+@pytest.mark.parametrize("dtype", [np.float64, np.float32])
+def test_long_rows_products_bitexact(fgb, oracle, dtype):
+    """Products with rows (and columns, for F^T) of 17 to 6000 entries: the
+    long-row kernels follow the chunked row order of the oracle bit for bit,
+    for F X and F^T X and in both product modes."""
+    rng = np.random.default_rng(31)
+    dims = [6200, 6100, 6300]
+    facs = _long_row_factors(rng, dims, dtype, [17, 33, 255, 257, 1000, 4096, 4097, 6000])
+    F = fgb.Faust(facs, dtype=dtype)
+    X = synth.dense_colmajor(dims[-1], 45, rng, dtype)
+    ref = oracle.chain_mul(facs, X)
+    for mode in (0, 1):
+        assert np.array_equal(_to_np(F.matmul_device(_colmajor_cuda(X), mode=mode)), ref), mode
+    Xt = synth.dense_colmajor(dims[0], 40, rng, dtype)
+    ref_t = oracle.chain_mul([f.T.tocsr() for f in facs[::-1]], Xt)
+    assert np.array_equal(_to_np(F.matmul_op_device("T", _colmajor_cuda(Xt))), ref_t)
+    F.close()
+
+
 @pytest.mark.parametrize("shape", [(1024, 1024), (700, 900)])
 def test_spectral_norm_long_rows_matches_oracle(fgb, oracle, shape):
     """Rows and columns far longer than the 16-entry chunk of the power

@@ -156,3 +156,29 @@ def test_toarray_butterfly_and_ldy(oracle):
     assert np.array_equal(Y.cpu().numpy(), want)
     assert torch.all(Ypad[1024:, :] == 7.0)
     F.close()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("dtype", [np.float64, np.float32])
+def test_product_long_rows_bitexact(oracle, dtype):
+    """DYNPROG products that multiply a dense intermediate by sparse factors
+    with long rows and columns (dense x CSR^T long-row kernel) and the default
+    order, bit for bit against the oracle."""
+    import scipy.sparse as sps
+    rng = np.random.default_rng(41)
+    facs = []
+    for (r, c) in [(300, 1200), (1200, 900), (900, 1300), (1300, 500)]:
+        A = sps.random(r, c, density=0.004, format="lil", dtype=dtype, random_state=rng)
+        for i in rng.choice(r, 6, replace=False):
+            L = int(rng.integers(17, c))
+            A[i, rng.choice(c, L, replace=False)] = rng.standard_normal(L).astype(dtype)
+        for j in rng.choice(c, 6, replace=False):
+            L = int(rng.integers(17, r))
+            A[rng.choice(r, L, replace=False), j] = rng.standard_normal(L).astype(dtype)
+        facs.append(sps.csr_matrix(A))
+    F = _faust(facs, dtype)
+    for order, code in (("DEFAULT_L2R", 0), ("DYNPROG", 5)):
+        for op in ("N", "T"):
+            got = F.product_device(op, order).cpu().numpy()
+            assert np.array_equal(got, oracle.faust_product(facs, op, code)), (order, op)
+    F.close()
