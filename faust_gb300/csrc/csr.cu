@@ -80,8 +80,17 @@ __global__ void __launch_bounds__(SPMM_THREADS)
   T* tile = reinterpret_cast<T*>(smem_raw);
   const int j0 = blockIdx.x * TC;
   if (STAGED) {
-    stage_tile<T, TC>(tile, X, ldx, inner, j0, ncols);
-    __syncthreads();
+    // the tile is only needed by rows this kernel computes (1 .. long_row-1
+    // entries); factors whose entries all sit in long rows skip it
+    int need = 0;
+    for (int r = threadIdx.x; r < rows; r += blockDim.x) {
+      const int L = rowptr[r + 1] - rowptr[r];
+      need |= (L > 0 && L < long_row);
+    }
+    if (__syncthreads_or(need)) {
+      stage_tile<T, TC>(tile, X, ldx, inner, j0, ncols);
+      __syncthreads();
+    }
   }
   const T s = epi.scal ? *epi.scal : T(0);
   for (int i = blockIdx.y * blockDim.x + threadIdx.x; i < rows; i += gridDim.y * blockDim.x) {

@@ -241,19 +241,11 @@ __device__ __noinline__ void b_spmm(const int* rp, const int* ci, const T* v, in
 #pragma unroll
       for (int u = 0; u < G; ++u) acc[u] = T(0);
       const int p0 = S.rp[i], p1 = S.rp[i + 1];
-      if (p1 - p0 > ROW_CHUNK) {
-        // rows of more than ROW_CHUNK entries: the chunked order of rowdot.cuh
-        row_long_g<T, G, 10>(S.ci, S.v, p0, p1, sg.p + g * G, sx,
-                             [](const T* q, T (&o)[G]) { Vec16<T>::load(q, o); }, acc);
-      } else {
-        for (int p = p0; p < p1; ++p) {
-          const T val = S.v[p];
-          T xv[G];
-          Vec16<T>::load(sg.p + S.ci[p] * sx + g * G, xv);
-#pragma unroll
-          for (int u = 0; u < G; ++u) acc[u] = fmad(val, xv[u], acc[u]);
-        }
-      }
+      // the canonical row order (rowdot.cuh) on one code path for every row
+      // length (a short row is a single chunk), so that long and short rows
+      // of one warp do not run one after the other
+      row_long_g<T, G, 10>(S.ci, S.v, p0, p1, sg.p + g * G, sx,
+                           [](const T* q, T (&o)[G]) { Vec16<T>::load(q, o); }, acc);
 #pragma unroll
       for (int u = 0; u < G; ++u) {
         const int c = g * G + u;
@@ -314,19 +306,11 @@ __device__ __noinline__ void b_dense_csrT(const T* X, int xrows, int xcols, cons
 #pragma unroll
       for (int u = 0; u < G; ++u) acc[u] = T(0);
       const int p0 = S.rp[c], p1 = S.rp[c + 1];
-      if (p1 - p0 > ROW_CHUNK) {
-        // rows of more than ROW_CHUNK entries: the chunked order of rowdot.cuh
-        row_long_g<T, G, 10>(S.ci, S.v, p0, p1, sg.p + g * G, nrp,
-                             [](const T* q, T (&o)[G]) { Vec16<T>::load(q, o); }, acc);
-      } else {
-        for (int p = p0; p < p1; ++p) {
-          const T val = S.v[p];
-          T xv[G];
-          Vec16<T>::load(sg.p + S.ci[p] * nrp + g * G, xv);
-#pragma unroll
-          for (int u = 0; u < G; ++u) acc[u] = fmad(val, xv[u], acc[u]);
-        }
-      }
+      // the canonical row order (rowdot.cuh) on one code path for every row
+      // length (a short row is a single chunk), so that long and short rows
+      // of one warp do not run one after the other
+      row_long_g<T, G, 10>(S.ci, S.v, p0, p1, sg.p + g * G, nrp,
+                           [](const T* q, T (&o)[G]) { Vec16<T>::load(q, o); }, acc);
 #pragma unroll
       for (int u = 0; u < G; ++u) {
         const int rl = g * G + u;

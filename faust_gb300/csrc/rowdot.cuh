@@ -96,7 +96,7 @@ struct TreeAccG {
   }
 };
 
-// A row of more than ROW_CHUNK entries for G consecutive columns: the dense
+// A row (any length; one chunk when short) for G consecutive columns: the dense
 // operand of column u is x[colind * stride + u] (a row-major tile), loaded
 // G at a time by LOAD(ptr, vals).
 template <typename T, int G, int LEVELS, typename Load>
@@ -121,7 +121,7 @@ __device__ __forceinline__ void row_long_g(const int* __restrict__ ci, const T* 
     T carry[G];
     t.push(m, P, carry);
   }
-  if (b < p1) {
+  if (b < p1 || m == 0) {
     T P[G];
 #pragma unroll
     for (int u = 0; u < G; ++u) P[u] = T(0);
