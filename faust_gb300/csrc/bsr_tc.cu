@@ -30,28 +30,40 @@ namespace fgb {
 namespace tc {
 
 constexpr int BLK = 64;         // BSR block size
-constexpr int TM = 128;         // columns of X per tile (MMA M)
-constexpr int STAGES = 8;
+constexpr int TM = 128;         // columns of X per MMA (M)
 constexpr int A_BYTES = TM * BLK * 2;   // 16 KB
 constexpr int B_BYTES = BLK * BLK * 2;  // 8 KB
-constexpr int STAGE_BYTES = A_BYTES + B_BYTES;
-constexpr int ACC_BUFS = 4;
-constexpr int TMEM_COLS = ACC_BUFS * BLK;  // 256
+constexpr int TMEM_COLS = 256;
 constexpr int THREADS = 192;
 
+// NS slabs of 128 columns of X per item share each block's load (NS = 2:
+// 40 KB per stage instead of 2 x 24 KB for the same work, the L2-to-SM stream
+// that bounds the kernel); the accumulators of an item take NS x 64 TMEM
+// columns.
+template <int NS>
+struct Cfg {
+  static constexpr int STAGES = NS == 2 ? 5 : 8;
+  static constexpr int STAGE_BYTES = NS * A_BYTES + B_BYTES;
+  static constexpr int ACC_BUFS = TMEM_COLS / (NS * BLK);
+  static constexpr int ITEM_COLS = NS * TM;
+};
+
 struct Shared {
-  uint64_t full[STAGES];
-  uint64_t empty[STAGES];
-  uint64_t acc_full[ACC_BUFS];
-  uint64_t acc_empty[ACC_BUFS];
+  uint64_t full[8];
+  uint64_t empty[8];
+  uint64_t acc_full[4];
+  uint64_t acc_empty[4];
   uint32_t tmem_base;
   int abort_flag;
 };
 
+template <int NS>
 __global__ void __launch_bounds__(THREADS, 1)
     k_bsr_tc(const __grid_constant__ CUtensorMap tmX, const __grid_constant__ CUtensorMap tmB,
              const int* __restrict__ browptr, const int* __restrict__ bcolind, int nbr, int nnzb, int stage_idx,
              int mtiles, __nv_bfloat16* __restrict__ Y, long ldy, int* __restrict__ err) {
+  constexpr int STAGES = Cfg<NS>::STAGES, STAGE_BYTES = Cfg<NS>::STAGE_BYTES, ACC_BUFS = Cfg<NS>::ACC_BUFS;
+  constexpr int ITEM_COLS = Cfg<NS>::ITEM_COLS;
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   // stage buffers start at a 1024-byte boundary (128-byte swizzle atoms)
   unsigned char* base = reinterpret_cast<unsigned char*>(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
@@ -122,8 +134,9 @@ __global__ void __launch_bounds__(THREADS, 1)
           if (lane == 0) {
             unsigned char* st = base + s * STAGE_BYTES;
             mbar_expect_tx(&sh->full[s], STAGE_BYTES);
-            tma_load_2d(st, &tmX, bc * BLK, mt * TM, &sh->full[s]);
-            tma_load_2d(st + A_BYTES, &tmB, 0, (pb + q) * BLK, &sh->full[s]);
+#pragma unroll
+            for (int h = 0; h < NS; ++h) tma_load_2d(st + h * A_BYTES, &tmX, bc * BLK, mt * ITEM_COLS + h * TM, &sh->full[s]);
+            tma_load_2d(st + NS * A_BYTES, &tmB, 0, (pb + q) * BLK, &sh->full[s]);
           }
           pend[s] = (int)ph;
           if (++s == STAGES) {
@@ -162,19 +175,23 @@ __global__ void __launch_bounds__(THREADS, 1)
           break;
         }
         fence_after();
-        const uint32_t d = tmem + (uint32_t)(a * BLK);
+        const uint32_t d = tmem + (uint32_t)(a * NS * BLK);
         for (int p = p0; p < p1; ++p) {
           if (!mbar_wait(&sh->full[s], ph, abort_flag)) {
             ok = false;
             break;
           }
           fence_after();
-          const uint32_t sa = su32(base + s * STAGE_BYTES), sb = sa + A_BYTES;
-          const uint64_t ad = sdesc_k128(sa), bd = sdesc_k128(sb);
+          const uint32_t sa = su32(base + s * STAGE_BYTES), sb = sa + NS * A_BYTES;
+          const uint64_t bd = sdesc_k128(sb);
 #pragma unroll
-          for (int k = 0; k < BLK / 16; ++k)
-            mma_bf16(d, ad + (uint64_t)((k * 32) >> 4), bd + (uint64_t)((k * 32) >> 4), idesc_bf16(TM, BLK),
-                     (p > p0 || k > 0) ? 1u : 0u);
+          for (int h = 0; h < NS; ++h) {
+            const uint64_t ad = sdesc_k128(sa + h * A_BYTES);
+#pragma unroll
+            for (int k = 0; k < BLK / 16; ++k)
+              mma_bf16(d + (uint32_t)(h * BLK), ad + (uint64_t)((k * 32) >> 4), bd + (uint64_t)((k * 32) >> 4),
+                       idesc_bf16(TM, BLK), (p > p0 || k > 0) ? 1u : 0u);
+          }
           mma_commit(&sh->empty[s]);
           if (++s == STAGES) {
             s = 0;
@@ -202,12 +219,15 @@ __global__ void __launch_bounds__(THREADS, 1)
     for (long it = blockIdx.x; it < items && ok; it += gridDim.x) {
       const int mt = (int)(it / nbr), br = (int)(it % nbr);
       const int p0 = rp[br], p1 = rp[br + 1];
-      const long j = (long)mt * TM + q * 32 + lane;
-      uint4* dst = reinterpret_cast<uint4*>(Y + j * ldy + (long)br * BLK);
       if (p1 == p0) {
         const uint4 z = make_uint4(0, 0, 0, 0);
 #pragma unroll
-        for (int u = 0; u < 8; ++u) dst[u] = z;
+        for (int h = 0; h < NS; ++h) {
+          const long j = (long)mt * ITEM_COLS + h * TM + q * 32 + lane;
+          uint4* dst = reinterpret_cast<uint4*>(Y + j * ldy + (long)br * BLK);
+#pragma unroll
+          for (int u = 0; u < 8; ++u) dst[u] = z;
+        }
         continue;
       }
       bool got = true;
@@ -219,22 +239,30 @@ __global__ void __launch_bounds__(THREADS, 1)
       }
       fence_after();
       uint32_t r[32];
-      uint32_t packed[32];
-      const uint32_t taddr = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(a * BLK);
-      tmem_ld32(taddr, r);
-      tmem_ld_wait();
+      uint32_t packed[NS][32];
 #pragma unroll
-      for (int u = 0; u < 16; ++u) packed[u] = pack_bf16(r[2 * u], r[2 * u + 1]);
-      tmem_ld32(taddr + 32, r);
-      tmem_ld_wait();
+      for (int h = 0; h < NS; ++h) {
+        const uint32_t taddr = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(a * NS * BLK + h * BLK);
+        tmem_ld32(taddr, r);
+        tmem_ld_wait();
 #pragma unroll
-      for (int u = 0; u < 16; ++u) packed[16 + u] = pack_bf16(r[2 * u], r[2 * u + 1]);
+        for (int u = 0; u < 16; ++u) packed[h][u] = pack_bf16(r[2 * u], r[2 * u + 1]);
+        tmem_ld32(taddr + 32, r);
+        tmem_ld_wait();
+#pragma unroll
+        for (int u = 0; u < 16; ++u) packed[h][16 + u] = pack_bf16(r[2 * u], r[2 * u + 1]);
+      }
       fence_before();
       __syncwarp();
       if (lane == 0) mbar_arrive(&sh->acc_empty[a]);
 #pragma unroll
-      for (int u = 0; u < 8; ++u)
-        dst[u] = make_uint4(packed[4 * u], packed[4 * u + 1], packed[4 * u + 2], packed[4 * u + 3]);
+      for (int h = 0; h < NS; ++h) {
+        const long j = (long)mt * ITEM_COLS + h * TM + q * 32 + lane;
+        uint4* dst = reinterpret_cast<uint4*>(Y + j * ldy + (long)br * BLK);
+#pragma unroll
+        for (int u = 0; u < 8; ++u)
+          dst[u] = make_uint4(packed[h][4 * u], packed[h][4 * u + 1], packed[h][4 * u + 2], packed[h][4 * u + 3]);
+      }
       if (++a == ACC_BUFS) {
         a = 0;
         aph ^= 1u;
@@ -315,8 +343,12 @@ fgb_status launch_bsr_tc(fgb_ctx* ctx, const DevFactor& f, const __nv_bfloat16* 
   if (f.bm != 64 || f.bn != 64 || f.nnz == 0) return FGB_OK;
   if (ncols % tc::TM || ldx % 8 || ldy % 8) return FGB_OK;
   if (((uintptr_t)X & 15) || ((uintptr_t)Y & 15)) return FGB_OK;
-  const int nbr = f.rows / tc::BLK, mtiles = ncols / tc::TM;
-  const size_t base_smem = tc::STAGES * tc::STAGE_BYTES + ((sizeof(tc::Shared) + 15) & ~(size_t)15) + 1024;
+  // two 128-column slabs per item when the columns come in pairs of tiles
+  const bool two = ncols % (2 * tc::TM) == 0;
+  const int nbr = f.rows / tc::BLK, mtiles = ncols / (two ? 2 * tc::TM : tc::TM);
+  const size_t stage_bytes = two ? (size_t)tc::Cfg<2>::STAGES * tc::Cfg<2>::STAGE_BYTES
+                                 : (size_t)tc::Cfg<1>::STAGES * tc::Cfg<1>::STAGE_BYTES;
+  const size_t base_smem = stage_bytes + ((sizeof(tc::Shared) + 15) & ~(size_t)15) + 1024;
   if (base_smem > ctx->smem_optin) return FGB_OK;
   const size_t idx_bytes = sizeof(int) * ((size_t)((nbr + 1 + 3) & ~3) + (size_t)f.nnz);
   const bool stage_idx = base_smem + idx_bytes <= ctx->smem_optin;
@@ -331,15 +363,16 @@ fgb_status launch_bsr_tc(fgb_ctx* ctx, const DevFactor& f, const __nv_bfloat16* 
     FGB_TRY(dmalloc(ctx, (void**)&g_err, sizeof(int)));
     FGB_CUDA(ctx, cudaMemset(g_err, 0, sizeof(int)));
   }
-  static size_t attr = 0;
-  if (smem > attr) {
-    FGB_CUDA(ctx, cudaFuncSetAttribute(tc::k_bsr_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    attr = smem;
+  auto kern = two ? tc::k_bsr_tc<2> : tc::k_bsr_tc<1>;
+  static size_t attr[2] = {0, 0};
+  if (smem > attr[two]) {
+    FGB_CUDA(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    attr[two] = smem;
   }
   const long items = (long)nbr * mtiles;
   const int grid = (int)std::min<long>(items, ctx->sm_count);
-  tc::k_bsr_tc<<<grid, tc::THREADS, smem, ctx->stream>>>(mx, mb, f.rowptr, f.colind, nbr, f.nnz, stage_idx ? 1 : 0,
-                                                         mtiles, Y, (long)ldy, g_err);
+  kern<<<grid, tc::THREADS, smem, ctx->stream>>>(mx, mb, f.rowptr, f.colind, nbr, f.nnz, stage_idx ? 1 : 0, mtiles,
+                                                 Y, (long)ldy, g_err);
   FGB_LAUNCHED(ctx);
   *taken = true;
   return FGB_OK;
