@@ -239,7 +239,7 @@ def run_faust_x(args, rank, world):
     elif W.name == "bsr":
         fl = W.flops / len(W.bsr)
         roof = {"bound": "tensor", "achieved": round(fl / launch_s / 1e12, 1), "peak": tflops, "unit": "TFLOP/s",
-                "frac": round(fl / launch_s / 1e12 / tflops, 4), "traffic": 255876096,
+                "frac": round(fl / launch_s / 1e12 / tflops, 4), "traffic": 259319552,
                 "traffic_note": "dram read + write bytes of one launch, ncu capture", "peak_kind": peak_kind,
                 "kernel": "k_bsr_tc", "algorithmic_flops_per_launch": int(fl), "algorithmic_bytes_per_launch": int(kb)}
     else:
