@@ -323,6 +323,17 @@ fgb_faust::~fgb_faust() {
   fgb::dfree(chain_desc);
   fgb::dfree(chain_desc_t);
   fgb::dfree(pws);
+  if (s_in) {
+    cudaStreamSynchronize(s_in);
+    cudaStreamSynchronize(s_out);
+    cudaStreamDestroy(s_in);
+    cudaStreamDestroy(s_out);
+    for (int c = 0; c < 4; ++c) {
+      cudaEventDestroy(ev_in[c]);
+      cudaEventDestroy(ev_done[c]);
+    }
+    cudaEventDestroy(ev_start);
+  }
   if (hx) cudaFreeHost(hx);
   if (hy) cudaFreeHost(hy);
 }
@@ -464,9 +475,48 @@ fgb_status fgb_faust_mul_host(fgb_faust* F, const void* X, int ncols, void* Y) {
     FGB_TRY(dmalloc(ctx, &F->dy, need));
     F->dxy_bytes = need;
   }
-  FGB_CUDA(ctx, cudaMemcpyAsync(F->dx, X, xb, cudaMemcpyHostToDevice, ctx->stream));
-  FGB_TRY(fgb_faust_mul(F, F->dx, inner, ncols, F->dy, rows, 0));
-  FGB_CUDA(ctx, cudaMemcpyAsync(Y, F->dy, yb, cudaMemcpyDeviceToHost, ctx->stream));
+  // Column chunks pipelined over three streams: the copy of chunk c + 1 in,
+  // the product of chunk c and the copy of chunk c - 1 out overlap (host
+  // buffers in pinned memory let the copy engines run beside the kernels).
+  // Columns are independent, so the result does not depend on the chunking.
+  int nchunk = 1;
+  if (xb + yb >= ((size_t)32 << 20)) nchunk = (int)std::min<long>(4, std::max<long>(1, ncols / 512));
+  if (nchunk == 1) {
+    FGB_CUDA(ctx, cudaMemcpyAsync(F->dx, X, xb, cudaMemcpyHostToDevice, ctx->stream));
+    FGB_TRY(fgb_faust_mul(F, F->dx, inner, ncols, F->dy, rows, 0));
+    FGB_CUDA(ctx, cudaMemcpyAsync(Y, F->dy, yb, cudaMemcpyDeviceToHost, ctx->stream));
+    FGB_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return FGB_OK;
+  }
+  if (!F->s_in) {
+    FGB_CUDA(ctx, cudaStreamCreateWithFlags(&F->s_in, cudaStreamNonBlocking));
+    FGB_CUDA(ctx, cudaStreamCreateWithFlags(&F->s_out, cudaStreamNonBlocking));
+    for (int c = 0; c < 4; ++c) {
+      FGB_CUDA(ctx, cudaEventCreateWithFlags(&F->ev_in[c], cudaEventDisableTiming));
+      FGB_CUDA(ctx, cudaEventCreateWithFlags(&F->ev_done[c], cudaEventDisableTiming));
+    }
+    FGB_CUDA(ctx, cudaEventCreateWithFlags(&F->ev_start, cudaEventDisableTiming));
+  }
+  // the copies start after the work already queued on the context's stream
+  FGB_CUDA(ctx, cudaEventRecord(F->ev_start, ctx->stream));
+  FGB_CUDA(ctx, cudaStreamWaitEvent(F->s_in, F->ev_start, 0));
+  // whole 256-column tiles per chunk keep the BSR tensor-core path
+  const int per = ((ncols + nchunk - 1) / nchunk + 255) / 256 * 256;
+  for (int c = 0; c < nchunk; ++c) {
+    const int c0 = c * per, nc = std::min(per, ncols - c0);
+    if (nc <= 0) break;
+    FGB_CUDA(ctx, cudaMemcpyAsync((char*)F->dx + es * (size_t)inner * c0, (const char*)X + es * (size_t)inner * c0,
+                                  es * (size_t)inner * nc, cudaMemcpyHostToDevice, F->s_in));
+    FGB_CUDA(ctx, cudaEventRecord(F->ev_in[c], F->s_in));
+    FGB_CUDA(ctx, cudaStreamWaitEvent(ctx->stream, F->ev_in[c], 0));
+    FGB_TRY(fgb_faust_mul(F, (char*)F->dx + es * (size_t)inner * c0, inner, nc, (char*)F->dy + es * (size_t)rows * c0,
+                          rows, 0));
+    FGB_CUDA(ctx, cudaEventRecord(F->ev_done[c], ctx->stream));
+    FGB_CUDA(ctx, cudaStreamWaitEvent(F->s_out, F->ev_done[c], 0));
+    FGB_CUDA(ctx, cudaMemcpyAsync((char*)Y + es * (size_t)rows * c0, (const char*)F->dy + es * (size_t)rows * c0,
+                                  es * (size_t)rows * nc, cudaMemcpyDeviceToHost, F->s_out));
+  }
+  FGB_CUDA(ctx, cudaStreamSynchronize(F->s_out));
   FGB_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
   return FGB_OK;
 }

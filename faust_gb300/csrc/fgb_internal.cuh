@@ -123,6 +123,9 @@ struct fgb_faust {
   // Workspace of the dense product (intermediates and dense images).
   void* pws = nullptr;
   size_t pws_bytes = 0;
+  // Copy streams and events of the pipelined host-buffer product.
+  cudaStream_t s_in = nullptr, s_out = nullptr;
+  cudaEvent_t ev_in[4] = {}, ev_done[4] = {}, ev_start = nullptr;
   // When set, the factor arrays are views into this shared device block
   // (results of one batched call) and are released with its last owner.
   std::shared_ptr<void> pool;

@@ -139,6 +139,9 @@ fgb_status fgb_dynprog_plan(int n, const int* rows, const int* cols, const int* 
                             int* split);
 
 /* Y = F X with X, Y in HOST memory: copy in, product, copy out, synchronous.
+ * Operands of 32 MB or more go in up to four column chunks whose copies
+ * (on two extra streams) overlap the products of their neighbours; with
+ * pinned host buffers the copy engines then run beside the kernels.
  * Replaces TransformHelper<FPP,Cpu>::multiply(const FPP* A, int A_ncols,
  * FPP* C) (CPU/faust_TransformHelper.hpp:406-433) and
  * TransformHelper<FPP,GPU2>::multiply(const MatDense<FPP,Cpu>&)
