@@ -203,6 +203,25 @@ static fgb_status launch_spmm_tc(fgb_ctx* ctx, const int* rowptr, const int* col
   return FGB_OK;
 }
 
+// The long-row kernel of a product runs on the context's side stream beside
+// the short-row kernel (they write disjoint rows of Y): fork before it, join
+// after the short-row launch.  In a captured graph the two become parallel
+// nodes.
+static fgb_status long_fork(fgb_ctx* ctx, cudaStream_t* s) {
+  *s = ctx->stream;
+  if (!ctx->s_long) return FGB_OK;
+  FGB_CUDA(ctx, cudaEventRecord(ctx->ev_long_fork, ctx->stream));
+  FGB_CUDA(ctx, cudaStreamWaitEvent(ctx->s_long, ctx->ev_long_fork, 0));
+  *s = ctx->s_long;
+  return FGB_OK;
+}
+static fgb_status long_join(fgb_ctx* ctx) {
+  if (!ctx->s_long) return FGB_OK;
+  FGB_CUDA(ctx, cudaEventRecord(ctx->ev_long_join, ctx->s_long));
+  FGB_CUDA(ctx, cudaStreamWaitEvent(ctx->stream, ctx->ev_long_join, 0));
+  return FGB_OK;
+}
+
 template <typename T>
 fgb_status launch_csr_spmm(fgb_ctx* ctx, const int* rowptr, const int* colind, const T* val, int rows, int inner,
                            const T* X, int ldx, int ncols, T* Y, int ldy, const Epi<T>& epi, int max_row) {
@@ -215,21 +234,26 @@ fgb_status launch_csr_spmm(fgb_ctx* ctx, const int* rowptr, const int* colind, c
   const bool has_long = max_row < 0 || max_row > ROW_CHUNK;
   const int long_row = has_long ? ROW_CHUNK + 1 : INT_MAX;
   if (has_long) {
+    cudaStream_t s;
+    FGB_TRY(long_fork(ctx, &s));
     dim3 g((unsigned)((ncols + 31) / 32), (unsigned)std::min((rows + 255) / 256 * 4, 16));
-    k_csr_spmm_long<T><<<g, 256, 0, ctx->stream>>>(rowptr, colind, val, rows, X, ldx, ncols, Y, ldy, epi);
+    k_csr_spmm_long<T><<<g, 256, 0, s>>>(rowptr, colind, val, rows, X, ldx, ncols, Y, ldy, epi);
     FGB_LAUNCHED(ctx);
   }
   // Stage when the tile fits comfortably and there are enough tiles to fill
   // the GPU; small problems (PALM blocks) gather straight from L2.
   if (staged <= 96 * 1024 && tiles >= ctx->sm_count)
-    return launch_spmm_tc<T, TC, true>(ctx, rowptr, colind, val, rows, inner, X, ldx, ncols, Y, ldy, epi, long_row);
+    FGB_TRY((launch_spmm_tc<T, TC, true>(ctx, rowptr, colind, val, rows, inner, X, ldx, ncols, Y, ldy, epi,
+                                         long_row)));
   // Half-width tiles when a full one does not fit (e.g. 4096 FP32 rows): the
   // gathers still come from shared memory instead of dependent L2 round trips.
-  if (staged / 2 <= 96 * 1024 && 2 * tiles >= 4L * ctx->sm_count)
-    return launch_spmm_tc<T, TC / 2, true>(ctx, rowptr, colind, val, rows, inner, X, ldx, ncols, Y, ldy, epi,
-                                           long_row);
-  return launch_spmm_tc<T, TC / 2, false>(ctx, rowptr, colind, val, rows, inner, X, ldx, ncols, Y, ldy, epi,
-                                          long_row);
+  else if (staged / 2 <= 96 * 1024 && 2 * tiles >= 4L * ctx->sm_count)
+    FGB_TRY((launch_spmm_tc<T, TC / 2, true>(ctx, rowptr, colind, val, rows, inner, X, ldx, ncols, Y, ldy, epi,
+                                             long_row)));
+  else
+    FGB_TRY((launch_spmm_tc<T, TC / 2, false>(ctx, rowptr, colind, val, rows, inner, X, ldx, ncols, Y, ldy, epi,
+                                              long_row)));
+  return has_long ? long_join(ctx) : FGB_OK;
 }
 
 // ------------------------------------------------------------------ Y = X S^T
@@ -256,9 +280,12 @@ fgb_status launch_dense_csrT(fgb_ctx* ctx, const T* X, int ldx, int xrows, const
                              const T* val, int srows, int scols, T* Y, int ldy, const Epi<T>& epi, int max_row) {
   (void)scols;
   if (srows == 0 || xrows == 0) return FGB_OK;
-  if (max_row < 0 || max_row > ROW_CHUNK) {
+  const bool has_long = max_row < 0 || max_row > ROW_CHUNK;
+  if (has_long) {
+    cudaStream_t s;
+    FGB_TRY(long_fork(ctx, &s));
     dim3 g((unsigned)((xrows + 31) / 32), (unsigned)std::min((srows + 255) / 256 * 4, 16));
-    k_dense_csrT_long<T><<<g, 256, 0, ctx->stream>>>(X, ldx, xrows, rowptr, colind, val, srows, Y, ldy, epi);
+    k_dense_csrT_long<T><<<g, 256, 0, s>>>(X, ldx, xrows, rowptr, colind, val, srows, Y, ldy, epi);
     FGB_LAUNCHED(ctx);
   }
   // rows of at most ROW_CHUNK entries: one block per output column
@@ -266,7 +293,7 @@ fgb_status launch_dense_csrT(fgb_ctx* ctx, const T* X, int ldx, int xrows, const
   dim3 grid(srows, rblocks);
   k_dense_csrT<T><<<grid, SPMM_THREADS, 0, ctx->stream>>>(X, ldx, xrows, rowptr, colind, val, srows, Y, ldy, epi);
   FGB_LAUNCHED(ctx);
-  return FGB_OK;
+  return has_long ? long_join(ctx) : FGB_OK;
 }
 
 // ------------------------------------------------------------------ fused chain

@@ -84,6 +84,15 @@ fgb_status fgb_ctx_create(int device, void* cuda_stream, fgb_ctx** out) {
     void* dp = nullptr;
     if (cudaHostGetDevicePointer(&dp, hp, 0) == cudaSuccess) ctx->cancel_dev = (int*)dp;
   }
+  if (cudaStreamCreateWithFlags(&ctx->s_long, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreateWithFlags(&ctx->ev_long_fork, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&ctx->ev_long_join, cudaEventDisableTiming) != cudaSuccess) {
+    if (ctx->s_long) cudaStreamDestroy(ctx->s_long);
+    if (ctx->ev_long_fork) cudaEventDestroy(ctx->ev_long_fork);
+    ctx->s_long = nullptr;
+    ctx->ev_long_fork = nullptr;
+    ctx->ev_long_join = nullptr;
+  }
   cudaGetLastError();
   *out = ctx;
   return FGB_OK;
@@ -98,6 +107,12 @@ fgb_status fgb_ctx_destroy(fgb_ctx* ctx) {
   if (ctx->rand_dev) cudaFree(ctx->rand_dev);
   if (ctx->x0_d) cudaFree(ctx->x0_d);
   if (ctx->x0_f) cudaFree(ctx->x0_f);
+  if (ctx->s_long) {
+    cudaStreamSynchronize(ctx->s_long);
+    cudaStreamDestroy(ctx->s_long);
+  }
+  if (ctx->ev_long_fork) cudaEventDestroy(ctx->ev_long_fork);
+  if (ctx->ev_long_join) cudaEventDestroy(ctx->ev_long_join);
   delete ctx;
   return FGB_OK;
 }

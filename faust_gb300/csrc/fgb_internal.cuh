@@ -37,6 +37,10 @@ struct fgb_ctx {
   // the power-iteration start vector -1 + 2*rand()/RAND_MAX in FP64 and FP32
   double* x0_d = nullptr;
   float* x0_f = nullptr;
+  // Side stream of the long-row product kernels, forked from and joined back
+  // to `stream` by the two events around each product (null: run in line).
+  cudaStream_t s_long = nullptr;
+  cudaEvent_t ev_long_fork = nullptr, ev_long_join = nullptr;
 };
 
 namespace fgb {

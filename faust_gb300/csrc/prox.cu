@@ -28,6 +28,7 @@ namespace fgb {
 
 constexpr int PX_THREADS = 256;
 constexpr int RS_MAX_PASSES = 6;  // passes of the single-launch radix select
+constexpr int RS_LIST_CAP = 32768;  // bucket size the radix select finishes in one block
 constexpr int LINE_KMAX = 64;
 
 __device__ __forceinline__ unsigned long long mag_key(double v) {
@@ -36,9 +37,25 @@ __device__ __forceinline__ unsigned long long mag_key(double v) {
 __device__ __forceinline__ unsigned long long mag_key(float v) {
   return (unsigned long long)(__float_as_uint(v) & 0x7fffffffu);
 }
+__device__ __forceinline__ unsigned long long raw_bits(double v) { return (unsigned long long)__double_as_longlong(v); }
+__device__ __forceinline__ unsigned long long raw_bits(float v) { return __float_as_uint(v); }
 template <typename T>
 __device__ __forceinline__ T pos_adj(T v, int pos) {
   return (pos && v < T(0)) ? T(0) : v;
+}
+
+// Magnitude key of pos_adj(v, pos) by integer operations only (v < 0 is a
+// set sign bit on a non-zero, non-NaN value), so that the scans issue no
+// floating-point instruction.
+__device__ __forceinline__ unsigned long long sel_key(double v, int pos) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+  const unsigned long long m = b & 0x7fffffffffffffffULL;
+  return (pos && (b >> 63) && m != 0 && m <= 0x7ff0000000000000ULL) ? 0ULL : m;
+}
+__device__ __forceinline__ unsigned long long sel_key(float v, int pos) {
+  const unsigned b = __float_as_uint(v);
+  const unsigned m = b & 0x7fffffffu;
+  return (pos && (b >> 31) && m != 0 && m <= 0x7f800000u) ? 0ULL : (unsigned long long)m;
 }
 
 // ------------------------------------------------------------------ workspace
@@ -55,8 +72,9 @@ fgb_status prox_work_reserve(fgb_ctx* ctx, ProxWork& w, long elems, int rows) {
   FGB_TRY(dmalloc(ctx, (void**)&w.row_cnt, sizeof(int) * (rows + 2)));
   FGB_CUDA(ctx, cudaMemsetAsync(w.flags, 0, (size_t)std::max(1L, elems), ctx->stream));
   FGB_CUDA(ctx, cudaMemsetAsync(w.hist, 0, sizeof(unsigned) * 2048, ctx->stream));
-  FGB_TRY(dmalloc(ctx, (void**)&w.hist_passes, sizeof(unsigned) * (RS_MAX_PASSES * 2048 + 2)));
-  FGB_CUDA(ctx, cudaMemsetAsync(w.hist_passes, 0, sizeof(unsigned) * (RS_MAX_PASSES * 2048 + 2), ctx->stream));
+  FGB_TRY(dmalloc(ctx, (void**)&w.hist_passes, sizeof(unsigned) * (RS_MAX_PASSES * 2048 + 4)));
+  FGB_CUDA(ctx, cudaMemsetAsync(w.hist_passes, 0, sizeof(unsigned) * (RS_MAX_PASSES * 2048 + 4), ctx->stream));
+  FGB_TRY(dmalloc(ctx, (void**)&w.rs_list, sizeof(unsigned long long) * RS_LIST_CAP));
   w.cap_elems = elems;
   w.cap_rows = rows;
   w.growable = 1;
@@ -68,6 +86,7 @@ void prox_work_free(ProxWork& w) {
   dfree(w.hist);
   dfree(w.hist_passes);
   w.hist_passes = nullptr;
+  dfree(w.rs_list);
   dfree(w.flags);
   dfree(w.chunk_cnt);
   dfree(w.partials);
@@ -97,7 +116,7 @@ __global__ void __launch_bounds__(PX_THREADS)
   __syncthreads();
   const unsigned long long prefix = st->prefix, mask = st->mask;
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < N; i += (long)gridDim.x * blockDim.x) {
-    const unsigned long long key = mag_key(pos_adj(M[i], pos));
+    const unsigned long long key = sel_key(M[i], pos);
     if ((key & mask) == prefix) atomicAdd(&sh[(key >> shift) & (nb - 1)], 1u);
   }
   __syncthreads();
@@ -186,118 +205,192 @@ __device__ __forceinline__ bool rs_grid_barrier(unsigned* bar, unsigned nblocks,
   return *s_ok != 0;
 }
 
+struct RsShared {
+  unsigned long long prefix, mask;
+  long long krem, G, E;
+  int ok, bad;
+  unsigned long long wsum[PX_THREADS / 32];
+};
+
+// The bucket of the histogram sh[0..nb) holding the k_rem-th largest key,
+// found by every block alike: thread t owns bins nb-1-t*per .. nb-per-t*per
+// (descending), a block scan of their sums finds the owner, which walks its
+// bins and narrows the prefix.  Every thread of the block calls.
+__device__ __forceinline__ void rs_pick(const unsigned* sh, int nb, int shift, unsigned long long prefix,
+                                        unsigned long long mask, RsShared& s) {
+  const int per = nb / PX_THREADS;  // 8, 2 or 1
+  const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+  unsigned long long sum = 0;
+  for (int j = 0; j < per; ++j) sum += sh[nb - 1 - (t * per + j)];
+  unsigned long long incl = sum;
+  for (int o = 1; o < 32; o <<= 1) {
+    const unsigned long long y = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += y;
+  }
+  if (lane == 31) s.wsum[warp] = incl;
+  __syncthreads();
+  if (warp == 0) {
+    unsigned long long w = lane < PX_THREADS / 32 ? s.wsum[lane] : 0;
+    for (int o = 1; o < 32; o <<= 1) {
+      const unsigned long long y = __shfl_up_sync(0xffffffffu, w, o);
+      if (lane >= o) w += y;
+    }
+    if (lane < PX_THREADS / 32) s.wsum[lane] = w;  // inclusive warp totals
+  }
+  __syncthreads();
+  incl += warp ? s.wsum[warp - 1] : 0ULL;
+  const unsigned long long excl = incl - sum;
+  const long long krem = s.krem;
+  const long long total = (long long)s.wsum[PX_THREADS / 32 - 1];
+  __syncthreads();  // everyone has read s.krem before the owner updates it
+  if ((long long)excl < krem && krem <= (long long)incl) {
+    unsigned long long cum = excl;
+    for (int j = 0; j < per; ++j) {
+      const int b = nb - 1 - (t * per + j);
+      const unsigned long long h = sh[b];
+      if ((long long)(cum + h) >= krem) {
+        s.G += (long long)cum;
+        s.krem = krem - (long long)cum;
+        s.prefix = prefix | ((unsigned long long)b << shift);
+        s.mask = mask | ((unsigned long long)(nb - 1) << shift);
+        s.E = (long long)h;
+        break;
+      }
+      cum += h;
+    }
+  }
+  if (t == 0 && total < krem) s.bad = 1;
+  __syncthreads();
+}
+
+// Pass p of the grid histograms the keys matching the prefix of passes
+// 0..p-1.  Pass 0 matches every key and its bins cluster (they are the
+// exponent bits), so its shared-memory increments are aggregated per warp.
+// When the bucket chosen so far holds at most RS_LIST_CAP keys and passes
+// remain, the pass also appends those keys to `list`; after its barrier
+// block 0 alone runs the remaining passes over the list (the other blocks
+// return), which replaces the last full scans and barriers by block-local
+// passes over a few thousand keys.  The list counter is the word after the
+// barrier's two; block 0 clears it and the histograms of passes 1.. at the
+// start (no block touches them before the first barrier), histogram p-1
+// after barrier p.
 template <typename T>
 __global__ void __launch_bounds__(PX_THREADS)
-    k_radix_select(const T* __restrict__ M, long N, int pos, int npass, TopkState* st, unsigned* hists) {
+    k_radix_select(const T* __restrict__ M, long N, int pos, int npass, TopkState* st, unsigned* hists,
+                   unsigned long long* __restrict__ list) {
   __shared__ unsigned sh[2048];
-  __shared__ unsigned long long s_prefix, s_mask;
-  __shared__ long long s_krem, s_G, s_E;
-  __shared__ int s_ok, s_bad;
-  __shared__ unsigned long long s_wsum[PX_THREADS / 32];
+  __shared__ RsShared s;
   unsigned* bar = hists + RS_MAX_PASSES * 2048;
+  unsigned* list_n = bar + 2;
   const int shifts8[6] = {52, 41, 30, 19, 8, 0}, bits8[6] = {11, 11, 11, 11, 11, 8};
   const int shifts4[3] = {20, 9, 0}, bits4[3] = {11, 11, 9};
   if (threadIdx.x == 0) {
-    s_prefix = 0;
-    s_mask = 0;
-    s_krem = st->k_rem;
-    s_G = 0;
-    s_E = 0;
-    s_bad = 0;
+    s.prefix = 0;
+    s.mask = 0;
+    s.krem = st->k_rem;
+    s.G = 0;
+    s.E = 0;
+    s.bad = 0;
   }
-  if (blockIdx.x == 0)
-    for (int i = threadIdx.x; i < 2048; i += blockDim.x) hists[(npass - 1) * 2048 + i] = 0;
-  bool timed_out = false;
-  for (int p = 0; p < npass; ++p) {
+  if (blockIdx.x == 0) {
+    for (int i = threadIdx.x; i < (RS_MAX_PASSES - 1) * 2048; i += blockDim.x) hists[2048 + i] = 0;
+    if (threadIdx.x == 0) *list_n = 0;
+  }
+  bool timed_out = false, tail = false;
+  int p = 0;
+  for (; p < npass; ++p) {
     const int shift = sizeof(T) == 8 ? shifts8[p] : shifts4[p];
     const int bits = sizeof(T) == 8 ? bits8[p] : bits4[p];
     const int nb = 1 << bits;
     unsigned* hist = hists + p * 2048;
     for (int i = threadIdx.x; i < nb; i += blockDim.x) sh[i] = 0;
     __syncthreads();
-    const unsigned long long prefix = s_prefix, mask = s_mask;
+    const unsigned long long prefix = s.prefix, mask = s.mask;
+    const bool collect = p > 0 && p + 1 < npass && s.E <= RS_LIST_CAP;
     {
-      // eight keys per thread in flight before their (rare after pass 0) atomics
+      // eight keys per thread in flight before their atomics
       const long stride = (long)gridDim.x * blockDim.x;
       long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
-      for (; i + 7 * stride < N; i += 8 * stride) {
-        unsigned long long key[8];
+      if (p == 0) {
+        for (; i + 7 * stride < N; i += 8 * stride) {
+          unsigned long long key[8];
 #pragma unroll
-        for (int u = 0; u < 8; ++u) key[u] = mag_key(pos_adj(M[i + u * stride], pos));
+          for (int u = 0; u < 8; ++u) key[u] = sel_key(M[i + u * stride], pos);
 #pragma unroll
-        for (int u = 0; u < 8; ++u)
-          if ((key[u] & mask) == prefix) atomicAdd(&sh[(key[u] >> shift) & (nb - 1)], 1u);
-      }
-      for (; i < N; i += stride) {
-        const unsigned long long key = mag_key(pos_adj(M[i], pos));
-        if ((key & mask) == prefix) atomicAdd(&sh[(key >> shift) & (nb - 1)], 1u);
+          for (int u = 0; u < 8; ++u) {
+            const unsigned b = (unsigned)(key[u] >> shift) & (unsigned)(nb - 1);
+            const unsigned peers = __match_any_sync(__activemask(), b);
+            if ((int)(threadIdx.x & 31) == __ffs(peers) - 1) atomicAdd(&sh[b], (unsigned)__popc(peers));
+          }
+        }
+        for (; i < N; i += stride) atomicAdd(&sh[(sel_key(M[i], pos) >> shift) & (nb - 1)], 1u);
+      } else {
+        for (; i + 7 * stride < N; i += 8 * stride) {
+          unsigned long long key[8];
+#pragma unroll
+          for (int u = 0; u < 8; ++u) key[u] = sel_key(M[i + u * stride], pos);
+#pragma unroll
+          for (int u = 0; u < 8; ++u)
+            if ((key[u] & mask) == prefix) {
+              atomicAdd(&sh[(key[u] >> shift) & (nb - 1)], 1u);
+              if (collect) {
+                const unsigned at = atomicAdd(list_n, 1u);
+                if (at < (unsigned)RS_LIST_CAP) list[at] = key[u];
+              }
+            }
+        }
+        for (; i < N; i += stride) {
+          const unsigned long long key = sel_key(M[i], pos);
+          if ((key & mask) == prefix) {
+            atomicAdd(&sh[(key >> shift) & (nb - 1)], 1u);
+            if (collect) {
+              const unsigned at = atomicAdd(list_n, 1u);
+              if (at < (unsigned)RS_LIST_CAP) list[at] = key;
+            }
+          }
+        }
       }
     }
     __syncthreads();
     for (int i = threadIdx.x; i < nb; i += blockDim.x)
       if (sh[i]) atomicAdd(&hist[i], sh[i]);
     __threadfence();
-    if (!rs_grid_barrier(bar, gridDim.x, &s_ok)) timed_out = true;
+    if (!rs_grid_barrier(bar, gridDim.x, &s.ok)) timed_out = true;
     if (p > 0 && blockIdx.x == 0)
       for (int i = threadIdx.x; i < 2048; i += blockDim.x) hists[(p - 1) * 2048 + i] = 0;
     for (int i = threadIdx.x; i < nb; i += blockDim.x) sh[i] = __ldcg(&hist[i]);
     __syncthreads();
-    // the bucket holding the k_rem-th largest key (every block alike):
-    // thread t owns bins nb-1-t*per .. nb-per-t*per (descending), a block
-    // scan of their sums finds the owner, which walks its bins
-    {
-      const int per = nb / PX_THREADS;  // 8, 2 or 1
-      const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
-      unsigned long long sum = 0;
-      for (int j = 0; j < per; ++j) sum += sh[nb - 1 - (t * per + j)];
-      unsigned long long incl = sum;
-      for (int o = 1; o < 32; o <<= 1) {
-        const unsigned long long y = __shfl_up_sync(0xffffffffu, incl, o);
-        if (lane >= o) incl += y;
-      }
-      if (lane == 31) s_wsum[warp] = incl;
-      __syncthreads();
-      if (warp == 0) {
-        unsigned long long w = lane < PX_THREADS / 32 ? s_wsum[lane] : 0;
-        for (int o = 1; o < 32; o <<= 1) {
-          const unsigned long long y = __shfl_up_sync(0xffffffffu, w, o);
-          if (lane >= o) w += y;
-        }
-        if (lane < PX_THREADS / 32) s_wsum[lane] = w;  // inclusive warp totals
-      }
-      __syncthreads();
-      incl += warp ? s_wsum[warp - 1] : 0ULL;
-      const unsigned long long excl = incl - sum;
-      const long long krem = s_krem;
-      const long long total = (long long)s_wsum[PX_THREADS / 32 - 1];
-      __syncthreads();  // everyone has read s_krem before the owner updates it
-      if ((long long)excl < krem && krem <= (long long)incl) {
-        unsigned long long cum = excl;
-        for (int j = 0; j < per; ++j) {
-          const int b = nb - 1 - (t * per + j);
-          const unsigned long long h = sh[b];
-          if ((long long)(cum + h) >= krem) {
-            s_G += (long long)cum;
-            s_krem = krem - (long long)cum;
-            s_prefix = prefix | ((unsigned long long)b << shift);
-            s_mask = mask | ((unsigned long long)(nb - 1) << shift);
-            s_E = (long long)h;
-            break;
-          }
-          cum += h;
-        }
-      }
-      if (t == 0 && total < krem) s_bad = 1;
+    rs_pick(sh, nb, shift, prefix, mask, s);
+    if (collect) {
+      ++p;
+      tail = true;
+      break;
     }
-    __syncthreads();
+  }
+  if (tail && blockIdx.x == 0) {
+    const unsigned n = min(__ldcg(list_n), (unsigned)RS_LIST_CAP);
+    for (; p < npass; ++p) {
+      const int shift = sizeof(T) == 8 ? shifts8[p] : shifts4[p];
+      const int bits = sizeof(T) == 8 ? bits8[p] : bits4[p];
+      const int nb = 1 << bits;
+      for (int i = threadIdx.x; i < nb; i += blockDim.x) sh[i] = 0;
+      __syncthreads();
+      const unsigned long long prefix = s.prefix, mask = s.mask;
+      for (unsigned i = threadIdx.x; i < n; i += blockDim.x) {
+        const unsigned long long key = __ldcg(&list[i]);
+        if ((key & mask) == prefix) atomicAdd(&sh[(key >> shift) & (nb - 1)], 1u);
+      }
+      __syncthreads();
+      rs_pick(sh, nb, shift, prefix, mask, s);
+    }
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) {
-    st->prefix = s_prefix;
-    st->mask = s_mask;
-    st->k_rem = s_krem;
-    st->G = s_G;
-    st->E = s_E;
-    if (s_bad) atomicCAS(&st->status, 0, (int)FGB_ERR_INVALID_ARG);
+    st->prefix = s.prefix;
+    st->mask = s.mask;
+    st->k_rem = s.krem;
+    st->G = s.G;
+    st->E = s.E;
+    if (s.bad) atomicCAS(&st->status, 0, (int)FGB_ERR_INVALID_ARG);
   }
   if (timed_out && threadIdx.x == 0) atomicCAS(&st->status, 0, (int)FGB_ERR_TIMEOUT);
 }
@@ -325,7 +418,7 @@ __global__ void __launch_bounds__(PX_THREADS)
   const long c0 = blockIdx.x * chunk, c1 = min(N, c0 + chunk);
   long long ge = 0, gt = 0;
   for (long i = c0 + threadIdx.x; i < c1; i += blockDim.x) {
-    const unsigned long long key = mag_key(pos_adj(M[i], pos));
+    const unsigned long long key = sel_key(M[i], pos);
     ge += key >= t;
     gt += key > t;
   }
@@ -377,7 +470,7 @@ __global__ void __launch_bounds__(PX_THREADS)
   ge = 0;
   gt = 0;
   for (long i = s0; i < s1; ++i) {
-    const unsigned long long key = mag_key(pos_adj(M[i], pos));
+    const unsigned long long key = sel_key(M[i], pos);
     ge += key >= t;
     gt += key > t;
   }
@@ -404,7 +497,7 @@ __global__ void __launch_bounds__(PX_THREADS)
   if ((long long)threadIdx.x == s_ge[0]) {
     long long run_ge = s_gt[0], run_gt = s_gt[1];
     for (long i = s0; i < s1; ++i) {
-      const unsigned long long key = mag_key(pos_adj(M[i], pos));
+      const unsigned long long key = sel_key(M[i], pos);
       run_ge += key >= t;
       run_gt += key > t;
       if (run_ge == c_target) {
@@ -541,7 +634,7 @@ __global__ void __launch_bounds__(PX_THREADS)
   HNode* cand = reinterpret_cast<HNode*>(smem_raw);  // HR_CHUNK candidates
   HeapView h;
   h.n = use_smem ? cand + HR_CHUNK : gheap;
-  for (int i = threadIdx.x; i < k; i += blockDim.x) h.n[i] = HNode{mag_key(pos_adj(M[i], pos)), i};
+  for (int i = threadIdx.x; i < k; i += blockDim.x) h.n[i] = HNode{sel_key(M[i], pos), i};
   __syncthreads();
   if (threadIdx.x == 0 && k >= 2) {
     int parent = (k - 2) / 2;
@@ -565,7 +658,7 @@ __global__ void __launch_bounds__(PX_THREADS)
 #pragma unroll
     for (int u = 0; u < HR_PER; ++u) {
       const long i = base + u;
-      kk[u] = (i < c1) ? mag_key(pos_adj(M[i], pos)) : 0ULL;
+      kk[u] = (i < c1) ? sel_key(M[i], pos) : 0ULL;
       cnt += (i < c1) && kk[u] > topk;
     }
     if (__syncthreads_count(cnt) == 0) continue;
@@ -747,7 +840,7 @@ __global__ void __launch_bounds__(RP_BLOCK)
     for (long b0 = lo; b0 < hi; b0 += RP_BLOCK) {
       const long i = b0 + threadIdx.x;
       const bool in = i < hi;
-      const unsigned long long key = in ? mag_key(pos_adj(M[i], pos)) : 0ULL;
+      const unsigned long long key = in ? sel_key(M[i], pos) : 0ULL;
       const bool take = in && (pass == 0 || (key >> S1) == (bound >> S1));
       const unsigned bin = (unsigned)((pass == 0 ? key >> S1 : key >> S2) & (RP_BINS - 1));
       rp_hist_add(hist, bin, take);
@@ -781,7 +874,7 @@ __global__ void __launch_bounds__(RP_BLOCK)
   // initial top: the smallest of the first k keys
   unsigned long long mn = ~0ULL;
   for (long i = t; i < k; i += RP_BLOCK) {
-    const unsigned long long key = mag_key(pos_adj(M[i], pos));
+    const unsigned long long key = sel_key(M[i], pos);
     mn = key < mn ? key : mn;
   }
   for (int o = 16; o >= 1; o >>= 1) {
@@ -807,7 +900,7 @@ __global__ void __launch_bounds__(RP_BLOCK)
 #pragma unroll
     for (int u = 0; u < U; ++u) {
       const long e = tb + (long)u * RP_BLOCK + t;
-      kk[u] = e < hi ? mag_key(pos_adj(M[e], pos)) : 0ULL;
+      kk[u] = e < hi ? sel_key(M[e], pos) : 0ULL;
       bal[u] = __ballot_sync(0xffffffffu, e < hi && kk[u] > bound);
       if (lane == 0) s_cnt[u * NW + warp] = __popc(bal[u]);
     }
@@ -1045,11 +1138,11 @@ __global__ void __launch_bounds__(PX_THREADS)
     hk = gk;
     hidx = gi;
   }
-  const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+  const int t = threadIdx.x, warp = t >> 5;
   const int lim = (int)((k - 1) / 2);
   const int half = (k & 1) == 0 ? (int)((k - 2) / 2) : -1;
   for (int i = t; i < (int)k; i += blockDim.x) {
-    hk[i + 1] = mag_key(pos_adj(M[i], pos));
+    hk[i + 1] = sel_key(M[i], pos);
     hidx[i + 1] = (unsigned)i;
   }
   if (t == 0) {
@@ -1112,17 +1205,30 @@ __global__ void k_sp_apply(T* __restrict__ M, long N, int pos, const TopkState* 
   const unsigned long long t = st->t;
   const int cs = st->sel_case;
   const long long tau = st->tau;
-  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < N; i += (long)gridDim.x * blockDim.x) {
-    const T v = pos_adj(M[i], pos);
-    const unsigned long long key = mag_key(v);
-    bool keep = key > t;
-    if (!keep && key == t) {
-      if (cs == 0) keep = true;
-      else if (cs == 1) keep = i <= tau;
-      else if (cs == 2) keep = flags[i] != 0;
+  // four entries per thread in flight; pos_adj(m, pos) is m unless pos
+  // turned it into +0 (a zero key on a non-zero magnitude); entries that
+  // keep their bits are not rewritten
+  const long stride = (long)gridDim.x * blockDim.x;
+  for (long i0 = blockIdx.x * (long)blockDim.x + threadIdx.x; i0 < N; i0 += 4 * stride) {
+    T m[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) m[u] = i0 + u * stride < N ? M[i0 + u * stride] : T(0);
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const long i = i0 + u * stride;
+      if (i >= N) break;
+      const unsigned long long key = sel_key(m[u], pos);
+      bool keep = key > t;
+      if (!keep && key == t) {
+        if (cs == 0) keep = true;
+        else if (cs == 1) keep = i <= tau;
+        else if (cs == 2) keep = flags[i] != 0;
+      }
+      if (cs == 2) flags[i] = 0;
+      const bool adjusted = key == 0 && mag_key(m[u]) != 0;
+      const T out = keep && !adjusted ? m[u] : T(0);
+      if (raw_bits(out) != raw_bits(m[u])) M[i] = out;
     }
-    if (cs == 2) flags[i] = 0;
-    M[i] = keep ? v : T(0);
   }
 }
 
@@ -1222,8 +1328,23 @@ template <typename T>
 __global__ void __launch_bounds__(PX_THREADS) k_chunk_sumsq(const T* __restrict__ M, long N, double* partials) {
   __shared__ T lane[PX_THREADS];
   const long c0 = blockIdx.x * CR_CHUNK, c1 = min(N, c0 + CR_CHUNK);
+  // A zero entry adds +0 to a non-negative partial, so a warp skips the FMA
+  // when all its lanes hold zeros (the sparse projections leave few
+  // non-zeros; an FP64 FMA issues at the same cost for 1 or 32 lanes).
   T acc = T(0);
-  for (long i = c0 + threadIdx.x; i < c1; i += CR_LANES) acc = fmad(M[i], M[i], acc);
+  long i = c0 + threadIdx.x;
+  for (; i + 7 * CR_LANES < c1; i += 8 * CR_LANES) {
+    T v[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) v[u] = M[i + u * CR_LANES];
+#pragma unroll
+    for (int u = 0; u < 8; ++u)
+      if (__any_sync(__activemask(), mag_key(v[u]) != 0)) acc = fmad(v[u], v[u], acc);
+  }
+  for (; i < c1; i += CR_LANES) {
+    const T v = M[i];
+    if (__any_sync(__activemask(), mag_key(v) != 0)) acc = fmad(v, v, acc);
+  }
   lane[threadIdx.x] = acc;
   const T part = lane_tree_256(lane);
   if (threadIdx.x == 0) reinterpret_cast<T*>(partials)[blockIdx.x] = part;
@@ -1249,136 +1370,34 @@ __global__ void k_norm_finalize(const double* partials, int nchunks, double* sca
 template <typename T>
 __global__ void k_scale(T* __restrict__ M, long N, const double* scal) {
   const T s = reinterpret_cast<const T*>(scal)[0];
-  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < N; i += (long)gridDim.x * blockDim.x)
-    M[i] = mulr(M[i], s);
+  // a zero times a finite non-negative scale keeps its bits: not rewritten,
+  // and a warp of zeros issues no multiply
+  const bool skip_zeros = raw_bits(s) < raw_bits(T(INFINITY));
+  const long stride = (long)gridDim.x * blockDim.x;
+  long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  for (; i + 3 * stride < N; i += 4 * stride) {
+    T v[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) v[u] = M[i + u * stride];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const bool need = !skip_zeros || mag_key(v[u]) != 0;
+      if (__any_sync(__activemask(), need))
+        if (need) M[i + u * stride] = mulr(v[u], s);
+    }
+  }
+  for (; i < N; i += stride) {
+    const T v = M[i];
+    const bool need = !skip_zeros || mag_key(v) != 0;
+    if (__any_sync(__activemask(), need))
+      if (need) M[i] = mulr(v, s);
+  }
 }
 
 __global__ void k_status_merge(const TopkState* st, int* status) {
   if (st->status) atomicCAS(status, 0, st->status);
 }
 
-// ------------------------------------------------------------------ dense -> CSR
-template <typename T>
-__global__ void k_d2c_count(const T* __restrict__ M, int rows, int cols, int* __restrict__ cnt) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= rows) return;
-  int c = 0;
-  for (int j = 0; j < cols; ++j) c += M[i + (long)j * rows] != T(0);
-  cnt[i] = c;
-}
-
-__global__ void __launch_bounds__(1024) k_d2c_scan(const int* __restrict__ cnt, int rows, int* __restrict__ rowptr,
-                                                   int cap, int* status) {
-  __shared__ int part[1024];
-  const int per = (rows + blockDim.x - 1) / blockDim.x;
-  const int r0 = threadIdx.x * per, r1 = min(rows, r0 + per);
-  int s = 0;
-  for (int r = r0; r < r1; ++r) s += cnt[r];
-  part[threadIdx.x] = s;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    int run = 0;
-    for (int u = 0; u < (int)blockDim.x; ++u) {
-      const int v = part[u];
-      part[u] = run;
-      run += v;
-    }
-    rowptr[rows] = run;
-    if (run > cap && status) atomicCAS(status, 0, (int)FGB_ERR_INVALID_ARG);
-  }
-  __syncthreads();
-  int run = part[threadIdx.x];
-  for (int r = r0; r < r1; ++r) {
-    rowptr[r] = run;
-    run += cnt[r];
-  }
-}
-
-template <typename T>
-__global__ void k_d2c_write(const T* __restrict__ M, int rows, int cols, const int* __restrict__ rowptr,
-                            int* __restrict__ colind, T* __restrict__ val, int cap) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= rows) return;
-  int p = rowptr[i];
-  for (int j = 0; j < cols; ++j) {
-    const T v = M[i + (long)j * rows];
-    if (v != T(0)) {
-      if (p < cap) {
-        colind[p] = j;
-        val[p] = v;
-      }
-      ++p;
-    }
-  }
-}
-
-template <typename T>
-__global__ void __launch_bounds__(1024)
-    k_csr_transpose_dev(const int* __restrict__ rowptr, const int* __restrict__ colind, const T* __restrict__ val,
-                        int rows, int cols, int* __restrict__ t_rowptr, int* __restrict__ t_colind,
-                        T* __restrict__ t_val, int* __restrict__ cursor, int cap) {
-  const int nnz = min(rowptr[rows], cap);
-  for (int c = threadIdx.x; c <= cols; c += blockDim.x) cursor[c] = 0;
-  __syncthreads();
-  for (int p = threadIdx.x; p < nnz; p += blockDim.x) atomicAdd(&cursor[colind[p] + 1], 1);
-  __syncthreads();
-  {
-    __shared__ int part[1024];
-    const int per = (cols + blockDim.x - 1) / blockDim.x;
-    const int c0 = threadIdx.x * per, c1 = min(cols, c0 + per);
-    int s = 0;
-    for (int c = c0; c < c1; ++c) s += cursor[c + 1];
-    part[threadIdx.x] = s;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      int run = 0;
-      for (int u = 0; u < (int)blockDim.x; ++u) {
-        const int v = part[u];
-        part[u] = run;
-        run += v;
-      }
-      t_rowptr[cols] = run;
-    }
-    __syncthreads();
-    int run = part[threadIdx.x];
-    for (int c = c0; c < c1; ++c) {
-      t_rowptr[c] = run;
-      run += cursor[c + 1];
-    }
-  }
-  __syncthreads();
-  for (int c = threadIdx.x; c < cols; c += blockDim.x) cursor[c] = t_rowptr[c];
-  __syncthreads();
-  if (threadIdx.x < 32) {
-    const unsigned lane = threadIdx.x;
-    for (int base = 0; base < nnz; base += 32) {
-      const int p = base + (int)lane;
-      const bool ok = p < nnz;
-      int r = 0;
-      if (ok) {
-        int lo = 0, hi = rows - 1;
-        while (lo < hi) {
-          const int mid = (lo + hi + 1) >> 1;
-          if (rowptr[mid] <= p) lo = mid;
-          else hi = mid - 1;
-        }
-        r = lo;
-      }
-      const int c = ok ? colind[p] : -1 - (int)lane;
-      const unsigned same = __match_any_sync(0xffffffffu, c);
-      const int rank = __popc(same & ((1u << lane) - 1u));
-      int slot = 0;
-      if (ok) slot = cursor[c] + rank;
-      __syncwarp();
-      if (ok) {
-        t_colind[slot] = r;
-        t_val[slot] = val[p];
-        if ((same >> lane) == 1u) cursor[c] = slot + 1;
-      }
-      __syncwarp();
-    }
-  }
-}
 
 __global__ void k_topk_init(TopkState* st, long long k) {
   TopkState z;
@@ -1487,7 +1506,7 @@ static fgb_status queue_sp(fgb_ctx* ctx, ProxWork& w, T* M, long N, long k, int 
     cfg.attrs = attr;
     cfg.numAttrs = 1;
     const T* Mc = M;
-    FGB_CUDA(ctx, cudaLaunchKernelEx(&cfg, k_radix_select<T>, Mc, N, pos, npass, w.state, w.hist_passes));
+    FGB_CUDA(ctx, cudaLaunchKernelEx(&cfg, k_radix_select<T>, Mc, N, pos, npass, w.state, w.hist_passes, w.rs_list));
     FGB_LAUNCHED(ctx);
   } else if (sizeof(T) == 8) {
     const int shifts[6] = {52, 41, 30, 19, 8, 0};
@@ -1632,45 +1651,62 @@ fgb_status launch_prox(fgb_ctx* ctx, ProxWork& w, const fgb_constraint& c, T* M,
 // columns) and one warp per column (lanes over rows) count the non-zero
 // entries, a block scans both count arrays, then the same warps write the
 // entries by ballot compaction, which keeps rows in column order and
-// columns in row order.
+// columns in row order.  Each warp loads eight 32-entry groups before it
+// uses them (the loop is otherwise one L2 round trip per group), and the
+// zero tests are on the bits.
 template <typename T>
 __global__ void __launch_bounds__(256)
     k_d2c_count_rc(const T* __restrict__ M, int rows, int cols, int* __restrict__ rcnt, int* __restrict__ ccnt,
                    int with_cols) {
   const long w = (blockIdx.x * (long)blockDim.x + threadIdx.x) / 32;
   const int lane = threadIdx.x & 31;
-  if (w < rows) {
-    int c = 0;
-    for (int j = lane; j < cols; j += 32) c += M[w + (long)j * rows] != T(0);
-    for (int o = 16; o; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
-    if (lane == 0) rcnt[w] = c;
-  } else if (with_cols && w < (long)rows + cols) {
-    const long col = w - rows;
-    int c = 0;
-    for (int i = lane; i < rows; i += 32) c += M[i + col * rows] != T(0);
-    for (int o = 16; o; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
-    if (lane == 0) ccnt[col] = c;
+  const bool is_row = w < rows;
+  if (!is_row && !(with_cols && w < (long)rows + cols)) return;
+  // entry e of the line: M[base + e * step]
+  const long base = is_row ? w : (w - rows) * (long)rows;
+  const long step = is_row ? rows : 1;
+  const int len = is_row ? cols : rows;
+  int c = 0;
+  int e = lane;
+  for (; e + 7 * 32 < len; e += 8 * 32) {
+    T v[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) v[u] = M[base + (long)(e + u * 32) * step];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) c += mag_key(v[u]) != 0;
   }
+  for (; e < len; e += 32) c += mag_key(M[base + (long)e * step]) != 0;
+  for (int o = 16; o; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+  if (lane == 0) (is_row ? rcnt[w] : ccnt[w - rows]) = c;
 }
 
+// Exclusive scan of cnt[0..n) into ptr[0..n] by one block (a multiple of 32
+// threads, at most 1024): per-thread runs, then a two-level shuffle scan.
+// part: at least 32 ints of shared memory.
 __device__ void block_excl_scan(const int* __restrict__ cnt, int n, int* __restrict__ ptr, int* part) {
   const int per = (n + blockDim.x - 1) / blockDim.x;
   const int r0 = threadIdx.x * per, r1 = min(n, r0 + per);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
   int s = 0;
   for (int r = r0; r < r1; ++r) s += cnt[r];
-  part[threadIdx.x] = s;
+  int incl = s;
+  for (int o = 1; o < 32; o <<= 1) {
+    const int y = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += y;
+  }
+  if (lane == 31) part[warp] = incl;
   __syncthreads();
-  if (threadIdx.x == 0) {
-    int run = 0;
-    for (int u = 0; u < (int)blockDim.x; ++u) {
-      const int v = part[u];
-      part[u] = run;
-      run += v;
+  if (warp == 0) {
+    int v = lane < nw ? part[lane] : 0;
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, v, o);
+      if (lane >= o) v += y;
     }
-    ptr[n] = run;
+    if (lane < nw) part[lane] = v;  // inclusive warp totals
   }
   __syncthreads();
-  int run = part[threadIdx.x];
+  int run = incl - s + (warp ? part[warp - 1] : 0);
+  if (threadIdx.x == 0) ptr[n] = part[nw - 1];
   for (int r = r0; r < r1; ++r) {
     ptr[r] = run;
     run += cnt[r];
@@ -1684,7 +1720,7 @@ __device__ void block_excl_scan(const int* __restrict__ cnt, int n, int* __restr
 __global__ void __launch_bounds__(1024) k_d2c_scan_rc(const int* __restrict__ rcnt, int rows, const int* __restrict__ ccnt,
                                                       int cols, int* __restrict__ rowptr, int* __restrict__ t_rowptr,
                                                       int with_cols, int cap, int* status) {
-  __shared__ int part[1024];
+  __shared__ int part[32];
   block_excl_scan(rcnt, rows, rowptr, part);
   if (with_cols) block_excl_scan(ccnt, cols, t_rowptr, part);
   if (rowptr[rows] > cap) {
@@ -1703,36 +1739,33 @@ __global__ void __launch_bounds__(256)
   const long w = (blockIdx.x * (long)blockDim.x + threadIdx.x) / 32;
   const unsigned lane = threadIdx.x & 31;
   const unsigned lt = (1u << lane) - 1u;
-  if (w < rows) {
-    int base = rowptr[w];
-    for (int j0 = 0; j0 < cols; j0 += 32) {
-      const int j = j0 + (int)lane;
-      const T v = j < cols ? M[w + (long)j * rows] : T(0);
-      const unsigned m = __ballot_sync(0xffffffffu, v != T(0));
-      if (v != T(0)) {
-        const int p = base + __popc(m & lt);
-        if (p < cap) {
-          colind[p] = j;
-          val[p] = v;
-        }
-      }
-      base += __popc(m);
+  const bool is_row = w < rows;
+  if (!is_row && !(with_cols && w < (long)rows + cols)) return;
+  const long base = is_row ? w : (w - rows) * (long)rows;
+  const long step = is_row ? rows : 1;
+  const int len = is_row ? cols : rows;
+  int* __restrict__ ind = is_row ? colind : t_colind;
+  T* __restrict__ out = is_row ? val : t_val;
+  int at = is_row ? rowptr[w] : t_rowptr[w - rows];
+  for (int e0 = 0; e0 < len; e0 += 8 * 32) {
+    T v[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      const int e = e0 + u * 32 + (int)lane;
+      v[u] = e < len ? M[base + (long)e * step] : T(0);
     }
-  } else if (with_cols && w < (long)rows + cols) {
-    const long col = w - rows;
-    int base = t_rowptr[col];
-    for (int i0 = 0; i0 < rows; i0 += 32) {
-      const int i = i0 + (int)lane;
-      const T v = i < rows ? M[i + col * rows] : T(0);
-      const unsigned m = __ballot_sync(0xffffffffu, v != T(0));
-      if (v != T(0)) {
-        const int p = base + __popc(m & lt);
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      const bool nz = mag_key(v[u]) != 0;
+      const unsigned m = __ballot_sync(0xffffffffu, nz);
+      if (nz) {
+        const int p = at + __popc(m & lt);
         if (p < cap) {
-          t_colind[p] = i;
-          t_val[p] = v;
+          ind[p] = e0 + u * 32 + (int)lane;
+          out[p] = v[u];
         }
       }
-      base += __popc(m);
+      at += __popc(m);
     }
   }
 }

@@ -46,8 +46,10 @@ struct ProxWork {
   void* heap2 = nullptr;             // split heap (keys, positions) when it does not fit on chip
   long heap2_cap = 0;
   // single-launch radix select (workspaces made by prox_work_reserve): one
-  // 2048-bin histogram per pass, then the grid barrier's two words
+  // 2048-bin histogram per pass, then the grid barrier's two words and the
+  // key-list counter; the key list of a small bucket
   unsigned* hist_passes = nullptr;
+  unsigned long long* rs_list = nullptr;
 };
 
 fgb_status prox_work_reserve(fgb_ctx* ctx, ProxWork& w, long elems, int rows);
