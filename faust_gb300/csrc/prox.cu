@@ -1328,22 +1328,33 @@ template <typename T>
 __global__ void __launch_bounds__(PX_THREADS) k_chunk_sumsq(const T* __restrict__ M, long N, double* partials) {
   __shared__ T lane[PX_THREADS];
   const long c0 = blockIdx.x * CR_CHUNK, c1 = min(N, c0 + CR_CHUNK);
-  // A zero entry adds +0 to a non-negative partial, so a warp skips the FMA
-  // when all its lanes hold zeros (the sparse projections leave few
-  // non-zeros; an FP64 FMA issues at the same cost for 1 or 32 lanes).
+  // A zero entry adds +0 to a non-negative partial, so a warp issues the
+  // FMA of a batch position only when one of its lanes holds a non-zero
+  // there (the sparse projections leave few non-zeros; an FP64 FMA issues at
+  // the same cost for 1 or 32 lanes).  The positions to do come from ballots
+  // and are walked by a loop, in order.
   T acc = T(0);
   long i = c0 + threadIdx.x;
   for (; i + 7 * CR_LANES < c1; i += 8 * CR_LANES) {
     T v[8];
 #pragma unroll
     for (int u = 0; u < 8; ++u) v[u] = M[i + u * CR_LANES];
+    const unsigned am = __activemask();
+    unsigned todo = 0;
 #pragma unroll
-    for (int u = 0; u < 8; ++u)
-      if (__any_sync(__activemask(), mag_key(v[u]) != 0)) acc = fmad(v[u], v[u], acc);
+    for (int u = 0; u < 8; ++u) todo |= (__ballot_sync(am, mag_key(v[u]) != 0) ? 1u : 0u) << u;
+    while (todo) {
+      const int u = __ffs(todo) - 1;
+      todo &= todo - 1;
+      T x = v[0];
+#pragma unroll
+      for (int q = 1; q < 8; ++q) x = u == q ? v[q] : x;
+      acc = fmad(x, x, acc);
+    }
   }
   for (; i < c1; i += CR_LANES) {
     const T v = M[i];
-    if (__any_sync(__activemask(), mag_key(v) != 0)) acc = fmad(v, v, acc);
+    if (mag_key(v) != 0) acc = fmad(v, v, acc);
   }
   lane[threadIdx.x] = acc;
   const T part = lane_tree_256(lane);
@@ -1379,18 +1390,22 @@ __global__ void k_scale(T* __restrict__ M, long N, const double* scal) {
     T v[4];
 #pragma unroll
     for (int u = 0; u < 4; ++u) v[u] = M[i + u * stride];
+    const unsigned am = __activemask();
+    unsigned todo = 0;
 #pragma unroll
-    for (int u = 0; u < 4; ++u) {
-      const bool need = !skip_zeros || mag_key(v[u]) != 0;
-      if (__any_sync(__activemask(), need))
-        if (need) M[i + u * stride] = mulr(v[u], s);
+    for (int u = 0; u < 4; ++u) todo |= (__ballot_sync(am, !skip_zeros || mag_key(v[u]) != 0) ? 1u : 0u) << u;
+    while (todo) {
+      const int u = __ffs(todo) - 1;
+      todo &= todo - 1;
+      T x = v[0];
+#pragma unroll
+      for (int q = 1; q < 4; ++q) x = u == q ? v[q] : x;
+      if (!skip_zeros || mag_key(x) != 0) M[i + u * stride] = mulr(x, s);
     }
   }
   for (; i < N; i += stride) {
     const T v = M[i];
-    const bool need = !skip_zeros || mag_key(v) != 0;
-    if (__any_sync(__activemask(), need))
-      if (need) M[i] = mulr(v, s);
+    if (!skip_zeros || mag_key(v) != 0) M[i] = mulr(v, s);
   }
 }
 
