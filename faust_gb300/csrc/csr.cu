@@ -79,21 +79,68 @@ __global__ void __launch_bounds__(SPMM_THREADS)
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T* tile = reinterpret_cast<T*>(smem_raw);
   const int j0 = blockIdx.x * TC;
+  const T s = epi.scal ? *epi.scal : T(0);
+  int first = blockIdx.y * blockDim.x + threadIdx.x;  // first row of the generic loop below
   if (STAGED) {
-    // the tile is only needed by rows this kernel computes (1 .. long_row-1
-    // entries); factors whose entries all sit in long rows skip it
-    int need = 0;
-    for (int r = threadIdx.x; r < rows; r += blockDim.x) {
+    // (one row block) The thread's first two rows and their first SP_PF
+    // entries are read before the tile is staged, so those L2 round trips
+    // overlap the staging.  The tile is only needed by rows this kernel
+    // computes (1 .. long_row-1 entries); factors whose entries all sit in
+    // long rows skip it.
+    const int i0 = threadIdx.x, i1 = threadIdx.x + blockDim.x;
+    int b0 = 0, e0 = 0, b1 = 0, e1 = 0;
+    if (i0 < rows) b0 = rowptr[i0], e0 = rowptr[i0 + 1];
+    if (i1 < rows) b1 = rowptr[i1], e1 = rowptr[i1 + 1];
+    if (e0 - b0 >= long_row) e0 = b0 = 0;  // a long row: written by the long-row kernel
+    if (e1 - b1 >= long_row) e1 = b1 = 0;
+    int need = e0 > b0 || e1 > b1;
+    for (int r = i1 + blockDim.x; r < rows; r += blockDim.x) {
       const int L = rowptr[r + 1] - rowptr[r];
       need |= (L > 0 && L < long_row);
+    }
+    constexpr int SP_PF = 4;
+    int c0[SP_PF], c1[SP_PF];
+    T v0[SP_PF], v1[SP_PF];
+#pragma unroll
+    for (int u = 0; u < SP_PF; ++u) {
+      c0[u] = b0 + u < e0 ? colind[b0 + u] : 0;
+      v0[u] = b0 + u < e0 ? val[b0 + u] : T(0);
+      c1[u] = b1 + u < e1 ? colind[b1 + u] : 0;
+      v1[u] = b1 + u < e1 ? val[b1 + u] : T(0);
     }
     if (__syncthreads_or(need)) {
       stage_tile<T, TC>(tile, X, ldx, inner, j0, ncols);
       __syncthreads();
     }
+    auto row = [&](int i, int b, int e, const int (&c)[SP_PF], const T (&v)[SP_PF]) {
+      T acc[TC];
+#pragma unroll
+      for (int t = 0; t < TC; ++t) acc[t] = T(0);
+#pragma unroll
+      for (int u = 0; u < SP_PF; ++u)
+        if (b + u < e) {
+          T x[TC];
+          load_row<T, TC>(tile + (long)c[u] * TC, x);
+#pragma unroll
+          for (int t = 0; t < TC; ++t) acc[t] = fmad(v[u], x[t], acc[t]);
+        }
+      for (int p = b + SP_PF; p < e; ++p) {
+        const T vp = val[p];
+        T x[TC];
+        load_row<T, TC>(tile + (long)colind[p] * TC, x);
+#pragma unroll
+        for (int t = 0; t < TC; ++t) acc[t] = fmad(vp, x[t], acc[t]);
+      }
+#pragma unroll
+      for (int t = 0; t < TC; ++t)
+        if (j0 + t < ncols) Y[i + (long)(j0 + t) * ldy] = epi_apply(epi, acc[t], i, j0 + t, s);
+    };
+    // rows without entries still write their zeros (and epilogue)
+    if (i0 < rows && rowptr[i0 + 1] - rowptr[i0] < long_row) row(i0, b0, e0, c0, v0);
+    if (i1 < rows && rowptr[i1 + 1] - rowptr[i1] < long_row) row(i1, b1, e1, c1, v1);
+    first = i1 + blockDim.x;
   }
-  const T s = epi.scal ? *epi.scal : T(0);
-  for (int i = blockIdx.y * blockDim.x + threadIdx.x; i < rows; i += gridDim.y * blockDim.x) {
+  for (int i = first; i < rows; i += gridDim.y * blockDim.x) {
     T acc[TC];
 #pragma unroll
     for (int t = 0; t < TC; ++t) acc[t] = T(0);

@@ -1333,22 +1333,24 @@ __global__ void __launch_bounds__(PX_THREADS) k_chunk_sumsq(const T* __restrict_
   // there (the sparse projections leave few non-zeros; an FP64 FMA issues at
   // the same cost for 1 or 32 lanes).  The positions to do come from ballots
   // and are walked by a loop, in order.
+  // Thirty-two loads per thread are issued before any is used (the loop is
+  // otherwise one memory round trip per batch).
   T acc = T(0);
   long i = c0 + threadIdx.x;
-  for (; i + 7 * CR_LANES < c1; i += 8 * CR_LANES) {
-    T v[8];
+  for (; i + 31 * CR_LANES < c1; i += 32 * CR_LANES) {
+    T v[32];
 #pragma unroll
-    for (int u = 0; u < 8; ++u) v[u] = M[i + u * CR_LANES];
+    for (int u = 0; u < 32; ++u) v[u] = M[i + u * CR_LANES];
     const unsigned am = __activemask();
     unsigned todo = 0;
 #pragma unroll
-    for (int u = 0; u < 8; ++u) todo |= (__ballot_sync(am, mag_key(v[u]) != 0) ? 1u : 0u) << u;
+    for (int u = 0; u < 32; ++u) todo |= (__ballot_sync(am, mag_key(v[u]) != 0) ? 1u : 0u) << u;
     while (todo) {
       const int u = __ffs(todo) - 1;
       todo &= todo - 1;
       T x = v[0];
 #pragma unroll
-      for (int q = 1; q < 8; ++q) x = u == q ? v[q] : x;
+      for (int q = 1; q < 32; ++q) x = u == q ? v[q] : x;
       acc = fmad(x, x, acc);
     }
   }
