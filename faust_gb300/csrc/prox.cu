@@ -276,7 +276,7 @@ __device__ __forceinline__ void rs_pick(const unsigned* sh, int nb, int shift, u
 // after barrier p.
 template <typename T>
 __global__ void __launch_bounds__(PX_THREADS)
-    k_radix_select(const T* __restrict__ M, long N, int pos, int npass, TopkState* st, unsigned* hists,
+    k_radix_select(const T* __restrict__ M, long N, int pos, int npass, long long k, TopkState* st, unsigned* hists,
                    unsigned long long* __restrict__ list) {
   __shared__ unsigned sh[2048];
   __shared__ RsShared s;
@@ -287,14 +287,23 @@ __global__ void __launch_bounds__(PX_THREADS)
   if (threadIdx.x == 0) {
     s.prefix = 0;
     s.mask = 0;
-    s.krem = st->k_rem;
+    s.krem = k;
     s.G = 0;
     s.E = 0;
     s.bad = 0;
   }
   if (blockIdx.x == 0) {
     for (int i = threadIdx.x; i < (RS_MAX_PASSES - 1) * 2048; i += blockDim.x) hists[2048 + i] = 0;
-    if (threadIdx.x == 0) *list_n = 0;
+    if (threadIdx.x == 0) {
+      // the state fields later kernels read (no block writes the state
+      // before its first barrier)
+      *list_n = 0;
+      st->t = 0;
+      st->tau = 0;
+      st->sel_case = 0;
+      st->status = 0;
+      st->blocks_done = 0;
+    }
   }
   bool timed_out = false, tail = false;
   int p = 0;
@@ -1201,7 +1210,10 @@ __global__ void __launch_bounds__(PX_THREADS)
 
 // ------------------------------------------------------------------ sp apply
 template <typename T>
-__global__ void k_sp_apply(T* __restrict__ M, long N, int pos, const TopkState* st, unsigned char* __restrict__ flags) {
+__global__ void k_sp_apply(T* __restrict__ M, long N, int pos, const TopkState* st, unsigned char* __restrict__ flags,
+                           int* d_status) {
+  // the selection is complete: its status goes to the caller's word
+  if (d_status && blockIdx.x == 0 && threadIdx.x == 0 && st->status) atomicCAS(d_status, 0, st->status);
   const unsigned long long t = st->t;
   const int cs = st->sel_case;
   const long long tau = st->tau;
@@ -1364,25 +1376,27 @@ __global__ void __launch_bounds__(PX_THREADS) k_chunk_sumsq(const T* __restrict_
 }
 
 // MatDense::normalize (faust_MatDense.hpp:1225-1250): scale = FPP(1.0/norm),
-// domain_error (here FGB_ERR_ZERO_NORM) on a zero norm.
+// domain_error (here FGB_ERR_ZERO_NORM) on a zero norm.  Every block of the
+// scaling kernel adds the chunk partials in order itself (one thread: the
+// FP64 square root and division are a few hundred cycles), which saves the
+// launch of a one-thread kernel.
 template <typename T>
-__global__ void k_norm_finalize(const double* partials, int nchunks, double* scal, int* status) {
-  T total = T(0);
-  for (int c = 0; c < nchunks; ++c) total = addr(total, reinterpret_cast<const T*>(partials)[c]);
-  const T n = sqrtr(total);
-  T inv = T(0);
-  if (n == T(0)) {
-    if (status) atomicCAS(status, 0, (int)FGB_ERR_ZERO_NORM);
-  } else {
-    inv = (T)__ddiv_rn(1.0, (double)n);
+__global__ void k_scale(T* __restrict__ M, long N, const double* __restrict__ partials, int nchunks, int* status) {
+  __shared__ T s_inv;
+  if (threadIdx.x == 0) {
+    T total = T(0);
+    for (int c = 0; c < nchunks; ++c) total = addr(total, reinterpret_cast<const T*>(partials)[c]);
+    const T n = sqrtr(total);
+    T inv = T(0);
+    if (n == T(0)) {
+      if (status && blockIdx.x == 0) atomicCAS(status, 0, (int)FGB_ERR_ZERO_NORM);
+    } else {
+      inv = (T)__ddiv_rn(1.0, (double)n);
+    }
+    s_inv = inv;
   }
-  reinterpret_cast<T*>(scal)[0] = inv;
-  scal[1] = (double)n;
-}
-
-template <typename T>
-__global__ void k_scale(T* __restrict__ M, long N, const double* scal) {
-  const T s = reinterpret_cast<const T*>(scal)[0];
+  __syncthreads();
+  const T s = s_inv;
   // a zero times a finite non-negative scale keeps its bits: not rewritten,
   // and a warp of zeros issues no multiply
   const bool skip_zeros = raw_bits(s) < raw_bits(T(INFINITY));
@@ -1411,10 +1425,6 @@ __global__ void k_scale(T* __restrict__ M, long N, const double* scal) {
   }
 }
 
-__global__ void k_status_merge(const TopkState* st, int* status) {
-  if (st->status) atomicCAS(status, 0, st->status);
-}
-
 
 __global__ void k_topk_init(TopkState* st, long long k) {
   TopkState z;
@@ -1434,9 +1444,7 @@ static fgb_status queue_normalize(fgb_ctx* ctx, ProxWork& w, T* M, long N, int* 
   const int nchunks = (int)((N + CR_CHUNK - 1) / CR_CHUNK);
   k_chunk_sumsq<T><<<nchunks, PX_THREADS, 0, ctx->stream>>>(M, N, w.partials);
   FGB_LAUNCHED(ctx);
-  k_norm_finalize<T><<<1, 1, 0, ctx->stream>>>(w.partials, nchunks, w.scal, d_status);
-  FGB_LAUNCHED(ctx);
-  k_scale<T><<<grid_for(ctx, N), PX_THREADS, 0, ctx->stream>>>(M, N, w.scal);
+  k_scale<T><<<grid_for(ctx, N), PX_THREADS, 0, ctx->stream>>>(M, N, w.partials, nchunks, d_status);
   FGB_LAUNCHED(ctx);
   return FGB_OK;
 }
@@ -1499,9 +1507,11 @@ static fgb_status queue_tie_replay(fgb_ctx* ctx, ProxWork& w, const T* M, long N
 
 template <typename T>
 static fgb_status queue_sp(fgb_ctx* ctx, ProxWork& w, T* M, long N, long k, int pos, int* d_status) {
-  k_topk_init<<<1, 1, 0, ctx->stream>>>(w.state, k);
-  FGB_LAUNCHED(ctx);
   const int g = grid_for(ctx, N);
+  if (!w.hist_passes) {
+    k_topk_init<<<1, 1, 0, ctx->stream>>>(w.state, k);
+    FGB_LAUNCHED(ctx);
+  }
   if (w.hist_passes) {
     // every pass in one cooperative launch (blocks co-resident for the barrier)
     static thread_local int coop_blocks[2] = {0, 0};
@@ -1523,7 +1533,8 @@ static fgb_status queue_sp(fgb_ctx* ctx, ProxWork& w, T* M, long N, long k, int 
     cfg.attrs = attr;
     cfg.numAttrs = 1;
     const T* Mc = M;
-    FGB_CUDA(ctx, cudaLaunchKernelEx(&cfg, k_radix_select<T>, Mc, N, pos, npass, w.state, w.hist_passes, w.rs_list));
+    FGB_CUDA(ctx, cudaLaunchKernelEx(&cfg, k_radix_select<T>, Mc, N, pos, npass, (long long)k, w.state, w.hist_passes,
+                                     w.rs_list));
     FGB_LAUNCHED(ctx);
   } else if (sizeof(T) == 8) {
     const int shifts[6] = {52, 41, 30, 19, 8, 0};
@@ -1576,12 +1587,8 @@ static fgb_status queue_sp(fgb_ctx* ctx, ProxWork& w, T* M, long N, long k, int 
     kern<<<1, PX_THREADS, smem, ctx->stream>>>(M, N, pos, (int)k, w.state, w.flags, gheap, use_smem ? 1 : 0);
     FGB_LAUNCHED(ctx);
   }
-  k_sp_apply<T><<<g, PX_THREADS, 0, ctx->stream>>>(M, N, pos, w.state, w.flags);
+  k_sp_apply<T><<<g, PX_THREADS, 0, ctx->stream>>>(M, N, pos, w.state, w.flags, d_status);
   FGB_LAUNCHED(ctx);
-  if (d_status) {
-    k_status_merge<<<1, 1, 0, ctx->stream>>>(w.state, d_status);
-    FGB_LAUNCHED(ctx);
-  }
   return FGB_OK;
 }
 
