@@ -82,6 +82,31 @@ def test_prox_sp_heap_order_large(oracle, rows, cols, k, levels):
         assert np.array_equal(got, ref), pos
 
 
+@pytest.mark.parametrize("dtype", [np.float64, np.float32])
+@pytest.mark.parametrize("espan,levels", [(40, 0), (20, 0), (40, 5), (3, 0)])
+def test_prox_sp_radix_key_list(oracle, dtype, espan, levels):
+    """1M entries whose magnitudes spread over `espan` binades, so the radix
+    select finishes in one block over its key list: after the first digit
+    when the k-th key's bucket holds at most 32,768 keys (espan 40: ~26,000
+    in FP64), after the second when it does not (espan 20 and 3: 52,000 and
+    349,000 after the first digit); `levels` > 0 puts ties inside the bucket
+    (thousands of equal keys).  Heavy ties that keep the bucket above the
+    list's size to the last digit are the tie tests above.  Support and
+    normalised values bit-exact against the oracle."""
+    rng = np.random.default_rng(espan * 10 + levels + (dtype == np.float32))
+    n = 1024
+    e = rng.integers(0, espan, size=(n, n))
+    frac = rng.integers(0, levels + 1, size=(n, n)) / 8.0 if levels else rng.random((n, n))
+    M = (np.where(rng.random((n, n)) < 0.5, -1.0, 1.0) * np.ldexp(1.0 + frac, -e)).astype(dtype)
+    for k, normalized, pos in [(2048, True, False), (int(rng.integers(1000, 100000)), True, True),
+                               (int(rng.integers(100000, 400000)), False, False)]:
+        c = fact.ConstraintInt("sp", n, n, k, normalized=normalized, pos=pos)
+        got = _gpu_prox(M, c)
+        ref = oracle.prox(oracle.SP, M, k=k, normalized=normalized, pos=pos)
+        assert np.array_equal(got, ref), (k, normalized, pos)
+        assert np.count_nonzero(got) == min(k, np.count_nonzero(np.maximum(M, 0) if pos else M))
+
+
 @pytest.mark.parametrize("name,kind", [("spcol", 1), ("splin", 2), ("splincol", 3)])
 @pytest.mark.parametrize("seed", range(4))
 def test_prox_lines_bitexact(oracle, name, kind, seed):
