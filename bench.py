@@ -791,11 +791,15 @@ def _barrier(world):
 
 
 def _max_over_ranks(x, world):
+    """The slowest rank's time: every rank's timed region ends at the same
+    barrier, so the job's time is the maximum (NCCL on the GPUs; gloo keeps
+    the tensor on the host)."""
     if world <= 1:
         return x
     import torch
     import torch.distributed as dist
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
 
