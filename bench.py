@@ -593,15 +593,24 @@ def palm_roofline(ctx, hbm, peak_kind):
 
 
 def cpu_baseline_palm(its=5):
+    """The oracle's palm4msa2 on all host cores, and on one core (the
+    reference's default CPU build is single-threaded), over the first `its`
+    iterations scaled to the full run."""
     from oracle import oracle as O
     H, cons, params = _palm_problem()
     threads = os.cpu_count() or 1
+    times = {}
+    for th in (threads, 1):
+        O.set_threads(th)
+        t0 = time.perf_counter()
+        O.palm4msa2(H, [c.oracle_dict() for c in cons], its, norm2_threshold=PALM_THR, norm2_max_iter=100)
+        times[th] = time.perf_counter() - t0
     O.set_threads(threads)
-    t0 = time.perf_counter()
-    O.palm4msa2(H, [c.oracle_dict() for c in cons], its, norm2_threshold=PALM_THR, norm2_max_iter=100)
-    dt = time.perf_counter() - t0
+    dt, d1 = times[threads], times[1]
     return {"value": round(dt * PALM_ITS / its, 3), "unit": "s", "cores": threads, "kind": "port",
-            "sample": "%d of %d iterations timed (%.2f s), scaled to the full run" % (its, PALM_ITS, dt)}
+            "sample": "%d of %d iterations timed (%.2f s), scaled to the full run" % (its, PALM_ITS, dt),
+            "single_core": {"value": round(d1 * PALM_ITS / its, 3), "unit": "s", "cores": 1,
+                            "sample": "the same %d iterations on one thread (%.2f s), scaled" % (its, d1)}}
 
 
 # ---------------------------------------------------------------- batched PALM4MSA
