@@ -58,8 +58,12 @@ typedef struct fgb_faust fgb_faust;
 
 /* ------------------------------------------------------------------ context
  * Replaces gp_funcs->set_dev / set_stream (faust_gpu_mod_utils.h:100-102).
- * All work of the context is queued on cuda_stream (a cudaStream_t; NULL is
- * the legacy default stream). */
+ * All work of the context is ordered on cuda_stream (a cudaStream_t; NULL is
+ * the legacy default stream): kernels the context runs beside it (the
+ * long-row part of a sparse product, the PALM power iterations) go to the
+ * context's own streams, forked from cuda_stream by an event and joined back
+ * before the next work queued on it, so the caller sees one stream (and a
+ * capture of cuda_stream captures them too). */
 fgb_status fgb_ctx_create(int device, void* cuda_stream, fgb_ctx** out);
 fgb_status fgb_ctx_destroy(fgb_ctx* ctx);
 const char* fgb_last_error(const fgb_ctx* ctx);
