@@ -177,6 +177,44 @@ def test_prox_sp_keeps_everything_when_k_large(oracle):
     assert np.array_equal(out, M)
 
 
+def test_prox_k_bounds(oracle):
+    """The k bounds of faust_prox.hpp: k <= 0 gives zeros (:78-79, :119-120,
+    :153-154); sp keeps everything unless k < rows*cols (:82), spcol unless
+    k < rows (:123), splin unless k < cols (:157)."""
+    rng = np.random.default_rng(11)
+    M = rng.standard_normal((7, 5))
+    for kind in (oracle.SP, oracle.SPCOL, oracle.SPLIN):
+        assert not np.any(oracle.prox(kind, M, k=0, normalized=False))
+    assert np.array_equal(oracle.prox(oracle.SP, M, k=35, normalized=False), M)
+    assert np.array_equal(oracle.prox(oracle.SPCOL, M, k=7, normalized=False), M)
+    assert np.array_equal(oracle.prox(oracle.SPLIN, M, k=5, normalized=False), M)
+    assert np.count_nonzero(oracle.prox(oracle.SP, M, k=34, normalized=False)) == 34
+    assert _nnz_cols(oracle.prox(oracle.SPCOL, M, k=6, normalized=False)).max() == 6
+    assert _nnz_rows(oracle.prox(oracle.SPLIN, M, k=4, normalized=False)).max() == 4
+
+
+def test_prox_normcol_zero_s_and_zero_columns(oracle):
+    """prox_normcol (faust_prox.hpp:204-246): s == 0 gives zeros; a zero
+    column stays zero (its scale factor stays 0); the others get norm s."""
+    rng = np.random.default_rng(12)
+    M = rng.standard_normal((6, 4))
+    assert not np.any(oracle.prox(oracle.NORMCOL, M, s=0.0, normalized=False))
+    M[:, 2] = 0
+    out = oracle.prox(oracle.NORMCOL, M, s=1.5, normalized=False)
+    assert not np.any(out[:, 2])
+    assert np.allclose(np.linalg.norm(out[:, [0, 1, 3]], axis=0), 1.5)
+
+
+def test_prox_pos_clamps_before_selection(oracle):
+    """pre_prox_pos (faust_prox.hpp:307-320) runs first: with every entry
+    negative the projection keeps only zeros, which the normalisation
+    rejects."""
+    M = -np.abs(np.random.default_rng(13).standard_normal((5, 5))) - 0.1
+    assert not np.any(oracle.prox(oracle.SP, M, k=4, normalized=False, pos=True))
+    with pytest.raises(RuntimeError):
+        oracle.prox(oracle.SP, M, k=4, normalized=True, pos=True)
+
+
 def test_prox_normcol_negative_s_is_an_error(oracle):
     with pytest.raises(RuntimeError):
         oracle.prox(oracle.NORMCOL, np.ones((3, 3)), s=-1.0)
