@@ -173,10 +173,9 @@ __global__ void __launch_bounds__(PX_THREADS)
 // every block histograms its share of the keys that match the prefix, adds
 // its bins to the pass's global histogram, waits at a grid barrier, and then
 // every block reads the histogram and picks the bucket itself (the same
-// choice everywhere), so only one barrier per pass is needed.  Histogram p-1
-// is cleared by block 0 after barrier p, the last one at the start of the
-// next call.  The barrier wait is bounded: on time-out the state's status is
-// set to FGB_ERR_TIMEOUT.
+// choice everywhere), so only one barrier per pass is needed (the clearing
+// of the histograms is described at k_radix_select).  The barrier wait is
+// bounded: on time-out the state's status is set to FGB_ERR_TIMEOUT.
 __device__ __forceinline__ bool rs_grid_barrier(unsigned* bar, unsigned nblocks, int* s_ok) {
   __syncthreads();
   if (threadIdx.x == 0) {
@@ -273,7 +272,9 @@ __device__ __forceinline__ void rs_pick(const unsigned* sh, int nb, int shift, u
 // passes over a few thousand keys.  The list counter is the word after the
 // barrier's two; block 0 clears it and the histograms of passes 1.. at the
 // start (no block touches them before the first barrier), histogram p-1
-// after barrier p.
+// after barrier p.  Block 0 also resets the selection state the later
+// kernels read (k comes as an argument), so no separate reset launch is
+// needed.
 template <typename T>
 __global__ void __launch_bounds__(PX_THREADS)
     k_radix_select(const T* __restrict__ M, long N, int pos, int npass, long long k, TopkState* st, unsigned* hists,
