@@ -41,6 +41,13 @@ struct fgb_ctx {
   // to `stream` by the two events around each product (null: run in line).
   cudaStream_t s_long = nullptr;
   cudaEvent_t ev_long_fork = nullptr, ev_long_join = nullptr;
+  // Per-device launch facts of the projection kernels, kept on the context
+  // (whose device is fixed): the cooperative grid of the radix select (FP32,
+  // FP64) and the dynamic shared memory already opted in for the two tie
+  // replay kernels.
+  int rs_coop_blocks[2] = {0, 0};
+  size_t rp_replay_smem[2] = {0, 0};
+  size_t heap_replay_smem = 0;
 };
 
 namespace fgb {

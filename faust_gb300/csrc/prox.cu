@@ -403,6 +403,18 @@ __global__ void __launch_bounds__(PX_THREADS)
     if (s.bad) atomicCAS(&st->status, 0, (int)FGB_ERR_INVALID_ARG);
   }
   if (timed_out && threadIdx.x == 0) atomicCAS(&st->status, 0, (int)FGB_ERR_TIMEOUT);
+  // The last block to leave clears the barrier's arrival count.  After a
+  // barrier time-out the late blocks' arrivals can leave it non-zero, and
+  // the next launch on this workspace would then release a barrier early.
+  // Every block has passed all its barriers once it counts itself out here.
+  if (threadIdx.x == 0) {
+    __threadfence();
+    if (atomicAdd(&bar[3], 1u) == gridDim.x - 1) {
+      bar[0] = 0;
+      bar[3] = 0;
+      __threadfence();
+    }
+  }
 }
 
 // ------------------------------------------------------------------ tie case
@@ -1495,10 +1507,10 @@ static fgb_status queue_tie_replay(fgb_ctx* ctx, ProxWork& w, const T* M, long N
                                                      reinterpret_cast<HNode*>(w.cand), w.wcount);
   FGB_LAUNCHED(ctx);
   auto kern = in_smem ? k_rp_replay<T, true> : k_rp_replay<T, false>;
-  static thread_local size_t attr_set[2] = {0, 0};
-  if (smem > attr_set[in_smem]) {
+  size_t& attr_set = ctx->rp_replay_smem[in_smem];
+  if (smem > attr_set) {
     FGB_CUDA(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    attr_set[in_smem] = smem;
+    attr_set = smem;
   }
   kern<<<1, PX_THREADS, smem, ctx->stream>>>(M, N, pos, k, wmax, nwin, w.state, w.flags,
                                              reinterpret_cast<const HNode*>(w.cand), w.wcount, gk, gi);
@@ -1515,8 +1527,7 @@ static fgb_status queue_sp(fgb_ctx* ctx, ProxWork& w, T* M, long N, long k, int 
   }
   if (w.hist_passes) {
     // every pass in one cooperative launch (blocks co-resident for the barrier)
-    static thread_local int coop_blocks[2] = {0, 0};
-    int& nb = coop_blocks[sizeof(T) == 8];
+    int& nb = ctx->rs_coop_blocks[sizeof(T) == 8];
     if (!nb) {
       int per_sm = 0;
       FGB_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_radix_select<T>, PX_THREADS, 0));
@@ -1580,7 +1591,7 @@ static fgb_status queue_sp(fgb_ctx* ctx, ProxWork& w, T* M, long N, long k, int 
     auto kern = k_heap_replay<T>;
     // the kernel also has static shared arrays: opt in whenever the dynamic
     // part approaches the default 48 KB limit (once per size, outside captures)
-    static thread_local size_t attr_set = 0;
+    size_t& attr_set = ctx->heap_replay_smem;
     if (smem > 40 * 1024 && smem > attr_set) {
       FGB_CUDA(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
       attr_set = smem;

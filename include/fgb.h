@@ -201,8 +201,12 @@ typedef struct fgb_constraint {
 fgb_status fgb_prox(fgb_ctx* ctx, fgb_dtype dtype, const fgb_constraint* cons, void* M);
 
 /* Same projection as fgb_prox, for callers that cannot allocate device
- * memory: no cudaMalloc/cudaFree or allocating library call is made.  This
- * entry point has no counterpart in the reference.  Its scratch memory is one
+ * memory: host applications that reserve all of a GPU's memory up front
+ * (a fixed serving budget, an embedder whose pool owns the device) and
+ * latency-critical loops that must not reach cudaMalloc / cudaFree, which
+ * can synchronise the device.  No cudaMalloc/cudaFree or allocating library
+ * call is made.  This entry point has no counterpart in the reference.  The
+ * caller's current device is restored before returning.  Its scratch memory is one
  * fixed 6 MiB device array inside the library (every GPU that loads the
  * library holds it until the process exits), which limits it to
  * rows*cols <= 4194304, rows+cols <= 65536 and, for FGB_SP / FGB_SP_POS,

@@ -646,26 +646,7 @@ static int topk_case(const std::vector<T>& v, long k) {
   for (size_t i = 0; i < N; ++i)
     if (mags[i] >= t && ++cnt == (size_t)k) { tau = i; break; }
   for (size_t i = tau + 1; i < N; ++i)
-    if (mags[i] > t) {
-      if (getenv("ORC_TOPK_STATS")) {
-        // number of heap replacements made by the selection
-        std::vector<T> h(mags.begin(), mags.begin() + k);
-        std::make_heap(h.begin(), h.end(), std::greater<T>());
-        size_t ins = 0, cand = 0;
-        for (size_t j = k; j < N; ++j) {
-          if (mags[j] > h.front()) {
-            std::pop_heap(h.begin(), h.end(), std::greater<T>());
-            h.back() = mags[j];
-            std::push_heap(h.begin(), h.end(), std::greater<T>());
-            ++ins;
-          }
-        }
-        T m0 = *std::min_element(mags.begin(), mags.begin() + k);
-        for (size_t j = k; j < N; ++j) cand += mags[j] > m0;
-        fprintf(stderr, "case2 N=%zu k=%ld G=%zu E=%zu tau=%zu ins=%zu cand=%zu\n", N, k, G, E, tau, ins, cand);
-      }
-      return 2;
-    }
+    if (mags[i] > t) return 2;
   return 1;
 }
 

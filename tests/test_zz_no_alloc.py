@@ -1,8 +1,9 @@
 """fgb_prox_noalloc: the projection for callers that cannot allocate device
-memory (code running inside strict stream capture, allocator-free real-time
-paths, embedders with pre-reserved memory).  It must give the same result as
-the allocating entry point fgb_prox, call after call, although its scratch is
-one fixed device array that keeps whatever the previous call left.
+memory (applications that reserve all GPU memory up front, loops that must
+not reach cudaMalloc / cudaFree because those can synchronise the device).
+It must give the same result as the allocating entry point fgb_prox, call
+after call, although its scratch is one fixed device array that keeps
+whatever the previous call left.
 
 This file is collected last on purpose: a failure here stops a -x run only
 after every other test has run."""
@@ -39,6 +40,11 @@ def _cases(rng):
         (np.float32, _ffi.SPLINCOL, 128, 96, 4, 1.0, ties(128, 96, 2)),
         (np.float64, _ffi.NORMCOL, 64, 80, 0, 2.0, rng.standard_normal((64, 80))),
         (np.float64, _ffi.SUPP, 40, 60, 0, 1.0, rng.standard_normal((40, 60))),
+        # pos clamping before the selection, and the normalisation, whose
+        # partial sums sit in the scratch array
+        (np.float64, _ffi.SP_POS, 200, 150, 500, 1.0, ties(200, 150, 3)),
+        (np.float32, _ffi.SPCOL, 96, 70, 5, 1.0, ties(96, 70, 2)),
+        (np.float64, _ffi.SPLIN, 50, 300, 7, 1.0, rng.standard_normal((50, 300))),
     ]
 
 
@@ -74,3 +80,36 @@ def test_noalloc_rejects_sizes_beyond_its_scratch():
     cons = _ffi.Constraint(_ffi.SP, 2048, 4096, 10, 1.0, 0, 0, None)
     st = _ffi.lib().fgb_prox_noalloc(ctx.handle, _ffi.F32, ctypes.byref(cons), M.data_ptr(), None)
     assert st == 1 and b"exceeds the fixed scratch" in _ffi.lib().fgb_last_error(ctx.handle)
+    # rows + cols above 65536 with few entries
+    M1 = torch.zeros((65536, 1), device="cuda", dtype=torch.float32).t()
+    cons = _ffi.Constraint(_ffi.SPLIN, 1, 65536, 4, 1.0, 0, 0, None)
+    st = _ffi.lib().fgb_prox_noalloc(ctx.handle, _ffi.F32, ctypes.byref(cons), M1.data_ptr(), None)
+    assert st == 1 and b"exceeds the fixed scratch" in _ffi.lib().fgb_last_error(ctx.handle)
+    # sp with k above the replay heap (k < rows * cols)
+    M2 = torch.zeros((512, 512), device="cuda", dtype=torch.float64).t()
+    for kind in (_ffi.SP, _ffi.SP_POS):
+        cons = _ffi.Constraint(kind, 512, 512, 65537, 1.0, 0, 0, None)
+        st = _ffi.lib().fgb_prox_noalloc(ctx.handle, _ffi.F64, ctypes.byref(cons), M2.data_ptr(), None)
+        assert st == 1 and b"exceeds the fixed scratch" in _ffi.lib().fgb_last_error(ctx.handle)
+    # the rejected calls left nothing behind: a valid call still matches fgb_prox
+    rng = np.random.default_rng(7)
+    M = rng.standard_normal((64, 48))
+    a = torch.from_numpy(np.ascontiguousarray(M.T)).cuda().t()
+    b = a.clone()
+    cons = _ffi.Constraint(_ffi.SP, 64, 48, 100, 1.0, 1, 0, None)
+    _call("fgb_prox", ctx, _ffi.F64, cons, a)
+    _call("fgb_prox_noalloc", ctx, _ffi.F64, cons, b)
+    torch.cuda.synchronize()
+    assert torch.equal(a, b)
+
+
+def test_noalloc_restores_the_current_device():
+    import torch
+    import faust_gb300 as fg
+    from faust_gb300 import _ffi
+    ctx = fg.Context(0)
+    before = torch.cuda.current_device()
+    M = torch.from_numpy(np.ascontiguousarray(np.random.default_rng(3).standard_normal((32, 16)).T)).cuda().t()
+    cons = _ffi.Constraint(_ffi.SP, 32, 16, 40, 1.0, 1, 0, None)
+    _call("fgb_prox_noalloc", ctx, _ffi.F64, cons, M)
+    assert torch.cuda.current_device() == before
