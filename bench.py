@@ -124,11 +124,13 @@ class FaustX:
         elif name == "bsr":
             import faust_gb300 as fg
             self.n, self.ncols, self.np_dtype, self.tdtype = 16384, 4096, None, torch.bfloat16
-            self.bsr = []
+            self.bsr, self.bsr_f32 = [], []
             sigma = 1.0 / np.sqrt(8 * 64)
             for _ in range(4):
                 bp, bc, blocks = synth.random_bsr(16384, 64, 8, rng, sigma)
-                self.bsr.append(fg.BSRFactor(16384, 16384, bp, bc, synth.bf16_bits(blocks)))
+                bits = synth.bf16_bits(blocks)
+                self.bsr.append(fg.BSRFactor(16384, 16384, bp, bc, bits))
+                self.bsr_f32.append((bp, bc, synth.bf16_to_f32(bits).reshape(blocks.shape)))
             self.desc = "4 BSR 16384^2, 64x64 BF16 blocks, 8 blocks/block-row, x X 16384x4096 BF16"
             self.dtype = "bf16"
         else:
@@ -264,9 +266,41 @@ def run_faust_x(args, rank, world):
         "gpu_launches": int(launches),
         "clocks": clk.summary(),
     }
+    if W.name == "bsr" and rank == 0 and not args.no_cpu_baseline:
+        out["config"]["error_vs_fp64"] = bsr_error_vs_fp64(W)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline_faust_x(W)
     return out
+
+
+def _bsr_oracle_chain(W, Xs):
+    """FP64 oracle of the BSR chain (BSRMat::mul per factor, right to left) on
+    the columns Xs (n x c, FP64) with the BF16-rounded blocks."""
+    from oracle import oracle as O
+    Z = np.asfortranarray(Xs)
+    for bp, bc, blocks in reversed(W.bsr_f32):
+        flat = np.ascontiguousarray(blocks.transpose(0, 2, 1).reshape(len(bc), -1), np.float64)
+        Z = O.bsr_mul_f64(W.n, W.n, 64, 64, bp, bc, flat, Z)
+    return Z
+
+
+def bsr_error_vs_fp64(W, ncols=32):
+    """Relative Frobenius error of the GPU result (BF16 storage, FP32
+    accumulation, BF16 intermediates) against the FP64 oracle of the same
+    BF16 inputs, on a seeded subset of the columns of X."""
+    import torch
+    from oracle import oracle as O
+    O.set_threads(os.cpu_count() or 1)
+    W.step()
+    torch.cuda.synchronize()
+    cols = np.sort(np.random.default_rng(5).choice(W.ncols, ncols, replace=False))
+    ci = torch.from_numpy(cols).cuda()
+    Xs = W.X.index_select(1, ci).float().cpu().numpy().astype(np.float64)
+    Ys = W.Y.index_select(1, ci).float().cpu().numpy().astype(np.float64)
+    ref = _bsr_oracle_chain(W, Xs)
+    return {"rel_frobenius": float(np.linalg.norm(Ys - ref) / np.linalg.norm(ref)),
+            "max_abs": float(np.abs(Ys - ref).max()), "ref_rms": float(np.sqrt(np.mean(ref * ref))),
+            "columns": ncols, "oracle": "FP64 BSR chain of the BF16-rounded blocks and X (no intermediate rounding)"}
 
 
 def cpu_baseline_faust_x(W, sample_cols=None):
@@ -274,8 +308,18 @@ def cpu_baseline_faust_x(W, sample_cols=None):
     threads = os.cpu_count() or 1
     O.set_threads(threads)
     if W.name == "bsr":
-        return {"value": None, "unit": "GB/s", "cores": threads, "kind": "port",
-                "sample": "not run for BSR (FP64 oracle too slow for a bounded sample)"}
+        cols = sample_cols or 32
+        Xs = np.random.default_rng(7).standard_normal((W.n, cols))
+        _bsr_oracle_chain(W, Xs[:, :2])
+        t0 = time.perf_counter()
+        _bsr_oracle_chain(W, Xs)
+        dt = time.perf_counter() - t0
+        bytes_ = sum(b + 2 * W.n * cols * 2 for b in W.factor_bytes())
+        flops = sum(2 * f.nnz_blocks * 64 * 64 * cols for f in W.bsr)
+        return {"value": round(bytes_ / dt / 1e9, 3), "unit": "GB/s", "cores": threads, "kind": "port",
+                "gflops": round(flops / dt / 1e9, 2),
+                "sample": "FP64 oracle chain on %d of %d columns of X (%.2f s); bytes counted as BF16 like the "
+                          "GPU line" % (cols, W.ncols, dt)}
     cols = sample_cols or (512 if W.name == "csr_butterfly" else W.ncols)
     rng = np.random.default_rng(7)
     X = np.asfortranarray(rng.standard_normal((W.n, cols)).astype(W.np_dtype))
@@ -475,22 +519,27 @@ def run_palm(args, rank, world):
     # relative error of the result (outside the timed region)
     err = ctypes.c_double()
     _ffi.check(_ffi.lib().fgb_rel_err(res.faust.handle, Hd.data_ptr(), res.lambda_, ctypes.byref(err)), ctx.handle)
+    run_factors = [res.faust.factors(i) for i in range(PALM_J)]
     res.faust.close()
-    # end to end through the host-memory C-ABI entry point: A from host
-    # memory in, every factor back to host memory
+    # end to end through the host-memory C-ABI entry point, under the same
+    # conditions as the device-resident runs (L2 flushed before each, mean of
+    # the same number of runs): A from host memory in, every factor back to
+    # host memory
     Hh = np.asfortranarray(H)
     e2e = []
     d2h = 0
-    for _ in range(max(2, min(args.steps, 3))):
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
         t0 = time.perf_counter()
         r = fact.palm4msa(Hh, cons, params, ctx=ctx)
         facs = [r.faust.factors(i) for i in range(PALM_J)]
         e2e.append(time.perf_counter() - t0)
         d2h = sum(f.nnz * 12 + (f.shape[0] + 1) * 4 for f in facs)
         r.faust.close()
-    e2e_s = float(np.median(e2e))
+    e2e_s = _max_over_ranks(float(np.mean(e2e)), world)
     hbm, tflops, peak_kind = _peaks()
-    roof, roof_spmm = palm_roofline(ctx, hbm, peak_kind)
+    roof_spmm, roof_pi = palm_roofline(ctx, run_factors)
     out = {
         "metric": METRIC, "submetric": "palm4msa2 FP64 time to the plain 200-iteration relative error (s per run)",
         "value": round(step_s, 5), "unit": "s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
@@ -500,15 +549,15 @@ def run_palm(args, rank, world):
                                "power-iteration tol 1e-8 (max 100), FP64",
                    "l2": "flushed (256 MB write) before every timed run", "rel_err": err.value,
                    "lambda": res.lambda_},
-        "roofline": roof,
-        "roofline_spmm": roof_spmm,
+        "roofline": roof_spmm,
+        "roofline_power_iteration": roof_pi,
         "e2e": {"value": round(e2e_s, 5), "unit": "s", "h2d_bytes_per_step": int(H.nbytes),
-                "d2h_bytes_per_step": int(d2h)},
+                "d2h_bytes_per_step": int(d2h), "runs": len(e2e)},
         "gpu_launches": int(launches),
         "clocks": clk.summary(),
     }
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        out["cpu_baseline"] = cpu_baseline_palm()
+        out["cpu_baseline"] = cpu_baseline_palm(single_core=args.cpu_single_core)
     return out
 
 
@@ -522,56 +571,64 @@ def fp64_peak(ctx):
     return out.value / 1e12
 
 
-def palm_roofline(ctx, hbm, peak_kind):
-    """Rooflines of the two FP64 kernels that bound the PALM run, each timed
-    alone with CUDA events: the power iteration (one CTA per chain; a
-    9-factor chain of the run's shape) against one SM's share of the FP64 FMA
-    peak, and the sparse x dense product of the gradient chain (k_csr_spmm,
-    1024 x 1024 FP64 factor with 2048 entries times a 1024 x 1024 block, 40
-    back-to-back launches per call) against the device FP64 FMA peak.  Both
-    work on L2-resident data: the scalar FP64 pipe, not HBM, bounds them."""
+def palm_roofline(ctx, run_factors):
+    """Rooflines of the two FP64 kernels of the PALM run, each timed alone with
+    CUDA events on the run's own final factors.
+
+    * The gradient product (the main stream's largest share): one factor of
+      the run times a 1024 x 1024 FP64 block, as an update launches it
+      (k_csr_spmm for rows of at most 16 entries beside k_csr_spmm_long for
+      the longer rows on a forked side stream), over each of the 10 factors;
+      against the device FP64 FMA rate.
+    * The power iteration (one CTA per chain, on a side stream in the run) on
+      the run's chain S_1 ... S_9: against one SM's share of the FP64 FMA
+      rate (it is one CTA) and against the whole device.
+    Both work on L2-resident data: the scalar FP64 pipe, not HBM, bounds them."""
     import ctypes
     import torch
     import faust_gb300 as fg
-    import scipy.sparse as sp
     from faust_gb300 import _ffi
     peak = fp64_peak(ctx)
     sm_count = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
     stream = torch.cuda.current_stream()
-    S = sp.random(PALM_N, PALM_N, density=PALM_K / PALM_N ** 2, random_state=3, format="csr")
-    S.sort_indices()
-    # --- k_csr_spmm
-    nf = 40
-    F = fg.Faust([S] * nf, ctx=ctx)
+    s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    # --- gradient products: each factor of the run times a 1024^2 block
     X = torch.randn((PALM_N, PALM_N), device="cuda", dtype=torch.float64).t()
     Y = torch.empty((PALM_N, PALM_N), device="cuda", dtype=torch.float64).t()
-    for _ in range(3):
-        F.matmul_device(X, Y, mode=1)
-    s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    calls = 10
+    singles = [fg.Faust([f], ctx=ctx) for f in run_factors]
+    for G in singles:
+        G.matmul_device(X, Y, mode=1)
+    torch.cuda.synchronize()
+    calls = 20
     s.record(stream)
     for _ in range(calls):
-        F.matmul_device(X, Y, mode=1)
+        for G in singles:
+            G.matmul_device(X, Y, mode=1)
     e.record(stream)
     torch.cuda.synchronize()
-    us = s.elapsed_time(e) * 1e3 / (calls * nf)
-    F.close()
-    flops = 2.0 * S.nnz * PALM_N
+    us = s.elapsed_time(e) * 1e3 / (calls * len(singles))
+    nnz = float(np.mean([f.nnz for f in run_factors]))
+    longest = max(int(np.diff(f.indptr).max()) for f in run_factors)
+    flops = 2.0 * nnz * PALM_N
     spmm = {"bound": "fp64", "achieved": round(flops / (us * 1e-6) / 1e12, 4), "peak": round(peak, 4),
             "unit": "TFLOP/s", "frac": round(flops / (us * 1e-6) / 1e12 / peak, 4),
-            "traffic": 8465408, "traffic_note": "dram bytes of one launch, ncu capture with cold L2",
-            "peak_kind": "measured in this run (FP64 FMA loop on all SMs)",
-            "kernel": "k_csr_spmm (PALM gradient product, 1024^2 FP64 factor with 2048 entries x 1024^2 block)",
-            "algorithmic_flops_per_launch": int(flops), "us_per_launch": round(us, 3)}
-    # --- power iteration on one 9-factor chain (one CTA)
-    G = fg.Faust([S] * 9, ctx=ctx)
+            "traffic": None, "traffic_note": "L2-resident operands (8 MB blocks); see profiles/",
+            "peak_kind": "measured in this run (FP64 FMA loop on all SMs; MEASURED_PEAKS.json has no FP64 figure)",
+            "kernel": "k_csr_spmm + k_csr_spmm_long (one gradient product: a factor of the run, %d entries on "
+                      "average, rows up to %d, x a 1024^2 FP64 block)" % (nnz, longest),
+            "algorithmic_flops_per_launch": int(flops), "us_per_launch": round(us, 3),
+            "timing": "CUDA events, %d back-to-back products of each of the 10 factors" % calls}
+    for G in singles:
+        G.close()
+    # --- power iteration on the run's chain S_1 ... S_9 (one CTA)
+    G = fg.Faust(run_factors[1:], ctx=ctx)
     out, flag = ctypes.c_double(), ctypes.c_int()
 
     def norm():
-        _ffi.check(_ffi.lib().fgb_faust_spectral_norm(G.handle, 100, 0.0, ctypes.byref(out), ctypes.byref(flag)),
-                   ctx.handle)
+        _ffi.check(_ffi.lib().fgb_faust_spectral_norm(G.handle, 100, PALM_THR, ctypes.byref(out),
+                                                      ctypes.byref(flag)), ctx.handle)
     norm()
-    reps = 3
+    reps = 5
     s.record(stream)
     for _ in range(reps):
         norm()
@@ -580,53 +637,51 @@ def palm_roofline(ctx, hbm, peak_kind):
     pi_us = s.elapsed_time(e) * 1e3 / reps
     G.close()
     its = 100 if flag.value < 0 else max(1, flag.value)
-    # per iteration: F F^H x over 18 products (2 flops per entry) and two
+    # per iteration: F F^H x over 2 x 9 products (2 flops per entry) and two
     # length-n dot products
-    pi_flops = its * (18 * 2.0 * S.nnz + 4.0 * PALM_N)
+    chain_nnz = float(sum(f.nnz for f in run_factors[1:]))
+    pi_flops = its * (2 * 2.0 * chain_nnz + 4.0 * PALM_N)
+    achieved = pi_flops / (pi_us * 1e-6) / 1e12
     sm_peak = peak / sm_count
-    pi = {"bound": "fp64", "achieved": round(pi_flops / (pi_us * 1e-6) / 1e12, 5), "peak": round(sm_peak, 5),
-          "unit": "TFLOP/s", "frac": round(pi_flops / (pi_us * 1e-6) / 1e12 / sm_peak, 4), "traffic": None,
-          "peak_kind": "one SM's share of the FP64 FMA peak measured in this run",
-          "kernel": "k_power_iteration (one CTA per chain; 9-factor chain, %d iterations)" % its,
+    pi = {"bound": "fp64", "achieved": round(achieved, 5), "peak": round(peak, 4), "unit": "TFLOP/s",
+          "frac": round(achieved / peak, 5), "peak_one_sm": round(sm_peak, 5),
+          "frac_of_one_sm": round(achieved / sm_peak, 4), "traffic": None,
+          "peak_kind": "the device FP64 FMA rate measured in this run; frac_of_one_sm against one SM's share "
+                       "(the kernel is one CTA per chain)",
+          "kernel": "k_power_iteration (the run's chain S_1..S_9, %d entries, %d iterations to tol 1e-8)"
+                    % (chain_nnz, its),
           "algorithmic_flops_per_launch": int(pi_flops), "us_per_launch": round(pi_us, 1)}
-    return pi, spmm
+    return spmm, pi
 
 
-def cpu_baseline_palm(its=5):
-    """The oracle's palm4msa2 on all host cores, and on one core (the
-    reference's default CPU build is single-threaded), over the first `its`
-    iterations scaled to the full run."""
+def cpu_baseline_palm(single_core=False):
+    """The oracle's palm4msa2 over the whole 200-iteration run on all host
+    cores (and, with single_core, the whole run again on one core: the
+    reference's default CPU build is single-threaded)."""
     from oracle import oracle as O
     H, cons, params = _palm_problem()
     threads = os.cpu_count() or 1
-    times = {}
-    for th in (threads, 1):
+    runs = [(threads, "all host threads")] + ([(1, "one thread")] if single_core else [])
+    out = None
+    for th, what in runs:
         O.set_threads(th)
         t0 = time.perf_counter()
-        O.palm4msa2(H, [c.oracle_dict() for c in cons], its, norm2_threshold=PALM_THR, norm2_max_iter=100)
-        times[th] = time.perf_counter() - t0
+        O.palm4msa2(H, [c.oracle_dict() for c in cons], _palm_its, norm2_threshold=PALM_THR, norm2_max_iter=100)
+        dt = time.perf_counter() - t0
+        rec = {"value": round(dt, 3), "unit": "s", "cores": th, "kind": "port",
+               "sample": "the whole %d-iteration run once on %s" % (_palm_its, what)}
+        if out is None:
+            out = rec
+        else:
+            out["single_core"] = rec
     O.set_threads(threads)
-    dt, d1 = times[threads], times[1]
-    return {"value": round(dt * PALM_ITS / its, 3), "unit": "s", "cores": threads, "kind": "port",
-            "sample": "%d of %d iterations timed (%.2f s), scaled to the full run" % (its, PALM_ITS, dt),
-            "single_core": {"value": round(d1 * PALM_ITS / its, 3), "unit": "s", "cores": 1,
-                            "sample": "the same %d iterations on one thread (%.2f s), scaled" % (its, d1)}}
+    return out
 
 
 # ---------------------------------------------------------------- batched PALM4MSA
 def batched_problem(rng, count=512):
-    """count instances, n = round16(exp(U[ln 64, ln 512])), target = P1 P2 P3 +
-    1e-3 N(0,1) with each Pi n x n with 4 distinct random columns per row,
-    N(0,1) values; FP32."""
     from faust_gb300 import synth
-    ns = (np.round(np.exp(rng.uniform(np.log(64), np.log(512), size=count)) / 16) * 16).astype(int)
-    ns = np.clip(ns, 64, 512)
-    mats = []
-    for n in ns:
-        P = [synth.random_csr(int(n), int(n), 4, rng, np.float64) for _ in range(3)]
-        A = (P[0] @ (P[1] @ P[2].toarray())) + 1e-3 * rng.standard_normal((n, n))
-        mats.append(np.asarray(A, np.float32))
-    return ns, mats
+    return synth.batched_palm_targets(rng, count)
 
 
 def run_batched(args, rank, world):
@@ -827,6 +882,8 @@ def main():
     ap.add_argument("--ws-test", type=int, default=1024)
     ap.add_argument("--ws-epochs", type=int, default=20)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-single-core", action="store_true",
+                    help="palm: also time the CPU baseline's whole run on one core (about 75 s)")
     ap.add_argument("--palm-its", type=int, default=PALM_ITS,
                     help="iterations of the PALM workload (profiling captures only; the bench uses 200)")
     args = ap.parse_args()
@@ -861,20 +918,51 @@ def main():
         dist.destroy_process_group()
 
 
+def reference_arm_palm(args, world):
+    """The oracle's palm4msa2 (CPU restatement of the reference, all host
+    threads) on the PALM workload.  The K timed steps walk through ONE whole
+    run: step i runs iterations [i*m, (i+1)*m) with m = ceil(200 / K),
+    starting from the factors and lambda step i-1 ended with (the first step
+    from the identity initialisation), so every iteration of the run is timed
+    once; the value is the total time scaled to 200 iterations (exactly the
+    run's time when K divides 200).  The W warm-up steps run the first m
+    iterations untimed."""
+    from oracle import oracle as O
+    H, cons, params = _palm_problem()
+    threads = os.cpu_count() or 1
+    O.set_threads(threads)
+    ocons = [c.oracle_dict() for c in cons]
+    K = max(1, args.steps)
+    m = -(-_palm_its // K)
+    for _ in range(args.warmup):
+        O.palm4msa2(H, ocons, m, norm2_threshold=PALM_THR, norm2_max_iter=100)
+    facts, lam = None, 1.0
+    total = 0.0
+    for _ in range(K):
+        t0 = time.perf_counter()
+        facts, lam, _tr = O.palm4msa2(H, ocons, m, norm2_threshold=PALM_THR, norm2_max_iter=100,
+                                      init_facts=facts, init_lambda=lam)
+        total += time.perf_counter() - t0
+    its = K * m
+    v = round(total * _palm_its / its, 3)
+    rel = O.rel_err(H, facts, lam)
+    return {"impl": "reference", "metric": METRIC, "value": v, "unit": "s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(total / K * 1e3, 1),
+            "higher_is_better": False,
+            "config": {"workload": "palm4msa2 Hadamard 1024/32, 10 factors sp k=2048, identity init, 200 its, "
+                                   "power-iteration tol 1e-8 (max 100), FP64",
+                       "rel_err": rel, "lambda": lam},
+            "cpu_baseline": {"value": v, "unit": "s", "cores": threads, "kind": "port",
+                             "sample": "one whole run: %d steps of %d consecutive iterations (%d timed), each "
+                                       "resuming from the previous step's factors" % (K, m, its)},
+            "e2e": {"value": v, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
 def reference_arm(args, world):
     import faust_gb300.synth  # noqa: F401  (generators only)
     rng = np.random.default_rng(2024)
     if args.workload == "palm":
-        vals = [cpu_baseline_palm(its=3) for _ in range(max(1, args.steps))]
-        v = float(np.median([x["value"] for x in vals]))
-        cb = dict(vals[0])
-        cb["value"] = v
-        return {"impl": "reference", "metric": METRIC, "value": v, "unit": "s", "n_gpus": world,
-                "steps": args.steps, "warmup": args.warmup, "higher_is_better": False,
-                "config": {"workload": "palm4msa2 Hadamard 1024/32, 10 factors sp k=2048, identity init, 200 its, "
-                                       "power-iteration tol 1e-8 (max 100), FP64"},
-                "cpu_baseline": cb,
-                "e2e": {"value": v, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        return reference_arm_palm(args, world)
 
     if args.workload == "product":
         facs = _product_faust(rng)
@@ -887,12 +975,45 @@ def reference_arm(args, world):
                 "config": {"workload": "product"}, "cpu_baseline": cb,
                 "e2e": {"value": v, "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
+    if args.workload == "warmstart":
+        return {"impl": "reference", "unavailable": "the learned warm start has no reference counterpart; "
+                "its line times plain palm4msa2 initialisation beside it"}
+
+    if args.workload == "batched":
+        ns, mats = batched_problem(np.random.default_rng(4), args.batch_count)
+        vals = [cpu_baseline_batched(ns, mats) for _ in range(max(1, args.steps))]
+        v = float(np.median([x["value"] for x in vals]))
+        cb = dict(vals[0])
+        cb["value"] = v
+        return {"impl": "reference", "metric": METRIC, "value": v, "unit": "instances/s", "n_gpus": world,
+                "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
+                "config": {"workload": "batched"}, "cpu_baseline": cb,
+                "e2e": {"value": v, "unit": "instances/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
     class _W:
         pass
 
     from faust_gb300 import synth
     W = _W()
     W.name = args.workload
+    if W.name == "bsr":
+        import types
+        W.n, W.ncols = 16384, 4096
+        sigma = 1.0 / np.sqrt(8 * 64)
+        W.bsr_f32 = []
+        for _ in range(4):
+            bp, bc, blocks = synth.random_bsr(16384, 64, 8, rng, sigma)
+            W.bsr_f32.append((bp, bc, synth.bf16_to_f32(synth.bf16_bits(blocks)).reshape(blocks.shape)))
+        W.bsr = [types.SimpleNamespace(nnz_blocks=len(bc)) for _, bc, _ in W.bsr_f32]
+        W.factor_bytes = lambda: [len(bc) * 64 * 64 * 2 + len(bc) * 4 + len(bp) * 4 for bp, bc, _ in W.bsr_f32]
+        vals = [cpu_baseline_faust_x(W) for _ in range(max(1, args.steps))]
+        v = float(np.median([x["value"] for x in vals]))
+        cb = dict(vals[0])
+        cb["value"] = v
+        return {"impl": "reference", "metric": METRIC, "value": v, "unit": "GB/s", "n_gpus": world,
+                "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
+                "config": {"workload": "bsr"}, "cpu_baseline": cb,
+                "e2e": {"value": v, "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     if W.name == "csr_butterfly":
         W.facs = synth.butterfly_faust_factors(12, rng, np.float32)
         W.n, W.ncols, W.np_dtype = 4096, 8192, np.float32

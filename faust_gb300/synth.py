@@ -90,3 +90,26 @@ def random_bsr(n, bs, blocks_per_row, rng, sigma):
     browptr = np.arange(0, nb * k + 1, k, dtype=np.int32)
     blocks = (rng.standard_normal((nb * k, bs, bs)) * sigma).astype(np.float32)
     return browptr, bcol.ravel().astype(np.int32), blocks
+
+
+def batched_palm_targets(rng, count=512):
+    """Targets of the batched palm4msa2 workload: `count` instances of size
+    n = round16(exp(U[ln 64, ln 512])), each P1 P2 P3 + 1e-3 N(0,1) with every
+    Pi an n x n matrix of 4 distinct random columns per row with N(0,1)
+    values; FP32.  Returns (sizes, matrices)."""
+    ns = (np.round(np.exp(rng.uniform(np.log(64), np.log(512), size=count)) / 16) * 16).astype(int)
+    ns = np.clip(ns, 64, 512)
+    mats = []
+    for n in ns:
+        P = [random_csr(int(n), int(n), 4, rng, np.float64) for _ in range(3)]
+        A = (P[0] @ (P[1] @ P[2].toarray())) + 1e-3 * rng.standard_normal((n, n))
+        mats.append(np.asarray(A, np.float32))
+    return ns, mats
+
+
+def gaussian_kernel(npts, sigma, rng, dim=3):
+    """K_ij = exp(-||x_i - x_j||^2 / (2 sigma^2)) over npts points uniform in
+    [0, 1]^dim, FP32."""
+    x = rng.random((npts, dim))
+    d2 = ((x[:, None, :] - x[None, :, :]) ** 2).sum(-1)
+    return np.exp(-d2 / (2.0 * sigma * sigma)).astype(np.float32)

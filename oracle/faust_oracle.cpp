@@ -623,7 +623,32 @@ struct PalmTrace {
   std::vector<double> c_values; // step constant c per factor update
   std::vector<int> norm_iters;  // power-iteration counts (R then L) per update
   std::vector<int> topk_case;   // per global top-k: 0 unique, 1 prefix rule, 2 heap order decides
+  // per factor update: support fingerprint of the projected factor (see
+  // support_hash) and its number of non-zeros
+  std::vector<unsigned long long> supp_hash;
+  std::vector<long long> supp_nnz;
 };
+
+// Order-independent fingerprint of a support: the wrapping sum of splitmix64
+// of the column-major linear indices of the non-zero entries.  Two factors
+// have equal fingerprints when their supports are equal (up to hash
+// collisions), whatever order the entries are visited in.
+static inline unsigned long long splitmix64(unsigned long long z) {
+  z += 0x9E3779B97F4A7C15ULL;
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+  return z ^ (z >> 31);
+}
+template <typename T>
+static void support_hash(const Dense<T>& D, unsigned long long& h, long long& nnz) {
+  h = 0;
+  nnz = 0;
+  for (size_t i = 0; i < D.a.size(); ++i)
+    if (D.a[i] != T(0)) {
+      h += splitmix64((unsigned long long)i);
+      ++nnz;
+    }
+}
 
 // Classifies a global top-k selection: with t the k-th largest magnitude,
 // G = #{|v| > t}, E = #{|v| == t}: case 0 when G + E == k (unique set);
@@ -751,6 +776,13 @@ static void palm4msa2(const Dense<T>& A, const std::vector<Cons<T>>& cons, std::
         trace->topk_case.push_back(topk_case(v, C[f].k));
       }
       project(C[f], D);
+      if (trace) {
+        unsigned long long h;
+        long long nz;
+        support_hash(D, h, nz);
+        trace->supp_hash.push_back(h);
+        trace->supp_nnz.push_back(nz);
+      }
       S[f] = Factor<T>(dense_to_csr(D));
     }
     // update_lambda (:441-493)
@@ -964,7 +996,8 @@ template <typename T>
 static int palm_impl(const T* A, int rows, int cols, int J, const int* ikind, const long* ik, const double* s,
                      const int* flags, const int* cdims, const T* supp, const PalmParams* p, const T* init_dense,
                      double init_lambda, T* out_factors, double* out_lambda, double* out_lambdas, double* out_c,
-                     int* out_norm_iters, int* out_topk_case) {
+                     int* out_norm_iters, int* out_topk_case, unsigned long long* out_supp_hash,
+                     long long* out_supp_nnz) {
   ORC_TRY({
     Dense<T> Am(rows, cols);
     std::memcpy(Am.a.data(), A, sizeof(T) * (size_t)rows * cols);
@@ -997,9 +1030,32 @@ static int palm_impl(const T* A, int rows, int cols, int J, const int* ikind, co
       for (size_t i = 0; i < tr.norm_iters.size(); ++i) out_norm_iters[i] = tr.norm_iters[i];
     if (out_topk_case)
       for (size_t i = 0; i < tr.topk_case.size(); ++i) out_topk_case[i] = tr.topk_case[i];
+    if (out_supp_hash)
+      for (size_t i = 0; i < tr.supp_hash.size(); ++i) out_supp_hash[i] = tr.supp_hash[i];
+    if (out_supp_nnz)
+      for (size_t i = 0; i < tr.supp_nnz.size(); ++i) out_supp_nnz[i] = tr.supp_nnz[i];
   })
 }
 
+// calc_rel_err for dense factors given column-major, concatenated (FPP
+// arithmetic, as the reference evaluates it for its scalar type).
+template <typename T>
+static int rel_err_impl(const T* A, int rows, int cols, int J, const int* cdims, const T* factors, double lambda,
+                        double* out) {
+  ORC_TRY({
+    Dense<T> Am(rows, cols);
+    std::memcpy(Am.a.data(), A, sizeof(T) * Am.a.size());
+    std::vector<Factor<T>> S;
+    size_t off = 0;
+    for (int i = 0; i < J; ++i) {
+      Dense<T> M(cdims[2 * i], cdims[2 * i + 1]);
+      std::memcpy(M.a.data(), factors + off, sizeof(T) * M.a.size());
+      off += M.a.size();
+      S.emplace_back(dense_to_csr(M));
+    }
+    *out = rel_err(S, Am, T(lambda));
+  })
+}
 extern "C" {
 
 const char* orc_last_error() { return g_err.c_str(); }
@@ -1131,34 +1187,27 @@ int orc_canonical_dot_f32(long n, const float* a, const float* b, float* out) {
 int orc_palm4msa2_f64(const double* A, int rows, int cols, int J, const int* kind, const long* k, const double* s,
                       const int* flags, const int* cdims, const double* supp, const PalmParams* p,
                       const double* init_dense, double init_lambda, double* out_factors, double* out_lambda,
-                      double* out_lambdas, double* out_c, int* out_norm_iters, int* out_topk_case) {
+                      double* out_lambdas, double* out_c, int* out_norm_iters, int* out_topk_case,
+                      unsigned long long* out_supp_hash, long long* out_supp_nnz) {
   return palm_impl<double>(A, rows, cols, J, kind, k, s, flags, cdims, supp, p, init_dense, init_lambda, out_factors,
-                           out_lambda, out_lambdas, out_c, out_norm_iters, out_topk_case);
+                           out_lambda, out_lambdas, out_c, out_norm_iters, out_topk_case, out_supp_hash, out_supp_nnz);
 }
 int orc_palm4msa2_f32(const float* A, int rows, int cols, int J, const int* kind, const long* k, const double* s,
                       const int* flags, const int* cdims, const float* supp, const PalmParams* p,
                       const float* init_dense, double init_lambda, float* out_factors, double* out_lambda,
-                      double* out_lambdas, double* out_c, int* out_norm_iters, int* out_topk_case) {
+                      double* out_lambdas, double* out_c, int* out_norm_iters, int* out_topk_case,
+                      unsigned long long* out_supp_hash, long long* out_supp_nnz) {
   return palm_impl<float>(A, rows, cols, J, kind, k, s, flags, cdims, supp, p, init_dense, init_lambda, out_factors,
-                          out_lambda, out_lambdas, out_c, out_norm_iters, out_topk_case);
+                          out_lambda, out_lambdas, out_c, out_norm_iters, out_topk_case, out_supp_hash, out_supp_nnz);
 }
 
-// calc_rel_err for dense factors given column-major, concatenated.
 int orc_rel_err_f64(const double* A, int rows, int cols, int J, const int* cdims, const double* factors,
                     double lambda, double* out) {
-  ORC_TRY({
-    Dense<double> Am(rows, cols);
-    std::memcpy(Am.a.data(), A, sizeof(double) * Am.a.size());
-    std::vector<Factor<double>> S;
-    size_t off = 0;
-    for (int i = 0; i < J; ++i) {
-      Dense<double> M(cdims[2 * i], cdims[2 * i + 1]);
-      std::memcpy(M.a.data(), factors + off, sizeof(double) * M.a.size());
-      off += M.a.size();
-      S.emplace_back(dense_to_csr(M));
-    }
-    *out = rel_err(S, Am, lambda);
-  })
+  return rel_err_impl<double>(A, rows, cols, J, cdims, factors, lambda, out);
+}
+int orc_rel_err_f32(const float* A, int rows, int cols, int J, const int* cdims, const float* factors,
+                    double lambda, double* out) {
+  return rel_err_impl<float>(A, rows, cols, J, cdims, factors, lambda, out);
 }
 
 }  // extern "C"

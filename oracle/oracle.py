@@ -194,26 +194,43 @@ def palm4msa2(A, cons, nb_it, is_update_way_R2L=False, packing_RL=True, no_norma
     cvals = np.zeros(max(nb_it * J, 1), np.float64)
     niters = np.zeros(max(2 * nb_it * J, 1), np.int32)
     tcase = np.full(max(nb_it * J, 1), -1, np.int32)
+    shash = np.zeros(max(nb_it * J, 1), np.uint64)
+    snnz = np.zeros(max(nb_it * J, 1), np.int64)
     fn = lib().orc_palm4msa2_f64 if dtype == np.float64 else lib().orc_palm4msa2_f32
     _check(fn(_p(Af), A.shape[0], A.shape[1], J, _p(kind), _p(k), _p(s), _p(flags), _p(cdims), _p(supp),
               ctypes.byref(p), _p(init), ctypes.c_double(init_lambda), _p(out), ctypes.byref(lam), _p(lambdas),
-              _p(cvals), _p(niters), _p(tcase)))
+              _p(cvals), _p(niters), _p(tcase), _p(shash), _p(snnz)))
     facts, off = [], 0
     for c, sz in zip(cons, sizes):
         facts.append(out[off:off + sz].reshape((c["rows"], c["cols"]), order="F"))
         off += sz
     return facts, lam.value, {"lambdas": lambdas[:nb_it], "c": cvals[:nb_it * J], "norm_iters": niters,
-                               "topk_case": tcase[tcase >= 0]}
+                               "topk_case": tcase[tcase >= 0], "supp_hash": shash[:nb_it * J],
+                               "supp_nnz": snnz[:nb_it * J]}
 
 
-def rel_err(A, facts, lam):
-    Af = np.asfortranarray(A, dtype=np.float64)
+def support_hash(M):
+    """The oracle's support fingerprint of a dense matrix: the wrapping sum of
+    splitmix64 of the column-major linear indices of its non-zero entries."""
+    idx = np.flatnonzero(np.asarray(M).ravel(order="F") != 0).astype(np.uint64)
+    with np.errstate(over="ignore"):
+        z = idx + np.uint64(0x9E3779B97F4A7C15)
+        z = (z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
+        z = (z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
+        z = z ^ (z >> np.uint64(31))
+    return int(z.sum(dtype=np.uint64)), int(idx.size)
+
+
+def rel_err(A, facts, lam, dtype=np.float64):
+    """calc_rel_err (faust_palm4msa2020.hpp:35-44) evaluated in `dtype`
+    (float64 or float32), the scalar type of the factorization."""
+    Af = np.asfortranarray(A, dtype=dtype)
     cd = np.array(sum([[f.shape[0], f.shape[1]] for f in facts], []), np.int32)
-    fl = np.ascontiguousarray(np.concatenate([np.asfortranarray(f, dtype=np.float64).ravel(order="F")
+    fl = np.ascontiguousarray(np.concatenate([np.asfortranarray(f, dtype=dtype).ravel(order="F")
                                               for f in facts]))
     out = ctypes.c_double()
-    _check(lib().orc_rel_err_f64(_p(Af), A.shape[0], A.shape[1], len(facts), _p(cd), _p(fl), ctypes.c_double(lam),
-                                 ctypes.byref(out)))
+    fn = lib().orc_rel_err_f64 if np.dtype(dtype) == np.float64 else lib().orc_rel_err_f32
+    _check(fn(_p(Af), A.shape[0], A.shape[1], len(facts), _p(cd), _p(fl), ctypes.c_double(lam), ctypes.byref(out)))
     return out.value
 
 

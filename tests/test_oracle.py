@@ -383,3 +383,21 @@ def test_row_order_chunked_tree(oracle):
         vals, xs = list(S.data[p0:p1]), [x[c, 0] for c in S.indices[p0:p1]]
         assert got[i] == _row_value(vals, xs), lens[i]
         assert seq[i] == got[i], lens[i]
+
+
+def test_palm_resumed_in_segments_equals_one_run(oracle):
+    """The CPU baseline of the PALM workload times one run as consecutive
+    segments, each resuming from the factors and lambda the previous one
+    ended with: the result equals the uninterrupted run bit for bit."""
+    import numpy as np
+    from faust_gb300 import synth
+    n = 64
+    H = synth.hadamard(n) / 8.0
+    cons = [dict(kind=oracle.SP, k=2 * n, s=1.0, normalized=True, pos=False, rows=n, cols=n, supp=None)
+            for _ in range(6)]
+    f1, l1, _ = oracle.palm4msa2(H, cons, 30, norm2_threshold=1e-8)
+    facts, lam = None, 1.0
+    for _ in range(3):
+        facts, lam, _ = oracle.palm4msa2(H, cons, 10, norm2_threshold=1e-8, init_facts=facts, init_lambda=lam)
+    assert lam == l1
+    assert all(np.array_equal(a, b) for a, b in zip(f1, facts))
