@@ -43,11 +43,11 @@ struct fgb_ctx {
   cudaEvent_t ev_long_fork = nullptr, ev_long_join = nullptr;
   // Per-device launch facts of the projection kernels, kept on the context
   // (whose device is fixed): the cooperative grid of the radix select (FP32,
-  // FP64) and the dynamic shared memory already opted in for the two tie
-  // replay kernels.
+  // FP64) and the dynamic shared memory already opted in for the tie replay
+  // kernels (per kernel instance: [FP64][on-chip heap] and [FP64]).
   int rs_coop_blocks[2] = {0, 0};
-  size_t rp_replay_smem[2] = {0, 0};
-  size_t heap_replay_smem = 0;
+  size_t rp_replay_smem[2][2] = {{0, 0}, {0, 0}};
+  size_t heap_replay_smem[2] = {0, 0};
 };
 
 namespace fgb {

@@ -1507,7 +1507,7 @@ static fgb_status queue_tie_replay(fgb_ctx* ctx, ProxWork& w, const T* M, long N
                                                      reinterpret_cast<HNode*>(w.cand), w.wcount);
   FGB_LAUNCHED(ctx);
   auto kern = in_smem ? k_rp_replay<T, true> : k_rp_replay<T, false>;
-  size_t& attr_set = ctx->rp_replay_smem[in_smem];
+  size_t& attr_set = ctx->rp_replay_smem[sizeof(T) == 8][in_smem];
   if (smem > attr_set) {
     FGB_CUDA(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     attr_set = smem;
@@ -1591,7 +1591,7 @@ static fgb_status queue_sp(fgb_ctx* ctx, ProxWork& w, T* M, long N, long k, int 
     auto kern = k_heap_replay<T>;
     // the kernel also has static shared arrays: opt in whenever the dynamic
     // part approaches the default 48 KB limit (once per size, outside captures)
-    size_t& attr_set = ctx->heap_replay_smem;
+    size_t& attr_set = ctx->heap_replay_smem[sizeof(T) == 8];
     if (smem > 40 * 1024 && smem > attr_set) {
       FGB_CUDA(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
       attr_set = smem;

@@ -293,7 +293,21 @@ typedef struct fgb_palm_result {
 } fgb_palm_result;
 
 typedef struct fgb_batch_opts {
-  int ctas_per_sm;   /* resident instances per SM (0 = default 2) */
+  int ctas_per_sm;   /* resident instances per SM (0 = the tuned table's choice, else 2) */
+  /* Seeding from values already on the device (the learned warm start):
+   * when init_values is set, every instance has the same nfacts and the same
+   * SUPP constraints (same shapes and support pointers); instance i starts
+   * from factors whose entries on the supports are
+   * init_values_scale * init_values[i * values_per_instance + q], q running
+   * over the support entries factor by factor in row-major (CSR) order, and
+   * problems[i].init_facts is ignored.  DEVICE memory, dtype of the run. */
+  const void* init_values;
+  int values_per_instance;
+  double init_values_scale;
+  /* 1: each instance starts from lambda = <A, S>_F / ||S||_F^2 with S the
+   * product of its initial factors (in place of problems[i].init_lambda);
+   * the same formula and summation order as update_lambda's. */
+  int lambda_from_init;
 } fgb_batch_opts;
 
 fgb_status fgb_palm4msa2_batched(fgb_ctx* ctx, fgb_dtype dtype, int nprob, const fgb_palm_problem* problems,
