@@ -774,9 +774,13 @@ def cpu_baseline_batched(ns, mats, sample=16):
 def run_warmstart(args, rank, world):
     """Gaussian-kernel butterfly factorizations: plain palm4msa2 (200
     iterations) against MLP-predicted factors refined by palm4msa2, on
-    held-out draws.  value = wall time for the held-out set to reach plain
-    palm4msa2's 200-iteration error (median over instances) from the learned
-    start; config carries the plain time and the speed-up."""
+    held-out draws.  Every held-out matrix is judged against its OWN plain
+    200-iteration relative error.  value = wall time, for the whole held-out
+    set, of the MLP inference plus the seeded refinement (the device writes
+    the predicted values into the supports and the optimal starting lambda)
+    at the smallest iteration count where every instance is at or below its
+    own plain error (if no count reaches that, the smallest count where 99%
+    of them are, and config says so)."""
     import torch
     import faust_gb300 as fg
     from faust_gb300 import warmstart as ws
@@ -806,43 +810,57 @@ def run_warmstart(args, rank, world):
             losses.append(net.train_step(X[idx].contiguous(), Y[idx].contiguous(), lr=3e-4))
     torch.cuda.synchronize()
     t_train = time.perf_counter() - t0
+    del X, Y
     Kte, _ = ws.kernel_matrices(ntest, rng)
+    Kd = ws.to_device(Kte)
+    Xte = ws.to_inputs(torch, Kte)
     for _ in range(args.warmup):
-        r, _t = ws.run_plain(prob, Kte[:64], 5)
-    plain, t_plain = ws.run_plain(prob, Kte, 200)
-    e_plain = ws.rel_errors(plain, Kte)
-    target = float(np.median(e_plain))
+        r, _t = ws.run_plain(prob, Kd[:64], 5)
+        for x in r:
+            x.faust.close()
+        for x in ws.run_warm(prob, Kd[:64], net.predict(Xte[:64]), 5):
+            x.faust.close()
     torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    pred = net.predict(ws.to_inputs(torch, Kte)).cpu().numpy()
-    t_infer = time.perf_counter() - t0
-    sweep = {}
-    best = None
-    for its in (0, 2, 5, 10, 20, 50, 100, 200):
-        warm, t_w = ws.run_warm(prob, Kte, pred, max(its, 1) if its else 1)
-        e_w = ws.rel_errors(warm, Kte)
-        sweep[its] = {"s": round(t_w + t_infer, 4), "median_rel_err": float(np.median(e_w)),
-                      "frac_at_or_below_plain": float(np.mean(e_w <= e_plain + 1e-12))}
-        for r in warm:
+    with ClockSampler(torch.cuda.current_device()) as clk:
+        plain, t_plain = ws.run_plain(prob, Kd, 200)
+        e_plain = ws.rel_errors(plain, Kd)
+        for r in plain:
             r.faust.close()
-        if best is None and np.median(e_w) <= target:
-            best = (its, t_w + t_infer)
-    for r in plain:
-        r.faust.close()
-    value = best[1] if best else None
+        sweep = {}
+        for its in (1, 2, 5, 10, 20, 50, 100, 200):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            pred = net.predict(Xte)
+            warm = ws.run_warm(prob, Kd, pred, its)
+            t_w = time.perf_counter() - t0
+            e_w = ws.rel_errors(warm, Kd)
+            for r in warm:
+                r.faust.close()
+            ok = e_w <= e_plain
+            sweep[its] = {"s": round(t_w, 4), "frac_at_or_below_own_plain": float(np.mean(ok)),
+                          "median_rel_err": float(np.median(e_w)),
+                          "median_ratio_to_own_plain": float(np.median(e_w / e_plain))}
+    all_ok = [k for k, v in sweep.items() if v["frac_at_or_below_own_plain"] >= 1.0]
+    most_ok = [k for k, v in sweep.items() if v["frac_at_or_below_own_plain"] >= 0.99]
+    crit, its_needed = (("every instance", all_ok[0]) if all_ok else
+                        ("99% of the instances", most_ok[0]) if most_ok else (None, None))
+    value = sweep[its_needed]["s"] if its_needed else None
     out = {
-        "metric": METRIC, "submetric": "time for %d held-out kernel matrices to reach plain palm4msa2's "
-                                       "200-iteration median relative error from the learned start (s)" % ntest,
+        "metric": METRIC, "submetric": "time for %d held-out kernel matrices to reach their own plain palm4msa2 "
+                                       "200-iteration relative error from the learned start (s)" % ntest,
         "value": round(value, 4) if value else None, "unit": "s", "n_gpus": world, "steps": 1,
-        "warmup": args.warmup, "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f32+bf16",
-        "data": "synthetic Gaussian kernel matrices (256 points U[0,1]^3, sigma log-U[0.05,0.5])",
+        "warmup": args.warmup, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32+bf16", "data": "synthetic Gaussian kernel matrices (256 points U[0,1]^3, sigma log-U[0.05,0.5])",
         "config": {"workload": "warmstart: 8 butterfly supp factors of 256x256, MLP 65536-1024-1024-4096 BF16",
                    "train_instances": ntrain, "test_instances": ntest, "epochs": args.ws_epochs,
-                   "plain_200_s": round(t_plain, 4), "plain_median_rel_err": target,
-                   "speedup_vs_plain": round(t_plain / value, 3) if value else None,
-                   "iterations_needed": best[0] if best else None, "sweep": sweep,
+                   "timed": "MLP inference + seeded batched refinement (values and starting lambda set on the "
+                            "device), matrices already on the device; plain: the batched 200-iteration run",
+                   "plain_200_s": round(t_plain, 4), "plain_median_rel_err": float(np.median(e_plain)),
+                   "criterion": crit, "iterations_needed": its_needed,
+                   "speedup_vs_plain": round(t_plain / value, 3) if value else None, "sweep": sweep,
                    "data_gen_s": round(t_gen, 2), "train_s": round(t_train, 2),
                    "final_train_loss": losses[-1] if losses else None},
+        "clocks": clk.summary(),
     }
     return out
 

@@ -47,11 +47,14 @@ class PalmProblem(ctypes.Structure):
 
 
 class PalmResultC(ctypes.Structure):
-    _fields_ = [("faust", ctypes.c_void_p), ("lambda_", ctypes.c_double), ("status", ctypes.c_int)]
+    _fields_ = [("faust", ctypes.c_void_p), ("lambda_", ctypes.c_double), ("status", ctypes.c_int),
+                ("cycles", ctypes.c_longlong)]
 
 
 class BatchOpts(ctypes.Structure):
-    _fields_ = [("ctas_per_sm", ctypes.c_int)]
+    _fields_ = [("ctas_per_sm", ctypes.c_int), ("init_values", ctypes.c_void_p),
+                ("values_per_instance", ctypes.c_int), ("init_values_scale", ctypes.c_double),
+                ("lambda_from_init", ctypes.c_int)]
 
 
 class FgbError(RuntimeError):

@@ -50,6 +50,7 @@ struct Inst {
   Fac<T> f[MAXJ];
   Cons<T> c[MAXJ];
   int nnz[MAXJ];  // out: entries of each factor
+  long long cycles;  // out: SM clock cycles its CTA spent on the instance
 };
 
 template <typename T>
@@ -68,6 +69,7 @@ struct Params {
   long maxdim2;
   int ninst;
   int stage_elems;  // shared-memory staging area of a CTA, in elements of T
+  int lambda_from_init;  // start from lambda = <A, S> / ||S||^2 of the initial factors
 };
 
 // ------------------------------------------------------------------ block ops
@@ -761,6 +763,41 @@ __device__ __noinline__ bool b_dense_to_csr(const T* M, Fac<T>& f, int* cnt, int
 }
 
 // ------------------------------------------------------------------ one instance
+// S = S_0 ... S_{J-1} as a dense block: the last factor's dense image, then
+// the factors applied right to left (update_lambda's product without a
+// packed operand).  Returns the buffer holding S.
+template <typename T>
+__device__ T* b_full_product(const Fac<T>* S, int J, T* const buf[2], int acols, Stage<T>& sg) {
+  int cur = 0;
+  b_csr_to_dense(S[J - 1], buf[cur]);
+  for (int l = J - 2; l >= 0; --l) {
+    b_spmm<T>(S[l].rowptr, S[l].colind, S[l].val, S[l].rows, S[l].cols, buf[cur], S[l].cols, acols, buf[cur ^ 1],
+              E_STORE, nullptr, T(0), sg);
+    cur ^= 1;
+  }
+  return buf[cur];
+}
+
+// <A, S> and ||S||_F^2 over N entries in the canonical order (256 lanes per
+// chunk of 65536 entries, lane trees, chunk partials in order).
+template <typename T>
+__device__ void b_tr_ss(const T* A, const T* Smat, long N, T* lane, T& tr, T& ss) {
+  tr = T(0);
+  ss = T(0);
+  for (long c0 = 0; c0 < N; c0 += CR_CHUNK) {
+    const long c1 = min(N, c0 + CR_CHUNK);
+    T a = T(0), s2 = T(0);
+    for (long i = c0 + threadIdx.x; i < c1; i += CR_LANES) {
+      a = fmad(A[i], Smat[i], a);
+      s2 = fmad(Smat[i], Smat[i], s2);
+    }
+    lane[threadIdx.x] = a;
+    tr = addr(tr, bat_tree(lane));
+    lane[threadIdx.x] = s2;
+    ss = addr(ss, bat_tree(lane));
+  }
+}
+
 template <typename T, typename TN>
 __device__ void run_instance(Inst<T>& I, const Slot<T>& W, const Params& P, const TN* x0, TN* vbuf, int maxn,
                              T* lane, TN* lane_n, Stage<T> sg) {
@@ -776,6 +813,19 @@ __device__ void run_instance(Inst<T>& I, const Slot<T>& W, const Params& P, cons
   for (int i = 0; i < J; ++i) packed[i] = W.packed + (long)i * P.maxdim2;
   T* buf[2] = {W.buf0, W.buf1};
   const int arows = I.arows, acols = I.acols;
+  if (P.lambda_from_init) {
+    // lambda = <A, S> / ||S||_F^2 of the seeded factors; an empty or NaN
+    // product keeps the given lambda
+    T tr, ss;
+    b_tr_ss(I.A, b_full_product(S, J, buf, acols, sg), (long)arows * acols, lane, tr, ss);
+    if (threadIdx.x == 0) {
+      sh_c = sqrtr(ss);
+      sh_alpha = (sh_c == T(0) || isnan(tr) || isnan(sh_c)) ? lam : divr(tr, mulr(sh_c, sh_c));
+    }
+    __syncthreads();
+    lam = sh_alpha;
+    __syncthreads();
+  }
   for (int it = 0; it < P.nb_it; ++it) {
     // init_ite
     if (J >= 2) {
@@ -911,28 +961,10 @@ __device__ void run_instance(Inst<T>& I, const Slot<T>& W, const Params& P, cons
         b_dense_csrT<T>(packed[J - 1], arows, S[J - 1].rows, S[J - 1].t_rowptr, S[J - 1].t_colind, S[J - 1].t_val, S[J - 1].cols, buf[0], E_STORE, nullptr, T(0), sg);
         Smat = buf[0];
       } else {
-        int cur = 0;
-        b_csr_to_dense(S[J - 1], buf[cur]);
-        for (int l = J - 2; l >= 0; --l) {
-          b_spmm<T>(S[l].rowptr, S[l].colind, S[l].val, S[l].rows, S[l].cols, buf[cur], S[l].cols, acols, buf[cur ^ 1], E_STORE, nullptr, T(0), sg);
-          cur ^= 1;
-        }
-        Smat = buf[cur];
+        Smat = b_full_product(S, J, buf, acols, sg);
       }
-      const long N = (long)arows * acols;
-      T tr = T(0), ss = T(0);
-      for (long c0 = 0; c0 < N; c0 += CR_CHUNK) {
-        const long c1 = min(N, c0 + CR_CHUNK);
-        T a = T(0), s2 = T(0);
-        for (long i = c0 + threadIdx.x; i < c1; i += CR_LANES) {
-          a = fmad(I.A[i], Smat[i], a);
-          s2 = fmad(Smat[i], Smat[i], s2);
-        }
-        lane[threadIdx.x] = a;
-        tr = addr(tr, bat_tree(lane));
-        lane[threadIdx.x] = s2;
-        ss = addr(ss, bat_tree(lane));
-      }
+      T tr, ss;
+      b_tr_ss(I.A, Smat, (long)arows * acols, lane, tr, ss);
       if (threadIdx.x == 0) {
         sh_c = sqrtr(ss);
         sh_alpha = (sh_c == T(0) || isnan(tr) || isnan(sh_c)) ? T(0) : divr(tr, mulr(sh_c, sh_c));
@@ -983,7 +1015,26 @@ __global__ void __launch_bounds__(BT, 2) k_palm_batched(Inst<T>* insts, const in
     const int q = next;
     __syncthreads();
     if (q >= P.ninst) break;
+    const long long c0 = clock64();
     run_instance<T, TN>(insts[order[q]], W, P, x0, vbuf, maxn, lane, lane_n, sg);
+    if (threadIdx.x == 0) insts[order[q]].cycles = clock64() - c0;
+  }
+}
+
+// Writes the seeded factor values: thread (i, q) stores
+// scale * vals[i * V + q] at entry pos[q] of factor fac[q] of instance i and
+// at slot tpos[q] of that factor's transpose.
+template <typename T>
+__global__ void k_seed_values(Inst<T>* insts, int ninst, int V, const T* __restrict__ vals, double scale,
+                              const int* __restrict__ fac, const int* __restrict__ pos,
+                              const int* __restrict__ tpos) {
+  const long total = (long)ninst * V;
+  for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < total; t += (long)gridDim.x * blockDim.x) {
+    const int i = (int)(t / V), q = (int)(t % V);
+    const T v = (T)(scale * (double)vals[t]);
+    Fac<T>& F = insts[i].f[fac[q]];
+    F.val[pos[q]] = v;
+    F.t_val[tpos[q]] = v;
   }
 }
 
@@ -1078,6 +1129,58 @@ static fgb_status batched_impl(fgb_ctx* ctx, fgb_dtype dt, int nprob, const fgb_
     size_t off = 0;
   };
   std::vector<std::vector<HostCSR>> hc(nprob);
+  // Seeding from device values: every instance shares the structure of the
+  // SUPP supports (stored entries = the support, values written on the
+  // device by k_seed_values), built once from the first problem.
+  const bool seed = opts && opts->init_values;
+  std::vector<HostCSR> seed_csr;
+  std::vector<int> seed_fac, seed_pos, seed_tpos;
+  if (seed) {
+    const fgb_palm_problem& q0 = probs[0];
+    for (int i = 1; i < nprob; ++i) {
+      if (probs[i].nfacts != q0.nfacts)
+        return fail(ctx, FGB_ERR_INVALID_ARG, "seeded batch: instance %d has another factor count", i);
+      for (int f = 0; f < q0.nfacts; ++f) {
+        const fgb_constraint &a = probs[i].cons[f], &b = q0.cons[f];
+        if (a.kind != FGB_SUPP || a.supp != b.supp || a.rows != b.rows || a.cols != b.cols)
+          return fail(ctx, FGB_ERR_INVALID_ARG, "seeded batch: instance %d factor %d differs from instance 0's "
+                      "SUPP constraint", i, f);
+      }
+    }
+    seed_csr.resize(q0.nfacts);
+    for (int f = 0; f < q0.nfacts; ++f) {
+      const fgb_constraint& c = q0.cons[f];
+      if (c.kind != FGB_SUPP) return fail(ctx, FGB_ERR_INVALID_ARG, "seeded batch: SUPP constraints only");
+      HostCSR& H = seed_csr[f];
+      const T* d = (const T*)c.supp;
+      H.rp.assign(c.rows + 1, 0);
+      for (int r = 0; r < c.rows; ++r) {
+        for (int col = 0; col < c.cols; ++col)
+          if (d[(size_t)col * c.rows + r] != T(0)) {
+            H.ci.push_back(col);
+            H.vv.push_back(T(0));
+          }
+        H.rp[r + 1] = (int)H.ci.size();
+      }
+      H.trp.assign(c.cols + 1, 0);
+      H.tci.resize(H.ci.size());
+      H.tvv.assign(H.ci.size(), T(0));
+      for (int col : H.ci) H.trp[col + 1]++;
+      for (int col = 0; col < c.cols; ++col) H.trp[col + 1] += H.trp[col];
+      std::vector<int> fill(H.trp.begin(), H.trp.end() - 1);
+      for (int r = 0; r < c.rows; ++r)
+        for (int pp = H.rp[r]; pp < H.rp[r + 1]; ++pp) {
+          const int slot = fill[H.ci[pp]]++;
+          H.tci[slot] = r;
+          seed_fac.push_back(f);
+          seed_pos.push_back(pp);
+          seed_tpos.push_back(slot);
+        }
+    }
+    if ((long)seed_fac.size() != (long)opts->values_per_instance)
+      return fail(ctx, FGB_ERR_INVALID_ARG, "seeded batch: %d values per instance given, the supports hold %zu",
+                  opts->values_per_instance, seed_fac.size());
+  }
   size_t pool_bytes = 0;
   for (int i = 0; i < nprob; ++i) {
     const fgb_palm_problem& q = probs[i];
@@ -1085,6 +1188,14 @@ static fgb_status batched_impl(fgb_ctx* ctx, fgb_dtype dt, int nprob, const fgb_
     for (int f = 0; f < q.nfacts; ++f) {
       const fgb_constraint& c = q.cons[f];
       HostCSR& H = hc[i][f];
+      if (seed) {
+        H = seed_csr[f];
+        H.cap = std::max<long>(palm_factor_capacity(c), (long)H.ci.size());
+        H.off = pool_bytes;
+        pool_bytes += al(sizeof(int) * (c.rows + 1)) + al(sizeof(int) * (c.cols + 1)) + 2 * al(sizeof(int) * H.cap) +
+                      2 * al(es * H.cap);
+        continue;
+      }
       H.rp.assign(c.rows + 1, 0);
       if (q.init_facts) {
         const T* d = (const T*)q.init_facts[f];
@@ -1215,6 +1326,27 @@ static fgb_status batched_impl(fgb_ctx* ctx, fgb_dtype dt, int nprob, const fgb_
     cudaMemcpy(d_order, order.data(), sizeof(int) * nprob, cudaMemcpyHostToDevice);
     s = cuda_check(ctx, cudaMemsetAsync(d_queue, 0, sizeof(int), ctx->stream), "memset");
   }
+  if (s == FGB_OK && seed) {
+    const int V = opts->values_per_instance;
+    int* d_seed = nullptr;
+    s = alloc((void**)&d_seed, sizeof(int) * 3 * (size_t)V);
+    if (s == FGB_OK) {
+      std::vector<int> tab;
+      tab.reserve(3 * (size_t)V);
+      tab.insert(tab.end(), seed_fac.begin(), seed_fac.end());
+      tab.insert(tab.end(), seed_pos.begin(), seed_pos.end());
+      tab.insert(tab.end(), seed_tpos.begin(), seed_tpos.end());
+      s = cuda_check(ctx, cudaMemcpy(d_seed, tab.data(), sizeof(int) * tab.size(), cudaMemcpyHostToDevice), "seed");
+    }
+    if (s == FGB_OK) {
+      const long total = (long)nprob * V;
+      const int grid = (int)std::min<long>((total + 255) / 256, 8L * ctx->sm_count);
+      k_seed_values<T><<<grid, 256, 0, ctx->stream>>>(d_inst, nprob, V, (const T*)opts->init_values,
+                                                      opts->init_values_scale, d_seed, d_seed + V, d_seed + 2 * V);
+      ctx->launches.fetch_add(1);
+      s = cuda_check(ctx, cudaGetLastError(), "seed launch");
+    }
+  }
   if (s == FGB_OK) {
     Params P;
     std::memset(&P, 0, sizeof(P));
@@ -1230,6 +1362,7 @@ static fgb_status batched_impl(fgb_ctx* ctx, fgb_dtype dt, int nprob, const fgb_
     P.step_size = p->step_size;
     P.maxdim2 = md2;
     P.ninst = nprob;
+    P.lambda_from_init = opts ? opts->lambda_from_init : 0;
     const bool fp64n = sizeof(T) == 8 || p->norm2_fp64;
     // power-iteration vectors, their reduction lanes, then the staging area
     // of the block products (a share of the SM's shared memory per CTA)
@@ -1264,6 +1397,7 @@ static fgb_status batched_impl(fgb_ctx* ctx, fgb_dtype dt, int nprob, const fgb_
     for (int i = 0; i < nprob; ++i) {
       res[i].lambda = hi[i].lambda;
       res[i].status = hi[i].status;
+      res[i].cycles = hi[i].cycles;
       fgb_faust* F = new fgb_faust();
       F->ctx = ctx;
       F->dtype = dt;

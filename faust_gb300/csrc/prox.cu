@@ -1512,9 +1512,20 @@ static fgb_status queue_tie_replay(fgb_ctx* ctx, ProxWork& w, const T* M, long N
     FGB_CUDA(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     attr_set = smem;
   }
+  {
+    const cudaError_t pre = cudaGetLastError();
+    if (pre != cudaSuccess) return cuda_check(ctx, pre, "error pending before the tie replay launch");
+  }
   kern<<<1, PX_THREADS, smem, ctx->stream>>>(M, N, pos, k, wmax, nwin, w.state, w.flags,
                                              reinterpret_cast<const HNode*>(w.cand), w.wcount, gk, gi);
-  FGB_LAUNCHED(ctx);
+  {
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess)
+      return fail(ctx, FGB_ERR_CUDA, "k_rp_replay launch (FP%d, %s heap, %zu B dynamic shared memory, %zu opted "
+                  "in): %s", (int)sizeof(T) * 8, in_smem ? "on-chip" : "global", smem, attr_set,
+                  cudaGetErrorString(e));
+    ctx->launches.fetch_add(1, std::memory_order_relaxed);
+  }
   return FGB_OK;
 }
 

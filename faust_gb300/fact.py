@@ -208,12 +208,18 @@ def hierarchical(M, p, ret_lambda=True, ctx=None):
     return PalmResult(Faust._from_handle(h, ctx, dtype), lam.value)
 
 
-def palm4msa_batched(problems, params, ctx=None, ctas_per_sm=0):
+def palm4msa_batched(problems, params, ctx=None, ctas_per_sm=0, init_values=None, values_scale=1.0,
+                     lambda_from_init=False):
     """Runs many palm4msa2 instances in one persistent launch.
 
     problems: list of (M, constraints[, init_facts]) with M a column-major
     CUDA tensor (float32 or float64, all the same dtype).  params: one
     ParamsPalm4MSA for every instance (its constraints are ignored).
+    init_values: optional CUDA tensor (instances x values) of starting values
+    on the SUPP supports shared by every instance (factor by factor, row-major
+    order), multiplied by values_scale; lambda_from_init starts each instance
+    from the optimal scale <M, S> / ||S||^2 of its starting factors.
+    ctas_per_sm = 0 takes the tuned table's choice for the batch.
     Returns a list of PalmResult; an instance that failed carries .status."""
     import torch
     ctx = ctx or default_context()
@@ -240,7 +246,16 @@ def palm4msa_batched(problems, params, ctx=None, ctas_per_sm=0):
         arr[i] = _ffi.PalmProblem(rows, cols, M.data_ptr(), len(cons), ca, ip, float(params.init_lambda))
     out = (_ffi.PalmResultC * n)()
     p = params._c()
-    opts = _ffi.BatchOpts(int(ctas_per_sm))
+    if not ctas_per_sm:
+        ctas_per_sm = tuned_ctas_per_sm(max(max(p[0].shape) for p in problems), len(problems), dtype)
+    vals, nv = None, 0
+    if init_values is not None:
+        tdt = torch.float64 if dtype == np.float64 else torch.float32
+        if not (init_values.is_cuda and init_values.dtype == tdt and init_values.shape[0] == n
+                and init_values.is_contiguous()):
+            raise ValueError("init_values: a contiguous (instances x values) CUDA tensor of the run's dtype")
+        vals, nv = init_values.data_ptr(), int(init_values.shape[1])
+    opts = _ffi.BatchOpts(int(ctas_per_sm), vals, nv, float(values_scale), int(bool(lambda_from_init)))
     check(_ffi.lib().fgb_palm4msa2_batched(ctx.handle, _ffi.F64 if dtype == np.float64 else _ffi.F32, n, arr,
                                            ctypes.byref(p), ctypes.byref(opts), out), ctx.handle)
     results = []
@@ -248,8 +263,29 @@ def palm4msa_batched(problems, params, ctx=None, ctas_per_sm=0):
         F = Faust._from_handle(ctypes.c_void_p(out[i].faust), ctx, dtype)
         r = PalmResult(F, out[i].lambda_)
         r.status = out[i].status
+        r.cycles = out[i].cycles
         results.append(r)
     return results
+
+
+def tuned_ctas_per_sm(maxdim, count, dtype):
+    """Resident instances per SM for a batched launch, from the table the
+    offline sweep wrote (faust_gb300/tuning/batched_palm.json, keyed by the
+    batch's largest dimension); 2 when no entry covers the batch."""
+    import json
+    import os
+    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "tuning", "batched_palm.json")
+    try:
+        with open(path) as f:
+            table = json.load(f)
+    except OSError:
+        return 2
+    key = "f64" if np.dtype(dtype) == np.float64 else "f32"
+    best = None
+    for e in table.get(key, []):
+        if maxdim <= e["maxdim"] and (best is None or e["maxdim"] < best["maxdim"]):
+            best = e
+    return int(best["ctas_per_sm"]) if best else 2
 
 
 def prox(M, constraint, ctx=None):

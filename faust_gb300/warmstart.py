@@ -70,30 +70,35 @@ class ButterflyProblem:
 
     def factor_values(self, faust):
         """4096 support values of a palm4msa2 result (scaled to O(1))."""
-        vals = np.zeros(N_VALUES, np.float32)
-        dense = [faust.factors(i).toarray() for i in range(N_FACTORS)]
-        for q, (f, r, c) in enumerate(self.pos):
-            vals[q] = dense[f][r, c]
-        return vals * VALUE_SCALE
+        dense = np.stack([faust.factors(i).toarray() for i in range(N_FACTORS)])
+        return (dense[self.pos[:, 0], self.pos[:, 1], self.pos[:, 2]] * VALUE_SCALE).astype(np.float32)
 
     def init_factors(self, values):
-        """Dense factors on the supports from 4096 predicted values."""
-        facs = [np.zeros((N_POINTS, N_POINTS), np.float32) for _ in range(N_FACTORS)]
-        v = np.asarray(values, np.float32) / VALUE_SCALE
-        for q, (f, r, c) in enumerate(self.pos):
-            facs[f][r, c] = v[q]
-        return facs
+        """Dense factors on the supports from 4096 predicted values, as the
+        seeded batched run forms them (value / VALUE_SCALE, rounded once to
+        FP32)."""
+        facs = np.zeros((N_FACTORS, N_POINTS, N_POINTS), np.float32)
+        v = (np.asarray(values, np.float32).astype(np.float64) * (1.0 / VALUE_SCALE)).astype(np.float32)
+        facs[self.pos[:, 0], self.pos[:, 1], self.pos[:, 2]] = v
+        return list(facs)
 
 
 def _colmajor(torch, M):
     return torch.from_numpy(np.ascontiguousarray(np.asarray(M).T)).cuda().t()
 
 
+def to_device(Ks):
+    """Column-major CUDA copies of host kernel matrices."""
+    torch = _torch()
+    return [_colmajor(torch, K) for K in Ks]
+
+
 def run_plain(problem, Ks, its, ctx=None, ctas_per_sm=0):
     """Plain palm4msa2 (default zero/identity initialisation) on each K in one
-    batched launch.  Returns (results, wall seconds)."""
+    batched launch; Ks host arrays or column-major CUDA tensors.  Returns
+    (results, wall seconds of the batched call)."""
     torch = _torch()
-    mats = [_colmajor(torch, K) for K in Ks]
+    mats = [K if isinstance(K, torch.Tensor) else _colmajor(torch, K) for K in Ks]
     probs = [(M, problem.cons) for M in mats]
     torch.cuda.synchronize()
     t0 = time.perf_counter()
@@ -105,7 +110,7 @@ def rel_errors(results, Ks, ctx=None):
     torch = _torch()
     out = []
     for r, K in zip(results, Ks):
-        A = _colmajor(torch, K)
+        A = K if isinstance(K, torch.Tensor) else _colmajor(torch, K)
         e = ctypes.c_double()
         check(_ffi.lib().fgb_rel_err(r.faust.handle, A.data_ptr(), r.lambda_, ctypes.byref(e)),
               (ctx or default_context()).handle)
@@ -246,30 +251,13 @@ def to_inputs(torch, Ks):
     return torch.from_numpy(np.ascontiguousarray(Ks.reshape(len(Ks), -1))).cuda().to(torch.bfloat16)
 
 
-def warm_lambda(problem, K, facs):
-    """Optimal scale of the predicted factors: <K, S> / |S|^2 (S their product)."""
-    S = facs[0].astype(np.float64)
-    for f in facs[1:]:
-        S = S @ f
-    ss = float((S * S).sum())
-    return float((K * S).sum() / ss) if ss > 0 else 1.0
-
-
-def run_warm(problem, Ks, values, its, ctx=None, ctas_per_sm=0):
-    """palm4msa2 seeded with predicted factor values (batched).  Returns
-    (results, wall seconds of the refinement)."""
-    torch = _torch()
-    probs = []
-    lams = []
-    for K, v in zip(Ks, values):
-        facs = problem.init_factors(v)
-        lams.append(warm_lambda(problem, K, facs))
-        probs.append((_colmajor(torch, K), problem.cons, facs))
-    # instances share params except the initial lambda: one call per distinct
-    # lambda would split the batch, so the batch starts from lambda = mean and
-    # each instance's own first lambda update corrects it
-    params = problem.params(its, init_lambda=float(np.median(lams)))
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    res = fact.palm4msa_batched(probs, params, ctx=ctx, ctas_per_sm=ctas_per_sm)
-    return res, time.perf_counter() - t0
+def run_warm(problem, Ks_dev, values_dev, its, ctx=None, ctas_per_sm=0):
+    """palm4msa2 seeded with predicted factor values, all on the device: the
+    batched driver writes the values (values_dev, (instances, 4096) FP32 CUDA
+    tensor, divided by VALUE_SCALE) into the butterfly supports and starts
+    each instance from lambda = <K, S> / ||S||^2 of its seeded factors.
+    Ks_dev: column-major CUDA tensors.  Returns the results."""
+    probs = [(K, problem.cons) for K in Ks_dev]
+    return fact.palm4msa_batched(probs, problem.params(max(1, its)), ctx=ctx, ctas_per_sm=ctas_per_sm,
+                                 init_values=values_dev.contiguous(), values_scale=1.0 / VALUE_SCALE,
+                                 lambda_from_init=True)

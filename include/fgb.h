@@ -290,6 +290,7 @@ typedef struct fgb_palm_result {
   fgb_faust* faust;  /* release with fgb_faust_destroy */
   double lambda;
   int status;        /* fgb_status of this instance */
+  long long cycles;  /* batched runs: SM clock cycles its CTA spent on the instance */
 } fgb_palm_result;
 
 typedef struct fgb_batch_opts {

@@ -1056,6 +1056,31 @@ static int rel_err_impl(const T* A, int rows, int cols, int J, const int* cdims,
     *out = rel_err(S, Am, T(lambda));
   })
 }
+// Optimal scale of a Faust against A: <A, S>_F / ||S||_F^2 with S the full
+// product (update_lambda's formula, faust_palm4msa2020.hpp:441-493, without
+// the packed reuse), in FPP arithmetic; the starting lambda of a seeded
+// batched run.
+template <typename T>
+static int lambda_of_impl(const T* A, int rows, int cols, int J, const int* cdims, const T* factors, double in,
+                          double* out) {
+  ORC_TRY({
+    std::vector<Factor<T>> S;
+    size_t off = 0;
+    for (int i = 0; i < J; ++i) {
+      Dense<T> M(cdims[2 * i], cdims[2 * i + 1]);
+      std::memcpy(M.a.data(), factors + off, sizeof(T) * M.a.size());
+      off += M.a.size();
+      S.emplace_back(dense_to_csr(M));
+    }
+    Dense<T> P = chain_apply(S, 0, J - 1, csr_to_dense(S[J - 1].S));
+    T tr = cdot(A, P.a.data(), (size_t)rows * cols);
+    T nS = cnorm(P.a.data(), P.a.size());
+    T lam = T(in);
+    if (!(nS == T(0) || std::isnan(tr) || std::isnan(nS))) lam = tr / (nS * nS);
+    *out = (double)lam;
+  })
+}
+
 extern "C" {
 
 const char* orc_last_error() { return g_err.c_str(); }
@@ -1208,6 +1233,15 @@ int orc_rel_err_f64(const double* A, int rows, int cols, int J, const int* cdims
 int orc_rel_err_f32(const float* A, int rows, int cols, int J, const int* cdims, const float* factors,
                     double lambda, double* out) {
   return rel_err_impl<float>(A, rows, cols, J, cdims, factors, lambda, out);
+}
+
+int orc_lambda_of_factors_f64(const double* A, int rows, int cols, int J, const int* cdims, const double* factors,
+                              double in, double* out) {
+  return lambda_of_impl<double>(A, rows, cols, J, cdims, factors, in, out);
+}
+int orc_lambda_of_factors_f32(const float* A, int rows, int cols, int J, const int* cdims, const float* factors,
+                              double in, double* out) {
+  return lambda_of_impl<float>(A, rows, cols, J, cdims, factors, in, out);
 }
 
 }  // extern "C"

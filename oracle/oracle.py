@@ -234,6 +234,21 @@ def rel_err(A, facts, lam, dtype=np.float64):
     return out.value
 
 
+def lambda_of_factors(A, facts, lam_in=1.0):
+    """<A, S> / ||S||_F^2 with S the product of the dense factors `facts`, in
+    A's dtype (lam_in when S is zero or NaN): the starting lambda of a seeded
+    batched run."""
+    dtype = A.dtype
+    Af = np.asfortranarray(A)
+    cd = np.array(sum([[f.shape[0], f.shape[1]] for f in facts], []), np.int32)
+    fl = np.ascontiguousarray(np.concatenate([np.asfortranarray(f, dtype=dtype).ravel(order="F") for f in facts]))
+    out = ctypes.c_double()
+    fn = lib().orc_lambda_of_factors_f64 if dtype == np.float64 else lib().orc_lambda_of_factors_f32
+    _check(fn(_p(Af), A.shape[0], A.shape[1], len(facts), _p(cd), _p(fl), ctypes.c_double(lam_in),
+              ctypes.byref(out)))
+    return out.value
+
+
 def hierarchical(A, fac_cons, res_cons, its_2facts, its_global, is_fact_side_left=False, is_update_way_R2L=False,
                  **palm_kw):
     """Faust::hierarchical, 2020 version (src/algorithm/factorization/

@@ -111,10 +111,13 @@ def test_learned_warm_start_gains_over_plain_init():
         for s in range(0, len(Ktr), 128):
             idx = perm[s:s + 128]
             net.train_step(X[idx].contiguous(), Y[idx].contiguous(), lr=3e-4)
-    pred = net.predict(ws.to_inputs(torch, Kte)).cpu().numpy()
+    pred = net.predict(ws.to_inputs(torch, Kte))
+    Kd = ws.to_device(Kte)
     its = 5
-    plain, _ = ws.run_plain(prob, Kte, its)
-    warm, _ = ws.run_warm(prob, Kte, pred, its)
-    e_plain = ws.rel_errors(plain, Kte)
-    e_warm = ws.rel_errors(warm, Kte)
+    plain, _ = ws.run_plain(prob, Kd, its)
+    warm = ws.run_warm(prob, Kd, pred, its)
+    e_plain = ws.rel_errors(plain, Kd)
+    e_warm = ws.rel_errors(warm, Kd)
+    # each held-out matrix against its own plain run
     assert np.median(e_warm) < np.median(e_plain), (np.median(e_warm), np.median(e_plain))
+    assert np.mean(e_warm < e_plain) >= 0.75, (e_warm, e_plain)

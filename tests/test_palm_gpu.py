@@ -352,3 +352,38 @@ def test_hierarchical_left_side_sp_bitexact(oracle, dtype):
     assert np.float64(res.lambda_) == np.float64(lam)
     assert all(np.array_equal(a, b) for a, b in zip(got, ref))
     res.faust.close()
+
+
+def test_palm_batched_seeded_from_device_values(oracle):
+    """Starting values given on the device (the learned warm start's path):
+    factors seeded on shared butterfly supports from a values tensor, lambda
+    started at <K, S> / ||S||^2 of the seeded factors; every instance equals
+    the oracle run from the same dense factors and lambda."""
+    import torch
+    rng = np.random.default_rng(43)
+    J, n = 6, 64
+    sups = synth.butterfly_supports(J, np.float32)
+    cons = [fact.ConstraintMat("supp", s.toarray()) for s in sups]
+    V = sum(s.nnz for s in sups)
+    Ks = [synth.gaussian_kernel(n, s, rng) for s in (0.1, 0.2, 0.3, 0.45, 0.07)]
+    vals = rng.standard_normal((len(Ks), V)).astype(np.float32)
+    scale = 0.5
+    res = fact.palm4msa_batched([(_cuda_colmajor(K), cons) for K in Ks], fact.ParamsPalm4MSA(cons, 15),
+                                init_values=torch.from_numpy(vals).cuda(), values_scale=scale,
+                                lambda_from_init=True)
+    for i, (K, r) in enumerate(zip(Ks, res)):
+        init, q = [], 0
+        for s in sups:
+            d = np.zeros((n, n), np.float32)
+            rows = np.repeat(np.arange(n), np.diff(s.indptr))
+            d[rows, s.indices] = (scale * vals[i, q:q + s.nnz].astype(np.float64)).astype(np.float32)
+            q += s.nnz
+            init.append(d)
+        lam0 = oracle.lambda_of_factors(K, init)
+        facts_o, lam_o, _ = oracle.palm4msa2(K, [c.oracle_dict() for c in cons], 15, init_facts=init,
+                                             init_lambda=lam0)
+        assert r.status == 0
+        assert r.lambda_ == lam_o, i
+        for f in range(J):
+            assert np.array_equal(r.faust.factors(f).toarray().astype(np.float32), facts_o[f]), (i, f)
+        r.faust.close()
