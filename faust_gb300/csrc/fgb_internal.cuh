@@ -41,13 +41,9 @@ struct fgb_ctx {
   // to `stream` by the two events around each product (null: run in line).
   cudaStream_t s_long = nullptr;
   cudaEvent_t ev_long_fork = nullptr, ev_long_join = nullptr;
-  // Per-device launch facts of the projection kernels, kept on the context
-  // (whose device is fixed): the cooperative grid of the radix select (FP32,
-  // FP64) and the dynamic shared memory already opted in for the tie replay
-  // kernels (per kernel instance: [FP64][on-chip heap] and [FP64]).
+  // Cooperative grid of the projection's radix select on this context's
+  // device (FP32, FP64), computed on first use.
   int rs_coop_blocks[2] = {0, 0};
-  size_t rp_replay_smem[2][2] = {{0, 0}, {0, 0}};
-  size_t heap_replay_smem[2] = {0, 0};
 };
 
 namespace fgb {

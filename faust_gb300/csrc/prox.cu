@@ -1462,6 +1462,33 @@ static fgb_status queue_normalize(fgb_ctx* ctx, ProxWork& w, T* M, long N, int* 
   return FGB_OK;
 }
 
+// Largest dynamic shared memory the tie-replay kernels are launched with on a
+// device of `optin` bytes per block (the on-chip heap variants are taken only
+// when the heap fits under these caps).
+static size_t rp_replay_cap(size_t optin) { return std::min<size_t>(optin > 24 * 1024 ? optin - 24 * 1024 : 0, 200 * 1024); }
+static size_t heap_replay_cap(size_t optin) { return std::min<size_t>(optin > 8192 ? optin - 8192 : 0, 200 * 1024); }
+
+// Opts the tie-replay kernels into their largest dynamic shared memory, once
+// per device for the whole process.  The attribute belongs to the kernel on
+// the device, not to a context: setting it per launch size from several
+// contexts could lower it under a launch another context has already sized,
+// so it is set once to the cap every launch stays under.
+static fgb_status replay_opt_in(fgb_ctx* ctx) {
+  static std::atomic<int> done[64];
+  const int dev = ctx->device;
+  if (dev >= 0 && dev < 64 && done[dev].load(std::memory_order_acquire)) return FGB_OK;
+  const int rp = (int)rp_replay_cap(ctx->smem_optin), hr = (int)heap_replay_cap(ctx->smem_optin);
+  const int stage = (int)(2 * (size_t)RP_STAGE * sizeof(HNode));
+  FGB_CUDA(ctx, cudaFuncSetAttribute(k_rp_replay<float, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, rp));
+  FGB_CUDA(ctx, cudaFuncSetAttribute(k_rp_replay<double, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, rp));
+  FGB_CUDA(ctx, cudaFuncSetAttribute(k_rp_replay<float, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, stage));
+  FGB_CUDA(ctx, cudaFuncSetAttribute(k_rp_replay<double, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, stage));
+  FGB_CUDA(ctx, cudaFuncSetAttribute(k_heap_replay<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, hr));
+  FGB_CUDA(ctx, cudaFuncSetAttribute(k_heap_replay<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, hr));
+  if (dev >= 0 && dev < 64) done[dev].store(1, std::memory_order_release);
+  return FGB_OK;
+}
+
 // Pre-filtered tie replay (k_rp_bounds, k_rp_filter, k_rp_replay); every
 // kernel returns at once unless the selection needs the heap order.
 template <typename T>
@@ -1485,7 +1512,7 @@ static fgb_status queue_tie_replay(fgb_ctx* ctx, ProxWork& w, const T* M, long N
   const long hkn = rp_key_len(k);  // key array (padded), then k + 2 positions
   const size_t stage_bytes = 2 * (size_t)RP_STAGE * sizeof(HNode);
   const size_t heap_bytes = (sizeof(unsigned long long) + sizeof(unsigned)) * (size_t)hkn;
-  const size_t cap = std::min<size_t>(ctx->smem_optin > 24 * 1024 ? ctx->smem_optin - 24 * 1024 : 0, 200 * 1024);
+  const size_t cap = rp_replay_cap(ctx->smem_optin);
   const bool in_smem = stage_bytes + heap_bytes <= cap;
   const size_t smem = stage_bytes + (in_smem ? heap_bytes : 0);
   unsigned long long* gk = nullptr;
@@ -1507,11 +1534,7 @@ static fgb_status queue_tie_replay(fgb_ctx* ctx, ProxWork& w, const T* M, long N
                                                      reinterpret_cast<HNode*>(w.cand), w.wcount);
   FGB_LAUNCHED(ctx);
   auto kern = in_smem ? k_rp_replay<T, true> : k_rp_replay<T, false>;
-  size_t& attr_set = ctx->rp_replay_smem[sizeof(T) == 8][in_smem];
-  if (smem > attr_set) {
-    FGB_CUDA(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    attr_set = smem;
-  }
+  FGB_TRY(replay_opt_in(ctx));
   {
     const cudaError_t pre = cudaGetLastError();
     if (pre != cudaSuccess) return cuda_check(ctx, pre, "error pending before the tie replay launch");
@@ -1521,9 +1544,8 @@ static fgb_status queue_tie_replay(fgb_ctx* ctx, ProxWork& w, const T* M, long N
   {
     const cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess)
-      return fail(ctx, FGB_ERR_CUDA, "k_rp_replay launch (FP%d, %s heap, %zu B dynamic shared memory, %zu opted "
-                  "in): %s", (int)sizeof(T) * 8, in_smem ? "on-chip" : "global", smem, attr_set,
-                  cudaGetErrorString(e));
+      return fail(ctx, FGB_ERR_CUDA, "k_rp_replay launch (FP%d, %s heap, %zu B dynamic shared memory): %s",
+                  (int)sizeof(T) * 8, in_smem ? "on-chip" : "global", smem, cudaGetErrorString(e));
     ctx->launches.fetch_add(1, std::memory_order_relaxed);
   }
   return FGB_OK;
@@ -1585,7 +1607,7 @@ static fgb_status queue_sp(fgb_ctx* ctx, ProxWork& w, T* M, long N, long k, int 
     // larger heaps live in the workspace
     const size_t cand_bytes = (size_t)HR_CHUNK * sizeof(HNode);
     const size_t heap_bytes = (size_t)k * sizeof(HNode);
-    const size_t cap = std::min<size_t>(ctx->smem_optin > 8192 ? ctx->smem_optin - 8192 : 0, 200 * 1024);
+    const size_t cap = heap_replay_cap(ctx->smem_optin);
     const bool use_smem = cand_bytes + heap_bytes <= cap;
     size_t smem = use_smem ? cand_bytes + heap_bytes : cand_bytes;
     HNode* gheap = nullptr;
@@ -1600,13 +1622,7 @@ static fgb_status queue_sp(fgb_ctx* ctx, ProxWork& w, T* M, long N, long k, int 
       gheap = reinterpret_cast<HNode*>(w.heap);
     }
     auto kern = k_heap_replay<T>;
-    // the kernel also has static shared arrays: opt in whenever the dynamic
-    // part approaches the default 48 KB limit (once per size, outside captures)
-    size_t& attr_set = ctx->heap_replay_smem[sizeof(T) == 8];
-    if (smem > 40 * 1024 && smem > attr_set) {
-      FGB_CUDA(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-      attr_set = smem;
-    }
+    FGB_TRY(replay_opt_in(ctx));
     kern<<<1, PX_THREADS, smem, ctx->stream>>>(M, N, pos, (int)k, w.state, w.flags, gheap, use_smem ? 1 : 0);
     FGB_LAUNCHED(ctx);
   }
