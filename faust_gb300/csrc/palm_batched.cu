@@ -9,7 +9,8 @@
 // oracle run of that instance.  Dense blocks live in a per-CTA workspace in
 // global memory (L2-resident for small n); power-iteration vectors in shared
 // memory.  Constraints: spcol, splin, splincol (k <= 64), normcol, normlin,
-// supp.  The launch is captured in a CUDA graph by the host driver.
+// supp.  CTAs per SM (1 to 3) come from the caller or from the table of the
+// offline sweep (faust_gb300/tune_batched.py).
 #include <algorithm>
 #include <cstring>
 #include <vector>
@@ -997,9 +998,12 @@ __device__ void run_instance(Inst<T>& I, const Slot<T>& W, const Params& P, cons
   }
 }
 
-template <typename T, typename TN>
-__global__ void __launch_bounds__(BT, 2) k_palm_batched(Inst<T>* insts, const int* order, int* queue, Slot<T>* slots,
-                                                     const __grid_constant__ Params P, const TN* x0, int maxn) {
+// MINB: resident CTAs per SM the register budget is cut for (2: up to 128
+// registers a thread; 3: up to 80, with some spilling) -- the tuned table
+// picks the CTAs per SM, and with it the variant.
+template <typename T, typename TN, int MINB>
+__global__ void __launch_bounds__(BT, MINB) k_palm_batched(Inst<T>* insts, const int* order, int* queue, Slot<T>* slots,
+                                                        const __grid_constant__ Params P, const TN* x0, int maxn) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   TN* vbuf = reinterpret_cast<TN*>(smem_raw);  // 3 * maxn
   TN* lane_n = vbuf + 3 * (long)maxn;
@@ -1079,7 +1083,7 @@ static fgb_status batched_impl(fgb_ctx* ctx, fgb_dtype dt, int nprob, const fgb_
   const size_t es = sizeof(T);
   const long md2 = (long)maxdim * maxdim;
   // slots (one device block for all of them)
-  int per_sm = opts && opts->ctas_per_sm > 0 ? opts->ctas_per_sm : 2;
+  int per_sm = opts && opts->ctas_per_sm > 0 ? std::min(opts->ctas_per_sm, 3) : 2;
   int nslots = std::min(nprob, per_sm * ctx->sm_count);
   std::vector<void*> allocs;
   auto alloc = [&](void** q, size_t b) -> fgb_status {
@@ -1324,11 +1328,11 @@ static fgb_status batched_impl(fgb_ctx* ctx, fgb_dtype dt, int nprob, const fgb_
     cudaMemcpy(d_inst, hi.data(), sizeof(Inst<T>) * nprob, cudaMemcpyHostToDevice);
     cudaMemcpy(d_slots, hs.data(), sizeof(Slot<T>) * nslots, cudaMemcpyHostToDevice);
     cudaMemcpy(d_order, order.data(), sizeof(int) * nprob, cudaMemcpyHostToDevice);
-    s = cuda_check(ctx, cudaMemsetAsync(d_queue, 0, sizeof(int), ctx->stream), "memset");
+    s = cuda_check(ctx, cudaGetLastError(), "batched upload");
   }
+  int* d_seed = nullptr;
+  const int V = seed ? opts->values_per_instance : 0;
   if (s == FGB_OK && seed) {
-    const int V = opts->values_per_instance;
-    int* d_seed = nullptr;
     s = alloc((void**)&d_seed, sizeof(int) * 3 * (size_t)V);
     if (s == FGB_OK) {
       std::vector<int> tab;
@@ -1337,14 +1341,6 @@ static fgb_status batched_impl(fgb_ctx* ctx, fgb_dtype dt, int nprob, const fgb_
       tab.insert(tab.end(), seed_pos.begin(), seed_pos.end());
       tab.insert(tab.end(), seed_tpos.begin(), seed_tpos.end());
       s = cuda_check(ctx, cudaMemcpy(d_seed, tab.data(), sizeof(int) * tab.size(), cudaMemcpyHostToDevice), "seed");
-    }
-    if (s == FGB_OK) {
-      const long total = (long)nprob * V;
-      const int grid = (int)std::min<long>((total + 255) / 256, 8L * ctx->sm_count);
-      k_seed_values<T><<<grid, 256, 0, ctx->stream>>>(d_inst, nprob, V, (const T*)opts->init_values,
-                                                      opts->init_values_scale, d_seed, d_seed + V, d_seed + 2 * V);
-      ctx->launches.fetch_add(1);
-      s = cuda_check(ctx, cudaGetLastError(), "seed launch");
     }
   }
   if (s == FGB_OK) {
@@ -1377,20 +1373,62 @@ static fgb_status batched_impl(fgb_ctx* ctx, fgb_dtype dt, int nprob, const fgb_
       s = fail(ctx, FGB_ERR_NOT_SUPPORTED, "batched palm4msa2: dimension %d too large for %d CTAs per SM", maxdim,
                per_sm);
     const size_t smem = vec_bytes + (size_t)P.stage_elems * es;
-    if (fp64n) {
-      auto kern = k_palm_batched<T, double>;
-      s = cuda_check(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem), "attr");
-      if (s == FGB_OK) kern<<<nslots, BT, smem, ctx->stream>>>(d_inst, d_order, d_queue, d_slots, P, ctx->x0_d, maxdim);
-    } else {
-      auto kern = k_palm_batched<T, float>;
-      s = cuda_check(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem), "attr");
-      if (s == FGB_OK) kern<<<nslots, BT, smem, ctx->stream>>>(d_inst, d_order, d_queue, d_slots, P, ctx->x0_f, maxdim);
+    const bool three = per_sm >= 3;
+    auto kern_d = three ? k_palm_batched<T, double, 3> : k_palm_batched<T, double, 2>;
+    auto kern_f = three ? k_palm_batched<T, float, 3> : k_palm_batched<T, float, 2>;
+    if (s == FGB_OK)
+      s = cuda_check(ctx, cudaFuncSetAttribute(fp64n ? (const void*)kern_d : (const void*)kern_f,
+                                               cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem), "attr");
+    // The launch sequence: queue reset, seeding (when asked), the persistent
+    // kernel, captured as one CUDA graph and launched as a unit.  It runs on
+    // the context's stream, or on a private stream when the context uses the
+    // legacy default stream (which cannot be captured; the uploads above are
+    // synchronous, so nothing of the caller's is pending).  The call reads
+    // its results back, so a stream that is being captured is refused.
+    cudaStream_t ls = ctx->stream, priv = nullptr;
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    if (s == FGB_OK && ls) s = cuda_check(ctx, cudaStreamIsCapturing(ls, &cap), "capture status");
+    if (s == FGB_OK && cap != cudaStreamCaptureStatusNone)
+      s = fail(ctx, FGB_ERR_NOT_SUPPORTED, "batched palm4msa2 reads its results back: not inside a stream capture");
+    if (s == FGB_OK && !ls) {
+      s = cuda_check(ctx, cudaStreamCreateWithFlags(&priv, cudaStreamNonBlocking), "stream");
+      ls = priv;
     }
+    auto enqueue = [&]() -> cudaError_t {
+      cudaError_t e = cudaMemsetAsync(d_queue, 0, sizeof(int), ls);
+      if (e != cudaSuccess) return e;
+      if (seed) {
+        const long total = (long)nprob * V;
+        const int grid = (int)std::min<long>((total + 255) / 256, 8L * ctx->sm_count);
+        k_seed_values<T><<<grid, 256, 0, ls>>>(d_inst, nprob, V, (const T*)opts->init_values,
+                                               opts->init_values_scale, d_seed, d_seed + V, d_seed + 2 * V);
+        e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+      }
+      if (fp64n)
+        kern_d<<<nslots, BT, smem, ls>>>(d_inst, d_order, d_queue, d_slots, P, ctx->x0_d, maxdim);
+      else
+        kern_f<<<nslots, BT, smem, ls>>>(d_inst, d_order, d_queue, d_slots, P, ctx->x0_f, maxdim);
+      return cudaGetLastError();
+    };
     if (s == FGB_OK) {
-      ctx->launches.fetch_add(1);
-      s = cuda_check(ctx, cudaGetLastError(), "batched palm launch");
+      cudaGraph_t graph = nullptr;
+      cudaGraphExec_t exec = nullptr;
+      cudaError_t e = cudaStreamBeginCapture(ls, cudaStreamCaptureModeThreadLocal);
+      if (e == cudaSuccess) {
+        const cudaError_t e1 = enqueue();
+        e = cudaStreamEndCapture(ls, &graph);
+        if (e == cudaSuccess) e = e1;
+      }
+      if (e == cudaSuccess) e = cudaGraphInstantiate(&exec, graph, 0);
+      if (e == cudaSuccess) e = cudaGraphLaunch(exec, ls);
+      if (e == cudaSuccess) e = cudaStreamSynchronize(ls);
+      if (exec) cudaGraphExecDestroy(exec);
+      if (graph) cudaGraphDestroy(graph);
+      s = cuda_check(ctx, e, "batched palm graph");
+      if (s == FGB_OK) ctx->launches.fetch_add(seed ? 2 : 1);
     }
-    if (s == FGB_OK) s = cuda_check(ctx, cudaStreamSynchronize(ctx->stream), "batched palm");
+    if (priv) cudaStreamDestroy(priv);
   }
   if (s == FGB_OK) {
     cudaMemcpy(hi.data(), d_inst, sizeof(Inst<T>) * nprob, cudaMemcpyDeviceToHost);

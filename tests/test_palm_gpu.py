@@ -387,3 +387,32 @@ def test_palm_batched_seeded_from_device_values(oracle):
         for f in range(J):
             assert np.array_equal(r.faust.factors(f).toarray().astype(np.float32), facts_o[f]), (i, f)
         r.faust.close()
+
+
+def test_palm_batched_graph_launch_on_created_stream():
+    """The batched launch (queue reset, seeding, the persistent kernel) runs as
+    one captured CUDA graph on a created stream and, through a private stream,
+    for a context on the legacy default stream; the results are the same in
+    both and for every CTAs-per-SM variant (1, 2, and 3 with the 80-register
+    kernel)."""
+    import torch
+    import faust_gb300 as fg
+    rng = np.random.default_rng(44)
+    sizes = [64, 96, 80, 128]
+    probs = []
+    for n in sizes:
+        A = _config4_instance(rng, n)
+        probs.append((_cuda_colmajor(A), [fact.ConstraintInt("splincol", n, n, 4) for _ in range(4)]))
+    params = fact.ParamsPalm4MSA(probs[0][1], 10, norm2_fp64=True)
+    ref = fact.palm4msa_batched(probs, params, ctx=fg.Context(0, stream=0), ctas_per_sm=2)
+    s = torch.cuda.Stream()
+    ctx = fg.Context(0, stream=s.cuda_stream)
+    for cps in (1, 2, 3):
+        got = fact.palm4msa_batched(probs, params, ctx=ctx, ctas_per_sm=cps)
+        for a, b in zip(ref, got):
+            assert a.lambda_ == b.lambda_ and b.status == 0 and b.cycles > 0
+            for i in range(4):
+                assert (a.faust.factors(i) != b.faust.factors(i)).nnz == 0
+            b.faust.close()
+    for a in ref:
+        a.faust.close()
