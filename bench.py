@@ -740,7 +740,8 @@ def run_batched(args, rank, world):
         "config": {"workload": "%d palm4msa2 instances, n in [64, 512] log-uniform (multiples of 16), "
                                "target P1P2P3 + 1e-3 noise, 4 factors splincol k=4, 100 iterations" % len(mats),
                    "sum_n2": int(np.sum(ns.astype(np.int64) ** 2)), "failed_instances": bad,
-                   "ctas_per_sm": args.ctas_per_sm},
+                   "ctas_per_sm": args.ctas_per_sm or fact.tuned_ctas_per_sm(int(ns.max()), len(ns), np.float32),
+                   "ctas_per_sm_from": "argument" if args.ctas_per_sm else "faust_gb300/tuning/batched_palm.json"},
         "e2e": {"value": round(len(mats) / e2e_s, 2), "unit": "instances/s",
                 "h2d_bytes_per_step": int(sum(A.nbytes for A in mats)), "d2h_bytes_per_step": int(d2h)},
         "gpu_launches": 1,
@@ -902,7 +903,8 @@ def main():
     ap.add_argument("--workload", default="palm",
                     choices=["palm", "batched", "csr_butterfly", "csr_random", "bsr", "warmstart", "product"])
     ap.add_argument("--batch-count", type=int, default=512)
-    ap.add_argument("--ctas-per-sm", type=int, default=2)
+    ap.add_argument("--ctas-per-sm", type=int, default=0,
+                    help="batched: resident instances per SM (0 = the tuned table's choice)")
     ap.add_argument("--ws-train", type=int, default=20000)
     ap.add_argument("--ws-test", type=int, default=1024)
     ap.add_argument("--ws-epochs", type=int, default=60)

@@ -285,6 +285,22 @@ __device__ __forceinline__ void bfo_stage(T (&xs)[1 << G][CT], const typename V2
   }
 }
 
+// The same with the values of the orbit's rows already in registers.
+template <typename T, int G, int CT, int B>
+__device__ __forceinline__ void bfo_apply(T (&xs)[1 << G][CT], const typename V2<T>::type (&v)[1 << G]) {
+#pragma unroll
+  for (int k = 0; k < (1 << G); ++k) {
+    if ((k >> B) & 1) continue;
+    const int k1 = k | (1 << B);
+#pragma unroll
+    for (int t = 0; t < CT; ++t) {
+      const T a = xs[k][t], c = xs[k1][t];
+      xs[k][t] = fmad(v[k].y, c, fmad(v[k].x, a, T(0)));
+      xs[k1][t] = fmad(v[k1].y, c, fmad(v[k1].x, a, T(0)));
+    }
+  }
+}
+
 template <typename T, int G, int TC, int CT, int NT, int MINB>
 __global__ void __launch_bounds__(NT, MINB)
     k_bfly_orbit(const __grid_constant__ BflyPlanO p, const T* __restrict__ X, int ldx, int ncols,
@@ -327,15 +343,39 @@ __global__ void __launch_bounds__(NT, MINB)
         row[k] = r;
       }
       T xs[R][CT];
+      if (nf <= G) {
+        // every value of the pass's factors on the orbit's rows, loaded
+        // before any arithmetic so their latencies overlap
+        T2 v[G][R];
 #pragma unroll
-      for (int k = 0; k < R; ++k) ld_piece<T, CT>(tile + (long)bfo_slot<G>(row[k]) * TC + half * CT, xs[k]);
-      for (int f = 0; f < nf; ++f) {
-        const T2* vp = reinterpret_cast<const T2*>(p.val[first + f]);
-        const int b = p.step_bit[first + f];
-        if (b == 0) bfo_stage<T, G, CT, 0>(xs, vp, row);
-        else if (b == 1) bfo_stage<T, G, CT, 1>(xs, vp, row);
-        else if (G > 3 && b == 3) bfo_stage<T, G, CT, (G > 3 ? 3 : 0)>(xs, vp, row);
-        else bfo_stage<T, G, CT, 2>(xs, vp, row);
+        for (int f = 0; f < G; ++f)
+          if (f < nf) {
+            const T2* vp = reinterpret_cast<const T2*>(p.val[first + f]);
+#pragma unroll
+            for (int k = 0; k < R; ++k) v[f][k] = __ldg(vp + row[k]);
+          }
+#pragma unroll
+        for (int k = 0; k < R; ++k) ld_piece<T, CT>(tile + (long)bfo_slot<G>(row[k]) * TC + half * CT, xs[k]);
+#pragma unroll
+        for (int f = 0; f < G; ++f) {
+          if (f >= nf) break;
+          const int b = p.step_bit[first + f];
+          if (b == 0) bfo_apply<T, G, CT, 0>(xs, v[f]);
+          else if (b == 1) bfo_apply<T, G, CT, 1>(xs, v[f]);
+          else if (G > 3 && b == 3) bfo_apply<T, G, CT, (G > 3 ? 3 : 0)>(xs, v[f]);
+          else bfo_apply<T, G, CT, 2>(xs, v[f]);
+        }
+      } else {
+#pragma unroll
+        for (int k = 0; k < R; ++k) ld_piece<T, CT>(tile + (long)bfo_slot<G>(row[k]) * TC + half * CT, xs[k]);
+        for (int f = 0; f < nf; ++f) {
+          const T2* vp = reinterpret_cast<const T2*>(p.val[first + f]);
+          const int b = p.step_bit[first + f];
+          if (b == 0) bfo_stage<T, G, CT, 0>(xs, vp, row);
+          else if (b == 1) bfo_stage<T, G, CT, 1>(xs, vp, row);
+          else if (G > 3 && b == 3) bfo_stage<T, G, CT, (G > 3 ? 3 : 0)>(xs, vp, row);
+          else bfo_stage<T, G, CT, 2>(xs, vp, row);
+        }
       }
       if (last && p.last_direct) {
 #pragma unroll
@@ -551,11 +591,8 @@ fgb_status bfly_chain(fgb_faust* F, char op, int nfac, const void* X, int ldx, i
   if (!force && tiles < ctx->sm_count) return FGB_OK;
   *ran = true;
   BflyPlanO po;
-  if (build_plan_orbit(F, op, nfac, 3, po)) {
-    if (F->dtype == FGB_F32)
-      return launch_bfly_orbit<float, 3, 4, 4, 256, 3>(F, po, (const float*)X, ldx, ncols, (float*)Y, ldy);
-    return launch_bfly_orbit<double, 3, 2, 2, 256, 2>(F, po, (const double*)X, ldx, ncols, (double*)Y, ldy);
-  }
+  if (F->dtype == FGB_F32 && build_plan_orbit(F, op, nfac, 3, po))
+    return launch_bfly_orbit<float, 3, 4, 4, 256, 2>(F, po, (const float*)X, ldx, ncols, (float*)Y, ldy);
   if (F->dtype == FGB_F32)
     return launch_bfly<float, 4>(F, op, nfac, (const float*)X, ldx, ncols, (float*)Y, ldy);
   return launch_bfly<double, 2>(F, op, nfac, (const double*)X, ldx, ncols, (double*)Y, ldy);
