@@ -717,9 +717,23 @@ def run_batched(args, rank, world):
             res = fact.palm4msa_batched(probs, params, ctx=ctx, ctas_per_sm=args.ctas_per_sm)
             times.append(time.perf_counter() - t0)
             bad = sum(1 for r in res if r.status)
+            cycles = np.array([r.cycles for r in res], np.float64)
             for r in res:
                 r.faust.close()
     step_s = _max_over_ranks(float(np.mean(times)), world)
+    # per-instance time on its CTA (SM cycles at the sampled clock): the
+    # largest instances bound the launch
+    mhz = clk.summary().get("sm_mhz") or 2070.0
+    inst_s = cycles / (mhz * 1e6)
+    by_n = {}
+    lo = 0
+    for hi in (64, 128, 256, 384, 512):
+        sel = (ns > lo) & (ns <= hi)
+        if sel.any():
+            by_n["%d-%d" % (lo + 1, hi)] = round(float(np.median(inst_s[sel])), 4)
+        lo = hi
+    per_instance = {"max_s": round(float(inst_s.max()), 4), "median_s": round(float(np.median(inst_s)), 4),
+                    "sum_over_ctas_s": round(float(inst_s.sum()), 2), "median_s_by_n_bucket": by_n}
     # end to end: host matrices in, every factor back to host memory
     t0 = time.perf_counter()
     dev2 = [torch.from_numpy(np.ascontiguousarray(A.T)).cuda().t() for A in mats]
@@ -741,7 +755,8 @@ def run_batched(args, rank, world):
                                "target P1P2P3 + 1e-3 noise, 4 factors splincol k=4, 100 iterations" % len(mats),
                    "sum_n2": int(np.sum(ns.astype(np.int64) ** 2)), "failed_instances": bad,
                    "ctas_per_sm": args.ctas_per_sm or fact.tuned_ctas_per_sm(int(ns.max()), len(ns), np.float32),
-                   "ctas_per_sm_from": "argument" if args.ctas_per_sm else "faust_gb300/tuning/batched_palm.json"},
+                   "ctas_per_sm_from": "argument" if args.ctas_per_sm else "faust_gb300/tuning/batched_palm.json",
+                   "instance_time_on_its_cta": per_instance},
         "e2e": {"value": round(len(mats) / e2e_s, 2), "unit": "instances/s",
                 "h2d_bytes_per_step": int(sum(A.nbytes for A in mats)), "d2h_bytes_per_step": int(d2h)},
         "gpu_launches": 1,
@@ -907,7 +922,7 @@ def main():
                     help="batched: resident instances per SM (0 = the tuned table's choice)")
     ap.add_argument("--ws-train", type=int, default=20000)
     ap.add_argument("--ws-test", type=int, default=1024)
-    ap.add_argument("--ws-epochs", type=int, default=60)
+    ap.add_argument("--ws-epochs", type=int, default=20)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-single-core", action="store_true",
                     help="palm: also time the CPU baseline's whole run on one core (about 75 s)")

@@ -199,7 +199,7 @@ def _oracle_bsr_chain(oracle, n, f32, X, round_bf16):
     return Y
 
 
-@pytest.mark.parametrize("n,ncols", [(512, 256), (1024, 384)])
+@pytest.mark.parametrize("n,ncols", [(512, 256), (1024, 384), (512, 512), (1024, 1536)])
 def test_bsr_chain_bf16(fgb, oracle, n, ncols):
     """BF16 blocks, FP32 accumulation; tolerance: 1e-2 relative Frobenius
     against the FP64 oracle with BF16 rounding of each intermediate product
