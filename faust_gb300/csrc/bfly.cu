@@ -590,9 +590,6 @@ fgb_status bfly_chain(fgb_faust* F, char op, int nfac, const void* X, int ldx, i
   const long tiles = (ncols + tc - 1) / tc;
   if (!force && tiles < ctx->sm_count) return FGB_OK;
   *ran = true;
-  BflyPlanO po;
-  if (F->dtype == FGB_F32 && build_plan_orbit(F, op, nfac, 3, po))
-    return launch_bfly_orbit<float, 3, 4, 4, 256, 2>(F, po, (const float*)X, ldx, ncols, (float*)Y, ldy);
   if (F->dtype == FGB_F32)
     return launch_bfly<float, 4>(F, op, nfac, (const float*)X, ldx, ncols, (float*)Y, ldy);
   return launch_bfly<double, 2>(F, op, nfac, (const double*)X, ldx, ncols, (double*)Y, ldy);

@@ -33,19 +33,17 @@ constexpr int BLK = 64;         // BSR block size
 constexpr int TM = 128;         // columns of X per MMA (M)
 constexpr int A_BYTES = TM * BLK * 2;   // 16 KB
 constexpr int B_BYTES = BLK * BLK * 2;  // 8 KB
-constexpr int TMEM_COLS_MAX = 512;
+constexpr int TMEM_COLS = 256;
 constexpr int THREADS = 192;
 
 // NS slabs of 128 columns of X per item share each block's load (NS = 2:
-// 40 KB per stage instead of 2 x 24 KB for the same work; NS = 4: 72 KB for
-// four times the work), the L2-to-SM stream that bounds the kernel; the
-// accumulators of an item take NS x 64 TMEM columns, two items' worth
-// allocated so the epilogue of one overlaps the MMAs of the next.
+// 40 KB per stage instead of 2 x 24 KB for the same work, the L2-to-SM stream
+// that bounds the kernel); the accumulators of an item take NS x 64 TMEM
+// columns.
 template <int NS>
 struct Cfg {
-  static constexpr int STAGES = NS == 4 ? 3 : NS == 2 ? 5 : 8;
+  static constexpr int STAGES = NS == 2 ? 5 : 8;
   static constexpr int STAGE_BYTES = NS * A_BYTES + B_BYTES;
-  static constexpr int TMEM_COLS = NS == 4 ? 512 : 256;
   static constexpr int ACC_BUFS = TMEM_COLS / (NS * BLK);
   static constexpr int ITEM_COLS = NS * TM;
 };
@@ -65,7 +63,6 @@ __global__ void __launch_bounds__(THREADS, 1)
              const int* __restrict__ browptr, const int* __restrict__ bcolind, int nbr, int nnzb, int stage_idx,
              int mtiles, __nv_bfloat16* __restrict__ Y, long ldy, int* __restrict__ err) {
   constexpr int STAGES = Cfg<NS>::STAGES, STAGE_BYTES = Cfg<NS>::STAGE_BYTES, ACC_BUFS = Cfg<NS>::ACC_BUFS;
-  constexpr int TMEM_COLS = Cfg<NS>::TMEM_COLS;
   constexpr int ITEM_COLS = Cfg<NS>::ITEM_COLS;
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   // stage buffers start at a 1024-byte boundary (128-byte swizzle atoms)
@@ -347,13 +344,10 @@ fgb_status launch_bsr_tc(fgb_ctx* ctx, const DevFactor& f, const __nv_bfloat16* 
   if (ncols % tc::TM || ldx % 8 || ldy % 8) return FGB_OK;
   if (((uintptr_t)X & 15) || ((uintptr_t)Y & 15)) return FGB_OK;
   // two 128-column slabs per item when the columns come in pairs of tiles
-  // four slabs per item when the columns come in quadruples of tiles
-  const int ns = ncols % (4 * tc::TM) == 0 ? 4 : ncols % (2 * tc::TM) == 0 ? 2 : 1;
-  const bool two = ns == 2;
-  const int nbr = f.rows / tc::BLK, mtiles = ncols / (ns * tc::TM);
-  const size_t stage_bytes = ns == 4 ? (size_t)tc::Cfg<4>::STAGES * tc::Cfg<4>::STAGE_BYTES
-                             : two   ? (size_t)tc::Cfg<2>::STAGES * tc::Cfg<2>::STAGE_BYTES
-                                     : (size_t)tc::Cfg<1>::STAGES * tc::Cfg<1>::STAGE_BYTES;
+  const bool two = ncols % (2 * tc::TM) == 0;
+  const int nbr = f.rows / tc::BLK, mtiles = ncols / (two ? 2 * tc::TM : tc::TM);
+  const size_t stage_bytes = two ? (size_t)tc::Cfg<2>::STAGES * tc::Cfg<2>::STAGE_BYTES
+                                 : (size_t)tc::Cfg<1>::STAGES * tc::Cfg<1>::STAGE_BYTES;
   const size_t base_smem = stage_bytes + ((sizeof(tc::Shared) + 15) & ~(size_t)15) + 1024;
   if (base_smem > ctx->smem_optin) return FGB_OK;
   const size_t idx_bytes = sizeof(int) * ((size_t)((nbr + 1 + 3) & ~3) + (size_t)f.nnz);
@@ -363,18 +357,17 @@ fgb_status launch_bsr_tc(fgb_ctx* ctx, const DevFactor& f, const __nv_bfloat16* 
   if (!blocks) return FGB_OK;
   CUtensorMap mx, mb;
   if (!tc::make_map_bf16(&mx, X, (uint64_t)f.cols, (uint64_t)ncols, (uint64_t)ldx * 2, tc::BLK, tc::TM)) return FGB_OK;
-  const int vi = ns == 4 ? 2 : two ? 1 : 0;
   if (!tc::make_map_bf16(&mb, blocks, (uint64_t)tc::BLK, (uint64_t)f.nnz * tc::BLK, tc::BLK * 2, tc::BLK, tc::BLK))
     return FGB_OK;
   if (!g_err) {
     FGB_TRY(dmalloc(ctx, (void**)&g_err, sizeof(int)));
     FGB_CUDA(ctx, cudaMemset(g_err, 0, sizeof(int)));
   }
-  auto kern = ns == 4 ? tc::k_bsr_tc<4> : two ? tc::k_bsr_tc<2> : tc::k_bsr_tc<1>;
-  static size_t attr[3] = {0, 0, 0};
-  if (smem > attr[vi]) {
+  auto kern = two ? tc::k_bsr_tc<2> : tc::k_bsr_tc<1>;
+  static size_t attr[2] = {0, 0};
+  if (smem > attr[two]) {
     FGB_CUDA(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    attr[vi] = smem;
+    attr[two] = smem;
   }
   const long items = (long)nbr * mtiles;
   const int grid = (int)std::min<long>(items, ctx->sm_count);
