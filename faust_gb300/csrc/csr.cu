@@ -76,7 +76,6 @@ __global__ void __launch_bounds__(SPMM_THREADS)
     k_csr_spmm(const int* __restrict__ rowptr, const int* __restrict__ colind, const T* __restrict__ val, int rows,
                int inner, const T* __restrict__ X, int ldx, int ncols, T* __restrict__ Y, int ldy, Epi<T> epi,
                int long_row) {
-  pdl_entry();
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T* tile = reinterpret_cast<T*>(smem_raw);
   const int j0 = blockIdx.x * TC;
@@ -186,7 +185,6 @@ template <typename T>
 __global__ void __launch_bounds__(256)
     k_csr_spmm_long(const int* __restrict__ rowptr, const int* __restrict__ colind, const T* __restrict__ val,
                     int rows, const T* __restrict__ X, int ldx, int ncols, T* __restrict__ Y, int ldy, Epi<T> epi) {
-  pdl_entry();
   __shared__ T roots[ROW_GROUPS * 32];
   __shared__ int list[256], cnt;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -213,7 +211,6 @@ __global__ void __launch_bounds__(256)
     k_dense_csrT_long(const T* __restrict__ X, int ldx, int xrows, const int* __restrict__ rowptr,
                       const int* __restrict__ colind, const T* __restrict__ val, int srows, T* __restrict__ Y, int ldy,
                       Epi<T> epi) {
-  pdl_entry();
   __shared__ T roots[ROW_GROUPS * 32];
   __shared__ int list[256], cnt;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -247,8 +244,9 @@ static fgb_status launch_spmm_tc(fgb_ctx* ctx, const int* rowptr, const int* col
   auto kern = k_csr_spmm<T, TC, STAGED>;
   if (smem > 48 * 1024) FGB_CUDA(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   dim3 grid(tiles, rblocks);
-  FGB_LAUNCH(ctx, kern, grid, SPMM_THREADS, smem, ctx->stream, rowptr, colind, val, rows, inner, X, ldx, ncols, Y, ldy, epi,
+  kern<<<grid, SPMM_THREADS, smem, ctx->stream>>>(rowptr, colind, val, rows, inner, X, ldx, ncols, Y, ldy, epi,
                                                    long_row);
+  FGB_LAUNCHED(ctx);
   return FGB_OK;
 }
 
@@ -286,7 +284,8 @@ fgb_status launch_csr_spmm(fgb_ctx* ctx, const int* rowptr, const int* colind, c
     cudaStream_t s;
     FGB_TRY(long_fork(ctx, &s));
     dim3 g((unsigned)((ncols + 31) / 32), (unsigned)std::min((rows + 255) / 256 * 4, 16));
-    FGB_LAUNCH(ctx, (k_csr_spmm_long<T>), g, 256, 0, s, rowptr, colind, val, rows, X, ldx, ncols, Y, ldy, epi);
+    k_csr_spmm_long<T><<<g, 256, 0, s>>>(rowptr, colind, val, rows, X, ldx, ncols, Y, ldy, epi);
+    FGB_LAUNCHED(ctx);
   }
   // Stage when the tile fits comfortably and there are enough tiles to fill
   // the GPU; small problems (PALM blocks) gather straight from L2.
@@ -312,7 +311,6 @@ __global__ void __launch_bounds__(SPMM_THREADS)
     k_dense_csrT(const T* __restrict__ X, int ldx, int xrows, const int* __restrict__ rowptr,
                  const int* __restrict__ colind, const T* __restrict__ val, int srows, T* __restrict__ Y, int ldy,
                  Epi<T> epi) {
-  pdl_entry();
   const int c = blockIdx.x;
   const int p0 = rowptr[c], p1 = rowptr[c + 1];
   const T s = epi.scal ? *epi.scal : T(0);
@@ -334,12 +332,14 @@ fgb_status launch_dense_csrT(fgb_ctx* ctx, const T* X, int ldx, int xrows, const
     cudaStream_t s;
     FGB_TRY(long_fork(ctx, &s));
     dim3 g((unsigned)((xrows + 31) / 32), (unsigned)std::min((srows + 255) / 256 * 4, 16));
-    FGB_LAUNCH(ctx, (k_dense_csrT_long<T>), g, 256, 0, s, X, ldx, xrows, rowptr, colind, val, srows, Y, ldy, epi);
+    k_dense_csrT_long<T><<<g, 256, 0, s>>>(X, ldx, xrows, rowptr, colind, val, srows, Y, ldy, epi);
+    FGB_LAUNCHED(ctx);
   }
   // rows of at most ROW_CHUNK entries: one block per output column
   int rblocks = std::max(1, std::min((xrows + SPMM_THREADS - 1) / SPMM_THREADS, 8));
   dim3 grid(srows, rblocks);
-  FGB_LAUNCH(ctx, (k_dense_csrT<T>), grid, SPMM_THREADS, 0, ctx->stream, X, ldx, xrows, rowptr, colind, val, srows, Y, ldy, epi);
+  k_dense_csrT<T><<<grid, SPMM_THREADS, 0, ctx->stream>>>(X, ldx, xrows, rowptr, colind, val, srows, Y, ldy, epi);
+  FGB_LAUNCHED(ctx);
   return has_long ? long_join(ctx) : FGB_OK;
 }
 
@@ -370,7 +370,6 @@ template <typename T, int TC>
 __global__ void __launch_bounds__(CHAIN_THREADS)
     k_csr_chain_fused(const ChainDesc* __restrict__ desc, int nfac, const T* __restrict__ X, int ldx, int ncols,
                       T* __restrict__ Y, int ldy, int maxdim) {
-  pdl_entry();
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T* bufA = reinterpret_cast<T*>(smem_raw);
   T* bufB = bufA + (long)maxdim * TC;
@@ -448,7 +447,8 @@ static fgb_status launch_chain_tc(fgb_ctx* ctx, const ChainDesc* d_desc, int nfa
   auto kern = k_csr_chain_fused<T, TC>;
   if (smem > 48 * 1024) FGB_CUDA(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   const int tiles = (ncols + TC - 1) / TC;
-  FGB_LAUNCH(ctx, kern, tiles, CHAIN_THREADS, smem, ctx->stream, d_desc, nfac, X, ldx, ncols, Y, ldy, maxdim);
+  kern<<<tiles, CHAIN_THREADS, smem, ctx->stream>>>(d_desc, nfac, X, ldx, ncols, Y, ldy, maxdim);
+  FGB_LAUNCHED(ctx);
   return FGB_OK;
 }
 
@@ -575,14 +575,12 @@ fgb_status csr_build_transpose(fgb_ctx* ctx, fgb_dtype dt, DevFactor& f) {
 template <typename T>
 __global__ void k_csr_to_dense(const int* __restrict__ rowptr, const int* __restrict__ colind,
                                const T* __restrict__ val, int rows, int cols, T* __restrict__ out) {
-  pdl_entry();
   const long n = (long)rows * cols;
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) out[i] = T(0);
 }
 template <typename T>
 __global__ void k_csr_scatter(const int* __restrict__ rowptr, const int* __restrict__ colind,
                               const T* __restrict__ val, int rows, T* __restrict__ out) {
-  pdl_entry();
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < rows; i += gridDim.x * blockDim.x)
     for (int p = rowptr[i]; p < rowptr[i + 1]; ++p) out[i + (long)colind[p] * rows] = val[p];
 }
@@ -590,8 +588,11 @@ __global__ void k_csr_scatter(const int* __restrict__ rowptr, const int* __restr
 template <typename T>
 fgb_status launch_csr_to_dense(fgb_ctx* ctx, const DevFactor& f, T* out) {
   const int g = 2 * ctx->sm_count;
-  FGB_LAUNCH(ctx, (k_csr_to_dense<T>), g, 256, 0, ctx->stream, f.rowptr, f.colind, (const T*)f.val, f.rows, f.cols, out);
-  FGB_LAUNCH(ctx, (k_csr_scatter<T>), std::max(1, std::min(g, (f.rows + 255) / 256)), 256, 0, ctx->stream, f.rowptr, f.colind, (const T*)f.val, f.rows, out);
+  k_csr_to_dense<T><<<g, 256, 0, ctx->stream>>>(f.rowptr, f.colind, (const T*)f.val, f.rows, f.cols, out);
+  FGB_LAUNCHED(ctx);
+  k_csr_scatter<T><<<std::max(1, std::min(g, (f.rows + 255) / 256)), 256, 0, ctx->stream>>>(
+      f.rowptr, f.colind, (const T*)f.val, f.rows, out);
+  FGB_LAUNCHED(ctx);
   return FGB_OK;
 }
 

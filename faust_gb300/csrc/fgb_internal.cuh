@@ -44,10 +44,6 @@ struct fgb_ctx {
   // Cooperative grid of the projection's radix select on this context's
   // device (FP32, FP64), computed on first use.
   int rs_coop_blocks[2] = {0, 0};
-  // Set while a palm4msa2 run queues its iterations: kernels launched through
-  // fgb::launch on the context's stream then carry programmatic stream
-  // serialisation (see pdl_entry).
-  bool pdl = false;
 };
 
 namespace fgb {
@@ -80,49 +76,6 @@ fgb_status cuda_check(fgb_ctx* ctx, cudaError_t e, const char* what);
   } while (0)
 
 size_t dtype_size(fgb_dtype t);
-
-// ---------------------------------------------------------------- programmatic dependent launch
-// Kernels of the palm4msa2 iteration are launched with programmatic stream
-// serialisation: the next kernel of the stream may be scheduled while this
-// one runs, and starts by waiting for its predecessor's completion (and
-// memory) before it touches global memory.  Every kernel that fgb::launch
-// may launch that way calls pdl_entry() first; launched normally, both
-// instructions are no-ops.
-__device__ __forceinline__ void pdl_entry() {
-  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
-  asm volatile("griddepcontrol.wait;" ::: "memory");
-}
-
-// Launches kern on `stream`, with programmatic stream serialisation when the
-// context asks for it and the stream is the context's own (side streams keep
-// their event ordering).  Returns the launch error.
-template <typename... KArgs, typename... Args>
-inline cudaError_t launch(fgb_ctx* ctx, void (*kern)(KArgs...), dim3 grid, dim3 block, size_t smem,
-                          cudaStream_t stream, Args... args) {
-  if (!(ctx->pdl && stream == ctx->stream)) {
-    kern<<<grid, block, smem, stream>>>(args...);
-    return cudaGetLastError();
-  }
-  cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = grid;
-  cfg.blockDim = block;
-  cfg.dynamicSmemBytes = smem;
-  cfg.stream = stream;
-  cudaLaunchAttribute attr[1];
-  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-  attr[0].val.programmaticStreamSerializationAllowed = 1;
-  cfg.attrs = attr;
-  cfg.numAttrs = 1;
-  return cudaLaunchKernelEx(&cfg, kern, args...);
-}
-
-// Launch through fgb::launch, counted, returning on error.
-#define FGB_LAUNCH(ctx, kern, grid, block, smem, stream, ...)                                              \
-  do {                                                                                                  \
-    (ctx)->launches.fetch_add(1, std::memory_order_relaxed);                                            \
-    cudaError_t e__ = fgb::launch(ctx, kern, grid, block, smem, stream, __VA_ARGS__);                   \
-    if (e__ != cudaSuccess) return fgb::cuda_check(ctx, e__, "kernel launch at " __FILE__ ":" FGB_STR(__LINE__)); \
-  } while (0)
 
 // Device allocation helpers (report OOM as FGB_ERR_OOM).
 fgb_status dmalloc(fgb_ctx* ctx, void** p, size_t bytes);

@@ -29,7 +29,6 @@ void free_factor(DevFactor& f);
 template <typename T>
 __global__ void k_lambda_minus(const T* __restrict__ P, const T* __restrict__ A, long N, const T* lam,
                                T* __restrict__ out) {
-  pdl_entry();
   const T l = *lam;
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < N; i += (long)gridDim.x * blockDim.x)
     out[i] = subr(mulr(l, P[i]), A[i]);
@@ -37,7 +36,6 @@ __global__ void k_lambda_minus(const T* __restrict__ P, const T* __restrict__ A,
 
 template <typename T>
 __global__ void k_d_minus(T* __restrict__ D, const T* __restrict__ G, long N, const T* alpha) {
-  pdl_entry();
   const T a = *alpha;
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < N; i += (long)gridDim.x * blockDim.x)
     D[i] = subr(D[i], mulr(a, G[i]));
@@ -47,7 +45,6 @@ __global__ void k_d_minus(T* __restrict__ D, const T* __restrict__ G, long N, co
 template <typename T>
 __global__ void __launch_bounds__(256) k_chunk_dot2(const T* __restrict__ A, const T* __restrict__ S, long N,
                                                    double* part) {
-  pdl_entry();
   __shared__ T lane[256];
   const long c0 = blockIdx.x * CR_CHUNK, c1 = min(N, c0 + CR_CHUNK);
   T a = T(0), s = T(0);
@@ -68,7 +65,6 @@ __global__ void __launch_bounds__(256) k_chunk_dot2(const T* __restrict__ A, con
 // update_lambda (faust_palm4msa2020.hpp:441-493): lambda = tr / (nS*nS).
 template <typename T>
 __global__ void k_lambda_update(const double* part, int nchunks, T* lam, int* status, int no_lambda_error) {
-  pdl_entry();
   T tr = T(0), ss = T(0);
   for (int c = 0; c < nchunks; ++c) {
     tr = addr(tr, reinterpret_cast<const T*>(part)[2 * c]);
@@ -121,7 +117,6 @@ __global__ void k_relerr_final(const double* part, int nchunks, double* out) {
 
 template <typename T>
 __global__ void k_set_scalar(T* p, double v) {
-  pdl_entry();
   *p = (T)v;
 }
 
@@ -422,7 +417,8 @@ struct Palm {
       if (hasR) {
         FGB_TRY(mul_S(Sf, packed[f], acols, buf[cur], nL == 0 ? eE : st));
       } else if (nL == 0) {
-        FGB_LAUNCH(ctx, (k_lambda_minus<T>), grid((long)arows * acols), 256, 0, ctx->stream, D, A, (long)arows * acols, lam, buf[cur]);
+        k_lambda_minus<T><<<grid((long)arows * acols), 256, 0, ctx->stream>>>(D, A, (long)arows * acols, lam, buf[cur]);
+        FGB_LAUNCHED(ctx);
       } else {
         FGB_TRY(dense_of(Sf, buf[cur]));
       }
@@ -438,7 +434,8 @@ struct Palm {
       if (hasL) {
         FGB_TRY(mul_XS(packed[f], arows, Sf, buf[cur], nR == 0 ? eE : st));
       } else if (nR == 0) {
-        FGB_LAUNCH(ctx, (k_lambda_minus<T>), grid((long)arows * acols), 256, 0, ctx->stream, D, A, (long)arows * acols, lam, buf[cur]);
+        k_lambda_minus<T><<<grid((long)arows * acols), 256, 0, ctx->stream>>>(D, A, (long)arows * acols, lam, buf[cur]);
+        FGB_LAUNCHED(ctx);
       } else {
         FGB_TRY(dense_of(Sf, buf[cur]));
       }
@@ -461,7 +458,8 @@ struct Palm {
     }
     if (ops.empty()) {
       FGB_CUDA(ctx, cudaStreamWaitEvent(ctx->stream, ev_join, 0));
-      FGB_LAUNCH(ctx, (k_d_minus<T>), grid((long)Sf.rows * Sf.cols), 256, 0, ctx->stream, D, E, (long)Sf.rows * Sf.cols, alpha);
+      k_d_minus<T><<<grid((long)Sf.rows * Sf.cols), 256, 0, ctx->stream>>>(D, E, (long)Sf.rows * Sf.cols, alpha);
+      FGB_LAUNCHED(ctx);
     } else {
       const T* src = E;
       for (size_t q = 0; q < ops.size(); ++q) {
@@ -521,8 +519,10 @@ struct Palm {
     }
     const long N = (long)arows * acols;
     const int nch = (int)((N + CR_CHUNK - 1) / CR_CHUNK);
-    FGB_LAUNCH(ctx, (k_chunk_dot2<T>), nch, 256, 0, ctx->stream, A, Smat, N, part);
-    FGB_LAUNCH(ctx, (k_lambda_update<T>), 1, 1, 0, ctx->stream, part, nch, lam, status, p.no_lambda_error);
+    k_chunk_dot2<T><<<nch, 256, 0, ctx->stream>>>(A, Smat, N, part);
+    FGB_LAUNCHED(ctx);
+    k_lambda_update<T><<<1, 1, 0, ctx->stream>>>(part, nch, lam, status, p.no_lambda_error);
+    FGB_LAUNCHED(ctx);
     return FGB_OK;
   }
 
@@ -700,9 +700,6 @@ static fgb_status palm_entry(fgb_ctx* ctx, fgb_dtype dt, const void* A_dev, int 
   FGB_CUDA(ctx, cudaStreamSynchronize(user));
   FGB_CUDA(ctx, cudaStreamCreateWithFlags(&ps, cudaStreamNonBlocking));
   ctx->stream = ps;
-  // kernels of the run overlap their launch with their predecessor's tail
-  // (programmatic dependent launch; FGB_NO_PDL turns it off for comparison)
-  ctx->pdl = getenv("FGB_NO_PDL") == nullptr;
   fgb_status s;
   {
     Palm<T> P;
@@ -717,7 +714,6 @@ static fgb_status palm_entry(fgb_ctx* ctx, fgb_dtype dt, const void* A_dev, int 
     if (s == FGB_OK && out) s = palm_to_faust(P, dt, out);
     cudaStreamSynchronize(ps);
   }
-  ctx->pdl = false;
   ctx->stream = user;
   cudaStreamDestroy(ps);
   return s;

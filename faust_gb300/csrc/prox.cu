@@ -109,7 +109,6 @@ template <typename T>
 __global__ void __launch_bounds__(PX_THREADS)
     k_radix_pass(const T* __restrict__ M, long N, int pos, int shift, int bits, TopkState* st,
                  unsigned* __restrict__ hist) {
-  pdl_entry();
   __shared__ unsigned sh[2048];
   __shared__ int is_last;
   const int nb = 1 << bits;
@@ -424,7 +423,6 @@ __global__ void __launch_bounds__(PX_THREADS)
 template <typename T>
 __global__ void __launch_bounds__(PX_THREADS)
     k_tie_case(const T* __restrict__ M, long N, int pos, long chunk, TopkState* st, long long* __restrict__ cnt) {
-  pdl_entry();
   __shared__ int is_last;
   __shared__ long long s_ge[PX_THREADS], s_gt[PX_THREADS];
   __shared__ long long c_target, c_base_gt, c_idx;
@@ -651,7 +649,6 @@ template <typename T>
 __global__ void __launch_bounds__(PX_THREADS)
     k_heap_replay(const T* __restrict__ M, long N, int pos, int k, TopkState* st, unsigned char* __restrict__ flags,
                   HNode* gheap, int use_smem) {
-  pdl_entry();
   if (st->sel_case != 2) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ int warp_tot[PX_THREADS / 32];
@@ -844,7 +841,6 @@ template <typename T>
 __global__ void __launch_bounds__(RP_BLOCK)
     k_rp_bounds(const T* __restrict__ M, long N, int pos, long k, long wmax, const TopkState* st,
                 unsigned long long* __restrict__ wb) {
-  pdl_entry();
   if (st->sel_case != 2) return;
   __shared__ unsigned hist[RP_BINS];
   __shared__ int s_bin;
@@ -888,7 +884,6 @@ template <typename T>
 __global__ void __launch_bounds__(RP_BLOCK)
     k_rp_filter(const T* __restrict__ M, long N, int pos, long k, long wmax, const TopkState* st,
                 const unsigned long long* __restrict__ wb, HNode* __restrict__ cand, int* __restrict__ wcnt) {
-  pdl_entry();
   if (st->sel_case != 2) return;
   constexpr int U = 8, NW = RP_BLOCK / 32;
   __shared__ unsigned long long s_min[NW];
@@ -1150,7 +1145,6 @@ __global__ void __launch_bounds__(PX_THREADS)
     k_rp_replay(const T* __restrict__ M, long N, int pos, long k, long wmax, int nwin, TopkState* st,
                 unsigned char* __restrict__ flags, const HNode* __restrict__ cand, const int* __restrict__ wcnt,
                 unsigned long long* gk, unsigned* gi) {
-  pdl_entry();
   if (st->sel_case != 2) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ long s_off[RP_MAXWIN + 1];
@@ -1231,7 +1225,6 @@ __global__ void __launch_bounds__(PX_THREADS)
 template <typename T>
 __global__ void k_sp_apply(T* __restrict__ M, long N, int pos, const TopkState* st, unsigned char* __restrict__ flags,
                            int* d_status) {
-  pdl_entry();
   // the selection is complete: its status goes to the caller's word
   if (d_status && blockIdx.x == 0 && threadIdx.x == 0 && st->status) atomicCAS(d_status, 0, st->status);
   const unsigned long long t = st->t;
@@ -1266,14 +1259,12 @@ __global__ void k_sp_apply(T* __restrict__ M, long N, int pos, const TopkState* 
 
 template <typename T>
 __global__ void k_pos_only(T* __restrict__ M, long N) {
-  pdl_entry();
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < N; i += (long)gridDim.x * blockDim.x)
     if (M[i] < T(0)) M[i] = T(0);
 }
 
 template <typename T>
 __global__ void k_zero(T* __restrict__ M, long N) {
-  pdl_entry();
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < N; i += (long)gridDim.x * blockDim.x) M[i] = T(0);
 }
 
@@ -1283,7 +1274,6 @@ __global__ void k_zero(T* __restrict__ M, long N) {
 template <typename T>
 __global__ void k_line_topk(const T* __restrict__ M, int rows, int cols, int by_col, int k, int pos,
                             unsigned char* __restrict__ flags, unsigned char bit) {
-  pdl_entry();
   const int nlines = by_col ? cols : rows;
   const int len = by_col ? rows : cols;
   const int line = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1313,7 +1303,6 @@ __global__ void k_line_topk(const T* __restrict__ M, int rows, int cols, int by_
 
 template <typename T>
 __global__ void k_flag_apply(T* __restrict__ M, long N, int pos, unsigned char* __restrict__ flags) {
-  pdl_entry();
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < N; i += (long)gridDim.x * blockDim.x) {
     const T v = pos_adj(M[i], pos);
     M[i] = flags[i] ? v : T(0);
@@ -1327,7 +1316,6 @@ __global__ void k_flag_apply(T* __restrict__ M, long N, int pos, unsigned char* 
 template <typename T>
 __global__ void __launch_bounds__(PX_THREADS)
     k_normline(T* __restrict__ M, int rows, int cols, int by_col, double s, int pos) {
-  pdl_entry();
   __shared__ T lane[PX_THREADS];
   const int line = blockIdx.x;
   const int len = by_col ? rows : cols;
@@ -1356,7 +1344,6 @@ __global__ void __launch_bounds__(PX_THREADS)
 
 template <typename T>
 __global__ void k_supp(T* __restrict__ M, long N, const T* __restrict__ S, int pos) {
-  pdl_entry();
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < N; i += (long)gridDim.x * blockDim.x)
     M[i] = mulr(pos_adj(M[i], pos), S[i]);
 }
@@ -1364,7 +1351,6 @@ __global__ void k_supp(T* __restrict__ M, long N, const T* __restrict__ S, int p
 // Canonical sum of squares: one block per chunk of 65536 entries.
 template <typename T>
 __global__ void __launch_bounds__(PX_THREADS) k_chunk_sumsq(const T* __restrict__ M, long N, double* partials) {
-  pdl_entry();
   __shared__ T lane[PX_THREADS];
   const long c0 = blockIdx.x * CR_CHUNK, c1 = min(N, c0 + CR_CHUNK);
   // A zero entry adds +0 to a non-negative partial, so a warp issues the
@@ -1409,7 +1395,6 @@ __global__ void __launch_bounds__(PX_THREADS) k_chunk_sumsq(const T* __restrict_
 // launch of a one-thread kernel.
 template <typename T>
 __global__ void k_scale(T* __restrict__ M, long N, const double* __restrict__ partials, int nchunks, int* status) {
-  pdl_entry();
   __shared__ T s_inv;
   if (threadIdx.x == 0) {
     T total = T(0);
@@ -1455,7 +1440,6 @@ __global__ void k_scale(T* __restrict__ M, long N, const double* __restrict__ pa
 
 
 __global__ void k_topk_init(TopkState* st, long long k) {
-  pdl_entry();
   TopkState z;
   memset(&z, 0, sizeof(z));
   z.k_rem = k;
@@ -1471,8 +1455,10 @@ static int grid_for(fgb_ctx* ctx, long n) {
 template <typename T>
 static fgb_status queue_normalize(fgb_ctx* ctx, ProxWork& w, T* M, long N, int* d_status) {
   const int nchunks = (int)((N + CR_CHUNK - 1) / CR_CHUNK);
-  FGB_LAUNCH(ctx, (k_chunk_sumsq<T>), nchunks, PX_THREADS, 0, ctx->stream, M, N, w.partials);
-  FGB_LAUNCH(ctx, (k_scale<T>), grid_for(ctx, N), PX_THREADS, 0, ctx->stream, M, N, w.partials, nchunks, d_status);
+  k_chunk_sumsq<T><<<nchunks, PX_THREADS, 0, ctx->stream>>>(M, N, w.partials);
+  FGB_LAUNCHED(ctx);
+  k_scale<T><<<grid_for(ctx, N), PX_THREADS, 0, ctx->stream>>>(M, N, w.partials, nchunks, d_status);
+  FGB_LAUNCHED(ctx);
   return FGB_OK;
 }
 
@@ -1542,9 +1528,11 @@ static fgb_status queue_tie_replay(fgb_ctx* ctx, ProxWork& w, const T* M, long N
     gk = reinterpret_cast<unsigned long long*>(w.heap2);
     gi = reinterpret_cast<unsigned*>(gk + hkn);
   }
-  FGB_LAUNCH(ctx, (k_rp_bounds<T>), nwin, RP_BLOCK, 0, ctx->stream, M, N, pos, k, wmax, w.state, w.wbound);
-  FGB_LAUNCH(ctx, (k_rp_filter<T>), nwin, RP_BLOCK, 0, ctx->stream, M, N, pos, k, wmax, w.state, w.wbound,
+  k_rp_bounds<T><<<nwin, RP_BLOCK, 0, ctx->stream>>>(M, N, pos, k, wmax, w.state, w.wbound);
+  FGB_LAUNCHED(ctx);
+  k_rp_filter<T><<<nwin, RP_BLOCK, 0, ctx->stream>>>(M, N, pos, k, wmax, w.state, w.wbound,
                                                      reinterpret_cast<HNode*>(w.cand), w.wcount);
+  FGB_LAUNCHED(ctx);
   auto kern = in_smem ? k_rp_replay<T, true> : k_rp_replay<T, false>;
   FGB_TRY(replay_opt_in(ctx));
   {
@@ -1567,7 +1555,8 @@ template <typename T>
 static fgb_status queue_sp(fgb_ctx* ctx, ProxWork& w, T* M, long N, long k, int pos, int* d_status) {
   const int g = grid_for(ctx, N);
   if (!w.hist_passes) {
-    FGB_LAUNCH(ctx, k_topk_init, 1, 1, 0, ctx->stream, w.state, k);
+    k_topk_init<<<1, 1, 0, ctx->stream>>>(w.state, k);
+    FGB_LAUNCHED(ctx);
   }
   if (w.hist_passes) {
     // every pass in one cooperative launch (blocks co-resident for the barrier)
@@ -1596,18 +1585,21 @@ static fgb_status queue_sp(fgb_ctx* ctx, ProxWork& w, T* M, long N, long k, int 
     const int shifts[6] = {52, 41, 30, 19, 8, 0};
     const int bits[6] = {11, 11, 11, 11, 11, 8};
     for (int p = 0; p < 6; ++p) {
-      FGB_LAUNCH(ctx, (k_radix_pass<T>), g, PX_THREADS, 0, ctx->stream, M, N, pos, shifts[p], bits[p], w.state, w.hist);
+      k_radix_pass<T><<<g, PX_THREADS, 0, ctx->stream>>>(M, N, pos, shifts[p], bits[p], w.state, w.hist);
+      FGB_LAUNCHED(ctx);
     }
   } else {
     const int shifts[3] = {20, 9, 0};
     const int bits[3] = {11, 11, 9};
     for (int p = 0; p < 3; ++p) {
-      FGB_LAUNCH(ctx, (k_radix_pass<T>), g, PX_THREADS, 0, ctx->stream, M, N, pos, shifts[p], bits[p], w.state, w.hist);
+      k_radix_pass<T><<<g, PX_THREADS, 0, ctx->stream>>>(M, N, pos, shifts[p], bits[p], w.state, w.hist);
+      FGB_LAUNCHED(ctx);
     }
   }
   const long chunk = std::max(8192L, (N + 2047) / 2048);
   const int nch = (int)((N + chunk - 1) / chunk);
-  FGB_LAUNCH(ctx, (k_tie_case<T>), nch, PX_THREADS, 0, ctx->stream, M, N, pos, chunk, w.state, w.chunk_cnt);
+  k_tie_case<T><<<nch, PX_THREADS, 0, ctx->stream>>>(M, N, pos, chunk, w.state, w.chunk_cnt);
+  FGB_LAUNCHED(ctx);
   if (w.growable && N < (1L << 32) - 1) {
     FGB_TRY(queue_tie_replay<T>(ctx, w, M, N, k, pos));
   } else {
@@ -1631,9 +1623,11 @@ static fgb_status queue_sp(fgb_ctx* ctx, ProxWork& w, T* M, long N, long k, int 
     }
     auto kern = k_heap_replay<T>;
     FGB_TRY(replay_opt_in(ctx));
-    FGB_LAUNCH(ctx, kern, 1, PX_THREADS, smem, ctx->stream, M, N, pos, (int)k, w.state, w.flags, gheap, use_smem ? 1 : 0);
+    kern<<<1, PX_THREADS, smem, ctx->stream>>>(M, N, pos, (int)k, w.state, w.flags, gheap, use_smem ? 1 : 0);
+    FGB_LAUNCHED(ctx);
   }
-  FGB_LAUNCH(ctx, (k_sp_apply<T>), g, PX_THREADS, 0, ctx->stream, M, N, pos, w.state, w.flags, d_status);
+  k_sp_apply<T><<<g, PX_THREADS, 0, ctx->stream>>>(M, N, pos, w.state, w.flags, d_status);
+  FGB_LAUNCHED(ctx);
   return FGB_OK;
 }
 
@@ -1651,11 +1645,13 @@ fgb_status launch_prox(fgb_ctx* ctx, ProxWork& w, const fgb_constraint& c, T* M,
     case FGB_SP: {
       // prox_sp (faust_prox.hpp:71-96)
       if (c.k <= 0) {
-        FGB_LAUNCH(ctx, (k_zero<T>), g, PX_THREADS, 0, ctx->stream, M, N);
+        k_zero<T><<<g, PX_THREADS, 0, ctx->stream>>>(M, N);
+        FGB_LAUNCHED(ctx);
       } else if (c.k < N) {
         FGB_TRY(queue_sp<T>(ctx, w, M, N, (long)c.k, pos, d_status));
       } else if (pos) {
-        FGB_LAUNCH(ctx, (k_pos_only<T>), g, PX_THREADS, 0, ctx->stream, M, N);
+        k_pos_only<T><<<g, PX_THREADS, 0, ctx->stream>>>(M, N);
+        FGB_LAUNCHED(ctx);
       }
       break;
     }
@@ -1666,7 +1662,8 @@ fgb_status launch_prox(fgb_ctx* ctx, ProxWork& w, const fgb_constraint& c, T* M,
       // splincol ignores pos, as the reference applies it after copying.
       if (c.kind == FGB_SPLINCOL) pos = 0;
       if (c.k <= 0) {
-        FGB_LAUNCH(ctx, (k_zero<T>), g, PX_THREADS, 0, ctx->stream, M, N);
+        k_zero<T><<<g, PX_THREADS, 0, ctx->stream>>>(M, N);
+        FGB_LAUNCHED(ctx);
         break;
       }
       if (c.k > LINE_KMAX && !((c.kind == FGB_SPCOL && c.k >= rows) || (c.kind == FGB_SPLIN && c.k >= cols) ||
@@ -1674,30 +1671,36 @@ fgb_status launch_prox(fgb_ctx* ctx, ProxWork& w, const fgb_constraint& c, T* M,
         return fail(ctx, FGB_ERR_NOT_SUPPORTED, "per-line top-k supports k <= %d", LINE_KMAX);
       const int k = (int)std::min<long long>(c.k, LINE_KMAX + (long long)std::max(rows, cols));
       if (c.kind != FGB_SPLIN) {
-        FGB_LAUNCH(ctx, (k_line_topk<T>), (cols + 127) / 128, 128, 0, ctx->stream, M, rows, cols, 1, std::min(k, rows), pos,
+        k_line_topk<T><<<(cols + 127) / 128, 128, 0, ctx->stream>>>(M, rows, cols, 1, std::min(k, rows), pos,
                                                                    w.flags, 1);
+        FGB_LAUNCHED(ctx);
       }
       if (c.kind != FGB_SPCOL) {
-        FGB_LAUNCH(ctx, (k_line_topk<T>), (rows + 127) / 128, 128, 0, ctx->stream, M, rows, cols, 0, std::min(k, cols), pos,
+        k_line_topk<T><<<(rows + 127) / 128, 128, 0, ctx->stream>>>(M, rows, cols, 0, std::min(k, cols), pos,
                                                                    w.flags, 2);
+        FGB_LAUNCHED(ctx);
       }
-      FGB_LAUNCH(ctx, (k_flag_apply<T>), g, PX_THREADS, 0, ctx->stream, M, N, pos, w.flags);
+      k_flag_apply<T><<<g, PX_THREADS, 0, ctx->stream>>>(M, N, pos, w.flags);
+      FGB_LAUNCHED(ctx);
       break;
     }
     case FGB_NORMCOL:
     case FGB_NORMLIN: {
       if (c.s < 0) return fail(ctx, FGB_ERR_INVALID_ARG, "Faust::prox_normcol : s < 0 ");
       if (c.s == 0) {
-        FGB_LAUNCH(ctx, (k_zero<T>), g, PX_THREADS, 0, ctx->stream, M, N);
+        k_zero<T><<<g, PX_THREADS, 0, ctx->stream>>>(M, N);
+        FGB_LAUNCHED(ctx);
       } else {
         const bool by_col = c.kind == FGB_NORMCOL;
-        FGB_LAUNCH(ctx, (k_normline<T>), by_col ? cols : rows, PX_THREADS, 0, ctx->stream, M, rows, cols, by_col ? 1 : 0, c.s, pos);
+        k_normline<T><<<by_col ? cols : rows, PX_THREADS, 0, ctx->stream>>>(M, rows, cols, by_col ? 1 : 0, c.s, pos);
+        FGB_LAUNCHED(ctx);
       }
       break;
     }
     case FGB_SUPP: {
       if (!supp_dev) return fail(ctx, FGB_ERR_INVALID_ARG, "prox_supp: missing support");
-      FGB_LAUNCH(ctx, (k_supp<T>), g, PX_THREADS, 0, ctx->stream, M, N, supp_dev, pos);
+      k_supp<T><<<g, PX_THREADS, 0, ctx->stream>>>(M, N, supp_dev, pos);
+      FGB_LAUNCHED(ctx);
       break;
     }
     default:
@@ -1718,7 +1721,6 @@ template <typename T>
 __global__ void __launch_bounds__(256)
     k_d2c_count_rc(const T* __restrict__ M, int rows, int cols, int* __restrict__ rcnt, int* __restrict__ ccnt,
                    int with_cols) {
-  pdl_entry();
   const long w = (blockIdx.x * (long)blockDim.x + threadIdx.x) / 32;
   const int lane = threadIdx.x & 31;
   const bool is_row = w < rows;
@@ -1781,7 +1783,6 @@ __device__ void block_excl_scan(const int* __restrict__ cnt, int n, int* __restr
 __global__ void __launch_bounds__(1024) k_d2c_scan_rc(const int* __restrict__ rcnt, int rows, const int* __restrict__ ccnt,
                                                       int cols, int* __restrict__ rowptr, int* __restrict__ t_rowptr,
                                                       int with_cols, int cap, int* status) {
-  pdl_entry();
   __shared__ int part[32];
   block_excl_scan(rcnt, rows, rowptr, part);
   if (with_cols) block_excl_scan(ccnt, cols, t_rowptr, part);
@@ -1798,7 +1799,6 @@ __global__ void __launch_bounds__(256)
     k_d2c_write_rc(const T* __restrict__ M, int rows, int cols, const int* __restrict__ rowptr,
                    int* __restrict__ colind, T* __restrict__ val, const int* __restrict__ t_rowptr,
                    int* __restrict__ t_colind, T* __restrict__ t_val, int cap, int with_cols) {
-  pdl_entry();
   const long w = (blockIdx.x * (long)blockDim.x + threadIdx.x) / 32;
   const unsigned lane = threadIdx.x & 31;
   const unsigned lt = (1u << lane) - 1u;
@@ -1841,11 +1841,14 @@ fgb_status launch_dense_to_csr(fgb_ctx* ctx, ProxWork& w, const T* M, DevFactor&
   const int blocks = (int)((warps * 32 + 255) / 256);
   int* rcnt = w.row_cnt;
   int* ccnt = w.row_cnt + f.rows;
-  FGB_LAUNCH(ctx, (k_d2c_count_rc<T>), blocks, 256, 0, ctx->stream, M, f.rows, f.cols, rcnt, ccnt, with_cols);
-  FGB_LAUNCH(ctx, k_d2c_scan_rc, 1, 1024, 0, ctx->stream, rcnt, f.rows, ccnt, f.cols, f.rowptr, f.t_rowptr, with_cols, f.cap,
+  k_d2c_count_rc<T><<<blocks, 256, 0, ctx->stream>>>(M, f.rows, f.cols, rcnt, ccnt, with_cols);
+  FGB_LAUNCHED(ctx);
+  k_d2c_scan_rc<<<1, 1024, 0, ctx->stream>>>(rcnt, f.rows, ccnt, f.cols, f.rowptr, f.t_rowptr, with_cols, f.cap,
                                              status);
-  FGB_LAUNCH(ctx, (k_d2c_write_rc<T>), blocks, 256, 0, ctx->stream, M, f.rows, f.cols, f.rowptr, f.colind, (T*)f.val, f.t_rowptr,
+  FGB_LAUNCHED(ctx);
+  k_d2c_write_rc<T><<<blocks, 256, 0, ctx->stream>>>(M, f.rows, f.cols, f.rowptr, f.colind, (T*)f.val, f.t_rowptr,
                                                      f.t_colind, (T*)f.t_val, f.cap, with_cols);
+  FGB_LAUNCHED(ctx);
   return FGB_OK;
 }
 
