@@ -16,7 +16,6 @@
 // fma(v0, x[r&~h], +0)) with (v0, v1) row r's stored values in order, so the
 // result is bit-identical to the per-factor CSR product.
 #include <algorithm>
-#include <cstdlib>
 #include <cstdint>
 #include <vector>
 
@@ -222,269 +221,244 @@ __global__ void __launch_bounds__(BF_THREADS, sizeof(T) == 4 ? 3 : 2)
   }
 }
 
-// ------------------------------------------------------------------ two phases
-// For chains whose application order first uses only strides below 2^a and
-// then only strides of 2^a and above (the order of butterfly_support's
-// factors applied right to left), the rows split as r = q * 2^a + p: the
-// first phase only mixes rows of the same block q (in-block index p), the
-// second only rows of the same p (index q).  Each phase is a run of small
-// independent groups of rows, so a CTA owns a few groups, keeps their factor
-// values in shared memory once, and streams column tiles past them -- the
-// factor values are read once per CTA instead of once per column tile.
-// Between the phases the intermediate Z is stored block-transposed
-// (position p * (n / 2^a) + q), so both phases read and write their groups as
-// contiguous runs; the columns go in chunks whose Z stays in L2.  Entry
-// order per factor is the canonical one, so results equal the CSR chain's.
-//
-// In one phase: groups of S rows (in-group index i), NG groups; a CTA owns
-// BP_GPC consecutive groups and steps over tiles of BP_NT x 4 columns.  The
-// phase input holds group g's rows at positions g * S + i, the output at
-// i * NG + g; the factor values of (g, i) sit at row g * S + i (first phase)
-// or i * NG + g (second phase).  Orbits of 8 rows (three strides of the
-// in-group index) x 4 columns per thread, up to three factors per pass.
-constexpr int BP_GPC = 8;     // groups per CTA
-constexpr int BP_NT = 4;      // 4-column tiles per CTA step
-constexpr int BP_MAXF = 8;    // factors per phase
-constexpr int BP_MAXP = 8;    // passes per phase
+// ------------------------------------------------------------------ orbit passes
+// The same chain with passes of up to G distinct strides (any number of
+// consecutive factors using them).  A pass's orbit is the 2^G rows base +
+// any subset of its G span strides (padded with unused strides when the
+// pass has fewer), so a thread applies the pass's factors to 2^G rows x CT
+// columns in registers between one shared-memory load and one store: with
+// G = 3 and 4 columns, about 1.3 instructions per FMA instead of about 4
+// with two-factor passes.  Column tiles of TC columns; TC / CT threads share
+// an orbit.
+constexpr int BFO_MAXG = 4;
 
-struct BflyPhase {
-  int ng;        // groups of the phase (n / S)
-  int vmode;     // 0: value row g * S + i; 1: value row i * ng + g
-  int nf, npasses;
-  const float* val[BP_MAXF];    // 2 values per row, application order
-  int lbit[BP_MAXF];            // stride of factor f as a bit of the in-group index
-  int pass_first[BP_MAXP], pass_n[BP_MAXP];
-  int pass_pos[BP_MAXP][3];     // orbit span bits of the pass, ascending
-  int pass_local[BP_MAXF];      // factor f's bit among its pass's span (0..2)
-};
-
-// Local row R = i * BP_GPC + g of the CTA's groups, 16-byte slot with bits
-// 0-2 XORed with bits 3-5: conflict-free for eight consecutive groups at one
-// in-group row (the passes, the stores) and for eight consecutive in-group
-// rows of one group (the tile loads).
-__device__ __forceinline__ int bp_slot(int R) { return R ^ ((R >> 3) & 7); }
-
-template <int B>
-__device__ __forceinline__ void bp_stage(float4 (&xs)[8], const float2 (&v)[8]) {
-#pragma unroll
-  for (int k = 0; k < 8; ++k) {
-    if ((k >> B) & 1) continue;
-    const int k1 = k | (1 << B);
-    const float2 va = v[k], vb = v[k1];
-    const float4 a = xs[k], c = xs[k1];
-    xs[k] = make_float4(fmad(va.y, c.x, fmad(va.x, a.x, 0.f)), fmad(va.y, c.y, fmad(va.x, a.y, 0.f)),
-                        fmad(va.y, c.z, fmad(va.x, a.z, 0.f)), fmad(va.y, c.w, fmad(va.x, a.w, 0.f)));
-    xs[k1] = make_float4(fmad(vb.y, c.x, fmad(vb.x, a.x, 0.f)), fmad(vb.y, c.y, fmad(vb.x, a.y, 0.f)),
-                         fmad(vb.y, c.z, fmad(vb.x, a.z, 0.f)), fmad(vb.y, c.w, fmad(vb.x, a.w, 0.f)));
+template <typename T, int CT>
+__device__ __forceinline__ void ld_piece(const T* p, T (&x)[CT]) {
+  if constexpr (CT * sizeof(T) == 8 && sizeof(T) == 4) {
+    const float2 v = *reinterpret_cast<const float2*>(p);
+    x[0] = v.x, x[1] = v.y;
+  } else {
+    ld_row<T, CT>(p, x);
+  }
+}
+template <typename T, int CT>
+__device__ __forceinline__ void st_piece(T* p, const T (&x)[CT]) {
+  if constexpr (CT * sizeof(T) == 8 && sizeof(T) == 4) {
+    *reinterpret_cast<float2*>(p) = make_float2(x[0], x[1]);
+  } else {
+    st_row<T, CT>(p, x);
   }
 }
 
-template <int S>
-__global__ void __launch_bounds__(BP_NT * BP_GPC * S / 8, S == 64 ? 3 : 1)
-    k_bfly_phase(const __grid_constant__ BflyPhase P, const float* __restrict__ in, long ld_in,
-                 float* __restrict__ out, long ld_out, int ncols) {
-  constexpr int ROWS = BP_GPC * S;          // rows of the CTA
-  constexpr int NT = BP_NT * BP_GPC * S / 8;  // threads: one orbit x 4 columns each
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  float4* tiles = reinterpret_cast<float4*>(smem_raw);                  // [BP_NT][ROWS]
-  float2* vs = reinterpret_cast<float2*>(smem_raw + sizeof(float4) * BP_NT * ROWS);  // [nf][ROWS]
-  const int tid = threadIdx.x;
-  const int g0 = blockIdx.x * BP_GPC;
-  // the CTA's factor values, once
-  for (int f = 0; f < P.nf; ++f) {
-    const float2* v = reinterpret_cast<const float2*>(P.val[f]);
-    for (int R = tid; R < ROWS; R += NT) {
-      const int g = R % BP_GPC, i = R / BP_GPC;
-      const long r = P.vmode ? (long)i * P.ng + g0 + g : (long)(g0 + g) * S + i;
-      vs[f * ROWS + bp_slot(R)] = __ldg(v + r);
+struct BflyPlanO {
+  int n, npasses, last_direct, g;
+  const void* val[BF_MAXS];   // step s (application order): 2 values per row
+  int step_bit[BF_MAXS];      // local bit of step s's stride in its pass's span
+  int pass_first[BF_MAXS], pass_n[BF_MAXS];
+  int pass_pos[BF_MAXS][BFO_MAXG];  // span bit positions, ascending
+};
+
+// Row slot in the tile: bits 0-2 XORed with bits G..G+2, so the rows of eight
+// consecutive orbits (one phase of a warp's shared-memory access) fall in
+// distinct bank groups in every pass of consecutive strides.
+template <int G>
+__device__ __forceinline__ int bfo_slot(int r) { return r ^ ((r >> G) & 7); }
+
+// Factor with local bit B on the 2^G rows of an orbit (canonical entry
+// order); the values of each row pair are loaded as the pairs are worked
+// through.
+template <typename T, int G, int CT, int B>
+__device__ __forceinline__ void bfo_stage(T (&xs)[1 << G][CT], const typename V2<T>::type* __restrict__ vp,
+                                          const int (&row)[1 << G]) {
+  using T2 = typename V2<T>::type;
+#pragma unroll
+  for (int k = 0; k < (1 << G); ++k) {
+    if ((k >> B) & 1) continue;
+    const int k1 = k | (1 << B);
+    const T2 va = __ldg(vp + row[k]), vb = __ldg(vp + row[k1]);
+#pragma unroll
+    for (int t = 0; t < CT; ++t) {
+      const T a = xs[k][t], c = xs[k1][t];
+      xs[k][t] = fmad(va.y, c, fmad(va.x, a, T(0)));
+      xs[k1][t] = fmad(vb.y, c, fmad(vb.x, a, T(0)));
     }
   }
-  // this thread's orbit: 4-column tile tt, group g, orbit o of the group
-  const int tt = tid / (ROWS / 8), rem = tid % (ROWS / 8);
-  const int g = rem % BP_GPC, o = rem / BP_GPC;
-  const long in0 = (long)g0 * S;
-  for (long j0 = (long)blockIdx.y * BP_NT * 4; j0 < ncols; j0 += (long)gridDim.y * BP_NT * 4) {
-    __syncthreads();  // values stored; previous tile consumed
-    // tiles: group rows are contiguous in the input (positions g * S + i)
-    for (int idx = tid; idx < BP_NT * ROWS; idx += NT) {
-      const int t = idx / ROWS, Rin = idx % ROWS;
-      const int gg = Rin / S, i = Rin % S;
-      const long j = j0 + t * 4;
-      const float* src = in + in0 + Rin + j * ld_in;
-      float4 x;
-      x.x = j < ncols ? src[0] : 0.f;
-      x.y = j + 1 < ncols ? src[ld_in] : 0.f;
-      x.z = j + 2 < ncols ? src[2 * ld_in] : 0.f;
-      x.w = j + 3 < ncols ? src[3 * ld_in] : 0.f;
-      tiles[t * ROWS + bp_slot(i * BP_GPC + gg)] = x;
+}
+
+// The same with the values of the orbit's rows already in registers.
+template <typename T, int G, int CT, int B>
+__device__ __forceinline__ void bfo_apply(T (&xs)[1 << G][CT], const typename V2<T>::type (&v)[1 << G]) {
+#pragma unroll
+  for (int k = 0; k < (1 << G); ++k) {
+    if ((k >> B) & 1) continue;
+    const int k1 = k | (1 << B);
+#pragma unroll
+    for (int t = 0; t < CT; ++t) {
+      const T a = xs[k][t], c = xs[k1][t];
+      xs[k][t] = fmad(v[k].y, c, fmad(v[k].x, a, T(0)));
+      xs[k1][t] = fmad(v[k1].y, c, fmad(v[k1].x, a, T(0)));
     }
-    __syncthreads();
-    float4* tile = tiles + tt * ROWS;
-    for (int ps = 0; ps < P.npasses; ++ps) {
-      const bool last = ps + 1 == P.npasses;
-      const int p0 = P.pass_pos[ps][0], p1 = P.pass_pos[ps][1], p2 = P.pass_pos[ps][2];
+  }
+}
+
+template <typename T, int G, int TC, int CT, int NT, int MINB>
+__global__ void __launch_bounds__(NT, MINB)
+    k_bfly_orbit(const __grid_constant__ BflyPlanO p, const T* __restrict__ X, int ldx, int ncols,
+                 T* __restrict__ Y, int ldy) {
+  using T2 = typename V2<T>::type;
+  constexpr int R = 1 << G;
+  constexpr int TPO = TC / CT;  // threads per orbit, CT columns each
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T* tile = reinterpret_cast<T*>(smem_raw);  // n rows of TC values
+  const int n = p.n;
+  const int j0 = blockIdx.x * TC;
+  const int tid = threadIdx.x;
+  // X tile -> shared memory (coalesced along each column)
+  for (int r = tid; r < n; r += NT) {
+    T x[TC];
+#pragma unroll
+    for (int t = 0; t < TC; ++t) x[t] = (j0 + t < ncols) ? X[r + (long)(j0 + t) * ldx] : T(0);
+    st_row<T, TC>(tile + (long)bfo_slot<G>(r) * TC, x);
+  }
+  __syncthreads();
+  const int half = tid % TPO;
+  const int norb = n >> G;
+  for (int ps = 0; ps < p.npasses; ++ps) {
+    const bool last = ps + 1 == p.npasses;
+    const int first = p.pass_first[ps], nf = p.pass_n[ps];
+    int pos[G];
+#pragma unroll
+    for (int i = 0; i < G; ++i) pos[i] = p.pass_pos[ps][i];
+    for (int o = tid / TPO; o < norb; o += NT / TPO) {
+      // base: o with zero bits inserted at the span positions (ascending)
       int base = o;
-      base = ((base >> p0) << (p0 + 1)) | (base & ((1 << p0) - 1));
-      base = ((base >> p1) << (p1 + 1)) | (base & ((1 << p1) - 1));
-      base = ((base >> p2) << (p2 + 1)) | (base & ((1 << p2) - 1));
-      int R[8];
 #pragma unroll
-      for (int k = 0; k < 8; ++k)
-        R[k] = (base + ((k & 1) << p0) + (((k >> 1) & 1) << p1) + (((k >> 2) & 1) << p2)) * BP_GPC + g;
-      float4 xs[8];
+      for (int i = 0; i < G; ++i) base = ((base >> pos[i]) << (pos[i] + 1)) | (base & ((1 << pos[i]) - 1));
+      int row[R];
 #pragma unroll
-      for (int k = 0; k < 8; ++k) xs[k] = tile[bp_slot(R[k])];
-      const int first = P.pass_first[ps], nfp = P.pass_n[ps];
-      for (int f = first; f < first + nfp; ++f) {
-        const float2* vf = vs + f * ROWS;
-        float2 v[8];
+      for (int k = 0; k < R; ++k) {
+        int r = base;
 #pragma unroll
-        for (int k = 0; k < 8; ++k) v[k] = vf[bp_slot(R[k])];
-        const int b = P.pass_local[f];
-        if (b == 0) bp_stage<0>(xs, v);
-        else if (b == 1) bp_stage<1>(xs, v);
-        else bp_stage<2>(xs, v);
+        for (int i = 0; i < G; ++i) r += ((k >> i) & 1) << pos[i];
+        row[k] = r;
       }
-      if (last) {
-        // output position i * ng + g: eight consecutive groups are one
-        // 32-byte run per column
-        const long j = j0 + tt * 4;
+      T xs[R][CT];
+      if (nf <= G) {
+        // every value of the pass's factors on the orbit's rows, loaded
+        // before any arithmetic so their latencies overlap
+        T2 v[G][R];
 #pragma unroll
-        for (int k = 0; k < 8; ++k) {
-          const int i = R[k] / BP_GPC;
-          float* dst = out + (long)i * P.ng + g0 + g + j * ld_out;
-          if (j < ncols) dst[0] = xs[k].x;
-          if (j + 1 < ncols) dst[ld_out] = xs[k].y;
-          if (j + 2 < ncols) dst[2 * ld_out] = xs[k].z;
-          if (j + 3 < ncols) dst[3 * ld_out] = xs[k].w;
+        for (int f = 0; f < G; ++f)
+          if (f < nf) {
+            const T2* vp = reinterpret_cast<const T2*>(p.val[first + f]);
+#pragma unroll
+            for (int k = 0; k < R; ++k) v[f][k] = __ldg(vp + row[k]);
+          }
+#pragma unroll
+        for (int k = 0; k < R; ++k) ld_piece<T, CT>(tile + (long)bfo_slot<G>(row[k]) * TC + half * CT, xs[k]);
+#pragma unroll
+        for (int f = 0; f < G; ++f) {
+          if (f >= nf) break;
+          const int b = p.step_bit[first + f];
+          if (b == 0) bfo_apply<T, G, CT, 0>(xs, v[f]);
+          else if (b == 1) bfo_apply<T, G, CT, 1>(xs, v[f]);
+          else if (G > 3 && b == 3) bfo_apply<T, G, CT, (G > 3 ? 3 : 0)>(xs, v[f]);
+          else bfo_apply<T, G, CT, 2>(xs, v[f]);
         }
       } else {
 #pragma unroll
-        for (int k = 0; k < 8; ++k) tile[bp_slot(R[k])] = xs[k];
-        __syncthreads();
+        for (int k = 0; k < R; ++k) ld_piece<T, CT>(tile + (long)bfo_slot<G>(row[k]) * TC + half * CT, xs[k]);
+        for (int f = 0; f < nf; ++f) {
+          const T2* vp = reinterpret_cast<const T2*>(p.val[first + f]);
+          const int b = p.step_bit[first + f];
+          if (b == 0) bfo_stage<T, G, CT, 0>(xs, vp, row);
+          else if (b == 1) bfo_stage<T, G, CT, 1>(xs, vp, row);
+          else if (G > 3 && b == 3) bfo_stage<T, G, CT, (G > 3 ? 3 : 0)>(xs, vp, row);
+          else bfo_stage<T, G, CT, 2>(xs, vp, row);
+        }
+      }
+      if (last && p.last_direct) {
+#pragma unroll
+        for (int k = 0; k < R; ++k)
+#pragma unroll
+          for (int t = 0; t < CT; ++t) {
+            const int j = j0 + half * CT + t;
+            if (j < ncols) Y[row[k] + (long)j * ldy] = xs[k][t];
+          }
+      } else {
+#pragma unroll
+        for (int k = 0; k < R; ++k) st_piece<T, CT>(tile + (long)bfo_slot<G>(row[k]) * TC + half * CT, xs[k]);
       }
     }
+    if (!last || !p.last_direct) __syncthreads();
   }
-}
-
-// Plan of one phase: factors (application order) first..first+cnt, strides
-// as bits of the phase's in-group index (stride bit - shift); passes of up to
-// three distinct bits, padded with the lowest unused ones.
-static bool build_phase(const std::vector<const float*>& vals, const std::vector<int>& bits, int first, int cnt,
-                        int shift, int slog, int ng, int vmode, BflyPhase& P) {
-  if (cnt > BP_MAXF || slog < 3) return false;
-  P.ng = ng;
-  P.vmode = vmode;
-  P.nf = cnt;
-  P.npasses = 0;
-  for (int u = 0; u < cnt; ++u) {
-    P.val[u] = vals[first + u];
-    P.lbit[u] = bits[first + u] - shift;
-  }
-  for (int s = 0; s < cnt;) {
-    if (P.npasses == BP_MAXP) return false;
-    const int ps = P.npasses++;
-    std::vector<int> pos;
-    int e = s;
-    while (e < cnt) {
-      const bool have = std::find(pos.begin(), pos.end(), P.lbit[e]) != pos.end();
-      if (!have && (int)pos.size() == 3) break;
-      if (!have) pos.push_back(P.lbit[e]);
-      ++e;
+  if (!p.last_direct) {
+    // the last pass's rows are not consecutive across threads: copy out
+    // column by column
+    for (int r = tid; r < n; r += NT) {
+#pragma unroll
+      for (int t = 0; t < TC; ++t)
+        if (j0 + t < ncols) Y[r + (long)(j0 + t) * ldy] = tile[(long)bfo_slot<G>(r) * TC + t];
     }
-    for (int b = 0; (int)pos.size() < 3 && b < slog; ++b)
-      if (std::find(pos.begin(), pos.end(), b) == pos.end()) pos.push_back(b);
-    std::sort(pos.begin(), pos.end());
-    P.pass_first[ps] = s;
-    P.pass_n[ps] = e - s;
-    for (int q = 0; q < 3; ++q) P.pass_pos[ps][q] = pos[q];
-    for (int u = s; u < e; ++u) P.pass_local[u] = (int)(std::find(pos.begin(), pos.end(), P.lbit[u]) - pos.begin());
-    s = e;
   }
-  return true;
 }
 
-template <int S>
-static fgb_status launch_phase(fgb_ctx* ctx, const BflyPhase& P, const float* in, long ld_in, float* out,
-                               long ld_out, int ncols) {
-  constexpr int ROWS = BP_GPC * S;
-  const size_t smem = sizeof(float4) * BP_NT * ROWS + sizeof(float2) * (size_t)P.nf * ROWS;
-  auto kern = k_bfly_phase<S>;
-  if (smem > 48 * 1024)
-    FGB_CUDA(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  // column steps of the chunk spread evenly over about one wave of CTAs
-  const int steps = (ncols + BP_NT * 4 - 1) / (BP_NT * 4);
-  const int ymax = std::max(1, (int)(3L * ctx->sm_count * BP_GPC / P.ng));
-  const int spc = (steps + ymax - 1) / ymax;
-  dim3 grid(P.ng / BP_GPC, (steps + spc - 1) / spc);
-  kern<<<grid, BP_NT * ROWS / 8, smem, ctx->stream>>>(P, in, ld_in, out, ld_out, ncols);
-  FGB_LAUNCHED(ctx);
-  return FGB_OK;
-}
-
-static fgb_status launch_phase_s(fgb_ctx* ctx, int slog, const BflyPhase& P, const float* in, long ld_in,
-                                 float* out, long ld_out, int ncols) {
-  if (slog == 5) return launch_phase<32>(ctx, P, in, ld_in, out, ld_out, ncols);
-  if (slog == 6) return launch_phase<64>(ctx, P, in, ld_in, out, ld_out, ncols);
-  return launch_phase<128>(ctx, P, in, ld_in, out, ld_out, ncols);
-}
-
-// The two-phase chain when the application order allows it (FP32, forward
-// split of the strides, group sizes 32, 64 or 128); *ran tells whether it ran.
-static fgb_status bfly_two_phase(fgb_faust* F, char op, int nfac, const float* X, int ldx, int ncols, float* Y,
-                                 int ldy, bool* ran) {
-  *ran = false;
-  fgb_ctx* ctx = F->ctx;
+// Passes of consecutive steps (application order) spanning at most G
+// distinct strides; spans padded to G bit positions with the lowest unused
+// ones.  False when n < 2^G.
+static bool build_plan_orbit(fgb_faust* F, char op, int nfac, int G, BflyPlanO& p) {
   const int J = (int)F->f.size();
-  const int n = F->f[0].rows;
-  int m = 0;
-  while ((1 << m) < n) ++m;
-  std::vector<const float*> vals(nfac);
-  std::vector<int> bits(nfac);
+  p.n = F->f[0].rows;
+  p.g = G;
+  int logn = 0;
+  while ((1 << logn) < p.n) ++logn;
+  if (logn < G) return false;
+  std::vector<int> bit(nfac);
   for (int s = 0; s < nfac; ++s) {
     const int q = nfac - 1 - s;
     const DevFactor& f = F->f[op == 'N' ? q : J - 1 - q];
-    vals[s] = (const float*)(op == 'N' ? f.val : f.t_val);
+    p.val[s] = op == 'N' ? f.val : f.t_val;
     int b = 0;
     while ((1 << b) < f.bfly) ++b;
-    bits[s] = b;
+    bit[s] = b;
   }
-  // split point: prefix bits all < a <= suffix bits, a as close to m / 2 as
-  // the order allows, both group sizes 32..128
-  int best_a = -1, best_L = -1;
-  for (int L = 1; L < nfac; ++L) {
-    int mx = 0, mn = m;
-    for (int s = 0; s < L; ++s) mx = std::max(mx, bits[s]);
-    for (int s = L; s < nfac; ++s) mn = std::min(mn, bits[s]);
-    for (int a = mx + 1; a <= mn; ++a)
-      if (a >= 5 && a <= 7 && m - a >= 5 && m - a <= 7 && (best_a < 0 || std::abs(2 * a - m) < std::abs(2 * best_a - m)))
-        best_a = a, best_L = L;
+  p.npasses = 0;
+  for (int s = 0; s < nfac;) {
+    const int ps = p.npasses++;
+    std::vector<int> pos;
+    int e = s;
+    while (e < nfac) {
+      const bool have = std::find(pos.begin(), pos.end(), bit[e]) != pos.end();
+      if (!have && (int)pos.size() == G) break;
+      if (!have) pos.push_back(bit[e]);
+      ++e;
+    }
+    for (int b = 0; (int)pos.size() < G && b < logn; ++b)
+      if (std::find(pos.begin(), pos.end(), b) == pos.end()) pos.push_back(b);
+    std::sort(pos.begin(), pos.end());
+    p.pass_first[ps] = s;
+    p.pass_n[ps] = e - s;
+    for (int i = 0; i < BFO_MAXG; ++i) p.pass_pos[ps][i] = i < G ? pos[i] : 0;
+    for (int u = s; u < e; ++u) p.step_bit[u] = (int)(std::find(pos.begin(), pos.end(), bit[u]) - pos.begin());
+    s = e;
   }
-  if (best_a < 0) return FGB_OK;
-  const int a = best_a, L = best_L;
-  const int SA = 1 << a, SB = n >> a;
-  BflyPhase PA, PB;
-  if (!build_phase(vals, bits, 0, L, 0, a, n / SA, 0, PA)) return FGB_OK;
-  if (!build_phase(vals, bits, L, nfac - L, a, m - a, SA, 1, PB)) return FGB_OK;
-  // column chunks whose intermediate (n x cw FP32) stays in L2
-  const long zcap = 32L << 20;
-  long cw = std::max<long>(BP_NT * 4, (zcap / ((long)n * 4)) / (BP_NT * 4) * (BP_NT * 4));
-  cw = std::min<long>(cw, ncols);
-  const size_t need = (size_t)n * cw * sizeof(float);
-  if (F->bz_bytes < need) {
-    dfree(F->bz);
-    F->bz = nullptr;
-    F->bz_bytes = 0;
-    FGB_TRY(dmalloc(ctx, &F->bz, need));
-    F->bz_bytes = need;
-  }
-  float* Z = (float*)F->bz;
-  *ran = true;
-  for (long c0 = 0; c0 < ncols; c0 += cw) {
-    const int w = (int)std::min<long>(cw, ncols - c0);
-    FGB_TRY(launch_phase_s(ctx, a, PA, X + c0 * ldx, ldx, Z, n, w));
-    FGB_TRY(launch_phase_s(ctx, m - a, PB, Z, n, Y + c0 * ldy, ldy, w));
-  }
+  // the last pass stores Y straight from registers when 32 consecutive orbits
+  // are 32 consecutive rows (no span position below 5)
+  p.last_direct = p.pass_pos[p.npasses - 1][0] >= 5 ? 1 : 0;
+  return true;
+}
+
+template <typename T, int G, int TC, int CT, int NT, int MINB>
+static fgb_status launch_bfly_orbit(fgb_faust* F, const BflyPlanO& p, const T* X, int ldx, int ncols, T* Y,
+                                    int ldy) {
+  fgb_ctx* ctx = F->ctx;
+  const size_t smem = (size_t)p.n * TC * sizeof(T);
+  auto kern = k_bfly_orbit<T, G, TC, CT, NT, MINB>;
+  if (smem > 48 * 1024)
+    FGB_CUDA(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  const int tiles = (ncols + TC - 1) / TC;
+  kern<<<tiles, NT, smem, ctx->stream>>>(p, X, ldx, ncols, Y, ldy);
+  FGB_LAUNCHED(ctx);
   return FGB_OK;
 }
 
@@ -615,10 +589,6 @@ fgb_status bfly_chain(fgb_faust* F, char op, int nfac, const void* X, int ldx, i
   const int tc = 16 / (int)dtype_size(F->dtype);
   const long tiles = (ncols + tc - 1) / tc;
   if (!force && tiles < ctx->sm_count) return FGB_OK;
-  if (F->dtype == FGB_F32 && !getenv("FGB_BFLY_ONE_PHASE")) {
-    FGB_TRY(bfly_two_phase(F, op, nfac, (const float*)X, ldx, ncols, (float*)Y, ldy, ran));
-    if (*ran) return FGB_OK;
-  }
   *ran = true;
   if (F->dtype == FGB_F32)
     return launch_bfly<float, 4>(F, op, nfac, (const float*)X, ldx, ncols, (float*)Y, ldy);

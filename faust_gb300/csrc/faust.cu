@@ -323,7 +323,6 @@ fgb_faust::~fgb_faust() {
   fgb::dfree(chain_desc);
   fgb::dfree(chain_desc_t);
   fgb::dfree(pws);
-  fgb::dfree(bz);
   if (s_in) {
     cudaStreamSynchronize(s_in);
     cudaStreamSynchronize(s_out);

@@ -130,9 +130,6 @@ struct fgb_faust {
   // Workspace of the dense product (intermediates and dense images).
   void* pws = nullptr;
   size_t pws_bytes = 0;
-  // Intermediate of the two-phase butterfly chain (one column chunk).
-  void* bz = nullptr;
-  size_t bz_bytes = 0;
   // Copy streams and events of the pipelined host-buffer product.
   cudaStream_t s_in = nullptr, s_out = nullptr;
   cudaEvent_t ev_in[4] = {}, ev_done[4] = {}, ev_start = nullptr;

@@ -150,30 +150,6 @@ def test_butterfly_kernel_shuffled_and_repeated_strides(fgb, oracle, dtype):
         F.close()
 
 
-@pytest.mark.parametrize("nf,order,ncols", [
-    (10, [3, 0, 4, 1, 2, 7, 5, 9, 6, 8], 1000),     # shuffled within each phase, group sizes 32 x 32
-    (11, [0, 0, 2, 1, 4, 3, 5, 8, 6, 10, 7, 9], 37),  # repeated stride, 32 x 64, ragged columns
-    (12, list(range(12)), 5),                          # 64 x 64, fewer columns than one tile step
-    (13, list(range(13)), 129),                        # 64 x 128
-])
-def test_butterfly_two_phase_bitexact(fgb, oracle, monkeypatch, nf, order, ncols):
-    """FP32 chains whose strides first stay below 2^a and then at or above it
-    run as two phases (in-block groups, then strided groups, through a
-    block-transposed intermediate); the result equals the oracle's CSR chain
-    and the single-kernel butterfly chain bit for bit."""
-    rng = np.random.default_rng(nf * 7 + ncols)
-    facs = _bfly_perm_factors(nf, order[::-1], rng, np.float32)  # application order = order
-    F = fgb.Faust(facs, dtype=np.float32)
-    X = synth.dense_colmajor(1 << nf, ncols, rng, np.float32)
-    ref = oracle.chain_mul(facs, X)
-    two = _to_np(F.matmul_device(_colmajor_cuda(X), mode=3))
-    assert np.array_equal(two, ref)
-    monkeypatch.setenv("FGB_BFLY_ONE_PHASE", "1")
-    one = _to_np(F.matmul_device(_colmajor_cuda(X), mode=3))
-    assert np.array_equal(one, ref)
-    F.close()
-
-
 def test_butterfly_kernel_rejects_other_supports(fgb):
     rng = np.random.default_rng(4)
     facs = [synth.random_csr(64, 64, 2, rng) for _ in range(3)]
