@@ -221,247 +221,6 @@ __global__ void __launch_bounds__(BF_THREADS, sizeof(T) == 4 ? 3 : 2)
   }
 }
 
-// ------------------------------------------------------------------ orbit passes
-// The same chain with passes of up to G distinct strides (any number of
-// consecutive factors using them).  A pass's orbit is the 2^G rows base +
-// any subset of its G span strides (padded with unused strides when the
-// pass has fewer), so a thread applies the pass's factors to 2^G rows x CT
-// columns in registers between one shared-memory load and one store: with
-// G = 3 and 4 columns, about 1.3 instructions per FMA instead of about 4
-// with two-factor passes.  Column tiles of TC columns; TC / CT threads share
-// an orbit.
-constexpr int BFO_MAXG = 4;
-
-template <typename T, int CT>
-__device__ __forceinline__ void ld_piece(const T* p, T (&x)[CT]) {
-  if constexpr (CT * sizeof(T) == 8 && sizeof(T) == 4) {
-    const float2 v = *reinterpret_cast<const float2*>(p);
-    x[0] = v.x, x[1] = v.y;
-  } else {
-    ld_row<T, CT>(p, x);
-  }
-}
-template <typename T, int CT>
-__device__ __forceinline__ void st_piece(T* p, const T (&x)[CT]) {
-  if constexpr (CT * sizeof(T) == 8 && sizeof(T) == 4) {
-    *reinterpret_cast<float2*>(p) = make_float2(x[0], x[1]);
-  } else {
-    st_row<T, CT>(p, x);
-  }
-}
-
-struct BflyPlanO {
-  int n, npasses, last_direct, g;
-  const void* val[BF_MAXS];   // step s (application order): 2 values per row
-  int step_bit[BF_MAXS];      // local bit of step s's stride in its pass's span
-  int pass_first[BF_MAXS], pass_n[BF_MAXS];
-  int pass_pos[BF_MAXS][BFO_MAXG];  // span bit positions, ascending
-};
-
-// Row slot in the tile: bits 0-2 XORed with bits G..G+2, so the rows of eight
-// consecutive orbits (one phase of a warp's shared-memory access) fall in
-// distinct bank groups in every pass of consecutive strides.
-template <int G>
-__device__ __forceinline__ int bfo_slot(int r) { return r ^ ((r >> G) & 7); }
-
-// Factor with local bit B on the 2^G rows of an orbit (canonical entry
-// order); the values of each row pair are loaded as the pairs are worked
-// through.
-template <typename T, int G, int CT, int B>
-__device__ __forceinline__ void bfo_stage(T (&xs)[1 << G][CT], const typename V2<T>::type* __restrict__ vp,
-                                          const int (&row)[1 << G]) {
-  using T2 = typename V2<T>::type;
-#pragma unroll
-  for (int k = 0; k < (1 << G); ++k) {
-    if ((k >> B) & 1) continue;
-    const int k1 = k | (1 << B);
-    const T2 va = __ldg(vp + row[k]), vb = __ldg(vp + row[k1]);
-#pragma unroll
-    for (int t = 0; t < CT; ++t) {
-      const T a = xs[k][t], c = xs[k1][t];
-      xs[k][t] = fmad(va.y, c, fmad(va.x, a, T(0)));
-      xs[k1][t] = fmad(vb.y, c, fmad(vb.x, a, T(0)));
-    }
-  }
-}
-
-// The same with the values of the orbit's rows already in registers.
-template <typename T, int G, int CT, int B>
-__device__ __forceinline__ void bfo_apply(T (&xs)[1 << G][CT], const typename V2<T>::type (&v)[1 << G]) {
-#pragma unroll
-  for (int k = 0; k < (1 << G); ++k) {
-    if ((k >> B) & 1) continue;
-    const int k1 = k | (1 << B);
-#pragma unroll
-    for (int t = 0; t < CT; ++t) {
-      const T a = xs[k][t], c = xs[k1][t];
-      xs[k][t] = fmad(v[k].y, c, fmad(v[k].x, a, T(0)));
-      xs[k1][t] = fmad(v[k1].y, c, fmad(v[k1].x, a, T(0)));
-    }
-  }
-}
-
-template <typename T, int G, int TC, int CT, int NT, int MINB>
-__global__ void __launch_bounds__(NT, MINB)
-    k_bfly_orbit(const __grid_constant__ BflyPlanO p, const T* __restrict__ X, int ldx, int ncols,
-                 T* __restrict__ Y, int ldy) {
-  using T2 = typename V2<T>::type;
-  constexpr int R = 1 << G;
-  constexpr int TPO = TC / CT;  // threads per orbit, CT columns each
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  T* tile = reinterpret_cast<T*>(smem_raw);  // n rows of TC values
-  const int n = p.n;
-  const int j0 = blockIdx.x * TC;
-  const int tid = threadIdx.x;
-  // X tile -> shared memory (coalesced along each column)
-  for (int r = tid; r < n; r += NT) {
-    T x[TC];
-#pragma unroll
-    for (int t = 0; t < TC; ++t) x[t] = (j0 + t < ncols) ? X[r + (long)(j0 + t) * ldx] : T(0);
-    st_row<T, TC>(tile + (long)bfo_slot<G>(r) * TC, x);
-  }
-  __syncthreads();
-  const int half = tid % TPO;
-  const int norb = n >> G;
-  for (int ps = 0; ps < p.npasses; ++ps) {
-    const bool last = ps + 1 == p.npasses;
-    const int first = p.pass_first[ps], nf = p.pass_n[ps];
-    int pos[G];
-#pragma unroll
-    for (int i = 0; i < G; ++i) pos[i] = p.pass_pos[ps][i];
-    for (int o = tid / TPO; o < norb; o += NT / TPO) {
-      // base: o with zero bits inserted at the span positions (ascending)
-      int base = o;
-#pragma unroll
-      for (int i = 0; i < G; ++i) base = ((base >> pos[i]) << (pos[i] + 1)) | (base & ((1 << pos[i]) - 1));
-      int row[R];
-#pragma unroll
-      for (int k = 0; k < R; ++k) {
-        int r = base;
-#pragma unroll
-        for (int i = 0; i < G; ++i) r += ((k >> i) & 1) << pos[i];
-        row[k] = r;
-      }
-      T xs[R][CT];
-      if (nf <= G) {
-        // every value of the pass's factors on the orbit's rows, loaded
-        // before any arithmetic so their latencies overlap
-        T2 v[G][R];
-#pragma unroll
-        for (int f = 0; f < G; ++f)
-          if (f < nf) {
-            const T2* vp = reinterpret_cast<const T2*>(p.val[first + f]);
-#pragma unroll
-            for (int k = 0; k < R; ++k) v[f][k] = __ldg(vp + row[k]);
-          }
-#pragma unroll
-        for (int k = 0; k < R; ++k) ld_piece<T, CT>(tile + (long)bfo_slot<G>(row[k]) * TC + half * CT, xs[k]);
-#pragma unroll
-        for (int f = 0; f < G; ++f) {
-          if (f >= nf) break;
-          const int b = p.step_bit[first + f];
-          if (b == 0) bfo_apply<T, G, CT, 0>(xs, v[f]);
-          else if (b == 1) bfo_apply<T, G, CT, 1>(xs, v[f]);
-          else if (G > 3 && b == 3) bfo_apply<T, G, CT, (G > 3 ? 3 : 0)>(xs, v[f]);
-          else bfo_apply<T, G, CT, 2>(xs, v[f]);
-        }
-      } else {
-#pragma unroll
-        for (int k = 0; k < R; ++k) ld_piece<T, CT>(tile + (long)bfo_slot<G>(row[k]) * TC + half * CT, xs[k]);
-        for (int f = 0; f < nf; ++f) {
-          const T2* vp = reinterpret_cast<const T2*>(p.val[first + f]);
-          const int b = p.step_bit[first + f];
-          if (b == 0) bfo_stage<T, G, CT, 0>(xs, vp, row);
-          else if (b == 1) bfo_stage<T, G, CT, 1>(xs, vp, row);
-          else if (G > 3 && b == 3) bfo_stage<T, G, CT, (G > 3 ? 3 : 0)>(xs, vp, row);
-          else bfo_stage<T, G, CT, 2>(xs, vp, row);
-        }
-      }
-      if (last && p.last_direct) {
-#pragma unroll
-        for (int k = 0; k < R; ++k)
-#pragma unroll
-          for (int t = 0; t < CT; ++t) {
-            const int j = j0 + half * CT + t;
-            if (j < ncols) Y[row[k] + (long)j * ldy] = xs[k][t];
-          }
-      } else {
-#pragma unroll
-        for (int k = 0; k < R; ++k) st_piece<T, CT>(tile + (long)bfo_slot<G>(row[k]) * TC + half * CT, xs[k]);
-      }
-    }
-    if (!last || !p.last_direct) __syncthreads();
-  }
-  if (!p.last_direct) {
-    // the last pass's rows are not consecutive across threads: copy out
-    // column by column
-    for (int r = tid; r < n; r += NT) {
-#pragma unroll
-      for (int t = 0; t < TC; ++t)
-        if (j0 + t < ncols) Y[r + (long)(j0 + t) * ldy] = tile[(long)bfo_slot<G>(r) * TC + t];
-    }
-  }
-}
-
-// Passes of consecutive steps (application order) spanning at most G
-// distinct strides; spans padded to G bit positions with the lowest unused
-// ones.  False when n < 2^G.
-static bool build_plan_orbit(fgb_faust* F, char op, int nfac, int G, BflyPlanO& p) {
-  const int J = (int)F->f.size();
-  p.n = F->f[0].rows;
-  p.g = G;
-  int logn = 0;
-  while ((1 << logn) < p.n) ++logn;
-  if (logn < G) return false;
-  std::vector<int> bit(nfac);
-  for (int s = 0; s < nfac; ++s) {
-    const int q = nfac - 1 - s;
-    const DevFactor& f = F->f[op == 'N' ? q : J - 1 - q];
-    p.val[s] = op == 'N' ? f.val : f.t_val;
-    int b = 0;
-    while ((1 << b) < f.bfly) ++b;
-    bit[s] = b;
-  }
-  p.npasses = 0;
-  for (int s = 0; s < nfac;) {
-    const int ps = p.npasses++;
-    std::vector<int> pos;
-    int e = s;
-    while (e < nfac) {
-      const bool have = std::find(pos.begin(), pos.end(), bit[e]) != pos.end();
-      if (!have && (int)pos.size() == G) break;
-      if (!have) pos.push_back(bit[e]);
-      ++e;
-    }
-    for (int b = 0; (int)pos.size() < G && b < logn; ++b)
-      if (std::find(pos.begin(), pos.end(), b) == pos.end()) pos.push_back(b);
-    std::sort(pos.begin(), pos.end());
-    p.pass_first[ps] = s;
-    p.pass_n[ps] = e - s;
-    for (int i = 0; i < BFO_MAXG; ++i) p.pass_pos[ps][i] = i < G ? pos[i] : 0;
-    for (int u = s; u < e; ++u) p.step_bit[u] = (int)(std::find(pos.begin(), pos.end(), bit[u]) - pos.begin());
-    s = e;
-  }
-  // the last pass stores Y straight from registers when 32 consecutive orbits
-  // are 32 consecutive rows (no span position below 5)
-  p.last_direct = p.pass_pos[p.npasses - 1][0] >= 5 ? 1 : 0;
-  return true;
-}
-
-template <typename T, int G, int TC, int CT, int NT, int MINB>
-static fgb_status launch_bfly_orbit(fgb_faust* F, const BflyPlanO& p, const T* X, int ldx, int ncols, T* Y,
-                                    int ldy) {
-  fgb_ctx* ctx = F->ctx;
-  const size_t smem = (size_t)p.n * TC * sizeof(T);
-  auto kern = k_bfly_orbit<T, G, TC, CT, NT, MINB>;
-  if (smem > 48 * 1024)
-    FGB_CUDA(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  const int tiles = (ncols + TC - 1) / TC;
-  kern<<<tiles, NT, smem, ctx->stream>>>(p, X, ldx, ncols, Y, ldy);
-  FGB_LAUNCHED(ctx);
-  return FGB_OK;
-}
-
 // ------------------------------------------------------------------ detection
 // bad[q] = 1 unless factor q is a butterfly factor of stride h[q].
 __global__ void k_bfly_detect(const int* __restrict__ rowptr, const int* __restrict__ colind, int n,

@@ -150,6 +150,23 @@ def test_butterfly_kernel_shuffled_and_repeated_strides(fgb, oracle, dtype):
         F.close()
 
 
+@pytest.mark.parametrize("nf,order,ncols", [
+    (10, [3, 0, 4, 1, 2, 7, 5, 9, 6, 8], 1000),     # shuffled strides
+    (11, [0, 0, 2, 1, 4, 3, 5, 8, 6, 10, 7, 9], 37),  # a repeated stride, ragged columns
+    (12, list(range(12)), 5),                          # fewer columns than one tile
+    (13, list(range(13)), 129),                        # 8192 rows (128 KB tile rows of 16 bytes)
+])
+def test_butterfly_kernel_orders_and_sizes(fgb, oracle, nf, order, ncols):
+    """FP32 butterfly chains in given application orders (order[0] applied
+    first), against the oracle's CSR chain bit for bit."""
+    rng = np.random.default_rng(nf * 7 + ncols)
+    facs = _bfly_perm_factors(nf, order[::-1], rng, np.float32)
+    F = fgb.Faust(facs, dtype=np.float32)
+    X = synth.dense_colmajor(1 << nf, ncols, rng, np.float32)
+    assert np.array_equal(_to_np(F.matmul_device(_colmajor_cuda(X), mode=3)), oracle.chain_mul(facs, X))
+    F.close()
+
+
 def test_butterfly_kernel_rejects_other_supports(fgb):
     rng = np.random.default_rng(4)
     facs = [synth.random_csr(64, 64, 2, rng) for _ in range(3)]
