@@ -3,7 +3,8 @@ scaling: every rank runs its own copy of the workload, no collective on the
 data path).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                  [--workload palm|csr_butterfly|csr_random|bsr]
+                  [--workload palm|csr_butterfly|csr_random|csr_random_f32|bsr|
+                              batched|warmstart|product]
 
 One JSON line is printed by rank 0.  Workloads (all inputs seeded, synthetic):
   palm           palm4msa2 FP64, target = Sylvester Hadamard 1024 / 32,
@@ -13,6 +14,9 @@ One JSON line is printed by rank 0.  Workloads (all inputs seeded, synthetic):
                  FP32, times X 4096 x 8192
   csr_random     5 CSR factors 1024^2 with 10 random nnz/row, FP64, times
                  X 1024 x 512
+  csr_random_f32 12 CSR factors 4096^2 with 2 random nnz/row, FP32, times
+                 X 4096 x 8192 (the butterfly chain's shape without its
+                 structure: the generic kernels where HBM is the bound)
   bsr            4 BSR factors 16384^2, 64x64 BF16 blocks, 8 blocks per block
                  row, times X 16384 x 4096 BF16 (FP32 accumulation)
   product        dense product (get_product, DEFAULT_L2R) of the 12 CSR
@@ -115,6 +119,11 @@ class FaustX:
             self.facs = synth.butterfly_faust_factors(12, rng, np.float32)
             self.n, self.ncols, self.np_dtype, self.tdtype = 4096, 8192, np.float32, torch.float32
             self.desc = "12 CSR butterfly factors 4096^2 (2 nnz/row) FP32 x X 4096x8192"
+            self.dtype = "f32"
+        elif name == "csr_random_f32":
+            self.facs = [synth.random_csr(4096, 4096, 2, rng, np.float32) for _ in range(12)]
+            self.n, self.ncols, self.np_dtype, self.tdtype = 4096, 8192, np.float32, torch.float32
+            self.desc = "12 CSR 4096^2 (2 random nnz/row) FP32 x X 4096x8192"
             self.dtype = "f32"
         elif name == "csr_random":
             self.facs = [synth.random_csr(1024, 1024, 10, rng) for _ in range(5)]
@@ -320,7 +329,7 @@ def cpu_baseline_faust_x(W, sample_cols=None):
                 "gflops": round(flops / dt / 1e9, 2),
                 "sample": "FP64 oracle chain on %d of %d columns of X (%.2f s); bytes counted as BF16 like the "
                           "GPU line" % (cols, W.ncols, dt)}
-    cols = sample_cols or (512 if W.name == "csr_butterfly" else W.ncols)
+    cols = sample_cols or (512 if W.name in ("csr_butterfly", "csr_random_f32") else W.ncols)
     rng = np.random.default_rng(7)
     X = np.asfortranarray(rng.standard_normal((W.n, cols)).astype(W.np_dtype))
     O.chain_mul(W.facs, X[:, :8])
@@ -916,7 +925,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="palm",
-                    choices=["palm", "batched", "csr_butterfly", "csr_random", "bsr", "warmstart", "product"])
+                    choices=["palm", "batched", "csr_butterfly", "csr_random", "csr_random_f32", "bsr", "warmstart",
+                             "product"])
     ap.add_argument("--batch-count", type=int, default=512)
     ap.add_argument("--ctas-per-sm", type=int, default=0,
                     help="batched: resident instances per SM (0 = the tuned table's choice)")
@@ -1058,6 +1068,9 @@ def reference_arm(args, world):
                 "e2e": {"value": v, "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     if W.name == "csr_butterfly":
         W.facs = synth.butterfly_faust_factors(12, rng, np.float32)
+        W.n, W.ncols, W.np_dtype = 4096, 8192, np.float32
+    elif W.name == "csr_random_f32":
+        W.facs = [synth.random_csr(4096, 4096, 2, rng, np.float32) for _ in range(12)]
         W.n, W.ncols, W.np_dtype = 4096, 8192, np.float32
     else:
         W.facs = [synth.random_csr(1024, 1024, 10, rng) for _ in range(5)]
