@@ -132,6 +132,13 @@ __device__ __forceinline__ void row_long_g(const int* __restrict__ ci, const T* 
 #pragma unroll
       for (int u = 0; u < G; ++u) P[u] = fmad(v, xv[u], P[u]);
     }
+    if (m == 0) {
+      // a row of one chunk: its partial is the result (the tree is not
+      // touched, so short rows never reach its spilled levels)
+#pragma unroll
+      for (int u = 0; u < G; ++u) out[u] = P[u];
+      return;
+    }
     T carry[G];
     t.push(m++, P, carry);
   }
