@@ -221,6 +221,231 @@ __global__ void __launch_bounds__(BF_THREADS, sizeof(T) == 4 ? 3 : 2)
   }
 }
 
+// ------------------------------------------------- radix kernel (FP32)
+// The full chain of an n = 2^L butterfly Faust applied in one of its two
+// natural orders: strides 1, 2, ..., n/2 in application order (F X with the
+// factors of butterfly_support, whose factor i has stride n / 2^(i+1)) or
+// n/2, ..., 1 (F^T X).  With the strides known at compile time a pass takes
+// PG consecutive factors: an orbit is the R = 2^PG rows base + {0..R-1} << lb,
+// held in registers for 4 columns, and every shared-memory address is a
+// per-thread base plus an immediate.  The first pass reads X from global
+// memory and the last writes Y, so the tile makes ceil(L/PG) - 1 trips
+// through shared memory.
+//
+// Shared tile: row r at 16-byte slot r + (r >> PG) (one pad slot per 2^PG
+// rows).  slot(base | off) = slot(base) + slot(off) for disjoint bits, and
+// the 8 rows one quarter-warp touches land in distinct bank groups for the
+// aligned stride groups of n = 4096.
+//
+// Factor values are read from a copy laid out in the kernel's order
+// (k_br_layout): for pass P, step j, row pair h and orbit o, one float4
+// holding (v0, v1) of the pair's two rows, orbits innermost, so each warp
+// load is 512 contiguous bytes.
+constexpr int BR_TC = 4;
+constexpr int BR_MAXT = 256;
+#ifndef FGB_BR_PG
+#define FGB_BR_PG 4
+#endif
+constexpr int BR_PG = FGB_BR_PG;
+
+template <int L, bool ASC, int PG>
+struct BrShape {
+  static constexpr int n = 1 << L;
+  static constexpr int NP = (L + PG - 1) / PG;
+  static constexpr int T = (n >> PG) < BR_MAXT ? (n >> PG) : BR_MAXT;
+  __host__ __device__ static constexpr int g(int P) { return L - PG * P < PG ? L - PG * P : PG; }
+  __host__ __device__ static constexpr int lb(int P) { return ASC ? PG * P : L - PG * P - g(P); }
+  __host__ __device__ static constexpr int slot(int r) { return r + (r >> PG); }
+  // float4 offset of pass P's values
+  __host__ __device__ static constexpr long voff(int P) { return P == 0 ? 0 : voff(P - 1) + (long)g(P - 1) * (n / 2); }
+  __host__ __device__ static constexpr int base(int P, int o) {
+    return (o & ((1 << lb(P)) - 1)) | ((o >> lb(P)) << (lb(P) + g(P)));
+  }
+};
+
+struct BrSrc {
+  const float2* val[32];  // step s (application order): (v0, v1) per row
+};
+
+template <int L, bool ASC, int PG>
+__global__ void k_br_layout(const __grid_constant__ BrSrc src, float4* __restrict__ out) {
+  using S = BrShape<L, ASC, PG>;
+  const long total = (long)L * (S::n / 2);
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < total; i += (long)gridDim.x * blockDim.x) {
+    int P = 0;
+    long rem = i;
+    while (rem >= (long)S::g(P) * (S::n / 2)) rem -= (long)S::g(P++) * (S::n / 2);
+    const int lb = S::lb(P), R = 1 << S::g(P), orb = S::n >> S::g(P);
+    const int o = (int)(rem % orb), jh = (int)(rem / orb);
+    const int j = jh / (R / 2), h = jh % (R / 2);
+    const int base = S::base(P, o);
+    const float2* v = src.val[PG * P + j];
+    const float2 a = v[base + ((2 * h) << lb)], b = v[base + ((2 * h + 1) << lb)];
+    out[i] = make_float4(a.x, a.y, b.x, b.y);
+  }
+}
+
+struct BrArgs {
+  const float4* vals;  // k_br_layout order
+  const float* X;
+  float* Y;
+  int ldx, ldy, ncols;
+};
+
+// R consecutive floats at p (R = 2, 4, 8 or 16; p aligned to min(R, 4) floats).
+template <int R>
+__device__ __forceinline__ void br_ld_run(const float* p, float (&v)[R]) {
+  if constexpr (R == 2) {
+    const float2 a = __ldcs(reinterpret_cast<const float2*>(p));
+    v[0] = a.x, v[1] = a.y;
+  } else {
+#pragma unroll
+    for (int q = 0; q < R / 4; ++q) {
+      const float4 a = __ldcs(reinterpret_cast<const float4*>(p) + q);
+      v[4 * q] = a.x, v[4 * q + 1] = a.y, v[4 * q + 2] = a.z, v[4 * q + 3] = a.w;
+    }
+  }
+}
+
+template <int R>
+__device__ __forceinline__ void br_st_run(float* p, const float (&v)[R]) {
+  if constexpr (R == 2) {
+    __stcs(reinterpret_cast<float2*>(p), make_float2(v[0], v[1]));
+  } else {
+#pragma unroll
+    for (int q = 0; q < R / 4; ++q)
+      __stcs(reinterpret_cast<float4*>(p) + q, make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]));
+  }
+}
+
+// Values of step j of pass P on the R rows of orbit o.
+template <int R, int ORB>
+__device__ __forceinline__ void br_vals(const float4* __restrict__ pv, int o, float2 (&v)[R]) {
+#pragma unroll
+  for (int h = 0; h < R / 2; ++h) {
+    const float4 a = __ldg(pv + h * ORB + o);
+    v[2 * h] = make_float2(a.x, a.y);
+    v[2 * h + 1] = make_float2(a.z, a.w);
+  }
+}
+
+// One factor on an orbit's rows: pairs (k, k | 2^B) of local rows.
+template <int R, int B>
+__device__ __forceinline__ void br_stage(float (&x)[R][BR_TC], const float2 (&v)[R]) {
+#pragma unroll
+  for (int k = 0; k < R; ++k) {
+    if ((k >> B) & 1) continue;
+    const int k1 = k | (1 << B);
+#pragma unroll
+    for (int t = 0; t < BR_TC; ++t) {
+      const float a = x[k][t], c = x[k1][t];
+      x[k][t] = fmad(v[k].y, c, fmad(v[k].x, a, 0.0f));
+      x[k1][t] = fmad(v[k1].y, c, fmad(v[k1].x, a, 0.0f));
+    }
+  }
+}
+
+// Steps J.. of a pass (local bit of step J's stride: J ascending, G-1-J
+// descending), the values of step J+1 loaded before step J's arithmetic.
+template <bool ASC, int G, int R, int ORB, int J>
+__device__ __forceinline__ void br_steps(const float4* __restrict__ pv, int o, float (&x)[R][BR_TC],
+                                         float2 (&v)[R]) {
+  float2 vn[R];
+  if constexpr (J + 1 < G) br_vals<R, ORB>(pv + (J + 1) * (R / 2) * ORB, o, vn);
+  br_stage<R, ASC ? J : G - 1 - J>(x, v);
+  if constexpr (J + 1 < G) {
+#pragma unroll
+    for (int k = 0; k < R; ++k) v[k] = vn[k];
+    br_steps<ASC, G, R, ORB, J + 1>(pv, o, x, v);
+  }
+}
+
+template <int L, bool ASC, int PG, int P>
+__device__ __forceinline__ void br_pass(const BrArgs& a, float* tile, int tid, int j0, bool full) {
+  using S = BrShape<L, ASC, PG>;
+  constexpr int G = S::g(P), LB = S::lb(P), R = 1 << G;
+  constexpr int ORB = S::n >> G;
+  constexpr int OPT = ORB / S::T;
+  constexpr bool FIRST = P == 0, LAST = P == S::NP - 1;
+  const float4* pv = a.vals + S::voff(P);
+#pragma unroll 1
+  for (int u = 0; u < OPT; ++u) {
+    const int o = tid + u * S::T;
+    const int base = S::base(P, o);
+    float2 v[R];
+    br_vals<R, ORB>(pv, o, v);
+    float x[R][BR_TC];
+    if constexpr (FIRST) {
+      if constexpr (LB == 0) {
+#pragma unroll
+        for (int t = 0; t < BR_TC; ++t) {
+          float c[R];
+          if (full || j0 + t < a.ncols) {
+            br_ld_run<R>(a.X + (long)(j0 + t) * a.ldx + base, c);
+          } else {
+#pragma unroll
+            for (int k = 0; k < R; ++k) c[k] = 0.0f;
+          }
+#pragma unroll
+          for (int k = 0; k < R; ++k) x[k][t] = c[k];
+        }
+      } else {
+#pragma unroll
+        for (int t = 0; t < BR_TC; ++t) {
+          const float* xc = a.X + (long)(j0 + t) * a.ldx + base;
+#pragma unroll
+          for (int k = 0; k < R; ++k) x[k][t] = (full || j0 + t < a.ncols) ? __ldcs(xc + (k << LB)) : 0.0f;
+        }
+      }
+    } else {
+      const float* s = tile + S::slot(base) * BR_TC;
+#pragma unroll
+      for (int k = 0; k < R; ++k) {
+        const float4 q = *reinterpret_cast<const float4*>(s + S::slot(k << LB) * BR_TC);
+        x[k][0] = q.x, x[k][1] = q.y, x[k][2] = q.z, x[k][3] = q.w;
+      }
+    }
+    br_steps<ASC, G, R, ORB, 0>(pv, o, x, v);
+    if constexpr (LAST) {
+      if constexpr (LB == 0) {
+#pragma unroll
+        for (int t = 0; t < BR_TC; ++t) {
+          if (!full && j0 + t >= a.ncols) continue;
+          float c[R];
+#pragma unroll
+          for (int k = 0; k < R; ++k) c[k] = x[k][t];
+          br_st_run<R>(a.Y + (long)(j0 + t) * a.ldy + base, c);
+        }
+      } else {
+#pragma unroll
+        for (int t = 0; t < BR_TC; ++t) {
+          if (!full && j0 + t >= a.ncols) continue;
+          float* yc = a.Y + (long)(j0 + t) * a.ldy + base;
+#pragma unroll
+          for (int k = 0; k < R; ++k) __stcs(yc + (k << LB), x[k][t]);
+        }
+      }
+    } else {
+      float* s = tile + S::slot(base) * BR_TC;
+#pragma unroll
+      for (int k = 0; k < R; ++k)
+        *reinterpret_cast<float4*>(s + S::slot(k << LB) * BR_TC) = make_float4(x[k][0], x[k][1], x[k][2], x[k][3]);
+    }
+  }
+  if constexpr (!LAST) {
+    __syncthreads();
+    br_pass<L, ASC, PG, P + 1>(a, tile, tid, j0, full);
+  }
+}
+
+// One block per tile of BR_TC columns.
+template <int L, bool ASC, int PG>
+__global__ void __launch_bounds__(BrShape<L, ASC, PG>::T, PG >= 4 ? 2 : 3) k_bfly_radix(const __grid_constant__ BrArgs a) {
+  extern __shared__ __align__(16) float br_tile[];
+  const int j0 = blockIdx.x * BR_TC;
+  br_pass<L, ASC, PG, 0>(a, br_tile, threadIdx.x, j0, j0 + BR_TC <= a.ncols);
+}
+
 // ------------------------------------------------------------------ detection
 // bad[q] = 1 unless factor q is a butterfly factor of stride h[q].
 __global__ void k_bfly_detect(const int* __restrict__ rowptr, const int* __restrict__ colind, int n,
@@ -306,11 +531,78 @@ static void build_plan(fgb_faust* F, char op, int nfac, BflyPlan& p) {
   }
 }
 
+template <int L, bool ASC>
+static fgb_status launch_radix(fgb_faust* F, int slot, const BflyPlan& p, BrArgs a) {
+  using S = BrShape<L, ASC, BR_PG>;
+  fgb_ctx* ctx = F->ctx;
+  if (!F->brv[slot]) {
+    BrSrc src;
+    for (int s = 0; s < L; ++s) src.val[s] = reinterpret_cast<const float2*>(p.val[s]);
+    void* d = nullptr;
+    FGB_TRY(dmalloc(ctx, &d, sizeof(float) * 2 * (size_t)L * S::n));
+    const long total = (long)L * (S::n / 2);
+    const int g = (int)std::min<long>(4L * ctx->sm_count, (total + 255) / 256);
+    k_br_layout<L, ASC, BR_PG><<<g, 256, 0, ctx->stream>>>(src, reinterpret_cast<float4*>(d));
+    FGB_LAUNCHED(ctx);
+    F->brv[slot] = d;
+  }
+  a.vals = reinterpret_cast<const float4*>(F->brv[slot]);
+  auto kern = k_bfly_radix<L, ASC, BR_PG>;
+  const size_t smem = (size_t)S::slot(S::n) * BR_TC * sizeof(float);
+  if (smem > 48 * 1024)
+    FGB_CUDA(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  const int tiles = (a.ncols + BR_TC - 1) / BR_TC;
+  kern<<<tiles, S::T, smem, ctx->stream>>>(a);
+  FGB_LAUNCHED(ctx);
+  return FGB_OK;
+}
+
+// The radix kernel when the plan is the whole chain of an FP32 butterfly
+// Faust with 2^8 <= n <= 2^12 in one of the two natural stride orders and
+// every pointer and leading dimension allows its 16-byte accesses; *ran
+// tells whether it ran.
+static fgb_status try_radix(fgb_faust* F, char op, const BflyPlan& p, const float* X, int ldx, int ncols, float* Y,
+                            int ldy, bool* ran) {
+  *ran = false;
+  int L = 0;
+  while ((1 << L) < p.n) ++L;
+  if (L < 8 || L > 12 || p.nsteps != L || (int)F->f.size() != L) return FGB_OK;
+  bool asc = true, desc = true;
+  for (int s = 0; s < L; ++s) {
+    asc = asc && p.stride[s] == (1 << s);
+    desc = desc && p.stride[s] == (1 << (L - 1 - s));
+  }
+  if (!asc && !desc) return FGB_OK;
+  if ((uintptr_t)X % 16 || (uintptr_t)Y % 16 || ldx % 4 || ldy % 4) return FGB_OK;
+  BrArgs a;
+  a.vals = nullptr;
+  a.X = X, a.Y = Y, a.ldx = ldx, a.ldy = ldy, a.ncols = ncols;
+  *ran = true;
+  const int slot = op == 'N' ? 0 : 1;
+  switch (L * 2 + (asc ? 1 : 0)) {
+    case 17: return launch_radix<8, true>(F, slot, p, a);
+    case 16: return launch_radix<8, false>(F, slot, p, a);
+    case 19: return launch_radix<9, true>(F, slot, p, a);
+    case 18: return launch_radix<9, false>(F, slot, p, a);
+    case 21: return launch_radix<10, true>(F, slot, p, a);
+    case 20: return launch_radix<10, false>(F, slot, p, a);
+    case 23: return launch_radix<11, true>(F, slot, p, a);
+    case 22: return launch_radix<11, false>(F, slot, p, a);
+    case 25: return launch_radix<12, true>(F, slot, p, a);
+    default: return launch_radix<12, false>(F, slot, p, a);
+  }
+}
+
 template <typename T, int TC>
 static fgb_status launch_bfly(fgb_faust* F, char op, int nfac, const T* X, int ldx, int ncols, T* Y, int ldy) {
   fgb_ctx* ctx = F->ctx;
   BflyPlan p;
   build_plan(F, op, nfac, p);
+  if constexpr (sizeof(T) == 4) {
+    bool ran = false;
+    FGB_TRY(try_radix(F, op, p, X, ldx, ncols, Y, ldy, &ran));
+    if (ran) return FGB_OK;
+  }
   const size_t smem = (size_t)p.n * TC * sizeof(T);
   auto kern = k_bfly_chain<T, TC>;
   if (smem > 48 * 1024)

@@ -323,6 +323,8 @@ fgb_faust::~fgb_faust() {
   fgb::dfree(chain_desc);
   fgb::dfree(chain_desc_t);
   fgb::dfree(pws);
+  fgb::dfree(brv[0]);
+  fgb::dfree(brv[1]);
   if (s_in) {
     cudaStreamSynchronize(s_in);
     cudaStreamSynchronize(s_out);

@@ -127,6 +127,9 @@ struct fgb_faust {
   // chain of transposed factors in reverse order).
   void* chain_desc = nullptr;
   void* chain_desc_t = nullptr;
+  // Factor values of the radix butterfly kernel in the order it reads them
+  // (for F and for F^T), built on first use.
+  void* brv[2] = {nullptr, nullptr};
   // Workspace of the dense product (intermediates and dense images).
   void* pws = nullptr;
   size_t pws_bytes = 0;
