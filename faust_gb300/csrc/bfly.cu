@@ -21,6 +21,7 @@
 
 #include "csr.cuh"
 #include "fgb_internal.cuh"
+#include "tc_common.cuh"
 
 namespace fgb {
 
@@ -222,40 +223,47 @@ __global__ void __launch_bounds__(BF_THREADS, sizeof(T) == 4 ? 3 : 2)
 }
 
 // ------------------------------------------------- radix kernel (FP32)
-// The full chain of an n = 2^L butterfly Faust applied in one of its two
-// natural orders: strides 1, 2, ..., n/2 in application order (F X with the
-// factors of butterfly_support, whose factor i has stride n / 2^(i+1)) or
-// n/2, ..., 1 (F^T X).  With the strides known at compile time a pass takes
-// PG consecutive factors: an orbit is the R = 2^PG rows base + {0..R-1} << lb,
-// held in registers for 4 columns, and every shared-memory address is a
-// per-thread base plus an immediate.  The first pass reads X from global
-// memory and the last writes Y, so the tile makes ceil(L/PG) - 1 trips
-// through shared memory.
+// The full chain of an n = 2^L butterfly Faust (1024 <= n <= 4096) applied in
+// one of its two natural orders: strides 1, 2, ..., n/2 in application order
+// (F X with the factors of butterfly_support, whose factor i has stride
+// n / 2^(i+1)) or n/2, ..., 1 (F^T X).  With the strides known at compile
+// time a pass takes four consecutive factors: an orbit is the 16 rows
+// base + {0..15} << lb, held in registers for the tile's 4 columns, and every
+// shared-memory address is a per-thread base plus an immediate.  A 4096-row
+// chain is three passes and two barriers.
 //
-// Shared tile: row r at 16-byte slot r + (r >> PG) (one pad slot per 2^PG
-// rows).  slot(base | off) = slot(base) + slot(off) for disjoint bits, and
-// the 8 rows one quarter-warp touches land in distinct bank groups for the
-// aligned stride groups of n = 4096.
+// Shared tile: column-major, column c at word c * CW, row r at word
+// r + 16 (r >> 8) (a 64-byte pad every 256 rows), CW = 4 (mod 32).  X arrives
+// by bulk asynchronous copies of 256-row runs (one per run and column, on an
+// mbarrier with a bounded wait), so no thread loads it.  Conflict-free
+// accesses: a pass whose rows are contiguous (lb = 0) reads 16-byte vectors
+// and lane l takes the columns in the order rotated by (l >> 1) & 3 (CW = 4
+// puts the columns 16 bytes apart in the banks); the pad moves rows r and
+// r + 256 16 banks apart for the scalar accesses of the lb = 4 pass.  The
+// last pass writes Y from registers (lb > 0: every warp store is 128
+// contiguous bytes) or through the tile and bulk stores (lb = 0).
 //
 // Factor values are read from a copy laid out in the kernel's order
-// (k_br_layout): for pass P, step j, row pair h and orbit o, one float4
-// holding (v0, v1) of the pair's two rows, orbits innermost, so each warp
-// load is 512 contiguous bytes.
+// (k_br_layout): for pass P, step j, butterfly pair h of the step's stage and
+// orbit o, one float4 holding (v0, v1) of the pair's two rows, orbits
+// innermost, so each warp load is 512 contiguous bytes and a pair's values
+// arrive in one load.
 constexpr int BR_TC = 4;
 constexpr int BR_MAXT = 256;
-#ifndef FGB_BR_PG
-#define FGB_BR_PG 4
-#endif
-constexpr int BR_PG = FGB_BR_PG;
+constexpr int BR_PG = 4;
 
-template <int L, bool ASC, int PG>
+template <int L, bool ASC>
 struct BrShape {
+  static constexpr int PG = BR_PG;
   static constexpr int n = 1 << L;
   static constexpr int NP = (L + PG - 1) / PG;
   static constexpr int T = (n >> PG) < BR_MAXT ? (n >> PG) : BR_MAXT;
+  static constexpr int NRUN = n / 256;                     // 256-row runs per column
+  static constexpr int CW = (n + 16 * NRUN + 31) / 32 * 32 + 4;  // column stride (words)
+  static constexpr size_t SMEM = (size_t)BR_TC * CW * 4 + 16;   // tile + mbarrier
   __host__ __device__ static constexpr int g(int P) { return L - PG * P < PG ? L - PG * P : PG; }
   __host__ __device__ static constexpr int lb(int P) { return ASC ? PG * P : L - PG * P - g(P); }
-  __host__ __device__ static constexpr int slot(int r) { return r + (r >> PG); }
+  __host__ __device__ static constexpr int word(int r) { return r + 16 * (r >> 8); }
   // float4 offset of pass P's values
   __host__ __device__ static constexpr long voff(int P) { return P == 0 ? 0 : voff(P - 1) + (long)g(P - 1) * (n / 2); }
   __host__ __device__ static constexpr int base(int P, int o) {
@@ -267,9 +275,9 @@ struct BrSrc {
   const float2* val[32];  // step s (application order): (v0, v1) per row
 };
 
-template <int L, bool ASC, int PG>
+template <int L, bool ASC>
 __global__ void k_br_layout(const __grid_constant__ BrSrc src, float4* __restrict__ out) {
-  using S = BrShape<L, ASC, PG>;
+  using S = BrShape<L, ASC>;
   const long total = (long)L * (S::n / 2);
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < total; i += (long)gridDim.x * blockDim.x) {
     int P = 0;
@@ -279,8 +287,11 @@ __global__ void k_br_layout(const __grid_constant__ BrSrc src, float4* __restric
     const int o = (int)(rem % orb), jh = (int)(rem / orb);
     const int j = jh / (R / 2), h = jh % (R / 2);
     const int base = S::base(P, o);
-    const float2* v = src.val[PG * P + j];
-    const float2 a = v[base + ((2 * h) << lb)], b = v[base + ((2 * h + 1) << lb)];
+    // the h-th pair (k, k | 2^B) of step j's stage, B its local bit
+    const int B = ASC ? j : S::g(P) - 1 - j;
+    const int k = ((h >> B) << (B + 1)) | (h & ((1 << B) - 1)), k1 = k | (1 << B);
+    const float2* v = src.val[S::PG * P + j];
+    const float2 a = v[base + (k << lb)], b = v[base + (k1 << lb)];
     out[i] = make_float4(a.x, a.y, b.x, b.y);
   }
 }
@@ -290,160 +301,219 @@ struct BrArgs {
   const float* X;
   float* Y;
   int ldx, ldy, ncols;
+  int* err;            // set when the bounded wait for the tile runs out
 };
 
-// R consecutive floats at p (R = 2, 4, 8 or 16; p aligned to min(R, 4) floats).
+// R contiguous words at p (R = 2, 4, 8 or 16; p aligned to min(R, 4) words).
 template <int R>
-__device__ __forceinline__ void br_ld_run(const float* p, float (&v)[R]) {
+__device__ __forceinline__ void br_lds_run(const float* p, float (&v)[R]) {
   if constexpr (R == 2) {
-    const float2 a = __ldcs(reinterpret_cast<const float2*>(p));
+    const float2 a = *reinterpret_cast<const float2*>(p);
     v[0] = a.x, v[1] = a.y;
   } else {
 #pragma unroll
     for (int q = 0; q < R / 4; ++q) {
-      const float4 a = __ldcs(reinterpret_cast<const float4*>(p) + q);
+      const float4 a = *(reinterpret_cast<const float4*>(p) + q);
       v[4 * q] = a.x, v[4 * q + 1] = a.y, v[4 * q + 2] = a.z, v[4 * q + 3] = a.w;
     }
   }
 }
 
 template <int R>
-__device__ __forceinline__ void br_st_run(float* p, const float (&v)[R]) {
+__device__ __forceinline__ void br_sts_run(float* p, const float (&v)[R]) {
   if constexpr (R == 2) {
-    __stcs(reinterpret_cast<float2*>(p), make_float2(v[0], v[1]));
+    *reinterpret_cast<float2*>(p) = make_float2(v[0], v[1]);
   } else {
 #pragma unroll
     for (int q = 0; q < R / 4; ++q)
-      __stcs(reinterpret_cast<float4*>(p) + q, make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]));
+      *(reinterpret_cast<float4*>(p) + q) = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
   }
 }
 
-// Values of step j of pass P on the R rows of orbit o.
-template <int R, int ORB>
-__device__ __forceinline__ void br_vals(const float4* __restrict__ pv, int o, float2 (&v)[R]) {
-#pragma unroll
-  for (int h = 0; h < R / 2; ++h) {
-    const float4 a = __ldg(pv + h * ORB + o);
-    v[2 * h] = make_float2(a.x, a.y);
-    v[2 * h + 1] = make_float2(a.z, a.w);
+// Items of a thread: (pass P, orbit round U); an item applies the pass's G
+// steps to orbit o = tid + U * T, i.e. NPAIR = G * R / 2 butterfly pairs whose
+// value float4s sit at pv + i * ORB + o (i = step * R / 2 + pair).  A ring of
+// D value loads runs ahead of the arithmetic across steps, items and passes
+// (values do not depend on the tile).
+template <int L, bool ASC, int P>
+struct BrItem {
+  using S = BrShape<L, ASC>;
+  static constexpr int G = S::g(P), LB = S::lb(P), R = 1 << G;
+  static constexpr int ORB = S::n >> G;
+  static constexpr int OPT = ORB / S::T;
+  static constexpr int NPAIR = G * R / 2;
+};
+
+template <int L, bool ASC, int P = 0>
+__host__ __device__ constexpr int br_min_pairs() {
+  if constexpr (P + 1 < BrShape<L, ASC>::NP) {
+    constexpr int a = BrItem<L, ASC, P>::NPAIR, b = br_min_pairs<L, ASC, P + 1>();
+    return a < b ? a : b;
+  } else {
+    return BrItem<L, ASC, P>::NPAIR;
   }
 }
 
-// One factor on an orbit's rows: pairs (k, k | 2^B) of local rows.
-template <int R, int B>
-__device__ __forceinline__ void br_stage(float (&x)[R][BR_TC], const float2 (&v)[R]) {
+template <int L, bool ASC>
+__host__ __device__ constexpr int br_ring() {
+  return br_min_pairs<L, ASC>() < 8 ? br_min_pairs<L, ASC>() : 8;
+}
+
+// Value float4 of pair i of item (P, U) for thread tid.
+template <int L, bool ASC, int P, int U>
+__device__ __forceinline__ float4 br_val(const float4* __restrict__ vals, int tid, int i) {
+  using I = BrItem<L, ASC, P>;
+  return __ldg(vals + BrShape<L, ASC>::voff(P) + (long)i * I::ORB + tid + U * BrShape<L, ASC>::T);
+}
+
+// C0: pairs of the thread's earlier items; pair i of this item is in ring
+// slot (C0 + i) % D.
+template <int L, bool ASC, int P, int U, int D, int C0>
+__device__ __forceinline__ void br_item(const BrArgs& a, float* tile, int tid, int j0, float4 (&ring)[D]) {
+  using S = BrShape<L, ASC>;
+  using I = BrItem<L, ASC, P>;
+  constexpr int G = I::G, LB = I::LB, R = I::R, NPAIR = I::NPAIR;
+  constexpr bool LAST_PASS = P == S::NP - 1;
+  constexpr bool LAST_ITEM = LAST_PASS && U + 1 == I::OPT;
+  constexpr int NP2 = U + 1 < I::OPT ? P : P + 1;  // next item
+  constexpr int NU2 = U + 1 < I::OPT ? U + 1 : 0;
+  const int o = tid + U * S::T;
+  const int base = S::base(P, o);
+  // contiguous rows: columns in an order rotated per lane pair
+  const int rot = LB == 0 ? (tid >> 1) & 3 : 0;
+  float x[R][BR_TC];
+  const float* rowp = tile + S::word(base);
 #pragma unroll
-  for (int k = 0; k < R; ++k) {
-    if ((k >> B) & 1) continue;
-    const int k1 = k | (1 << B);
+  for (int t = 0; t < BR_TC; ++t) {
+    const float* cp = rowp + ((t + rot) & 3) * S::CW;
+    if constexpr (LB == 0) {
+      float c[R];
+      br_lds_run<R>(cp, c);
+#pragma unroll
+      for (int k = 0; k < R; ++k) x[k][t] = c[k];
+    } else {
+#pragma unroll
+      for (int k = 0; k < R; ++k) x[k][t] = cp[S::word(k << LB)];
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < NPAIR; ++i) {
+    const int slot = (C0 + i) % D;
+    const float4 w = ring[slot];
+    if (i + D < NPAIR) {
+      ring[slot] = br_val<L, ASC, P, U>(a.vals, tid, i + D);
+    } else if constexpr (!LAST_ITEM) {
+      ring[slot] = br_val<L, ASC, NP2, NU2>(a.vals, tid, i + D - NPAIR);
+    }
+    const int J = i / (R / 2), h = i % (R / 2);
+    const int B = ASC ? J : G - 1 - J;
+    const int k = ((h >> B) << (B + 1)) | (h & ((1 << B) - 1)), k1 = k | (1 << B);
 #pragma unroll
     for (int t = 0; t < BR_TC; ++t) {
-      const float a = x[k][t], c = x[k1][t];
-      x[k][t] = fmad(v[k].y, c, fmad(v[k].x, a, 0.0f));
-      x[k1][t] = fmad(v[k1].y, c, fmad(v[k1].x, a, 0.0f));
+      const float p0 = x[k][t], p1 = x[k1][t];
+      x[k][t] = fmad(w.y, p1, fmad(w.x, p0, 0.0f));
+      x[k1][t] = fmad(w.w, p1, fmad(w.z, p0, 0.0f));
     }
+  }
+  if constexpr (LAST_PASS && LB > 0) {
+#pragma unroll
+    for (int t = 0; t < BR_TC; ++t) {
+      if (j0 + t >= a.ncols) continue;
+      float* yc = a.Y + (long)(j0 + t) * a.ldy + base;
+#pragma unroll
+      for (int k = 0; k < R; ++k) __stcs(yc + (k << LB), x[k][t]);
+    }
+  } else {
+    float* wp = tile + S::word(base);
+#pragma unroll
+    for (int t = 0; t < BR_TC; ++t) {
+      float* cp = wp + ((t + rot) & 3) * S::CW;
+      if constexpr (LB == 0) {
+        float c[R];
+#pragma unroll
+        for (int k = 0; k < R; ++k) c[k] = x[k][t];
+        br_sts_run<R>(cp, c);
+      } else {
+#pragma unroll
+        for (int k = 0; k < R; ++k) cp[S::word(k << LB)] = x[k][t];
+      }
+    }
+  }
+  if constexpr (!LAST_ITEM) {
+    if constexpr (NP2 != P) __syncthreads();
+    br_item<L, ASC, NP2, NU2, D, C0 + NPAIR>(a, tile, tid, j0, ring);
   }
 }
 
-// Steps J.. of a pass (local bit of step J's stride: J ascending, G-1-J
-// descending), the values of step J+1 loaded before step J's arithmetic.
-template <bool ASC, int G, int R, int ORB, int J>
-__device__ __forceinline__ void br_steps(const float4* __restrict__ pv, int o, float (&x)[R][BR_TC],
-                                         float2 (&v)[R]) {
-  float2 vn[R];
-  if constexpr (J + 1 < G) br_vals<R, ORB>(pv + (J + 1) * (R / 2) * ORB, o, vn);
-  br_stage<R, ASC ? J : G - 1 - J>(x, v);
-  if constexpr (J + 1 < G) {
-#pragma unroll
-    for (int k = 0; k < R; ++k) v[k] = vn[k];
-    br_steps<ASC, G, R, ORB, J + 1>(pv, o, x, v);
-  }
+__device__ __forceinline__ void br_bulk_load(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                   tc::su32(dst)),
+               "l"(src), "r"(bytes), "r"(tc::su32(bar))
+               : "memory");
 }
 
-template <int L, bool ASC, int PG, int P>
-__device__ __forceinline__ void br_pass(const BrArgs& a, float* tile, int tid, int j0, bool full) {
-  using S = BrShape<L, ASC, PG>;
-  constexpr int G = S::g(P), LB = S::lb(P), R = 1 << G;
-  constexpr int ORB = S::n >> G;
-  constexpr int OPT = ORB / S::T;
-  constexpr bool FIRST = P == 0, LAST = P == S::NP - 1;
-  const float4* pv = a.vals + S::voff(P);
-#pragma unroll 1
-  for (int u = 0; u < OPT; ++u) {
-    const int o = tid + u * S::T;
-    const int base = S::base(P, o);
-    float2 v[R];
-    br_vals<R, ORB>(pv, o, v);
-    float x[R][BR_TC];
-    if constexpr (FIRST) {
-      if constexpr (LB == 0) {
-#pragma unroll
-        for (int t = 0; t < BR_TC; ++t) {
-          float c[R];
-          if (full || j0 + t < a.ncols) {
-            br_ld_run<R>(a.X + (long)(j0 + t) * a.ldx + base, c);
-          } else {
-#pragma unroll
-            for (int k = 0; k < R; ++k) c[k] = 0.0f;
-          }
-#pragma unroll
-          for (int k = 0; k < R; ++k) x[k][t] = c[k];
-        }
-      } else {
-#pragma unroll
-        for (int t = 0; t < BR_TC; ++t) {
-          const float* xc = a.X + (long)(j0 + t) * a.ldx + base;
-#pragma unroll
-          for (int k = 0; k < R; ++k) x[k][t] = (full || j0 + t < a.ncols) ? __ldcs(xc + (k << LB)) : 0.0f;
-        }
-      }
-    } else {
-      const float* s = tile + S::slot(base) * BR_TC;
-#pragma unroll
-      for (int k = 0; k < R; ++k) {
-        const float4 q = *reinterpret_cast<const float4*>(s + S::slot(k << LB) * BR_TC);
-        x[k][0] = q.x, x[k][1] = q.y, x[k][2] = q.z, x[k][3] = q.w;
-      }
-    }
-    br_steps<ASC, G, R, ORB, 0>(pv, o, x, v);
-    if constexpr (LAST) {
-      if constexpr (LB == 0) {
-#pragma unroll
-        for (int t = 0; t < BR_TC; ++t) {
-          if (!full && j0 + t >= a.ncols) continue;
-          float c[R];
-#pragma unroll
-          for (int k = 0; k < R; ++k) c[k] = x[k][t];
-          br_st_run<R>(a.Y + (long)(j0 + t) * a.ldy + base, c);
-        }
-      } else {
-#pragma unroll
-        for (int t = 0; t < BR_TC; ++t) {
-          if (!full && j0 + t >= a.ncols) continue;
-          float* yc = a.Y + (long)(j0 + t) * a.ldy + base;
-#pragma unroll
-          for (int k = 0; k < R; ++k) __stcs(yc + (k << LB), x[k][t]);
-        }
-      }
-    } else {
-      float* s = tile + S::slot(base) * BR_TC;
-#pragma unroll
-      for (int k = 0; k < R; ++k)
-        *reinterpret_cast<float4*>(s + S::slot(k << LB) * BR_TC) = make_float4(x[k][0], x[k][1], x[k][2], x[k][3]);
-    }
-  }
-  if constexpr (!LAST) {
-    __syncthreads();
-    br_pass<L, ASC, PG, P + 1>(a, tile, tid, j0, full);
-  }
+__device__ __forceinline__ void br_bulk_store(void* dst, const void* src, uint32_t bytes) {
+  asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(dst), "r"(tc::su32(src)),
+               "r"(bytes)
+               : "memory");
 }
 
 // One block per tile of BR_TC columns.
-template <int L, bool ASC, int PG>
-__global__ void __launch_bounds__(BrShape<L, ASC, PG>::T, PG >= 4 ? 2 : 3) k_bfly_radix(const __grid_constant__ BrArgs a) {
-  extern __shared__ __align__(16) float br_tile[];
+template <int L, bool ASC>
+__global__ void __launch_bounds__(BrShape<L, ASC>::T, 2) k_bfly_radix(const __grid_constant__ BrArgs a) {
+  using S = BrShape<L, ASC>;
+  extern __shared__ __align__(128) float br_tile[];
+  uint64_t* bar = reinterpret_cast<uint64_t*>(br_tile + BR_TC * S::CW);
+  const int tid = threadIdx.x;
   const int j0 = blockIdx.x * BR_TC;
-  br_pass<L, ASC, PG, 0>(a, br_tile, threadIdx.x, j0, j0 + BR_TC <= a.ncols);
+  const int nc = min(BR_TC, a.ncols - j0);
+  if (tid == 0) {
+    tc::mbar_init(bar, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  if (tid < 32) {
+    if (tid == 0) tc::mbar_expect_tx(bar, (uint32_t)(nc * S::n * 4));
+    __syncwarp();
+    for (int i = tid; i < nc * S::NRUN; i += 32) {
+      const int c = i / S::NRUN, g = i % S::NRUN;
+      br_bulk_load(br_tile + c * S::CW + S::word(g * 256), a.X + (long)(j0 + c) * a.ldx + g * 256, 1024, bar);
+    }
+  }
+  // the first value loads go out while the tile is in flight
+  constexpr int D = br_ring<L, ASC>();
+  float4 ring[D];
+#pragma unroll
+  for (int i = 0; i < D; ++i) ring[i] = br_val<L, ASC, 0, 0>(a.vals, tid, i);
+  bool ok = false;
+  for (unsigned i = 0; i < tc::WAIT_LIMIT; ++i)
+    if (tc::mbar_try_wait(bar, 0)) {
+      ok = true;
+      break;
+    }
+  if (__syncthreads_or(!ok)) {
+    if (tid == 0) {
+      atomicExch(a.err, 1);
+      // the copies in flight land before the shared memory is released
+      for (unsigned i = 0; i < tc::WAIT_LIMIT && !tc::mbar_try_wait(bar, 0); ++i) {
+      }
+    }
+    return;
+  }
+  br_item<L, ASC, 0, 0, D, 0>(a, br_tile, tid, j0, ring);
+  if constexpr (S::lb(S::NP - 1) == 0) {
+    // the last pass left Y's tile in shared memory
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    __syncthreads();
+    if (tid < 32) {
+      for (int i = tid; i < nc * S::NRUN; i += 32) {
+        const int c = i / S::NRUN, g = i % S::NRUN;
+        br_bulk_store(a.Y + (long)(j0 + c) * a.ldy + g * 256, br_tile + c * S::CW + S::word(g * 256), 1024);
+      }
+      asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+      asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
+    }
+  }
 }
 
 // ------------------------------------------------------------------ detection
@@ -533,7 +603,7 @@ static void build_plan(fgb_faust* F, char op, int nfac, BflyPlan& p) {
 
 template <int L, bool ASC>
 static fgb_status launch_radix(fgb_faust* F, int slot, const BflyPlan& p, BrArgs a) {
-  using S = BrShape<L, ASC, BR_PG>;
+  using S = BrShape<L, ASC>;
   fgb_ctx* ctx = F->ctx;
   if (!F->brv[slot]) {
     BrSrc src;
@@ -542,23 +612,22 @@ static fgb_status launch_radix(fgb_faust* F, int slot, const BflyPlan& p, BrArgs
     FGB_TRY(dmalloc(ctx, &d, sizeof(float) * 2 * (size_t)L * S::n));
     const long total = (long)L * (S::n / 2);
     const int g = (int)std::min<long>(4L * ctx->sm_count, (total + 255) / 256);
-    k_br_layout<L, ASC, BR_PG><<<g, 256, 0, ctx->stream>>>(src, reinterpret_cast<float4*>(d));
+    k_br_layout<L, ASC><<<g, 256, 0, ctx->stream>>>(src, reinterpret_cast<float4*>(d));
     FGB_LAUNCHED(ctx);
     F->brv[slot] = d;
   }
   a.vals = reinterpret_cast<const float4*>(F->brv[slot]);
-  auto kern = k_bfly_radix<L, ASC, BR_PG>;
-  const size_t smem = (size_t)S::slot(S::n) * BR_TC * sizeof(float);
-  if (smem > 48 * 1024)
-    FGB_CUDA(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  FGB_TRY(kernel_err_word(ctx, &a.err));
+  auto kern = k_bfly_radix<L, ASC>;
+  FGB_TRY(smem_opt_in(ctx, (const void*)kern, S::SMEM));
   const int tiles = (a.ncols + BR_TC - 1) / BR_TC;
-  kern<<<tiles, S::T, smem, ctx->stream>>>(a);
+  kern<<<tiles, S::T, S::SMEM, ctx->stream>>>(a);
   FGB_LAUNCHED(ctx);
   return FGB_OK;
 }
 
 // The radix kernel when the plan is the whole chain of an FP32 butterfly
-// Faust with 2^8 <= n <= 2^12 in one of the two natural stride orders and
+// Faust with 1024 <= n <= 4096 in one of the two natural stride orders and
 // every pointer and leading dimension allows its 16-byte accesses; *ran
 // tells whether it ran.
 static fgb_status try_radix(fgb_faust* F, char op, const BflyPlan& p, const float* X, int ldx, int ncols, float* Y,
@@ -566,7 +635,7 @@ static fgb_status try_radix(fgb_faust* F, char op, const BflyPlan& p, const floa
   *ran = false;
   int L = 0;
   while ((1 << L) < p.n) ++L;
-  if (L < 8 || L > 12 || p.nsteps != L || (int)F->f.size() != L) return FGB_OK;
+  if (L < 10 || L > 12 || p.nsteps != L || (int)F->f.size() != L) return FGB_OK;
   bool asc = true, desc = true;
   for (int s = 0; s < L; ++s) {
     asc = asc && p.stride[s] == (1 << s);
@@ -576,14 +645,11 @@ static fgb_status try_radix(fgb_faust* F, char op, const BflyPlan& p, const floa
   if ((uintptr_t)X % 16 || (uintptr_t)Y % 16 || ldx % 4 || ldy % 4) return FGB_OK;
   BrArgs a;
   a.vals = nullptr;
+  a.err = nullptr;
   a.X = X, a.Y = Y, a.ldx = ldx, a.ldy = ldy, a.ncols = ncols;
   *ran = true;
   const int slot = op == 'N' ? 0 : 1;
   switch (L * 2 + (asc ? 1 : 0)) {
-    case 17: return launch_radix<8, true>(F, slot, p, a);
-    case 16: return launch_radix<8, false>(F, slot, p, a);
-    case 19: return launch_radix<9, true>(F, slot, p, a);
-    case 18: return launch_radix<9, false>(F, slot, p, a);
     case 21: return launch_radix<10, true>(F, slot, p, a);
     case 20: return launch_radix<10, false>(F, slot, p, a);
     case 23: return launch_radix<11, true>(F, slot, p, a);
@@ -605,8 +671,7 @@ static fgb_status launch_bfly(fgb_faust* F, char op, int nfac, const T* X, int l
   }
   const size_t smem = (size_t)p.n * TC * sizeof(T);
   auto kern = k_bfly_chain<T, TC>;
-  if (smem > 48 * 1024)
-    FGB_CUDA(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  FGB_TRY(smem_opt_in(ctx, (const void*)kern, smem));
   const int tiles = (ncols + TC - 1) / TC;
   kern<<<tiles, BF_THREADS, smem, ctx->stream>>>(p, X, ldx, ncols, Y, ldy);
   FGB_LAUNCHED(ctx);

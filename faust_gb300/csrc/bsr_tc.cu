@@ -332,8 +332,6 @@ fgb_status bsr_tc_prepare(fgb_ctx* ctx, DevFactor& f) {
   return FGB_OK;
 }
 
-static int* g_err = nullptr;
-
 fgb_status launch_bsr_tc(fgb_ctx* ctx, const DevFactor& f, const __nv_bfloat16* X, int ldx, int ncols,
                          __nv_bfloat16* Y, int ldy, bool* taken) {
   *taken = false;
@@ -359,35 +357,16 @@ fgb_status launch_bsr_tc(fgb_ctx* ctx, const DevFactor& f, const __nv_bfloat16* 
   if (!tc::make_map_bf16(&mx, X, (uint64_t)f.cols, (uint64_t)ncols, (uint64_t)ldx * 2, tc::BLK, tc::TM)) return FGB_OK;
   if (!tc::make_map_bf16(&mb, blocks, (uint64_t)tc::BLK, (uint64_t)f.nnz * tc::BLK, tc::BLK * 2, tc::BLK, tc::BLK))
     return FGB_OK;
-  if (!g_err) {
-    FGB_TRY(dmalloc(ctx, (void**)&g_err, sizeof(int)));
-    FGB_CUDA(ctx, cudaMemset(g_err, 0, sizeof(int)));
-  }
+  int* err = nullptr;
+  FGB_TRY(kernel_err_word(ctx, &err));
   auto kern = two ? tc::k_bsr_tc<2> : tc::k_bsr_tc<1>;
-  static size_t attr[2] = {0, 0};
-  if (smem > attr[two]) {
-    FGB_CUDA(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    attr[two] = smem;
-  }
+  FGB_TRY(smem_opt_in(ctx, (const void*)kern, smem));
   const long items = (long)nbr * mtiles;
   const int grid = (int)std::min<long>(items, ctx->sm_count);
   kern<<<grid, tc::THREADS, smem, ctx->stream>>>(mx, mb, f.rowptr, f.colind, nbr, f.nnz, stage_idx ? 1 : 0, mtiles,
-                                                 Y, (long)ldy, g_err);
+                                                 Y, (long)ldy, err);
   FGB_LAUNCHED(ctx);
   *taken = true;
-  return FGB_OK;
-}
-
-// Error flag of the tensor-core kernel (a bounded wait ran out); cleared on read.
-fgb_status bsr_tc_status(fgb_ctx* ctx) {
-  if (!g_err) return FGB_OK;
-  int h = 0;
-  FGB_CUDA(ctx, cudaMemcpyAsync(&h, g_err, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
-  FGB_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-  if (h) {
-    FGB_CUDA(ctx, cudaMemset(g_err, 0, sizeof(int)));
-    return fail(ctx, FGB_ERR_TIMEOUT, "BSR tensor-core kernel: a bounded wait ran out");
-  }
   return FGB_OK;
 }
 

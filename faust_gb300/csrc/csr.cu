@@ -242,7 +242,7 @@ static fgb_status launch_spmm_tc(fgb_ctx* ctx, const int* rowptr, const int* col
     rblocks = (int)std::max(1L, std::min((long)((rows + SPMM_THREADS - 1) / SPMM_THREADS), want / std::max(1, tiles)));
   }
   auto kern = k_csr_spmm<T, TC, STAGED>;
-  if (smem > 48 * 1024) FGB_CUDA(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  FGB_TRY(smem_opt_in(ctx, (const void*)kern, smem));
   dim3 grid(tiles, rblocks);
   kern<<<grid, SPMM_THREADS, smem, ctx->stream>>>(rowptr, colind, val, rows, inner, X, ldx, ncols, Y, ldy, epi,
                                                    long_row);
@@ -445,7 +445,7 @@ static fgb_status launch_chain_tc(fgb_ctx* ctx, const ChainDesc* d_desc, int nfa
                                   T* Y, int ldy, int maxdim) {
   const size_t smem = 2 * (size_t)maxdim * TC * sizeof(T);
   auto kern = k_csr_chain_fused<T, TC>;
-  if (smem > 48 * 1024) FGB_CUDA(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  FGB_TRY(smem_opt_in(ctx, (const void*)kern, smem));
   const int tiles = (ncols + TC - 1) / TC;
   kern<<<tiles, CHAIN_THREADS, smem, ctx->stream>>>(d_desc, nfac, X, ldx, ncols, Y, ldy, maxdim);
   FGB_LAUNCHED(ctx);

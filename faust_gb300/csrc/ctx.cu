@@ -1,6 +1,9 @@
 // ctx.cu — context, errors and allocation helpers of libfaust_gb300.
 #include <cstdarg>
 #include <cstring>
+#include <map>
+#include <mutex>
+#include <utility>
 
 #include "fgb_internal.cuh"
 
@@ -42,6 +45,42 @@ fgb_status dmalloc(fgb_ctx* ctx, void** p, size_t bytes) {
     *p = nullptr;
     return cuda_check(ctx, e, "cudaMalloc");
   }
+  return FGB_OK;
+}
+
+fgb_status kernel_err_word(fgb_ctx* ctx, int** out) {
+  if (!ctx->kerr) {
+    void* d = nullptr;
+    FGB_TRY(dmalloc(ctx, &d, sizeof(int)));
+    cudaError_t e = cudaMemsetAsync(d, 0, sizeof(int), ctx->stream);
+    if (e != cudaSuccess) {
+      cudaFree(d);
+      return cuda_check(ctx, e, "kernel error word");
+    }
+    ctx->kerr = (int*)d;
+  }
+  *out = ctx->kerr;
+  return FGB_OK;
+}
+
+fgb_status check_kernel_err(fgb_ctx* ctx) {
+  if (!ctx->kerr) return FGB_OK;
+  int h = 0;
+  FGB_CUDA(ctx, cudaMemcpy(&h, ctx->kerr, sizeof(int), cudaMemcpyDeviceToHost));
+  if (!h) return FGB_OK;
+  FGB_CUDA(ctx, cudaMemset(ctx->kerr, 0, sizeof(int)));
+  return fail(ctx, FGB_ERR_TIMEOUT, "a bounded device-side wait ran out in a tensor-core or butterfly kernel");
+}
+
+fgb_status smem_opt_in(fgb_ctx* ctx, const void* func, size_t bytes) {
+  if (bytes <= 48 * 1024) return FGB_OK;
+  static std::mutex mu;
+  static std::map<std::pair<const void*, int>, size_t> done;
+  std::lock_guard<std::mutex> lock(mu);
+  size_t& cur = done[{func, ctx->device}];
+  if (cur >= bytes) return FGB_OK;
+  FGB_CUDA(ctx, cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+  cur = bytes;
   return FGB_OK;
 }
 
@@ -107,6 +146,7 @@ fgb_status fgb_ctx_destroy(fgb_ctx* ctx) {
   if (ctx->rand_dev) cudaFree(ctx->rand_dev);
   if (ctx->x0_d) cudaFree(ctx->x0_d);
   if (ctx->x0_f) cudaFree(ctx->x0_f);
+  if (ctx->kerr) cudaFree(ctx->kerr);
   if (ctx->s_long) {
     cudaStreamSynchronize(ctx->s_long);
     cudaStreamDestroy(ctx->s_long);
@@ -122,7 +162,7 @@ const char* fgb_last_error(const fgb_ctx* ctx) { return ctx ? ctx->err.c_str() :
 fgb_status fgb_ctx_synchronize(fgb_ctx* ctx) {
   if (!ctx) return FGB_ERR_INVALID_ARG;
   FGB_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-  return FGB_OK;
+  return check_kernel_err(ctx);
 }
 
 fgb_status fgb_cancel(fgb_ctx* ctx) {

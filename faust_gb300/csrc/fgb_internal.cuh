@@ -44,6 +44,10 @@ struct fgb_ctx {
   // Cooperative grid of the projection's radix select on this context's
   // device (FP32, FP64), computed on first use.
   int rs_coop_blocks[2] = {0, 0};
+  // Device word set by kernels whose bounded waits ran out (the tcgen05 BSR
+  // and GEMM kernels, the radix butterfly kernel); read and cleared by
+  // fgb_ctx_synchronize.
+  int* kerr = nullptr;
 };
 
 namespace fgb {
@@ -80,6 +84,14 @@ size_t dtype_size(fgb_dtype t);
 // Device allocation helpers (report OOM as FGB_ERR_OOM).
 fgb_status dmalloc(fgb_ctx* ctx, void** p, size_t bytes);
 void dfree(void* p);
+// The context's kernel error word (allocated and zeroed on first use).
+fgb_status kernel_err_word(fgb_ctx* ctx, int** out);
+// After a synchronisation of the context's stream: FGB_ERR_TIMEOUT (and the
+// word cleared) when a kernel recorded an expired bounded wait.
+fgb_status check_kernel_err(fgb_ctx* ctx);
+// Raises the kernel's dynamic shared-memory limit on the context's device to
+// at least `bytes` (a per device and kernel attribute, only ever raised).
+fgb_status smem_opt_in(fgb_ctx* ctx, const void* func, size_t bytes);
 
 // ---------------------------------------------------------------- device factors
 // A sparse factor resident on the device.  CSR keeps, beside its own arrays,

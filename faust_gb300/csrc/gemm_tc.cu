@@ -254,8 +254,6 @@ __global__ void k_bias_act(const float* __restrict__ in, long ldi, int M, int N,
 
 }  // namespace tc
 
-static int* g_gemm_err = nullptr;
-
 fgb_status launch_gemm_bf16(fgb_ctx* ctx, int M, int N, int K, const void* A, long lda, const void* B, long ldb,
                             void* C, long ldc, int c_f32, const float* bias, int act, int split_k, float* work) {
   using namespace tc;
@@ -269,23 +267,17 @@ fgb_status launch_gemm_bf16(fgb_ctx* ctx, int M, int N, int K, const void* A, lo
   if (!make_map_bf16(&ma, A, (uint64_t)K, (uint64_t)M, (uint64_t)lda * 2, GK, GM) ||
       !make_map_bf16(&mb, B, (uint64_t)K, (uint64_t)N, (uint64_t)ldb * 2, GK, GN))
     return fail(ctx, FGB_ERR_CUDA, "gemm: tensor map creation failed");
-  if (!g_gemm_err) {
-    FGB_TRY(dmalloc(ctx, (void**)&g_gemm_err, sizeof(int)));
-    FGB_CUDA(ctx, cudaMemset(g_gemm_err, 0, sizeof(int)));
-  }
+  int* err = nullptr;
+  FGB_TRY(kernel_err_word(ctx, &err));
   const size_t smem = G_STAGES * G_STAGE + sizeof(GShared) + 1024;
-  static bool attr = false;
-  if (!attr) {
-    FGB_CUDA(ctx, cudaFuncSetAttribute(k_gemm_tn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    attr = true;
-  }
+  FGB_TRY(smem_opt_in(ctx, (const void*)k_gemm_tn, smem));
   const int ksteps = K / GK;
   split_k = std::max(1, std::min(split_k, ksteps));
   const long tiles = (long)(M / GM) * (N / GN);
   const long items = tiles * split_k;
   const int grid = (int)std::min<long>(items, ctx->sm_count);
   if (split_k == 1) {
-    k_gemm_tn<<<grid, G_THREADS, smem, ctx->stream>>>(ma, mb, M, N, K, 1, C, ldc, c_f32, bias, act, 0, g_gemm_err);
+    k_gemm_tn<<<grid, G_THREADS, smem, ctx->stream>>>(ma, mb, M, N, K, 1, C, ldc, c_f32, bias, act, 0, err);
     FGB_LAUNCHED(ctx);
     return FGB_OK;
   }
@@ -299,23 +291,11 @@ fgb_status launch_gemm_bf16(fgb_ctx* ctx, int M, int N, int K, const void* A, lo
     FGB_CUDA(ctx, cudaMemsetAsync(acc, 0, (size_t)M * N * 4, ctx->stream));
   }
   k_gemm_tn<<<grid, G_THREADS, smem, ctx->stream>>>(ma, mb, M, N, K, split_k, acc, lda_acc, 1, nullptr, ACT_NONE, 1,
-                                                     g_gemm_err);
+                                                     err);
   FGB_LAUNCHED(ctx);
   if (acc != (float*)C) {
     k_bias_act<<<4 * ctx->sm_count, 256, 0, ctx->stream>>>(acc, N, M, N, bias, act, C, ldc, c_f32);
     FGB_LAUNCHED(ctx);
-  }
-  return FGB_OK;
-}
-
-fgb_status gemm_status(fgb_ctx* ctx) {
-  if (!g_gemm_err) return FGB_OK;
-  int h = 0;
-  FGB_CUDA(ctx, cudaMemcpyAsync(&h, g_gemm_err, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
-  FGB_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-  if (h) {
-    FGB_CUDA(ctx, cudaMemset(g_gemm_err, 0, sizeof(int)));
-    return fail(ctx, FGB_ERR_TIMEOUT, "tensor-core GEMM: a bounded wait ran out");
   }
   return FGB_OK;
 }

@@ -1376,9 +1376,7 @@ static fgb_status batched_impl(fgb_ctx* ctx, fgb_dtype dt, int nprob, const fgb_
     const bool three = per_sm >= 3;
     auto kern_d = three ? k_palm_batched<T, double, 3> : k_palm_batched<T, double, 2>;
     auto kern_f = three ? k_palm_batched<T, float, 3> : k_palm_batched<T, float, 2>;
-    if (s == FGB_OK)
-      s = cuda_check(ctx, cudaFuncSetAttribute(fp64n ? (const void*)kern_d : (const void*)kern_f,
-                                               cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem), "attr");
+    if (s == FGB_OK) s = smem_opt_in(ctx, fp64n ? (const void*)kern_d : (const void*)kern_f, smem);
     // The launch sequence: queue reset, seeding (when asked), the persistent
     // kernel, captured as one CUDA graph and launched as a unit.  It runs on
     // the context's stream, or on a private stream when the context uses the

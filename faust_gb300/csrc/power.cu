@@ -379,11 +379,7 @@ static fgb_status launch_pi_t(fgb_ctx* ctx, const PIChain& a, const PIChain& b, 
   // the rest of shared memory stages the chain's CSR arrays
   const size_t smem = cap;
   auto kern = k_power_iteration<TF, TC>;
-  static thread_local size_t attr_set = 0;
-  if (smem > attr_set) {
-    FGB_CUDA(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    attr_set = smem;
-  }
+  FGB_TRY(smem_opt_in(ctx, (const void*)kern, smem));
   const TC* x0 = sizeof(TC) == 8 ? (const TC*)(const void*)ctx->x0_d : (const TC*)(const void*)ctx->x0_f;
   (void)d_rand;
   kern<<<palm.ext_norm ? 1 : 2, PI_THREADS, smem, stream>>>(a, b, nullptr, max_iter, (TC)thr, x0, d_out, palm, maxn,
@@ -416,11 +412,7 @@ static fgb_status launch_pi_many_t(fgb_ctx* ctx, const PIChain* d_chains, int nc
     return fail(ctx, FGB_ERR_NOT_SUPPORTED, "power iteration: vector of %d entries does not fit on chip", maxn);
   const size_t smem = cap;
   auto kern = k_power_iteration<TF, TC>;
-  static thread_local size_t attr_set = 0;
-  if (smem > attr_set) {
-    FGB_CUDA(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    attr_set = smem;
-  }
+  FGB_TRY(smem_opt_in(ctx, (const void*)kern, smem));
   const TC* x0 = sizeof(TC) == 8 ? (const TC*)(const void*)ctx->x0_d : (const TC*)(const void*)ctx->x0_f;
   PIChain none;
   std::memset(&none, 0, sizeof(none));

@@ -67,6 +67,10 @@ typedef struct fgb_faust fgb_faust;
 fgb_status fgb_ctx_create(int device, void* cuda_stream, fgb_ctx** out);
 fgb_status fgb_ctx_destroy(fgb_ctx* ctx);
 const char* fgb_last_error(const fgb_ctx* ctx);
+/* Waits for the context's stream.  Returns FGB_ERR_TIMEOUT (and clears the
+ * record) when a kernel of the context gave up a bounded device-side wait
+ * since the last call (the tensor-core BSR and GEMM kernels, the radix
+ * butterfly kernel); the outputs of that launch are then undefined. */
 fgb_status fgb_ctx_synchronize(fgb_ctx* ctx);
 /* Asks a running palm4msa2 call of this context to stop at the next outer
  * iteration (the reference's palm4msa2 SIGINT flag,
