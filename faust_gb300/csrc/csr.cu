@@ -181,10 +181,20 @@ __device__ __forceinline__ int long_rows_scan(const int* __restrict__ rowptr, in
   return *cnt;
 }
 
+// d_max: the longest row on the device (null or negative: unknown); a factor
+// without long rows ends the kernel at once.
+__device__ __forceinline__ bool no_long_rows(const int* d_max) {
+  if (!d_max) return false;
+  const int m = __ldg(d_max);
+  return m >= 0 && m <= ROW_CHUNK;
+}
+
 template <typename T>
 __global__ void __launch_bounds__(256)
     k_csr_spmm_long(const int* __restrict__ rowptr, const int* __restrict__ colind, const T* __restrict__ val,
-                    int rows, const T* __restrict__ X, int ldx, int ncols, T* __restrict__ Y, int ldy, Epi<T> epi) {
+                    int rows, const T* __restrict__ X, int ldx, int ncols, T* __restrict__ Y, int ldy, Epi<T> epi,
+                    const int* __restrict__ d_max) {
+  if (no_long_rows(d_max)) return;
   __shared__ T roots[ROW_GROUPS * 32];
   __shared__ int list[256], cnt;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -210,7 +220,8 @@ template <typename T>
 __global__ void __launch_bounds__(256)
     k_dense_csrT_long(const T* __restrict__ X, int ldx, int xrows, const int* __restrict__ rowptr,
                       const int* __restrict__ colind, const T* __restrict__ val, int srows, T* __restrict__ Y, int ldy,
-                      Epi<T> epi) {
+                      Epi<T> epi, const int* __restrict__ d_max) {
+  if (no_long_rows(d_max)) return;
   __shared__ T roots[ROW_GROUPS * 32];
   __shared__ int list[256], cnt;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -271,7 +282,8 @@ static fgb_status long_join(fgb_ctx* ctx) {
 
 template <typename T>
 fgb_status launch_csr_spmm(fgb_ctx* ctx, const int* rowptr, const int* colind, const T* val, int rows, int inner,
-                           const T* X, int ldx, int ncols, T* Y, int ldy, const Epi<T>& epi, int max_row) {
+                           const T* X, int ldx, int ncols, T* Y, int ldy, const Epi<T>& epi, int max_row,
+                           const int* d_max_row) {
   if (rows == 0 || ncols == 0) return FGB_OK;
   constexpr int TC = 16 / sizeof(T) * 2;  // 8 floats or 4 doubles per thread
   const size_t staged = (size_t)inner * TC * sizeof(T);
@@ -284,7 +296,7 @@ fgb_status launch_csr_spmm(fgb_ctx* ctx, const int* rowptr, const int* colind, c
     cudaStream_t s;
     FGB_TRY(long_fork(ctx, &s));
     dim3 g((unsigned)((ncols + 31) / 32), (unsigned)std::min((rows + 255) / 256 * 4, 16));
-    k_csr_spmm_long<T><<<g, 256, 0, s>>>(rowptr, colind, val, rows, X, ldx, ncols, Y, ldy, epi);
+    k_csr_spmm_long<T><<<g, 256, 0, s>>>(rowptr, colind, val, rows, X, ldx, ncols, Y, ldy, epi, d_max_row);
     FGB_LAUNCHED(ctx);
   }
   // Stage when the tile fits comfortably and there are enough tiles to fill
@@ -324,7 +336,8 @@ __global__ void __launch_bounds__(SPMM_THREADS)
 
 template <typename T>
 fgb_status launch_dense_csrT(fgb_ctx* ctx, const T* X, int ldx, int xrows, const int* rowptr, const int* colind,
-                             const T* val, int srows, int scols, T* Y, int ldy, const Epi<T>& epi, int max_row) {
+                             const T* val, int srows, int scols, T* Y, int ldy, const Epi<T>& epi, int max_row,
+                             const int* d_max_row) {
   (void)scols;
   if (srows == 0 || xrows == 0) return FGB_OK;
   const bool has_long = max_row < 0 || max_row > ROW_CHUNK;
@@ -332,7 +345,7 @@ fgb_status launch_dense_csrT(fgb_ctx* ctx, const T* X, int ldx, int xrows, const
     cudaStream_t s;
     FGB_TRY(long_fork(ctx, &s));
     dim3 g((unsigned)((xrows + 31) / 32), (unsigned)std::min((srows + 255) / 256 * 4, 16));
-    k_dense_csrT_long<T><<<g, 256, 0, s>>>(X, ldx, xrows, rowptr, colind, val, srows, Y, ldy, epi);
+    k_dense_csrT_long<T><<<g, 256, 0, s>>>(X, ldx, xrows, rowptr, colind, val, srows, Y, ldy, epi, d_max_row);
     FGB_LAUNCHED(ctx);
   }
   // rows of at most ROW_CHUNK entries: one block per output column
@@ -597,13 +610,14 @@ fgb_status launch_csr_to_dense(fgb_ctx* ctx, const DevFactor& f, T* out) {
 }
 
 template fgb_status launch_csr_spmm<float>(fgb_ctx*, const int*, const int*, const float*, int, int, const float*, int,
-                                           int, float*, int, const Epi<float>&, int);
+                                           int, float*, int, const Epi<float>&, int, const int*);
 template fgb_status launch_csr_spmm<double>(fgb_ctx*, const int*, const int*, const double*, int, int, const double*,
-                                            int, int, double*, int, const Epi<double>&, int);
+                                            int, int, double*, int, const Epi<double>&, int, const int*);
 template fgb_status launch_dense_csrT<float>(fgb_ctx*, const float*, int, int, const int*, const int*, const float*,
-                                             int, int, float*, int, const Epi<float>&, int);
+                                             int, int, float*, int, const Epi<float>&, int, const int*);
 template fgb_status launch_dense_csrT<double>(fgb_ctx*, const double*, int, int, const int*, const int*,
-                                              const double*, int, int, double*, int, const Epi<double>&, int);
+                                              const double*, int, int, double*, int, const Epi<double>&, int,
+                                              const int*);
 template fgb_status launch_csr_to_dense<float>(fgb_ctx*, const DevFactor&, float*);
 template fgb_status launch_csr_to_dense<double>(fgb_ctx*, const DevFactor&, double*);
 

@@ -35,14 +35,17 @@ __device__ __forceinline__ T epi_apply(const Epi<T>& e, T acc, long i, long j, T
 // Launch helpers (csr.cu).
 // Y = S X  (S: rows x inner CSR; X: inner x ncols; Y: rows x ncols).
 // max_row: longest row of S if known (rows of more than 16 entries run in a
-// separate kernel), -1 when unknown.
+// separate kernel), -1 when unknown; d_max_row: the same figure in device
+// memory (or null), read by that kernel, which ends at once without long rows.
 template <typename T>
 fgb_status launch_csr_spmm(fgb_ctx* ctx, const int* rowptr, const int* colind, const T* val, int rows, int inner,
-                           const T* X, int ldx, int ncols, T* Y, int ldy, const Epi<T>& epi, int max_row = -1);
+                           const T* X, int ldx, int ncols, T* Y, int ldy, const Epi<T>& epi, int max_row = -1,
+                           const int* d_max_row = nullptr);
 // Y = X S^T given the CSR of S (S: srows x scols; X: xrows x scols; Y: xrows x srows).
 template <typename T>
 fgb_status launch_dense_csrT(fgb_ctx* ctx, const T* X, int ldx, int xrows, const int* rowptr, const int* colind,
-                             const T* val, int srows, int scols, T* Y, int ldy, const Epi<T>& epi, int max_row = -1);
+                             const T* val, int srows, int scols, T* Y, int ldy, const Epi<T>& epi, int max_row = -1,
+                             const int* d_max_row = nullptr);
 // Dense column-major (ld = rows) image of a CSR factor.
 template <typename T>
 fgb_status launch_csr_to_dense(fgb_ctx* ctx, const DevFactor& f, T* out);

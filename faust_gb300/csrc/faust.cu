@@ -22,6 +22,7 @@ void free_factor(DevFactor& f) {
   dfree(f.t_rowptr);
   dfree(f.t_colind);
   dfree(f.t_val);
+  dfree(f.d_maxrc);
   f = DevFactor();
 }
 
@@ -138,10 +139,12 @@ static fgb_status mul_per_factor(fgb_faust* F, const void* X, int ldx, int ncols
       FGB_TRY(launch_bsr_spmm(ctx, f, (const __nv_bfloat16*)in, ldin, ncols, (__nv_bfloat16*)out, ldout));
     } else if (F->dtype == FGB_F64) {
       FGB_TRY(launch_csr_spmm<double>(ctx, f.rowptr, f.colind, (const double*)f.val, f.rows, f.cols,
-                                      (const double*)in, ldin, ncols, (double*)out, ldout, Epi<double>(), f.max_row));
+                                      (const double*)in, ldin, ncols, (double*)out, ldout, Epi<double>(), f.max_row,
+                                      f.d_maxrc));
     } else {
       FGB_TRY(launch_csr_spmm<float>(ctx, f.rowptr, f.colind, (const float*)f.val, f.rows, f.cols,
-                                     (const float*)in, ldin, ncols, (float*)out, ldout, Epi<float>(), f.max_row));
+                                     (const float*)in, ldin, ncols, (float*)out, ldout, Epi<float>(), f.max_row,
+                                     f.d_maxrc));
     }
     in = out;
     ldin = ldout;
@@ -187,10 +190,12 @@ static fgb_status mul_per_factor_t(fgb_faust* F, const void* X, int ldx, int nco
     int ldout = (k == J - 1) ? ldy : f.cols;
     if (F->dtype == FGB_F64) {
       FGB_TRY(launch_csr_spmm<double>(ctx, f.t_rowptr, f.t_colind, (const double*)f.t_val, f.cols, f.rows,
-                                      (const double*)in, ldin, ncols, (double*)out, ldout, Epi<double>(), f.max_col));
+                                      (const double*)in, ldin, ncols, (double*)out, ldout, Epi<double>(), f.max_col,
+                                      f.d_maxrc ? f.d_maxrc + 1 : nullptr));
     } else {
       FGB_TRY(launch_csr_spmm<float>(ctx, f.t_rowptr, f.t_colind, (const float*)f.t_val, f.cols, f.rows,
-                                     (const float*)in, ldin, ncols, (float*)out, ldout, Epi<float>(), f.max_col));
+                                     (const float*)in, ldin, ncols, (float*)out, ldout, Epi<float>(), f.max_col,
+                                     f.d_maxrc ? f.d_maxrc + 1 : nullptr));
     }
     in = out;
     ldin = ldout;
@@ -294,12 +299,13 @@ fgb_status faust_apply_prefix(fgb_faust* F, char op, int nfac, const void* X, in
     void* out = (q == 0) ? Y : F->buf[(nfac - 1 - q) & 1];
     const int ldout = (q == 0) ? ldy : std::max(1, rows);
     const int ml = tr ? f.max_col : f.max_row;
+    const int* dml = f.d_maxrc ? f.d_maxrc + (tr ? 1 : 0) : nullptr;
     if (F->dtype == FGB_F64)
       FGB_TRY(launch_csr_spmm<double>(ctx, rp, ci, (const double*)v, rows, inner, (const double*)in, ldin, ncols,
-                                      (double*)out, ldout, Epi<double>(), ml));
+                                      (double*)out, ldout, Epi<double>(), ml, dml));
     else
       FGB_TRY(launch_csr_spmm<float>(ctx, rp, ci, (const float*)v, rows, inner, (const float*)in, ldin, ncols,
-                                     (float*)out, ldout, Epi<float>(), ml));
+                                     (float*)out, ldout, Epi<float>(), ml, dml));
     in = out;
     ldin = ldout;
   }

@@ -117,6 +117,9 @@ struct DevFactor {
   int bfly = -1;
   // Longest row / column (entries), -1 when not known on the host.
   int max_row = -1, max_col = -1;
+  // The same two figures on the device (written by the dense -> CSR
+  // conversion) for factors the host cannot see, e.g. PALM's, or null.
+  int* d_maxrc = nullptr;
 };
 
 }  // namespace fgb

@@ -200,27 +200,28 @@ struct Palm {
 
   int grid(long n) const { return (int)std::max(1L, std::min((n + 255) / 256, 4L * ctx->sm_count)); }
 
-  fgb_status spmm(const int* rp, const int* ci, const T* v, int rows, int inner, const T* X, int ldx, int ncols,
-                  T* Y, int ldy, const Epi<T>& e) {
-    return launch_csr_spmm<T>(ctx, rp, ci, v, rows, inner, X, ldx, ncols, Y, ldy, e);
-  }
+  // The factors' longest row (d_maxrc[0]) and column (d_maxrc[1]) are on the
+  // device; the long-row kernels read them and end at once without long rows.
+  static const int* dmax(const DevFactor& f, int which) { return f.d_maxrc ? f.d_maxrc + which : nullptr; }
   // Y = S X
   fgb_status mul_S(const DevFactor& f, const T* X, int ncols, T* Y, const Epi<T>& e) {
-    return spmm(f.rowptr, f.colind, (const T*)f.val, f.rows, f.cols, X, f.cols, ncols, Y, f.rows, e);
+    return launch_csr_spmm<T>(ctx, f.rowptr, f.colind, (const T*)f.val, f.rows, f.cols, X, f.cols, ncols, Y, f.rows, e,
+                              -1, dmax(f, 0));
   }
   // Y = S^H X (transpose CSR)
   fgb_status mul_SH(const DevFactor& f, const T* X, int ncols, T* Y, const Epi<T>& e) {
-    return spmm(f.t_rowptr, f.t_colind, (const T*)f.t_val, f.cols, f.rows, X, f.rows, ncols, Y, f.cols, e);
+    return launch_csr_spmm<T>(ctx, f.t_rowptr, f.t_colind, (const T*)f.t_val, f.cols, f.rows, X, f.rows, ncols, Y,
+                              f.cols, e, -1, dmax(f, 1));
   }
   // Y = X S (X: xrows x f.rows)
   fgb_status mul_XS(const T* X, int xrows, const DevFactor& f, T* Y, const Epi<T>& e) {
     return launch_dense_csrT<T>(ctx, X, xrows, xrows, f.t_rowptr, f.t_colind, (const T*)f.t_val, f.cols, f.rows, Y,
-                                xrows, e);
+                                xrows, e, -1, dmax(f, 1));
   }
   // Y = X S^H (X: xrows x f.cols)
   fgb_status mul_XSH(const T* X, int xrows, const DevFactor& f, T* Y, const Epi<T>& e) {
     return launch_dense_csrT<T>(ctx, X, xrows, xrows, f.rowptr, f.colind, (const T*)f.val, f.rows, f.cols, Y, xrows,
-                                e);
+                                e, -1, dmax(f, 0));
   }
   fgb_status dense_of(const DevFactor& f, T* out) { return launch_csr_to_dense<T>(ctx, f, out); }
 
@@ -270,6 +271,7 @@ struct Palm {
       FGB_TRY(dmalloc(ctx, (void**)&f.t_rowptr, sizeof(int) * (f.cols + 1)));
       FGB_TRY(dmalloc(ctx, (void**)&f.t_colind, sizeof(int) * f.cap));
       FGB_TRY(dmalloc(ctx, &f.t_val, es * f.cap));
+      FGB_TRY(dmalloc(ctx, (void**)&f.d_maxrc, 2 * sizeof(int)));
       if (cons[i].kind == FGB_SUPP) {
         FGB_TRY(dmalloc(ctx, (void**)&supp[i], es * (size_t)f.rows * f.cols));
         FGB_CUDA(ctx, cudaMemcpyAsync(supp[i], cons[i].supp, es * (size_t)f.rows * f.cols, cudaMemcpyHostToDevice,

@@ -1782,10 +1782,33 @@ __device__ void block_excl_scan(const int* __restrict__ cnt, int n, int* __restr
 // kernels stay inside the arrays.
 __global__ void __launch_bounds__(1024) k_d2c_scan_rc(const int* __restrict__ rcnt, int rows, const int* __restrict__ ccnt,
                                                       int cols, int* __restrict__ rowptr, int* __restrict__ t_rowptr,
-                                                      int with_cols, int cap, int* status) {
+                                                      int with_cols, int cap, int* status, int* maxrc) {
   __shared__ int part[32];
+  __shared__ int mx[2];
   block_excl_scan(rcnt, rows, rowptr, part);
   if (with_cols) block_excl_scan(ccnt, cols, t_rowptr, part);
+  if (maxrc) {
+    // longest row and column, for the long-row kernels of the products
+    if (threadIdx.x < 2) mx[threadIdx.x] = 0;
+    __syncthreads();
+    int a = 0, b = 0;
+    for (int r = threadIdx.x; r < rows; r += blockDim.x) a = max(a, rcnt[r]);
+    if (with_cols)
+      for (int c = threadIdx.x; c < cols; c += blockDim.x) b = max(b, ccnt[c]);
+    for (int s = 16; s >= 1; s >>= 1) {
+      a = max(a, __shfl_xor_sync(0xffffffffu, a, s));
+      b = max(b, __shfl_xor_sync(0xffffffffu, b, s));
+    }
+    if ((threadIdx.x & 31) == 0) {
+      atomicMax(&mx[0], a);
+      atomicMax(&mx[1], b);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      maxrc[0] = mx[0];
+      maxrc[1] = with_cols ? mx[1] : -1;
+    }
+  }
   if (rowptr[rows] > cap) {
     for (int r = threadIdx.x; r <= rows; r += blockDim.x) rowptr[r] = min(rowptr[r], cap);
     if (with_cols)
@@ -1844,7 +1867,7 @@ fgb_status launch_dense_to_csr(fgb_ctx* ctx, ProxWork& w, const T* M, DevFactor&
   k_d2c_count_rc<T><<<blocks, 256, 0, ctx->stream>>>(M, f.rows, f.cols, rcnt, ccnt, with_cols);
   FGB_LAUNCHED(ctx);
   k_d2c_scan_rc<<<1, 1024, 0, ctx->stream>>>(rcnt, f.rows, ccnt, f.cols, f.rowptr, f.t_rowptr, with_cols, f.cap,
-                                             status);
+                                             status, f.d_maxrc);
   FGB_LAUNCHED(ctx);
   k_d2c_write_rc<T><<<blocks, 256, 0, ctx->stream>>>(M, f.rows, f.cols, f.rowptr, f.colind, (T*)f.val, f.t_rowptr,
                                                      f.t_colind, (T*)f.t_val, f.cap, with_cols);
