@@ -30,6 +30,8 @@ constexpr int PX_THREADS = 256;
 constexpr int RS_MAX_PASSES = 6;  // passes of the single-launch radix select
 constexpr int RS_LIST_CAP = 32768;  // bucket size the radix select finishes in one block
 constexpr int LINE_KMAX = 64;
+constexpr int SQ_SEG = 16;                                // segments of a lane's values
+constexpr int SQ_PER = (int)(CR_CHUNK / CR_LANES / SQ_SEG);  // values per segment
 
 __device__ __forceinline__ unsigned long long mag_key(double v) {
   return (unsigned long long)__double_as_longlong(v) & 0x7fffffffffffffffULL;
@@ -75,6 +77,11 @@ fgb_status prox_work_reserve(fgb_ctx* ctx, ProxWork& w, long elems, int rows) {
   FGB_TRY(dmalloc(ctx, (void**)&w.hist_passes, sizeof(unsigned) * (RS_MAX_PASSES * 2048 + 4)));
   FGB_CUDA(ctx, cudaMemsetAsync(w.hist_passes, 0, sizeof(unsigned) * (RS_MAX_PASSES * 2048 + 4), ctx->stream));
   FGB_TRY(dmalloc(ctx, (void**)&w.rs_list, sizeof(unsigned long long) * RS_LIST_CAP));
+  w.sq_chunks = (elems + CR_CHUNK - 1) / CR_CHUNK;
+  FGB_TRY(dmalloc(ctx, (void**)&w.sq_seg, sizeof(double) * (size_t)std::max(1L, w.sq_chunks) * SQ_SEG * CR_LANES));
+  FGB_TRY(dmalloc(ctx, (void**)&w.sq_mask, sizeof(unsigned) * (size_t)std::max(1L, w.sq_chunks) * CR_LANES));
+  FGB_CUDA(ctx, cudaMemsetAsync(w.sq_mask, 0, sizeof(unsigned) * (size_t)std::max(1L, w.sq_chunks) * CR_LANES,
+                                ctx->stream));
   w.cap_elems = elems;
   w.cap_rows = rows;
   w.growable = 1;
@@ -98,6 +105,8 @@ void prox_work_free(ProxWork& w) {
   dfree(w.wbound);
   dfree(w.wcount);
   dfree(w.heap2);
+  dfree(w.sq_seg);
+  dfree(w.sq_mask);
   w = ProxWork();
 }
 
@@ -1388,6 +1397,70 @@ __global__ void __launch_bounds__(PX_THREADS) k_chunk_sumsq(const T* __restrict_
   if (threadIdx.x == 0) reinterpret_cast<T*>(partials)[blockIdx.x] = part;
 }
 
+// The same canonical sum of squares split over SQ_SEG blocks per chunk, for
+// the sparse results of the projections: block (c, s) computes, for every
+// lane t of chunk c, the sequential fma over the lane's values SQ_PER * s ..
+// SQ_PER * s + SQ_PER - 1 from +0 (zeros add +0 to a non-negative partial
+// and are skipped) and marks the segments that held a non-zero;
+// k_sumsq_lanes continues each lane's chain from its first marked segment
+// over the later marked ones, in order, then adds the lanes by the tree.
+// Most lanes of a sparse block have no or one marked segment, so the chain
+// rarely reloads anything; a dense block costs what k_chunk_sumsq costs.
+template <typename T>
+__global__ void __launch_bounds__(CR_LANES) k_sumsq_seg(const T* __restrict__ M, long N, double* __restrict__ seg,
+                                                         unsigned* __restrict__ mask) {
+  const int c = blockIdx.x / SQ_SEG, s = blockIdx.x % SQ_SEG, t = threadIdx.x;
+  const long base = (long)c * CR_CHUNK + t + (long)s * SQ_PER * CR_LANES;
+  T v[SQ_PER];
+#pragma unroll
+  for (int u = 0; u < SQ_PER; ++u) {
+    const long i = base + (long)u * CR_LANES;
+    v[u] = i < N ? M[i] : T(0);
+  }
+  T acc = T(0);
+  bool nz = false;
+#pragma unroll
+  for (int u = 0; u < SQ_PER; ++u)
+    if (mag_key(v[u]) != 0) {
+      acc = fmad(v[u], v[u], acc);
+      nz = true;
+    }
+  if (nz) {
+    reinterpret_cast<T*>(seg)[((long)c * SQ_SEG + s) * CR_LANES + t] = acc;
+    atomicOr(&mask[c * CR_LANES + t], 1u << s);
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(CR_LANES) k_sumsq_lanes(const T* __restrict__ M, long N,
+                                                           const double* __restrict__ seg, unsigned* __restrict__ mask,
+                                                           double* partials) {
+  __shared__ T lane[CR_LANES];
+  const int c = blockIdx.x, t = threadIdx.x;
+  unsigned m = mask[c * CR_LANES + t];
+  T acc = T(0);
+  if (m) {
+    acc = reinterpret_cast<const T*>(seg)[((long)c * SQ_SEG + (__ffs(m) - 1)) * CR_LANES + t];
+    m &= m - 1;
+    while (m) {
+      const int s = __ffs(m) - 1;
+      m &= m - 1;
+      const long base = (long)c * CR_CHUNK + t + (long)s * SQ_PER * CR_LANES;
+      for (int u = 0; u < SQ_PER; ++u) {
+        const long i = base + (long)u * CR_LANES;
+        if (i < N) {
+          const T x = M[i];
+          if (mag_key(x) != 0) acc = fmad(x, x, acc);
+        }
+      }
+    }
+    mask[c * CR_LANES + t] = 0;  // zero again for the next use
+  }
+  lane[t] = acc;
+  const T part = lane_tree_256(lane);
+  if (t == 0) reinterpret_cast<T*>(partials)[c] = part;
+}
+
 // MatDense::normalize (faust_MatDense.hpp:1225-1250): scale = FPP(1.0/norm),
 // domain_error (here FGB_ERR_ZERO_NORM) on a zero norm.  Every block of the
 // scaling kernel adds the chunk partials in order itself (one thread: the
@@ -1455,8 +1528,15 @@ static int grid_for(fgb_ctx* ctx, long n) {
 template <typename T>
 static fgb_status queue_normalize(fgb_ctx* ctx, ProxWork& w, T* M, long N, int* d_status) {
   const int nchunks = (int)((N + CR_CHUNK - 1) / CR_CHUNK);
-  k_chunk_sumsq<T><<<nchunks, PX_THREADS, 0, ctx->stream>>>(M, N, w.partials);
-  FGB_LAUNCHED(ctx);
+  if (w.sq_seg && w.sq_mask && nchunks <= w.sq_chunks) {
+    k_sumsq_seg<T><<<nchunks * SQ_SEG, CR_LANES, 0, ctx->stream>>>(M, N, w.sq_seg, w.sq_mask);
+    FGB_LAUNCHED(ctx);
+    k_sumsq_lanes<T><<<nchunks, CR_LANES, 0, ctx->stream>>>(M, N, w.sq_seg, w.sq_mask, w.partials);
+    FGB_LAUNCHED(ctx);
+  } else {
+    k_chunk_sumsq<T><<<nchunks, PX_THREADS, 0, ctx->stream>>>(M, N, w.partials);
+    FGB_LAUNCHED(ctx);
+  }
   k_scale<T><<<grid_for(ctx, N), PX_THREADS, 0, ctx->stream>>>(M, N, w.partials, nchunks, d_status);
   FGB_LAUNCHED(ctx);
   return FGB_OK;

@@ -50,6 +50,12 @@ struct ProxWork {
   // key-list counter; the key list of a small bucket
   unsigned* hist_passes = nullptr;
   unsigned long long* rs_list = nullptr;
+  // split sum of squares of the normalisation (workspaces made by
+  // prox_work_reserve): segment partials and per-lane masks (kept zero
+  // between uses)
+  double* sq_seg = nullptr;
+  unsigned* sq_mask = nullptr;
+  long sq_chunks = 0;
 };
 
 fgb_status prox_work_reserve(fgb_ctx* ctx, ProxWork& w, long elems, int rows);
