@@ -44,6 +44,7 @@ struct fgb_ctx {
   // Cooperative grid of the projection's radix select on this context's
   // device (FP32, FP64), computed on first use.
   int rs_coop_blocks[2] = {0, 0};
+  int rs_coop_blocks_reg[2] = {0, 0};  // the same for the register-resident variant
   // Device word set by kernels whose bounded waits ran out (the tcgen05 BSR
   // and GEMM kernels, the radix butterfly kernel); read and cleared by
   // fgb_ctx_synchronize.

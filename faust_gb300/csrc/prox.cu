@@ -426,6 +426,143 @@ __global__ void __launch_bounds__(PX_THREADS)
   }
 }
 
+// The same selection with every thread's keys held in registers (at most
+// RS_KREG per thread, i.e. N <= grid threads * RS_KREG): each full pass
+// reads registers instead of the matrix, and the key list is collected only
+// once the chosen bucket holds at most RS_TAIL_CAP keys (usually after the
+// third digit), so block 0 finishes from a list staged in shared memory.
+// The histograms, bucket picks and outputs are those of k_radix_select.
+constexpr int RS_KREG = 16;
+constexpr int RS_TAIL_CAP = 4096;
+
+template <typename T>
+__global__ void __launch_bounds__(PX_THREADS)
+    k_radix_select_reg(const T* __restrict__ M, long N, int pos, int npass, long long k, TopkState* st,
+                       unsigned* hists, unsigned long long* __restrict__ list) {
+  __shared__ unsigned sh[2048];
+  __shared__ RsShared s;
+  __shared__ unsigned long long tl[RS_TAIL_CAP];
+  unsigned* bar = hists + RS_MAX_PASSES * 2048;
+  unsigned* list_n = bar + 2;
+  const int shifts8[6] = {52, 41, 30, 19, 8, 0}, bits8[6] = {11, 11, 11, 11, 11, 8};
+  const int shifts4[3] = {20, 9, 0}, bits4[3] = {11, 11, 9};
+  if (threadIdx.x == 0) {
+    s.prefix = 0;
+    s.mask = 0;
+    s.krem = k;
+    s.G = 0;
+    s.E = 0;
+    s.bad = 0;
+  }
+  if (blockIdx.x == 0) {
+    for (int i = threadIdx.x; i < (RS_MAX_PASSES - 1) * 2048; i += blockDim.x) hists[2048 + i] = 0;
+    if (threadIdx.x == 0) {
+      *list_n = 0;
+      st->t = 0;
+      st->tau = 0;
+      st->sel_case = 0;
+      st->status = 0;
+      st->blocks_done = 0;
+    }
+  }
+  // the thread's keys, in the order of the strided scans
+  const long stride = (long)gridDim.x * blockDim.x;
+  const long i0 = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  unsigned long long key[RS_KREG];
+  int nk = 0;
+#pragma unroll
+  for (int u = 0; u < RS_KREG; ++u) {
+    const long i = i0 + u * stride;
+    key[u] = i < N ? sel_key(M[i], pos) : 0ULL;
+    nk += i < N;
+  }
+  bool timed_out = false, tail = false;
+  int p = 0;
+  for (; p < npass; ++p) {
+    const int shift = sizeof(T) == 8 ? shifts8[p] : shifts4[p];
+    const int bits = sizeof(T) == 8 ? bits8[p] : bits4[p];
+    const int nb = 1 << bits;
+    unsigned* hist = hists + p * 2048;
+    for (int i = threadIdx.x; i < nb; i += blockDim.x) sh[i] = 0;
+    __syncthreads();
+    const unsigned long long prefix = s.prefix, mask = s.mask;
+    const bool collect = p > 0 && p + 1 < npass && s.E <= RS_TAIL_CAP;
+    if (p == 0) {
+#pragma unroll
+      for (int u = 0; u < RS_KREG; ++u)
+        if (u < nk) {
+          const unsigned b = (unsigned)(key[u] >> shift) & (unsigned)(nb - 1);
+          const unsigned peers = __match_any_sync(__activemask(), b);
+          if ((int)(threadIdx.x & 31) == __ffs(peers) - 1) atomicAdd(&sh[b], (unsigned)__popc(peers));
+        }
+    } else {
+#pragma unroll
+      for (int u = 0; u < RS_KREG; ++u)
+        if (u < nk && (key[u] & mask) == prefix) {
+          atomicAdd(&sh[(key[u] >> shift) & (nb - 1)], 1u);
+          if (collect) {
+            const unsigned at = atomicAdd(list_n, 1u);
+            if (at < (unsigned)RS_TAIL_CAP) list[at] = key[u];
+          }
+        }
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < nb; i += blockDim.x)
+      if (sh[i]) atomicAdd(&hist[i], sh[i]);
+    __threadfence();
+    if (!rs_grid_barrier(bar, gridDim.x, &s.ok)) timed_out = true;
+    if (p > 0 && blockIdx.x == 0)
+      for (int i = threadIdx.x; i < 2048; i += blockDim.x) hists[(p - 1) * 2048 + i] = 0;
+    for (int i = threadIdx.x; i < nb; i += blockDim.x) sh[i] = __ldcg(&hist[i]);
+    __syncthreads();
+    rs_pick(sh, nb, shift, prefix, mask, s);
+    if (collect) {
+      ++p;
+      tail = true;
+      break;
+    }
+  }
+  if (tail && blockIdx.x == 0) {
+    // (the list holds exactly the keys of the bucket collected, at most
+    // RS_TAIL_CAP of them)
+    const unsigned n = min(__ldcg(list_n), (unsigned)RS_TAIL_CAP);
+    for (unsigned i = threadIdx.x; i < n; i += blockDim.x) tl[i] = __ldcg(&list[i]);
+    for (; p < npass; ++p) {
+      const int shift = sizeof(T) == 8 ? shifts8[p] : shifts4[p];
+      const int bits = sizeof(T) == 8 ? bits8[p] : bits4[p];
+      const int nb = 1 << bits;
+      for (int i = threadIdx.x; i < nb; i += blockDim.x) sh[i] = 0;
+      __syncthreads();
+      const unsigned long long prefix = s.prefix, mask = s.mask;
+      for (unsigned i = threadIdx.x; i < n; i += blockDim.x) {
+        const unsigned long long kk = tl[i];
+        if ((kk & mask) == prefix) atomicAdd(&sh[(kk >> shift) & (nb - 1)], 1u);
+      }
+      __syncthreads();
+      rs_pick(sh, nb, shift, prefix, mask, s);
+    }
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    st->prefix = s.prefix;
+    st->mask = s.mask;
+    st->k_rem = s.krem;
+    st->G = s.G;
+    st->E = s.E;
+    if (s.bad) atomicCAS(&st->status, 0, (int)FGB_ERR_INVALID_ARG);
+  }
+  if (timed_out && threadIdx.x == 0) atomicCAS(&st->status, 0, (int)FGB_ERR_TIMEOUT);
+  // the last block to leave clears the barrier's arrival count (as in
+  // k_radix_select)
+  if (threadIdx.x == 0) {
+    __threadfence();
+    if (atomicAdd(&bar[3], 1u) == gridDim.x - 1) {
+      bar[0] = 0;
+      bar[3] = 0;
+      __threadfence();
+    }
+  }
+}
+
 // ------------------------------------------------------------------ tie case
 // Decides the tie case; for ties with t > 0 finds tau and whether an entry
 // |v| > t lies after it.
@@ -1658,8 +1795,21 @@ static fgb_status queue_sp(fgb_ctx* ctx, ProxWork& w, T* M, long N, long k, int 
     cfg.attrs = attr;
     cfg.numAttrs = 1;
     const T* Mc = M;
-    FGB_CUDA(ctx, cudaLaunchKernelEx(&cfg, k_radix_select<T>, Mc, N, pos, npass, (long long)k, w.state, w.hist_passes,
-                                     w.rs_list));
+    // keys held in registers when every thread's share fits
+    int& nbr = ctx->rs_coop_blocks_reg[sizeof(T) == 8];
+    if (!nbr) {
+      int per_sm = 0;
+      FGB_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_radix_select_reg<T>, PX_THREADS, 0));
+      nbr = std::max(1, std::min(per_sm, 2)) * ctx->sm_count;
+    }
+    if (N <= (long)nbr * PX_THREADS * RS_KREG) {
+      cfg.gridDim = dim3((unsigned)std::min<long>(nbr, std::max(1L, (N + PX_THREADS - 1) / PX_THREADS)));
+      FGB_CUDA(ctx, cudaLaunchKernelEx(&cfg, k_radix_select_reg<T>, Mc, N, pos, npass, (long long)k, w.state,
+                                       w.hist_passes, w.rs_list));
+    } else {
+      FGB_CUDA(ctx, cudaLaunchKernelEx(&cfg, k_radix_select<T>, Mc, N, pos, npass, (long long)k, w.state,
+                                       w.hist_passes, w.rs_list));
+    }
     FGB_LAUNCHED(ctx);
   } else if (sizeof(T) == 8) {
     const int shifts[6] = {52, 41, 30, 19, 8, 0};
