@@ -1403,6 +1403,55 @@ __global__ void k_sp_apply(T* __restrict__ M, long N, int pos, const TopkState* 
   }
 }
 
+// k_sp_apply with the first half of the normalisation's sum of squares
+// (k_sumsq_seg) on the entries it leaves: block (c, s) of SQ_SEG blocks per
+// chunk, lane t owns the entries t + CR_LANES * (SQ_PER * s + u) of chunk c,
+// decides and writes them as k_sp_apply does and chains the squares of the
+// kept ones in order.
+template <typename T>
+__global__ void __launch_bounds__(CR_LANES)
+    k_sp_apply_sq(T* __restrict__ M, long N, int pos, const TopkState* st, unsigned char* __restrict__ flags,
+                  int* d_status, double* __restrict__ seg, unsigned* __restrict__ mask) {
+  if (d_status && blockIdx.x == 0 && threadIdx.x == 0 && st->status) atomicCAS(d_status, 0, st->status);
+  const unsigned long long t = st->t;
+  const int cs = st->sel_case;
+  const long long tau = st->tau;
+  const int c = blockIdx.x / SQ_SEG, s = blockIdx.x % SQ_SEG, ln = threadIdx.x;
+  const long base = (long)c * CR_CHUNK + ln + (long)s * SQ_PER * CR_LANES;
+  T m[SQ_PER];
+#pragma unroll
+  for (int u = 0; u < SQ_PER; ++u) {
+    const long i = base + (long)u * CR_LANES;
+    m[u] = i < N ? M[i] : T(0);
+  }
+  T acc = T(0);
+  bool nz = false;
+#pragma unroll
+  for (int u = 0; u < SQ_PER; ++u) {
+    const long i = base + (long)u * CR_LANES;
+    if (i >= N) break;
+    const unsigned long long key = sel_key(m[u], pos);
+    bool keep = key > t;
+    if (!keep && key == t) {
+      if (cs == 0) keep = true;
+      else if (cs == 1) keep = i <= tau;
+      else if (cs == 2) keep = flags[i] != 0;
+    }
+    if (cs == 2) flags[i] = 0;
+    const bool adjusted = key == 0 && mag_key(m[u]) != 0;
+    const T out = keep && !adjusted ? m[u] : T(0);
+    if (raw_bits(out) != raw_bits(m[u])) M[i] = out;
+    if (mag_key(out) != 0) {
+      acc = fmad(out, out, acc);
+      nz = true;
+    }
+  }
+  if (nz) {
+    reinterpret_cast<T*>(seg)[((long)c * SQ_SEG + s) * CR_LANES + ln] = acc;
+    atomicOr(&mask[c * CR_LANES + ln], 1u << s);
+  }
+}
+
 template <typename T>
 __global__ void k_pos_only(T* __restrict__ M, long N) {
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < N; i += (long)gridDim.x * blockDim.x)
@@ -1663,11 +1712,13 @@ static int grid_for(fgb_ctx* ctx, long n) {
 }
 
 template <typename T>
-static fgb_status queue_normalize(fgb_ctx* ctx, ProxWork& w, T* M, long N, int* d_status) {
+static fgb_status queue_normalize(fgb_ctx* ctx, ProxWork& w, T* M, long N, int* d_status, bool seg_done = false) {
   const int nchunks = (int)((N + CR_CHUNK - 1) / CR_CHUNK);
   if (w.sq_seg && w.sq_mask && nchunks <= w.sq_chunks) {
-    k_sumsq_seg<T><<<nchunks * SQ_SEG, CR_LANES, 0, ctx->stream>>>(M, N, w.sq_seg, w.sq_mask);
-    FGB_LAUNCHED(ctx);
+    if (!seg_done) {
+      k_sumsq_seg<T><<<nchunks * SQ_SEG, CR_LANES, 0, ctx->stream>>>(M, N, w.sq_seg, w.sq_mask);
+      FGB_LAUNCHED(ctx);
+    }
     k_sumsq_lanes<T><<<nchunks, CR_LANES, 0, ctx->stream>>>(M, N, w.sq_seg, w.sq_mask, w.partials);
     FGB_LAUNCHED(ctx);
   } else {
@@ -1769,7 +1820,8 @@ static fgb_status queue_tie_replay(fgb_ctx* ctx, ProxWork& w, const T* M, long N
 }
 
 template <typename T>
-static fgb_status queue_sp(fgb_ctx* ctx, ProxWork& w, T* M, long N, long k, int pos, int* d_status) {
+static fgb_status queue_sp(fgb_ctx* ctx, ProxWork& w, T* M, long N, long k, int pos, int* d_status,
+                           bool* seg_done = nullptr) {
   const int g = grid_for(ctx, N);
   if (!w.hist_passes) {
     k_topk_init<<<1, 1, 0, ctx->stream>>>(w.state, k);
@@ -1856,7 +1908,15 @@ static fgb_status queue_sp(fgb_ctx* ctx, ProxWork& w, T* M, long N, long k, int 
     kern<<<1, PX_THREADS, smem, ctx->stream>>>(M, N, pos, (int)k, w.state, w.flags, gheap, use_smem ? 1 : 0);
     FGB_LAUNCHED(ctx);
   }
-  k_sp_apply<T><<<g, PX_THREADS, 0, ctx->stream>>>(M, N, pos, w.state, w.flags, d_status);
+  const int nchunks = (int)((N + CR_CHUNK - 1) / CR_CHUNK);
+  if (seg_done && w.sq_seg && w.sq_mask && nchunks <= w.sq_chunks) {
+    // the normalisation follows: its segment sums come with the apply
+    k_sp_apply_sq<T><<<nchunks * SQ_SEG, CR_LANES, 0, ctx->stream>>>(M, N, pos, w.state, w.flags, d_status, w.sq_seg,
+                                                                   w.sq_mask);
+    *seg_done = true;
+  } else {
+    k_sp_apply<T><<<g, PX_THREADS, 0, ctx->stream>>>(M, N, pos, w.state, w.flags, d_status);
+  }
   FGB_LAUNCHED(ctx);
   return FGB_OK;
 }
@@ -1868,6 +1928,7 @@ fgb_status launch_prox(fgb_ctx* ctx, ProxWork& w, const fgb_constraint& c, T* M,
   FGB_TRY(prox_work_reserve(ctx, w, N, std::max(rows, cols)));
   const int g = grid_for(ctx, N);
   int pos = c.pos != 0;
+  bool seg_done = false;  // the sum of squares' segment pass already ran
   switch (c.kind) {
     case FGB_SP_POS:
       pos = 1;
@@ -1878,7 +1939,7 @@ fgb_status launch_prox(fgb_ctx* ctx, ProxWork& w, const fgb_constraint& c, T* M,
         k_zero<T><<<g, PX_THREADS, 0, ctx->stream>>>(M, N);
         FGB_LAUNCHED(ctx);
       } else if (c.k < N) {
-        FGB_TRY(queue_sp<T>(ctx, w, M, N, (long)c.k, pos, d_status));
+        FGB_TRY(queue_sp<T>(ctx, w, M, N, (long)c.k, pos, d_status, c.normalized ? &seg_done : nullptr));
       } else if (pos) {
         k_pos_only<T><<<g, PX_THREADS, 0, ctx->stream>>>(M, N);
         FGB_LAUNCHED(ctx);
@@ -1936,7 +1997,7 @@ fgb_status launch_prox(fgb_ctx* ctx, ProxWork& w, const fgb_constraint& c, T* M,
     default:
       return fail(ctx, FGB_ERR_INVALID_ARG, "project : cannot project with this constraint name");
   }
-  if (c.normalized) FGB_TRY(queue_normalize<T>(ctx, w, M, N, d_status));
+  if (c.normalized) FGB_TRY(queue_normalize<T>(ctx, w, M, N, d_status, seg_done));
   return FGB_OK;
 }
 
