@@ -41,35 +41,46 @@ __global__ void k_d_minus(T* __restrict__ D, const T* __restrict__ G, long N, co
     D[i] = subr(D[i], mulr(a, G[i]));
 }
 
-// Canonical <A,S> and ||S||^2 per chunk of 65536 entries.
+// Canonical <A,S> and ||S||^2 (lanes of 256 per chunk of 65536 entries, each
+// lane a sequential fma over its entries), every 32 lanes of a chunk on a
+// block of one warp: a lane's chain is sequential, and on GB300 an FP64 FMA
+// warp instruction takes a scheduler 64 cycles whatever the number of active
+// lanes, so the 4096 lanes of a 1024^2 block run on 128 SMs instead of 16.
+// The lane values go to `lanes` (chunk c: <A,S> lanes at 512 c, ||S||^2
+// lanes at 512 c + 256); k_lambda_lanes adds them by the lane tree.
 template <typename T>
-__global__ void __launch_bounds__(256) k_chunk_dot2(const T* __restrict__ A, const T* __restrict__ S, long N,
-                                                   double* part) {
-  __shared__ T lane[256];
-  const long c0 = blockIdx.x * CR_CHUNK, c1 = min(N, c0 + CR_CHUNK);
+__global__ void __launch_bounds__(32) k_lane_dot2(const T* __restrict__ A, const T* __restrict__ S, long N,
+                                                 double* __restrict__ lanes) {
+  const int c = blockIdx.x / (CR_LANES / 32), t = (blockIdx.x % (CR_LANES / 32)) * 32 + threadIdx.x;
+  const long c0 = (long)c * CR_CHUNK, c1 = min(N, c0 + CR_CHUNK);
   T a = T(0), s = T(0);
-  for (long i = c0 + threadIdx.x; i < c1; i += CR_LANES) {
-    a = fmad(A[i], S[i], a);
-    s = fmad(S[i], S[i], s);
+#pragma unroll 8
+  for (long i = c0 + t; i < c1; i += CR_LANES) {
+    const T x = A[i], y = S[i];
+    a = fmad(x, y, a);
+    s = fmad(y, y, s);
   }
-  lane[threadIdx.x] = a;
-  const T pa = lane_tree_256(lane);
-  lane[threadIdx.x] = s;
-  const T ps = lane_tree_256(lane);
-  if (threadIdx.x == 0) {
-    reinterpret_cast<T*>(part)[2 * blockIdx.x] = pa;
-    reinterpret_cast<T*>(part)[2 * blockIdx.x + 1] = ps;
-  }
+  reinterpret_cast<T*>(lanes)[(long)c * 2 * CR_LANES + t] = a;
+  reinterpret_cast<T*>(lanes)[(long)c * 2 * CR_LANES + CR_LANES + t] = s;
 }
 
-// update_lambda (faust_palm4msa2020.hpp:441-493): lambda = tr / (nS*nS).
+// update_lambda (faust_palm4msa2020.hpp:441-493), lambda = tr / (nS*nS),
+// from the lane values of k_lane_dot2: per chunk the pairwise lane tree, the
+// chunk partials added in order.  One block of CR_LANES threads.
 template <typename T>
-__global__ void k_lambda_update(const double* part, int nchunks, T* lam, int* status, int no_lambda_error) {
+__global__ void __launch_bounds__(CR_LANES) k_lambda_lanes(const double* lanes, int nchunks, T* lam, int* status,
+                                                          int no_lambda_error) {
+  __shared__ T lane[CR_LANES];
   T tr = T(0), ss = T(0);
   for (int c = 0; c < nchunks; ++c) {
-    tr = addr(tr, reinterpret_cast<const T*>(part)[2 * c]);
-    ss = addr(ss, reinterpret_cast<const T*>(part)[2 * c + 1]);
+    lane[threadIdx.x] = reinterpret_cast<const T*>(lanes)[(long)c * 2 * CR_LANES + threadIdx.x];
+    const T pa = lane_tree_256(lane);
+    lane[threadIdx.x] = reinterpret_cast<const T*>(lanes)[(long)c * 2 * CR_LANES + CR_LANES + threadIdx.x];
+    const T ps = lane_tree_256(lane);
+    tr = addr(tr, pa);
+    ss = addr(ss, ps);
   }
+  if (threadIdx.x) return;
   const T nS = sqrtr(ss);
   if (nS == T(0)) {
     if (!no_lambda_error) atomicCAS(status, 0, (int)FGB_ERR_ZERO_NORM);
@@ -153,6 +164,7 @@ struct Palm {
   int* status = nullptr;
   PIOut* pi = nullptr;
   double* part = nullptr;
+  double* lanes2 = nullptr;  // lane values of the update_lambda reduction
   const int* rnd = nullptr;
   ProxWork pw;
   fgb_palm_params p;
@@ -195,6 +207,7 @@ struct Palm {
     dfree(status);
     dfree(pi);
     dfree(part);
+    dfree(lanes2);
     prox_work_free(pw);
   }
 
@@ -249,6 +262,7 @@ struct Palm {
     FGB_TRY(dmalloc(ctx, (void**)&status, sizeof(int)));
     FGB_TRY(dmalloc(ctx, (void**)&pi, sizeof(PIOut)));
     FGB_TRY(dmalloc(ctx, (void**)&part, sizeof(double) * 2 * ((size_t)maxdim * maxdim / CR_CHUNK + 2)));
+    FGB_TRY(dmalloc(ctx, (void**)&lanes2, sizeof(double) * 2 * CR_LANES * ((size_t)maxdim * maxdim / CR_CHUNK + 2)));
     FGB_CUDA(ctx, cudaMemsetAsync(status, 0, sizeof(int), ctx->stream));
     FGB_CUDA(ctx, cudaMemsetAsync(pi, 0, sizeof(PIOut), ctx->stream));
     k_set_scalar<T><<<1, 1, 0, ctx->stream>>>(lam, init_lambda);
@@ -521,9 +535,9 @@ struct Palm {
     }
     const long N = (long)arows * acols;
     const int nch = (int)((N + CR_CHUNK - 1) / CR_CHUNK);
-    k_chunk_dot2<T><<<nch, 256, 0, ctx->stream>>>(A, Smat, N, part);
+    k_lane_dot2<T><<<nch * (CR_LANES / 32), 32, 0, ctx->stream>>>(A, Smat, N, lanes2);
     FGB_LAUNCHED(ctx);
-    k_lambda_update<T><<<1, 1, 0, ctx->stream>>>(part, nch, lam, status, p.no_lambda_error);
+    k_lambda_lanes<T><<<1, CR_LANES, 0, ctx->stream>>>(lanes2, nch, lam, status, p.no_lambda_error);
     FGB_LAUNCHED(ctx);
     return FGB_OK;
   }
