@@ -74,8 +74,8 @@ fgb_status prox_work_reserve(fgb_ctx* ctx, ProxWork& w, long elems, int rows) {
   FGB_TRY(dmalloc(ctx, (void**)&w.row_cnt, sizeof(int) * (rows + 2)));
   FGB_CUDA(ctx, cudaMemsetAsync(w.flags, 0, (size_t)std::max(1L, elems), ctx->stream));
   FGB_CUDA(ctx, cudaMemsetAsync(w.hist, 0, sizeof(unsigned) * 2048, ctx->stream));
-  FGB_TRY(dmalloc(ctx, (void**)&w.hist_passes, sizeof(unsigned) * (RS_MAX_PASSES * 2048 + 4)));
-  FGB_CUDA(ctx, cudaMemsetAsync(w.hist_passes, 0, sizeof(unsigned) * (RS_MAX_PASSES * 2048 + 4), ctx->stream));
+  FGB_TRY(dmalloc(ctx, (void**)&w.hist_passes, sizeof(unsigned) * (RS_MAX_PASSES * 2048 + 8)));
+  FGB_CUDA(ctx, cudaMemsetAsync(w.hist_passes, 0, sizeof(unsigned) * (RS_MAX_PASSES * 2048 + 8), ctx->stream));
   FGB_TRY(dmalloc(ctx, (void**)&w.rs_list, sizeof(unsigned long long) * RS_LIST_CAP));
   w.sq_chunks = (elems + CR_CHUNK - 1) / CR_CHUNK;
   FGB_TRY(dmalloc(ctx, (void**)&w.sq_seg, sizeof(double) * (size_t)std::max(1L, w.sq_chunks) * SQ_SEG * CR_LANES));
@@ -428,10 +428,12 @@ __global__ void __launch_bounds__(PX_THREADS)
 
 // The same selection with every thread's keys held in registers (at most
 // RS_KREG per thread, i.e. N <= grid threads * RS_KREG): each full pass
-// reads registers instead of the matrix, and the key list is collected only
-// once the chosen bucket holds at most RS_TAIL_CAP keys (usually after the
-// third digit), so block 0 finishes from a list staged in shared memory.
-// The histograms, bucket picks and outputs are those of k_radix_select.
+// reads registers instead of the matrix.  Once the chosen bucket holds at
+// most RS_TAIL_CAP keys, every block appends its keys of that bucket to the
+// list straight from its registers and counts itself in; block 0 alone
+// waits for all the blocks (a one-sided, bounded wait) and finishes the
+// remaining digits from the list staged in shared memory.  The histograms,
+// bucket picks and outputs are those of k_radix_select.
 constexpr int RS_KREG = 16;
 constexpr int RS_TAIL_CAP = 4096;
 
@@ -444,6 +446,7 @@ __global__ void __launch_bounds__(PX_THREADS)
   __shared__ unsigned long long tl[RS_TAIL_CAP];
   unsigned* bar = hists + RS_MAX_PASSES * 2048;
   unsigned* list_n = bar + 2;
+  unsigned* arrived = bar + 4;  // blocks whose keys are in the list
   const int shifts8[6] = {52, 41, 30, 19, 8, 0}, bits8[6] = {11, 11, 11, 11, 11, 8};
   const int shifts4[3] = {20, 9, 0}, bits4[3] = {11, 11, 9};
   if (threadIdx.x == 0) {
@@ -457,7 +460,9 @@ __global__ void __launch_bounds__(PX_THREADS)
   if (blockIdx.x == 0) {
     for (int i = threadIdx.x; i < (RS_MAX_PASSES - 1) * 2048; i += blockDim.x) hists[2048 + i] = 0;
     if (threadIdx.x == 0) {
+      // (no block touches these before the first barrier)
       *list_n = 0;
+      *arrived = 0;
       st->t = 0;
       st->tau = 0;
       st->sel_case = 0;
@@ -486,7 +491,6 @@ __global__ void __launch_bounds__(PX_THREADS)
     for (int i = threadIdx.x; i < nb; i += blockDim.x) sh[i] = 0;
     __syncthreads();
     const unsigned long long prefix = s.prefix, mask = s.mask;
-    const bool collect = p > 0 && p + 1 < npass && s.E <= RS_TAIL_CAP;
     if (p == 0) {
 #pragma unroll
       for (int u = 0; u < RS_KREG; ++u)
@@ -498,13 +502,7 @@ __global__ void __launch_bounds__(PX_THREADS)
     } else {
 #pragma unroll
       for (int u = 0; u < RS_KREG; ++u)
-        if (u < nk && (key[u] & mask) == prefix) {
-          atomicAdd(&sh[(key[u] >> shift) & (nb - 1)], 1u);
-          if (collect) {
-            const unsigned at = atomicAdd(list_n, 1u);
-            if (at < (unsigned)RS_TAIL_CAP) list[at] = key[u];
-          }
-        }
+        if (u < nk && (key[u] & mask) == prefix) atomicAdd(&sh[(key[u] >> shift) & (nb - 1)], 1u);
     }
     __syncthreads();
     for (int i = threadIdx.x; i < nb; i += blockDim.x)
@@ -516,30 +514,58 @@ __global__ void __launch_bounds__(PX_THREADS)
     for (int i = threadIdx.x; i < nb; i += blockDim.x) sh[i] = __ldcg(&hist[i]);
     __syncthreads();
     rs_pick(sh, nb, shift, prefix, mask, s);
-    if (collect) {
-      ++p;
+    if (p + 1 < npass && s.E <= RS_TAIL_CAP) {
       tail = true;
       break;
     }
   }
-  if (tail && blockIdx.x == 0) {
-    // (the list holds exactly the keys of the bucket collected, at most
-    // RS_TAIL_CAP of them)
-    const unsigned n = min(__ldcg(list_n), (unsigned)RS_TAIL_CAP);
-    for (unsigned i = threadIdx.x; i < n; i += blockDim.x) tl[i] = __ldcg(&list[i]);
-    for (; p < npass; ++p) {
-      const int shift = sizeof(T) == 8 ? shifts8[p] : shifts4[p];
-      const int bits = sizeof(T) == 8 ? bits8[p] : bits4[p];
-      const int nb = 1 << bits;
-      for (int i = threadIdx.x; i < nb; i += blockDim.x) sh[i] = 0;
-      __syncthreads();
-      const unsigned long long prefix = s.prefix, mask = s.mask;
-      for (unsigned i = threadIdx.x; i < n; i += blockDim.x) {
-        const unsigned long long kk = tl[i];
-        if ((kk & mask) == prefix) atomicAdd(&sh[(kk >> shift) & (nb - 1)], 1u);
+  if (tail) {
+    // the keys of the bucket just chosen (s.E of them over the grid)
+    const unsigned long long prefix = s.prefix, mask = s.mask;
+#pragma unroll
+    for (int u = 0; u < RS_KREG; ++u)
+      if (u < nk && (key[u] & mask) == prefix) {
+        const unsigned at = atomicAdd(list_n, 1u);
+        if (at < (unsigned)RS_TAIL_CAP) list[at] = key[u];
+      }
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) atomicAdd(arrived, 1u);
+    if (blockIdx.x == 0) {
+      if (threadIdx.x == 0) {
+        volatile unsigned* arr = arrived;
+        long spins = 0;
+        bool ok = true;
+        while (*arr < gridDim.x) {
+          if (++spins > (1L << 21)) {
+            ok = false;
+            break;
+          }
+          __nanosleep(64);
+        }
+        __threadfence();
+        s.ok = ok;
       }
       __syncthreads();
-      rs_pick(sh, nb, shift, prefix, mask, s);
+      if (!s.ok) timed_out = true;
+      // every block has read histogram p: clear it for the next launch
+      for (int i = threadIdx.x; i < 2048; i += blockDim.x) hists[p * 2048 + i] = 0;
+      const unsigned n = min(__ldcg(list_n), (unsigned)RS_TAIL_CAP);
+      for (unsigned i = threadIdx.x; i < n; i += blockDim.x) tl[i] = __ldcg(&list[i]);
+      for (++p; p < npass; ++p) {
+        const int shift = sizeof(T) == 8 ? shifts8[p] : shifts4[p];
+        const int bits = sizeof(T) == 8 ? bits8[p] : bits4[p];
+        const int nb = 1 << bits;
+        for (int i = threadIdx.x; i < nb; i += blockDim.x) sh[i] = 0;
+        __syncthreads();
+        const unsigned long long pf = s.prefix, mk = s.mask;
+        for (unsigned i = threadIdx.x; i < n; i += blockDim.x) {
+          const unsigned long long kk = tl[i];
+          if ((kk & mk) == pf) atomicAdd(&sh[(kk >> shift) & (nb - 1)], 1u);
+        }
+        __syncthreads();
+        rs_pick(sh, nb, shift, pf, mk, s);
+      }
     }
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) {
