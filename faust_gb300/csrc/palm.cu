@@ -65,20 +65,36 @@ __global__ void __launch_bounds__(32) k_lane_dot2(const T* __restrict__ A, const
 }
 
 // update_lambda (faust_palm4msa2020.hpp:441-493), lambda = tr / (nS*nS),
-// from the lane values of k_lane_dot2: per chunk the pairwise lane tree, the
-// chunk partials added in order.  One block of CR_LANES threads.
+// from the lane values of k_lane_dot2: per chunk the pairwise lane tree of
+// lane_tree_256, the chunk partials added in order.  One block of 1024
+// threads: warp w builds tree w (chunk w / 2, <A,S> or ||S||^2), 32 trees at a
+// time, so the trees of a 1024^2 block run side by side.
+constexpr int LT_WARPS = 32;
 template <typename T>
-__global__ void __launch_bounds__(CR_LANES) k_lambda_lanes(const double* lanes, int nchunks, T* lam, int* status,
-                                                          int no_lambda_error) {
-  __shared__ T lane[CR_LANES];
+__global__ void __launch_bounds__(LT_WARPS * 32) k_lambda_lanes(const double* lanes, int nchunks, T* lam,
+                                                               int* status, int no_lambda_error) {
+  __shared__ T part[LT_WARPS];
+  const int t = threadIdx.x & 31, w = threadIdx.x >> 5;
   T tr = T(0), ss = T(0);
-  for (int c = 0; c < nchunks; ++c) {
-    lane[threadIdx.x] = reinterpret_cast<const T*>(lanes)[(long)c * 2 * CR_LANES + threadIdx.x];
-    const T pa = lane_tree_256(lane);
-    lane[threadIdx.x] = reinterpret_cast<const T*>(lanes)[(long)c * 2 * CR_LANES + CR_LANES + threadIdx.x];
-    const T ps = lane_tree_256(lane);
-    tr = addr(tr, pa);
-    ss = addr(ss, ps);
+  for (int g = 0; g < 2 * nchunks; g += LT_WARPS) {
+    if (g + w < 2 * nchunks) {
+      const T* l = reinterpret_cast<const T*>(lanes) + (long)(g + w) * CR_LANES;
+      const T a0 = addr(l[t], l[t + 128]);
+      const T a1 = addr(l[t + 32], l[t + 160]);
+      const T a2 = addr(l[t + 64], l[t + 192]);
+      const T a3 = addr(l[t + 96], l[t + 224]);
+      T c = addr(addr(a0, a2), addr(a1, a3));
+#pragma unroll
+      for (int s = 16; s >= 1; s >>= 1) c = addr(c, __shfl_down_sync(0xffffffffu, c, s));
+      if (t == 0) part[w] = c;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0)
+      for (int q = 0; q < LT_WARPS && g + q < 2 * nchunks; q += 2) {
+        tr = addr(tr, part[q]);
+        ss = addr(ss, part[q + 1]);
+      }
+    __syncthreads();
   }
   if (threadIdx.x) return;
   const T nS = sqrtr(ss);
@@ -537,7 +553,7 @@ struct Palm {
     const int nch = (int)((N + CR_CHUNK - 1) / CR_CHUNK);
     k_lane_dot2<T><<<nch * (CR_LANES / 32), 32, 0, ctx->stream>>>(A, Smat, N, lanes2);
     FGB_LAUNCHED(ctx);
-    k_lambda_lanes<T><<<1, CR_LANES, 0, ctx->stream>>>(lanes2, nch, lam, status, p.no_lambda_error);
+    k_lambda_lanes<T><<<1, LT_WARPS * 32, 0, ctx->stream>>>(lanes2, nch, lam, status, p.no_lambda_error);
     FGB_LAUNCHED(ctx);
     return FGB_OK;
   }
