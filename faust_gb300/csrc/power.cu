@@ -95,7 +95,7 @@ __device__ __forceinline__ void pi_entries(const PIStaged& op, PIRow<TF>& R) {
 }
 
 template <typename TF, typename TC>
-__global__ void __launch_bounds__(PI_THREADS)
+__global__ void __launch_bounds__(PI_THREADS, 1)
     k_power_iteration(const __grid_constant__ PIChain ca, const __grid_constant__ PIChain cb,
                       const PIChain* __restrict__ dchains, int max_iter, TC thr, const TC* __restrict__ x0, PIOut* out,
                       const __grid_constant__ PIPalm palm, int maxn, int smem_bytes) {
@@ -106,6 +106,8 @@ __global__ void __launch_bounds__(PI_THREADS)
   // warp each after the thread-per-row pass (list in the dynamic area, room
   // for every row; two counters, used alternately)
   __shared__ int s_nlong[2];
+  __shared__ int s_nnz[PI_MAX_OPS];  // stored entries of every product
+  __shared__ int s_zero;
   TC* buf0 = reinterpret_cast<TC*>(smem_raw);
   TC* buf1 = buf0 + maxn;
   TC* buf2 = buf1 + maxn;
@@ -118,10 +120,17 @@ __global__ void __launch_bounds__(PI_THREADS)
   int flag = 0;
   int st = 0;
   // a factor without entries makes the product zero (nnz read on the device:
-  // factors produced by the PALM loop only know it there)
-  bool zero = false;
-  if (!ch.empty)
-    for (int o = 0; o < ch.nops; ++o) zero |= ch.ops[o].rowptr[ch.ops[o].rows] == 0;
+  // factors produced by the PALM loop only know it there); one thread per
+  // product reads its count
+  if (threadIdx.x == 0) s_zero = 0;
+  __syncthreads();
+  if (!ch.empty && (int)threadIdx.x < ch.nops) {
+    const int nz = ch.ops[threadIdx.x].rowptr[ch.ops[threadIdx.x].rows];
+    s_nnz[threadIdx.x] = nz;
+    if (nz == 0) s_zero = 1;
+  }
+  __syncthreads();
+  const bool zero = s_zero != 0;
   if (ch.empty) {
     result = 1.0;
   } else if (zero) {
@@ -133,7 +142,7 @@ __global__ void __launch_bounds__(PI_THREADS)
       long off = 0;
       for (int o = 0; o < ch.nops; ++o) {
         const PIOp op = ch.ops[o];
-        const int nnz = op.rowptr[op.rows];
+        const int nnz = s_nnz[o];
         const long need = ((long)(op.rows + 1) * 4 + 15) / 16 * 16 + ((long)nnz * 4 + 15) / 16 * 16 +
                           ((long)nnz * sizeof(TF) + 15) / 16 * 16;
         if (off + need <= pool_bytes) {
@@ -150,24 +159,26 @@ __global__ void __launch_bounds__(PI_THREADS)
       }
     }
     __syncthreads();
+    // copies of the staged products: the loads of all products are
+    // independent, so every thread walks them without waiting in between
     for (int o = 0; o < ch.nops; ++o) {
       if (!ops[o].pad) continue;
       const PIOp op = ch.ops[o];
-      const int nnz = op.rowptr[op.rows];
+      const int nnz = s_nnz[o];
       int* rp = const_cast<int*>(ops[o].rp);
       int* ci = const_cast<int*>(ops[o].ci);
       TF* v = reinterpret_cast<TF*>(const_cast<void*>(ops[o].v));
       const TF* gv = reinterpret_cast<const TF*>(op.val);
-      for (int i = threadIdx.x; i <= op.rows; i += blockDim.x) rp[i] = op.rowptr[i];
+      for (int i = threadIdx.x; i <= op.rows; i += blockDim.x) rp[i] = __ldg(op.rowptr + i);
       for (int i = threadIdx.x; i < nnz; i += blockDim.x) {
-        ci[i] = op.colind[i];
-        v[i] = gv[i];
+        ci[i] = __ldg(op.colind + i);
+        v[i] = __ldg(gv + i);
       }
     }
     __syncthreads();
-    TC* bufs[3] = {buf0, buf1, buf2};
+    // the three vectors are consecutive: vector i at buf0 + i * maxn
     int xi = 0;
-    for (int i = threadIdx.x; i < n; i += blockDim.x) bufs[0][i] = x0[i];
+    for (int i = threadIdx.x; i < n; i += blockDim.x) buf0[i] = x0[i];
     __syncthreads();
     // Software pipeline over the products (the same sequence every
     // iteration): while product o is computed, a thread reads the row
@@ -192,7 +203,7 @@ __global__ void __launch_bounds__(PI_THREADS)
     while ((absd(subr(lam_old, lam)) > athr || absd(lam) <= athr) && it < max_iter) {
       ++it;
       lam_old = lam;
-      TC* x = bufs[xi];
+      TC* x = buf0 + (long)xi * maxn;
       // scalar FP64 work (sqrt, division) by one thread: GB300's FP64 pipe
       // is narrow, 1024 redundant copies would saturate it
       const TC ss = block_cdot<TC>(x, x, n, lane);
@@ -215,8 +226,8 @@ __global__ void __launch_bounds__(PI_THREADS)
       for (int o = 0; o < nops; ++o) {
         const PIStaged op = ops[o];
         const TF* __restrict__ val = reinterpret_cast<const TF*>(op.v);
-        const TC* src = bufs[si];
-        TC* dst = bufs[di];
+        const TC* src = buf0 + (long)si * maxn;
+        TC* dst = buf0 + (long)di * maxn;
         // issue the loads for later products
         pi_rowptr<TF>(ops[(o + 3) % nops], r0, b3, e3);
         pi_entries<TF>(ops[(o + 1) % nops], P1);
@@ -263,7 +274,7 @@ __global__ void __launch_bounds__(PI_THREADS)
         si = di;
         di = 3 - xi - si;
       }
-      const TC* res = bufs[si];
+      const TC* res = buf0 + (long)si * maxn;
       int nz = 0;
       for (int i = threadIdx.x; i < n; i += blockDim.x) nz |= (res[i] != TC(0));
       if (!__syncthreads_or(nz)) {

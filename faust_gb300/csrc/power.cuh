@@ -8,7 +8,7 @@
 namespace fgb {
 
 constexpr int PI_MAX_OPS = 64;
-constexpr int PI_THREADS = 1024;
+constexpr int PI_THREADS = 512;
 constexpr int PI_MAX_CHAINS = 64;
 
 // One sparse product y = S x (or S^H x through the transpose's CSR).
