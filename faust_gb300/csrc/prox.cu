@@ -72,6 +72,7 @@ fgb_status prox_work_reserve(fgb_ctx* ctx, ProxWork& w, long elems, int rows) {
   FGB_TRY(dmalloc(ctx, (void**)&w.partials, sizeof(double) * (elems / CR_CHUNK + 2)));
   FGB_TRY(dmalloc(ctx, (void**)&w.scal, sizeof(double) * 4));
   FGB_TRY(dmalloc(ctx, (void**)&w.row_cnt, sizeof(int) * (rows + 2)));
+  FGB_CUDA(ctx, cudaMemsetAsync(w.row_cnt, 0, sizeof(int) * (rows + 2), ctx->stream));
   FGB_CUDA(ctx, cudaMemsetAsync(w.flags, 0, (size_t)std::max(1L, elems), ctx->stream));
   FGB_CUDA(ctx, cudaMemsetAsync(w.hist, 0, sizeof(unsigned) * 2048, ctx->stream));
   FGB_TRY(dmalloc(ctx, (void**)&w.hist_passes, sizeof(unsigned) * (RS_MAX_PASSES * 2048 + 8)));
@@ -1673,13 +1674,27 @@ __global__ void __launch_bounds__(CR_LANES) k_sumsq_lanes(const T* __restrict__ 
   if (t == 0) reinterpret_cast<T*>(partials)[c] = part;
 }
 
+// rcnt, ccnt (optional): per-row and per-column counts of the non-zero
+// results, added to (column-major M with `rows` rows), for the dense -> CSR
+// conversion that follows.
+template <typename T>
+__device__ __forceinline__ void scale_store(T* M, long i, T x, T s, int rows, int* rcnt, int* ccnt) {
+  const T y = mulr(x, s);
+  M[i] = y;
+  if (rcnt && mag_key(y) != 0) {
+    atomicAdd(&rcnt[i % rows], 1);
+    atomicAdd(&ccnt[i / rows], 1);
+  }
+}
+
 // MatDense::normalize (faust_MatDense.hpp:1225-1250): scale = FPP(1.0/norm),
 // domain_error (here FGB_ERR_ZERO_NORM) on a zero norm.  Every block of the
 // scaling kernel adds the chunk partials in order itself (one thread: the
 // FP64 square root and division are a few hundred cycles), which saves the
 // launch of a one-thread kernel.
 template <typename T>
-__global__ void k_scale(T* __restrict__ M, long N, const double* __restrict__ partials, int nchunks, int* status) {
+__global__ void k_scale(T* __restrict__ M, long N, const double* __restrict__ partials, int nchunks, int* status,
+                        int rows, int* __restrict__ rcnt, int* __restrict__ ccnt) {
   __shared__ T s_inv;
   if (threadIdx.x == 0) {
     T total = T(0);
@@ -1714,12 +1729,12 @@ __global__ void k_scale(T* __restrict__ M, long N, const double* __restrict__ pa
       T x = v[0];
 #pragma unroll
       for (int q = 1; q < 4; ++q) x = u == q ? v[q] : x;
-      if (!skip_zeros || mag_key(x) != 0) M[i + u * stride] = mulr(x, s);
+      if (!skip_zeros || mag_key(x) != 0) scale_store(M, i + u * stride, x, s, rows, rcnt, ccnt);
     }
   }
   for (; i < N; i += stride) {
     const T v = M[i];
-    if (!skip_zeros || mag_key(v) != 0) M[i] = mulr(v, s);
+    if (!skip_zeros || mag_key(v) != 0) scale_store(M, i, v, s, rows, rcnt, ccnt);
   }
 }
 
@@ -1738,7 +1753,8 @@ static int grid_for(fgb_ctx* ctx, long n) {
 }
 
 template <typename T>
-static fgb_status queue_normalize(fgb_ctx* ctx, ProxWork& w, T* M, long N, int* d_status, bool seg_done = false) {
+static fgb_status queue_normalize(fgb_ctx* ctx, ProxWork& w, T* M, long N, int* d_status, bool seg_done = false,
+                                  int rows = 0, int cols = 0) {
   const int nchunks = (int)((N + CR_CHUNK - 1) / CR_CHUNK);
   if (w.sq_seg && w.sq_mask && nchunks <= w.sq_chunks) {
     if (!seg_done) {
@@ -1751,7 +1767,17 @@ static fgb_status queue_normalize(fgb_ctx* ctx, ProxWork& w, T* M, long N, int* 
     k_chunk_sumsq<T><<<nchunks, PX_THREADS, 0, ctx->stream>>>(M, N, w.partials);
     FGB_LAUNCHED(ctx);
   }
-  k_scale<T><<<grid_for(ctx, N), PX_THREADS, 0, ctx->stream>>>(M, N, w.partials, nchunks, d_status);
+  // the non-zeros per row and column for a dense -> CSR conversion of M that
+  // may follow (when the workspace holds both count arrays)
+  int *rcnt = nullptr, *ccnt = nullptr;
+  if (rows > 0 && cols > 0 && (long)rows * cols == N && w.growable && w.cap_rows >= rows + cols + 2) {
+    if (w.counted)  // counts of an earlier matrix no conversion consumed
+      FGB_CUDA(ctx, cudaMemsetAsync(w.row_cnt, 0, sizeof(int) * (w.cap_rows + 2), ctx->stream));
+    rcnt = w.row_cnt;
+    ccnt = w.row_cnt + rows;
+    w.counted = M;
+  }
+  k_scale<T><<<grid_for(ctx, N), PX_THREADS, 0, ctx->stream>>>(M, N, w.partials, nchunks, d_status, rows, rcnt, ccnt);
   FGB_LAUNCHED(ctx);
   return FGB_OK;
 }
@@ -2023,7 +2049,7 @@ fgb_status launch_prox(fgb_ctx* ctx, ProxWork& w, const fgb_constraint& c, T* M,
     default:
       return fail(ctx, FGB_ERR_INVALID_ARG, "project : cannot project with this constraint name");
   }
-  if (c.normalized) FGB_TRY(queue_normalize<T>(ctx, w, M, N, d_status, seg_done));
+  if (c.normalized) FGB_TRY(queue_normalize<T>(ctx, w, M, N, d_status, seg_done, rows, cols));
   return FGB_OK;
 }
 
@@ -2097,9 +2123,11 @@ __device__ void block_excl_scan(const int* __restrict__ cnt, int n, int* __restr
 // An entry count above the factor's capacity (which the constraint bounds)
 // is reported through *status and the offsets are clamped so that later
 // kernels stay inside the arrays.
-__global__ void __launch_bounds__(1024) k_d2c_scan_rc(const int* __restrict__ rcnt, int rows, const int* __restrict__ ccnt,
-                                                      int cols, int* __restrict__ rowptr, int* __restrict__ t_rowptr,
+__global__ void __launch_bounds__(1024) k_d2c_scan_rc(int* rcnt_w, int rows, int* ccnt_w, int cols,
+                                                      int* __restrict__ rowptr, int* __restrict__ t_rowptr,
                                                       int with_cols, int cap, int* status, int* maxrc) {
+  const int* rcnt = rcnt_w;
+  const int* ccnt = ccnt_w;
   __shared__ int part[32];
   __shared__ int mx[2];
   block_excl_scan(rcnt, rows, rowptr, part);
@@ -2126,6 +2154,11 @@ __global__ void __launch_bounds__(1024) k_d2c_scan_rc(const int* __restrict__ rc
       maxrc[1] = with_cols ? mx[1] : -1;
     }
   }
+  // zero the counts for the next conversion (the normalisation of the
+  // projections adds to them)
+  __syncthreads();
+  for (int r = threadIdx.x; r < rows; r += blockDim.x) rcnt_w[r] = 0;
+  for (int c = threadIdx.x; c < cols; c += blockDim.x) ccnt_w[c] = 0;
   if (rowptr[rows] > cap) {
     for (int r = threadIdx.x; r <= rows; r += blockDim.x) rowptr[r] = min(rowptr[r], cap);
     if (with_cols)
@@ -2181,8 +2214,11 @@ fgb_status launch_dense_to_csr(fgb_ctx* ctx, ProxWork& w, const T* M, DevFactor&
   const int blocks = (int)((warps * 32 + 255) / 256);
   int* rcnt = w.row_cnt;
   int* ccnt = w.row_cnt + f.rows;
-  k_d2c_count_rc<T><<<blocks, 256, 0, ctx->stream>>>(M, f.rows, f.cols, rcnt, ccnt, with_cols);
-  FGB_LAUNCHED(ctx);
+  if (w.counted != (const void*)M) {
+    k_d2c_count_rc<T><<<blocks, 256, 0, ctx->stream>>>(M, f.rows, f.cols, rcnt, ccnt, with_cols);
+    FGB_LAUNCHED(ctx);
+  }  // else the normalisation of the projection counted them
+  w.counted = nullptr;
   k_d2c_scan_rc<<<1, 1024, 0, ctx->stream>>>(rcnt, f.rows, ccnt, f.cols, f.rowptr, f.t_rowptr, with_cols, f.cap,
                                              status, f.d_maxrc);
   FGB_LAUNCHED(ctx);

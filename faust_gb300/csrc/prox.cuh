@@ -56,6 +56,10 @@ struct ProxWork {
   double* sq_seg = nullptr;
   unsigned* sq_mask = nullptr;
   long sq_chunks = 0;
+  // the matrix whose non-zeros per row and column the normalisation counted
+  // into row_cnt (consumed by the dense -> CSR conversion, which zeroes the
+  // counts again), or null
+  const void* counted = nullptr;
 };
 
 fgb_status prox_work_reserve(fgb_ctx* ctx, ProxWork& w, long elems, int rows);

@@ -107,6 +107,25 @@ def test_prox_sp_radix_key_list(oracle, dtype, espan, levels):
         assert np.count_nonzero(got) == min(k, np.count_nonzero(np.maximum(M, 0) if pos else M))
 
 
+@pytest.mark.parametrize("dtype", [np.float64, np.float32])
+@pytest.mark.parametrize("espan,levels", [(40, 0), (3, 0), (20, 5)])
+def test_prox_sp_radix_select_beyond_registers(oracle, dtype, espan, levels):
+    """1,572,864 entries: more than the 16 keys per thread the register-
+    resident radix select holds on a full cooperative grid of a GB300, so the
+    select that re-reads the keys per digit runs (its key list and one-block
+    finish included); bit-exact against the oracle."""
+    rng = np.random.default_rng(espan + 7 * levels + (dtype == np.float32))
+    rows, cols = 1536, 1024
+    e = rng.integers(0, espan, size=(rows, cols))
+    frac = rng.integers(0, levels + 1, size=(rows, cols)) / 8.0 if levels else rng.random((rows, cols))
+    M = (np.where(rng.random((rows, cols)) < 0.5, -1.0, 1.0) * np.ldexp(1.0 + frac, -e)).astype(dtype)
+    for k, normalized, pos in [(2048, True, False), (int(rng.integers(20000, 200000)), False, True)]:
+        c = fact.ConstraintInt("sp", rows, cols, k, normalized=normalized, pos=pos)
+        got = _gpu_prox(M, c)
+        ref = oracle.prox(oracle.SP, M, k=k, normalized=normalized, pos=pos)
+        assert np.array_equal(got, ref), (k, normalized, pos)
+
+
 @pytest.mark.parametrize("name,kind", [("spcol", 1), ("splin", 2), ("splincol", 3)])
 @pytest.mark.parametrize("seed", range(4))
 def test_prox_lines_bitexact(oracle, name, kind, seed):
