@@ -83,6 +83,8 @@ fgb_status prox_work_reserve(fgb_ctx* ctx, ProxWork& w, long elems, int rows) {
   FGB_TRY(dmalloc(ctx, (void**)&w.sq_mask, sizeof(unsigned) * (size_t)std::max(1L, w.sq_chunks) * CR_LANES));
   FGB_CUDA(ctx, cudaMemsetAsync(w.sq_mask, 0, sizeof(unsigned) * (size_t)std::max(1L, w.sq_chunks) * CR_LANES,
                                 ctx->stream));
+  FGB_TRY(dmalloc(ctx, (void**)&w.sq_done, sizeof(unsigned) * (size_t)std::max(1L, w.sq_chunks)));
+  FGB_CUDA(ctx, cudaMemsetAsync(w.sq_done, 0, sizeof(unsigned) * (size_t)std::max(1L, w.sq_chunks), ctx->stream));
   w.cap_elems = elems;
   w.cap_rows = rows;
   w.growable = 1;
@@ -108,6 +110,7 @@ void prox_work_free(ProxWork& w) {
   dfree(w.heap2);
   dfree(w.sq_seg);
   dfree(w.sq_mask);
+  dfree(w.sq_done);
   w = ProxWork();
 }
 
@@ -1430,6 +1433,58 @@ __global__ void k_sp_apply(T* __restrict__ M, long N, int pos, const TopkState* 
   }
 }
 
+// The second half, run by the last of chunk c's SQ_SEG segment blocks to
+// finish (all of them have written their partials and marks): every lane
+// continues its chain from its first marked segment over the later marked
+// ones, in order, then the lanes are added by the tree.  The other blocks'
+// writes are read from L2.  Every thread of the block calls it.
+template <typename T>
+__device__ void sq_chunk_lanes(const T* __restrict__ M, long N, int c, const double* __restrict__ seg,
+                               unsigned* __restrict__ mask, double* partials, T* lane) {
+  const int t = threadIdx.x;
+  unsigned m = __ldcg(&mask[c * CR_LANES + t]);
+  T acc = T(0);
+  if (m) {
+    acc = __ldcg(reinterpret_cast<const T*>(seg) + ((long)c * SQ_SEG + (__ffs(m) - 1)) * CR_LANES + t);
+    m &= m - 1;
+    while (m) {
+      const int s = __ffs(m) - 1;
+      m &= m - 1;
+      const long base = (long)c * CR_CHUNK + t + (long)s * SQ_PER * CR_LANES;
+      for (int u = 0; u < SQ_PER; ++u) {
+        const long i = base + (long)u * CR_LANES;
+        if (i < N) {
+          const T x = __ldcg(M + i);
+          if (mag_key(x) != 0) acc = fmad(x, x, acc);
+        }
+      }
+    }
+    mask[c * CR_LANES + t] = 0;  // zero again for the next use
+  }
+  lane[t] = acc;
+  const T part = lane_tree_256(lane);
+  if (t == 0) reinterpret_cast<T*>(partials)[c] = part;
+}
+
+// After a segment block's partials and marks: the last block of the chunk
+// finishes it (per-chunk arrival counter, reset by that block).
+template <typename T>
+__device__ __forceinline__ void sq_segment_done(const T* __restrict__ M, long N, int c, const double* seg,
+                                                unsigned* mask, unsigned* done, double* partials) {
+  __shared__ T lane[CR_LANES];
+  __shared__ int last;
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    last = atomicAdd(&done[c], 1u) == (unsigned)(SQ_SEG - 1);
+    if (last) done[c] = 0;
+  }
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  sq_chunk_lanes<T>(M, N, c, seg, mask, partials, lane);
+}
+
 // k_sp_apply with the first half of the normalisation's sum of squares
 // (k_sumsq_seg) on the entries it leaves: block (c, s) of SQ_SEG blocks per
 // chunk, lane t owns the entries t + CR_LANES * (SQ_PER * s + u) of chunk c,
@@ -1438,7 +1493,8 @@ __global__ void k_sp_apply(T* __restrict__ M, long N, int pos, const TopkState* 
 template <typename T>
 __global__ void __launch_bounds__(CR_LANES)
     k_sp_apply_sq(T* __restrict__ M, long N, int pos, const TopkState* st, unsigned char* __restrict__ flags,
-                  int* d_status, double* __restrict__ seg, unsigned* __restrict__ mask) {
+                  int* d_status, double* __restrict__ seg, unsigned* __restrict__ mask,
+                  unsigned* __restrict__ done, double* partials) {
   if (d_status && blockIdx.x == 0 && threadIdx.x == 0 && st->status) atomicCAS(d_status, 0, st->status);
   const unsigned long long t = st->t;
   const int cs = st->sel_case;
@@ -1477,6 +1533,7 @@ __global__ void __launch_bounds__(CR_LANES)
     reinterpret_cast<T*>(seg)[((long)c * SQ_SEG + s) * CR_LANES + ln] = acc;
     atomicOr(&mask[c * CR_LANES + ln], 1u << s);
   }
+  sq_segment_done<T>(M, N, c, seg, mask, done, partials);
 }
 
 template <typename T>
@@ -1614,14 +1671,16 @@ __global__ void __launch_bounds__(PX_THREADS) k_chunk_sumsq(const T* __restrict_
 // the sparse results of the projections: block (c, s) computes, for every
 // lane t of chunk c, the sequential fma over the lane's values SQ_PER * s ..
 // SQ_PER * s + SQ_PER - 1 from +0 (zeros add +0 to a non-negative partial
-// and are skipped) and marks the segments that held a non-zero;
-// k_sumsq_lanes continues each lane's chain from its first marked segment
-// over the later marked ones, in order, then adds the lanes by the tree.
-// Most lanes of a sparse block have no or one marked segment, so the chain
-// rarely reloads anything; a dense block costs what k_chunk_sumsq costs.
+// and are skipped) and marks the segments that held a non-zero; the last
+// block of the chunk to finish continues each lane's chain from its first
+// marked segment over the later marked ones, in order, then adds the lanes by
+// the tree (sq_segment_done).  Most lanes of a sparse block have no or one
+// marked segment, so the chain rarely reloads anything; a dense block costs
+// what k_chunk_sumsq costs.
 template <typename T>
 __global__ void __launch_bounds__(CR_LANES) k_sumsq_seg(const T* __restrict__ M, long N, double* __restrict__ seg,
-                                                         unsigned* __restrict__ mask) {
+                                                         unsigned* __restrict__ mask, unsigned* __restrict__ done,
+                                                         double* partials) {
   const int c = blockIdx.x / SQ_SEG, s = blockIdx.x % SQ_SEG, t = threadIdx.x;
   const long base = (long)c * CR_CHUNK + t + (long)s * SQ_PER * CR_LANES;
   T v[SQ_PER];
@@ -1642,36 +1701,7 @@ __global__ void __launch_bounds__(CR_LANES) k_sumsq_seg(const T* __restrict__ M,
     reinterpret_cast<T*>(seg)[((long)c * SQ_SEG + s) * CR_LANES + t] = acc;
     atomicOr(&mask[c * CR_LANES + t], 1u << s);
   }
-}
-
-template <typename T>
-__global__ void __launch_bounds__(CR_LANES) k_sumsq_lanes(const T* __restrict__ M, long N,
-                                                           const double* __restrict__ seg, unsigned* __restrict__ mask,
-                                                           double* partials) {
-  __shared__ T lane[CR_LANES];
-  const int c = blockIdx.x, t = threadIdx.x;
-  unsigned m = mask[c * CR_LANES + t];
-  T acc = T(0);
-  if (m) {
-    acc = reinterpret_cast<const T*>(seg)[((long)c * SQ_SEG + (__ffs(m) - 1)) * CR_LANES + t];
-    m &= m - 1;
-    while (m) {
-      const int s = __ffs(m) - 1;
-      m &= m - 1;
-      const long base = (long)c * CR_CHUNK + t + (long)s * SQ_PER * CR_LANES;
-      for (int u = 0; u < SQ_PER; ++u) {
-        const long i = base + (long)u * CR_LANES;
-        if (i < N) {
-          const T x = M[i];
-          if (mag_key(x) != 0) acc = fmad(x, x, acc);
-        }
-      }
-    }
-    mask[c * CR_LANES + t] = 0;  // zero again for the next use
-  }
-  lane[t] = acc;
-  const T part = lane_tree_256(lane);
-  if (t == 0) reinterpret_cast<T*>(partials)[c] = part;
+  sq_segment_done<T>(M, N, c, seg, mask, done, partials);
 }
 
 // rcnt, ccnt (optional): per-row and per-column counts of the non-zero
@@ -1756,13 +1786,12 @@ template <typename T>
 static fgb_status queue_normalize(fgb_ctx* ctx, ProxWork& w, T* M, long N, int* d_status, bool seg_done = false,
                                   int rows = 0, int cols = 0) {
   const int nchunks = (int)((N + CR_CHUNK - 1) / CR_CHUNK);
-  if (w.sq_seg && w.sq_mask && nchunks <= w.sq_chunks) {
+  if (w.sq_seg && w.sq_mask && w.sq_done && nchunks <= w.sq_chunks) {
     if (!seg_done) {
-      k_sumsq_seg<T><<<nchunks * SQ_SEG, CR_LANES, 0, ctx->stream>>>(M, N, w.sq_seg, w.sq_mask);
+      k_sumsq_seg<T><<<nchunks * SQ_SEG, CR_LANES, 0, ctx->stream>>>(M, N, w.sq_seg, w.sq_mask, w.sq_done,
+                                                                     w.partials);
       FGB_LAUNCHED(ctx);
     }
-    k_sumsq_lanes<T><<<nchunks, CR_LANES, 0, ctx->stream>>>(M, N, w.sq_seg, w.sq_mask, w.partials);
-    FGB_LAUNCHED(ctx);
   } else {
     k_chunk_sumsq<T><<<nchunks, PX_THREADS, 0, ctx->stream>>>(M, N, w.partials);
     FGB_LAUNCHED(ctx);
@@ -1961,10 +1990,10 @@ static fgb_status queue_sp(fgb_ctx* ctx, ProxWork& w, T* M, long N, long k, int 
     FGB_LAUNCHED(ctx);
   }
   const int nchunks = (int)((N + CR_CHUNK - 1) / CR_CHUNK);
-  if (seg_done && w.sq_seg && w.sq_mask && nchunks <= w.sq_chunks) {
+  if (seg_done && w.sq_seg && w.sq_mask && w.sq_done && nchunks <= w.sq_chunks) {
     // the normalisation follows: its segment sums come with the apply
     k_sp_apply_sq<T><<<nchunks * SQ_SEG, CR_LANES, 0, ctx->stream>>>(M, N, pos, w.state, w.flags, d_status, w.sq_seg,
-                                                                   w.sq_mask);
+                                                                   w.sq_mask, w.sq_done, w.partials);
     *seg_done = true;
   } else {
     k_sp_apply<T><<<g, PX_THREADS, 0, ctx->stream>>>(M, N, pos, w.state, w.flags, d_status);

@@ -55,6 +55,7 @@ struct ProxWork {
   // between uses)
   double* sq_seg = nullptr;
   unsigned* sq_mask = nullptr;
+  unsigned* sq_done = nullptr;  // segment blocks finished per chunk (kept zero between uses)
   long sq_chunks = 0;
   // the matrix whose non-zeros per row and column the normalisation counted
   // into row_cnt (consumed by the dense -> CSR conversion, which zeroes the
