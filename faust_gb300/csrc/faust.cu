@@ -494,7 +494,7 @@ fgb_status fgb_faust_mul_host(fgb_faust* F, const void* X, int ncols, void* Y) {
     FGB_TRY(fgb_faust_mul(F, F->dx, inner, ncols, F->dy, rows, 0));
     FGB_CUDA(ctx, cudaMemcpyAsync(Y, F->dy, yb, cudaMemcpyDeviceToHost, ctx->stream));
     FGB_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-    return FGB_OK;
+    return check_kernel_err(ctx);
   }
   if (!F->s_in) {
     FGB_CUDA(ctx, cudaStreamCreateWithFlags(&F->s_in, cudaStreamNonBlocking));
@@ -526,7 +526,7 @@ fgb_status fgb_faust_mul_host(fgb_faust* F, const void* X, int ncols, void* Y) {
   }
   FGB_CUDA(ctx, cudaStreamSynchronize(F->s_out));
   FGB_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-  return FGB_OK;
+  return check_kernel_err(ctx);
 }
 
 fgb_status fgb_faust_spectral_norm(fgb_faust* F, int max_iter, double threshold, double* norm, int* flag) {

@@ -167,6 +167,30 @@ def test_butterfly_kernel_orders_and_sizes(fgb, oracle, nf, order, ncols):
     F.close()
 
 
+def test_bounded_wait_kernels_leave_no_timeout(fgb, oracle):
+    """The radix butterfly kernel and the tcgen05 BSR kernel record an expired
+    bounded wait in the context's error word; after ordinary products
+    fgb_ctx_synchronize reports none, and the host-buffer product (which
+    reads the word after its own synchronisation) returns the oracle's
+    result."""
+    rng = np.random.default_rng(91)
+    facs = synth.butterfly_faust_factors(10, rng, np.float32)
+    F = fgb.Faust(facs, dtype=np.float32)
+    X = synth.dense_colmajor(1024, 96, rng, np.float32)
+    Y = F.matmul_device(_colmajor_cuda(X), mode=3)
+    F.ctx.synchronize()
+    assert np.array_equal(_to_np(Y), oracle.chain_mul(facs, X))
+    assert np.array_equal(F @ np.asfortranarray(X), oracle.chain_mul(facs, X))
+    bfacs, _ = _bsr_factors(fgb, 512, 2, rng)
+    B = fgb.Faust(bfacs)
+    torch = _torch()
+    Xb = torch.randn((256, 512), device="cuda", dtype=torch.float32).to(torch.bfloat16).t()
+    B.matmul_device(Xb)
+    B.ctx.synchronize()
+    F.close()
+    B.close()
+
+
 def test_butterfly_kernel_rejects_other_supports(fgb):
     rng = np.random.default_rng(4)
     facs = [synth.random_csr(64, 64, 2, rng) for _ in range(3)]
