@@ -255,7 +255,7 @@ def run_faust_x(args, rank, world):
                 "kernel": "k_bsr_tc", "algorithmic_flops_per_launch": int(fl), "algorithmic_bytes_per_launch": int(kb)}
     else:
         # dram read + write bytes of one launch from one ncu capture (the butterfly chain)
-        traffic = 216814592 if bfly else None
+        traffic = 212645376 if bfly else None
         roof = {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
                 "frac": round(achieved / hbm, 4), "traffic": traffic, "peak_kind": peak_kind,
                 "kernel": chain_kernel if fused else "k_csr_spmm", "algorithmic_bytes_per_launch": int(kb)}
