@@ -431,18 +431,19 @@ __global__ void __launch_bounds__(PX_THREADS)
 }
 
 // The same selection with every thread's keys held in registers (at most
-// RS_KREG per thread, i.e. N <= grid threads * RS_KREG): each full pass
-// reads registers instead of the matrix.  Once the chosen bucket holds at
+// RS_KREG per thread, i.e. N <= grid threads * RS_KREG; one block per SM, so
+// that fewer blocks meet at each grid barrier and merge their histograms):
+// each full pass reads registers instead of the matrix.  Once the chosen bucket holds at
 // most RS_TAIL_CAP keys, every block appends its keys of that bucket to the
 // list straight from its registers and counts itself in; block 0 alone
 // waits for all the blocks (a one-sided, bounded wait) and finishes the
 // remaining digits from the list staged in shared memory.  The histograms,
 // bucket picks and outputs are those of k_radix_select.
-constexpr int RS_KREG = 16;
+constexpr int RS_KREG = 32;
 constexpr int RS_TAIL_CAP = 4096;
 
 template <typename T>
-__global__ void __launch_bounds__(PX_THREADS)
+__global__ void __launch_bounds__(PX_THREADS, 1)
     k_radix_select_reg(const T* __restrict__ M, long N, int pos, int npass, long long k, TopkState* st,
                        unsigned* hists, unsigned long long* __restrict__ list) {
   __shared__ unsigned sh[2048];
@@ -1933,7 +1934,7 @@ static fgb_status queue_sp(fgb_ctx* ctx, ProxWork& w, T* M, long N, long k, int 
     if (!nbr) {
       int per_sm = 0;
       FGB_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_radix_select_reg<T>, PX_THREADS, 0));
-      nbr = std::max(1, std::min(per_sm, 2)) * ctx->sm_count;
+      nbr = std::max(1, std::min(per_sm, 1)) * ctx->sm_count;
     }
     if (N <= (long)nbr * PX_THREADS * RS_KREG) {
       cfg.gridDim = dim3((unsigned)std::min<long>(nbr, std::max(1L, (N + PX_THREADS - 1) / PX_THREADS)));
