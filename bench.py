@@ -816,7 +816,7 @@ def cpu_baseline_batched(ns, mats, sample=16):
 def run_warmstart(args, rank, world):
     """Gaussian-kernel butterfly factorizations: plain palm4msa2 (200
     iterations) against MLP-predicted factors refined by palm4msa2, on
-    held-out draws.  Every held-out matrix is judged against its OWN plain
+    held-out draws.  Every held-out matrix is compared with its OWN plain
     200-iteration relative error.  value = wall time, for the whole held-out
     set, of the MLP inference plus the seeded refinement (the device writes
     the predicted values into the supports and the optimal starting lambda)
