@@ -51,3 +51,21 @@ def test_single_rank_is_identity():
     import bench
     assert bench._max_over_ranks(1.5, 1) == 1.5
     bench._barrier(1)
+
+
+def test_faust_x_arms_divide_the_same_bytes():
+    """Every Faust x dense line (GPU value, e2e, CPU baseline, reference arm)
+    divides the problem's bytes: X read, Y written and the factor arrays,
+    charged to a column sample in proportion, so that two lines' ratio is the
+    ratio of their times.  BSR operands count as BF16."""
+    import types
+    sys.path.insert(0, ROOT)
+    import numpy as np
+    import bench
+    W = types.SimpleNamespace(name="csr_butterfly", n=4096, ncols=8192, np_dtype=np.float32,
+                              factor_bytes=lambda: [100, 200, 300])
+    full = 2 * 4096 * 8192 * 4 + 600
+    assert bench._problem_bytes(W) == full
+    assert bench._problem_bytes(W, 512) == full * 512 / 8192
+    B = types.SimpleNamespace(name="bsr", n=16384, ncols=4096, np_dtype=np.float32, factor_bytes=lambda: [1000])
+    assert bench._problem_bytes(B) == 2 * 16384 * 4096 * 2 + 1000
