@@ -69,3 +69,23 @@ def test_faust_x_arms_divide_the_same_bytes():
     assert bench._problem_bytes(W, 512) == full * 512 / 8192
     B = types.SimpleNamespace(name="bsr", n=16384, ncols=4096, np_dtype=np.float32, factor_bytes=lambda: [1000])
     assert bench._problem_bytes(B) == 2 * 16384 * 4096 * 2 + 1000
+
+
+def test_reference_arm_line_on_cpu():
+    """`bench.py --impl reference` runs on the host cores only and prints one
+    JSON line with the arm's value, its CPU baseline description and an e2e
+    entry without copies (the Faust x dense workload of 5 CSR 1024^2 FP64
+    factors, one bounded sample)."""
+    import json
+    import subprocess
+    out = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--workload",
+                          "csr_random", "--steps", "1", "--warmup", "0"], cwd=ROOT, capture_output=True, text=True,
+                         timeout=600)
+    assert out.returncode == 0, out.stderr[-2000:]
+    line = json.loads(out.stdout.strip().splitlines()[-1])
+    assert line["impl"] == "reference" and line["unit"] == "GB/s" and line["higher_is_better"] is True
+    assert line["value"] > 0 and line["config"]["workload"] == "csr_random"
+    cb = line["cpu_baseline"]
+    assert cb["kind"] == "port" and cb["cores"] >= 1 and cb["value"] == line["value"] and cb["sample"]
+    assert line["e2e"]["value"] == line["value"]
+    assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["e2e"]["d2h_bytes_per_step"] == 0
